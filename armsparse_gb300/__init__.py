@@ -1,0 +1,15 @@
+"""armsparse_gb300 -- GB300-native (sm_103a) sparse hot path of ARMSparse.
+
+CSR SpMM (fp32 bit-identical to the reference's rowBaseSpmm3; bf16 storage with fp32
+accumulation), CSR SpMV (plain and the reference's 1x4-blocked layout), SDDMM (FP32 CUDA
+cores and tcgen05 split-bf16) and a deterministic CSR->CSC transpose, behind the C ABI in
+include/armsparse_gpu.h. The ops need the CUDA library built in-tree and a GPU; there is no
+CPU fallback.
+"""
+from .sparse import (csr2csc, sddmm, spmm, spmm_default_variant, spmm_variants, spmv,
+                     spmv_vcsr4, sync_status, to_bf16, validate_csr)
+from ._native import NativeError, Context, context
+
+__all__ = ["spmm", "spmv", "spmv_vcsr4", "sddmm", "csr2csc", "validate_csr", "sync_status",
+           "to_bf16", "spmm_variants", "spmm_default_variant", "NativeError", "Context",
+           "context"]

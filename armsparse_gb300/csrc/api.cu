@@ -1,0 +1,313 @@
+// C-ABI entry points (include/armsparse_gpu.h): argument checks, context, dispatch.
+#include <stdio.h>
+
+#include <string>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace as {
+
+static thread_local std::string g_last_error = "no error";
+
+as_status fail(as_status s, const std::string &msg) {
+    g_last_error = msg;
+    return s;
+}
+
+as_status check_cuda(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return AS_OK;
+    return fail(AS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+as_status scratch(as_ctx *ctx, size_t bytes, void **out) {
+    bytes = (bytes + 255) & ~size_t(255);
+    if (bytes == 0) bytes = 256;
+    if (bytes > ctx->scratch_bytes) {
+        if (ctx->scratch) {
+            cudaError_t e = cudaDeviceSynchronize();
+            if (e != cudaSuccess) return check_cuda(e, "scratch sync");
+            cudaFree(ctx->scratch);
+            ctx->scratch = nullptr;
+            ctx->scratch_bytes = 0;
+        }
+        size_t grow = bytes + bytes / 4;
+        if (cudaMalloc(&ctx->scratch, grow) != cudaSuccess) {
+            cudaGetLastError();
+            if (cudaMalloc(&ctx->scratch, bytes) != cudaSuccess) {
+                cudaGetLastError();
+                return fail(AS_ERR_ALLOC, "scratch allocation of " + std::to_string(bytes) +
+                                              " bytes failed");
+            }
+            grow = bytes;
+        }
+        ctx->scratch_bytes = grow;
+    }
+    *out = ctx->scratch;
+    return AS_OK;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+static bool aligned_to(const void *p, size_t a) {
+    return (reinterpret_cast<uintptr_t>(p) % a) == 0;
+}
+
+static as_status check_csr_args(const char *fn, int M, int K, int nnz, const int *rowptr,
+                                const int *colind, const void *val, bool need_val) {
+    if (M < 0 || K < 0 || nnz < 0)
+        return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": negative size");
+    if (!rowptr) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": rowptr is NULL");
+    if (nnz > 0 && !colind)
+        return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": colind is NULL");
+    if (need_val && nnz > 0 && !val)
+        return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": val is NULL");
+    if (!aligned_to(rowptr, 4) || (colind && !aligned_to(colind, 4)))
+        return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": index arrays must be 4-byte aligned");
+    return AS_OK;
+}
+
+}  // namespace as
+
+using namespace as;
+
+extern "C" {
+
+const char *as_last_error(void) { return g_last_error.c_str(); }
+
+const char *as_status_string(as_status s) {
+    switch (s) {
+        case AS_OK: return "AS_OK";
+        case AS_ERR_INVALID_VALUE: return "AS_ERR_INVALID_VALUE";
+        case AS_ERR_INVALID_CSR: return "AS_ERR_INVALID_CSR";
+        case AS_ERR_UNSUPPORTED: return "AS_ERR_UNSUPPORTED";
+        case AS_ERR_CUDA: return "AS_ERR_CUDA";
+        case AS_ERR_TIMEOUT: return "AS_ERR_TIMEOUT";
+        case AS_ERR_ALLOC: return "AS_ERR_ALLOC";
+    }
+    return "AS_ERR_UNKNOWN";
+}
+
+as_status as_ctx_create(as_ctx **out, int device) {
+    if (!out) return fail(AS_ERR_INVALID_VALUE, "as_ctx_create: out is NULL");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) return check_cuda(e, "as_ctx_create: cudaGetDeviceCount");
+    if (device < 0 || device >= n)
+        return fail(AS_ERR_INVALID_VALUE, "as_ctx_create: no such device");
+    DeviceGuard g(device);
+    as_ctx *c = new as_ctx();
+    c->device = device;
+    e = cudaMalloc(&c->d_status, sizeof(unsigned));
+    if (e != cudaSuccess) {
+        delete c;
+        return check_cuda(e, "as_ctx_create: status word");
+    }
+    e = cudaMemset(c->d_status, 0, sizeof(unsigned));
+    if (e != cudaSuccess) {
+        cudaFree(c->d_status);
+        delete c;
+        return check_cuda(e, "as_ctx_create: memset");
+    }
+    *out = c;
+    return AS_OK;
+}
+
+as_status as_ctx_destroy(as_ctx *c) {
+    if (!c) return AS_OK;
+    DeviceGuard g(c->device);
+    cudaDeviceSynchronize();
+    if (c->scratch) cudaFree(c->scratch);
+    if (c->d_status) cudaFree(c->d_status);
+    delete c;
+    return AS_OK;
+}
+
+uint64_t as_ctx_launch_count(const as_ctx *c) { return c ? c->launches : 0; }
+
+as_status as_ctx_sync_status(as_ctx *c, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_ctx_sync_status: ctx is NULL");
+    DeviceGuard g(c->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, c->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, sizeof(unsigned), s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return check_cuda(e, "as_ctx_sync_status");
+    if (h & kFlagTimeout) return fail(AS_ERR_TIMEOUT, "a bounded device wait gave up");
+    if (h & (kFlagBadRowptr | kFlagBadColind))
+        return fail(AS_ERR_INVALID_CSR,
+                    (h & kFlagBadRowptr) ? "malformed rowptr seen on the device"
+                                         : "column index out of range seen on the device");
+    return AS_OK;
+}
+
+as_status as_csr_validate(as_ctx *c, int n_rows, int n_cols, int nnz, const int *rowptr,
+                          const int *colind, int require_sorted, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_csr_validate: ctx is NULL");
+    as_status st = check_csr_args("as_csr_validate", n_rows, n_cols, nnz, rowptr, colind,
+                                  nullptr, false);
+    if (st != AS_OK) return st;
+    DeviceGuard g(c->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    void *w = nullptr;
+    if ((st = scratch(c, sizeof(unsigned), &w)) != AS_OK) return st;
+    unsigned *res = static_cast<unsigned *>(w);
+    st = csr_validate_launch(c, n_rows, n_cols, nnz, rowptr, colind, require_sorted, res, s);
+    if (st != AS_OK) return st;
+    unsigned h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, res, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return check_cuda(e, "as_csr_validate");
+    if (h & 1u) return fail(AS_ERR_INVALID_CSR, "rowptr[0] != 0 or rowptr[n_rows] != nnz");
+    if (h & 2u) return fail(AS_ERR_INVALID_CSR, "rowptr is not non-decreasing");
+    if (h & 4u) return fail(AS_ERR_INVALID_CSR, "column index out of range");
+    if (h & 8u) return fail(AS_ERR_INVALID_CSR, "columns not strictly ascending in a row");
+    return AS_OK;
+}
+
+static as_status spmm_common(const char *fn, int dtype, as_ctx *c, int M, int K, int N, int nnz,
+                             const int *rowptr, const int *colind, const void *val,
+                             const void *B, long ldb, float *C, long ldc, float beta,
+                             int variant, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": ctx is NULL");
+    as_status st = check_csr_args(fn, M, K, nnz, rowptr, colind, val, true);
+    if (st != AS_OK) return st;
+    if (N < 0) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": negative N");
+    if (M == 0 || N == 0) return AS_OK;
+    if (!C) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": C is NULL");
+    if (K > 0 && nnz > 0 && !B) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": B is NULL");
+    if (ldb < N || ldc < N)
+        return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": leading dimension below N");
+    if (variant < 0 || variant > spmm_variant_count(dtype))
+        return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": unknown variant");
+    DeviceGuard g(c->device);
+    SpmmArgs a{M, K, N, nnz, rowptr, colind, val, B, ldb, C, ldc, beta, c->d_status};
+    if (variant == 0) variant = spmm_default_variant(dtype, M, K, N, nnz, ldb, ldc, B, C);
+    return spmm_launch(c, dtype, variant, a, static_cast<cudaStream_t>(stream));
+}
+
+as_status as_spmm_csr_f32(as_ctx *c, int M, int K, int N, int nnz, const int *rowptr,
+                          const int *colind, const float *val, const float *B, long ldb,
+                          float *C, long ldc, float beta, int variant, void *stream) {
+    return spmm_common("as_spmm_csr_f32", 0, c, M, K, N, nnz, rowptr, colind, val, B, ldb, C,
+                       ldc, beta, variant, stream);
+}
+
+as_status as_spmm_csr_bf16(as_ctx *c, int M, int K, int N, int nnz, const int *rowptr,
+                           const int *colind, const uint16_t *val, const uint16_t *B,
+                           long ldb, float *C, long ldc, float beta, int variant,
+                           void *stream) {
+    return spmm_common("as_spmm_csr_bf16", 1, c, M, K, N, nnz, rowptr, colind, val, B, ldb, C,
+                       ldc, beta, variant, stream);
+}
+
+int as_spmm_variant_count(int dtype) { return spmm_variant_count(dtype); }
+const char *as_spmm_variant_name(int dtype, int variant) {
+    return spmm_variant_name(dtype, variant);
+}
+int as_spmm_default_variant(int dtype, int M, int K, int N, int nnz, long ldb, long ldc,
+                            const void *B, const void *C) {
+    return spmm_default_variant(dtype, M, K, N, nnz, ldb, ldc, B, C);
+}
+
+as_status as_spmv_csr_f32(as_ctx *c, int M, int K, int nnz, const int *rowptr,
+                          const int *colind, const float *val, const float *x, float *y,
+                          float beta, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_spmv_csr_f32: ctx is NULL");
+    as_status st = check_csr_args("as_spmv_csr_f32", M, K, nnz, rowptr, colind, val, true);
+    if (st != AS_OK) return st;
+    if (M == 0) return AS_OK;
+    if (!y || (nnz > 0 && !x)) return fail(AS_ERR_INVALID_VALUE, "as_spmv_csr_f32: x or y is NULL");
+    DeviceGuard g(c->device);
+    return spmv_csr_launch(c, M, K, nnz, rowptr, colind, val, x, y, beta,
+                           static_cast<cudaStream_t>(stream));
+}
+
+as_status as_spmv_vcsr4_f32(as_ctx *c, int M, int K, int nslots, const int *rowptr,
+                            const int *colind, const float *val, const float *x, float *y,
+                            float beta, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_spmv_vcsr4_f32: ctx is NULL");
+    as_status st = check_csr_args("as_spmv_vcsr4_f32", M, K, nslots, rowptr, colind, val, true);
+    if (st != AS_OK) return st;
+    if (nslots % 4 != 0)
+        return fail(AS_ERR_INVALID_VALUE, "as_spmv_vcsr4_f32: slot count is not a multiple of 4");
+    if (M == 0) return AS_OK;
+    if (!y || (nslots > 0 && !x))
+        return fail(AS_ERR_INVALID_VALUE, "as_spmv_vcsr4_f32: x or y is NULL");
+    DeviceGuard g(c->device);
+    return spmv_vcsr4_launch(c, M, K, nslots, rowptr, colind, val, x, y, beta,
+                             static_cast<cudaStream_t>(stream));
+}
+
+static as_status sddmm_common(const char *fn, bool tc, as_ctx *c, int M, int N, int K, int nnz,
+                              const int *rowptr, const int *colind, const float *aval,
+                              const float *X, long ldx, const float *Y, long ldy, float *out,
+                              void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": ctx is NULL");
+    as_status st = check_csr_args(fn, M, N, nnz, rowptr, colind, nullptr, false);
+    if (st != AS_OK) return st;
+    if (K < 0) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": negative K");
+    if (nnz == 0) return AS_OK;
+    if (!out) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": out is NULL");
+    if (K > 0 && (!X || !Y)) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": X or Y is NULL");
+    if (ldx < K || ldy < K)
+        return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": leading dimension below K");
+    DeviceGuard g(c->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (tc) return sddmm_bf16x3_launch(c, M, N, K, nnz, rowptr, colind, aval, X, ldx, Y, ldy, out, s);
+    return sddmm_f32_launch(c, M, N, K, nnz, rowptr, colind, aval, X, ldx, Y, ldy, out, s);
+}
+
+as_status as_sddmm_csr_f32(as_ctx *c, int M, int N, int K, int nnz, const int *rowptr,
+                           const int *colind, const float *aval, const float *X, long ldx,
+                           const float *Y, long ldy, float *out, void *stream) {
+    return sddmm_common("as_sddmm_csr_f32", false, c, M, N, K, nnz, rowptr, colind, aval, X,
+                        ldx, Y, ldy, out, stream);
+}
+
+as_status as_sddmm_csr_bf16x3(as_ctx *c, int M, int N, int K, int nnz, const int *rowptr,
+                              const int *colind, const float *aval, const float *X, long ldx,
+                              const float *Y, long ldy, float *out, void *stream) {
+    return sddmm_common("as_sddmm_csr_bf16x3", true, c, M, N, K, nnz, rowptr, colind, aval, X,
+                        ldx, Y, ldy, out, stream);
+}
+
+as_status as_csr2csc(as_ctx *c, int M, int N, int nnz, const int *rowptr, const int *colind,
+                     const float *val, int *colptr, int *rowind, float *cscval, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_csr2csc: ctx is NULL");
+    as_status st = check_csr_args("as_csr2csc", M, N, nnz, rowptr, colind, nullptr, false);
+    if (st != AS_OK) return st;
+    if (!colptr) return fail(AS_ERR_INVALID_VALUE, "as_csr2csc: colptr is NULL");
+    if (nnz > 0 && !rowind) return fail(AS_ERR_INVALID_VALUE, "as_csr2csc: rowind is NULL");
+    if ((val == nullptr) != (cscval == nullptr))
+        return fail(AS_ERR_INVALID_VALUE, "as_csr2csc: val and cscval must both be given or both NULL");
+    DeviceGuard g(c->device);
+    void *w = nullptr;
+    st = scratch(c, csr2csc_scratch_bytes(nnz, N, val != nullptr), &w);
+    if (st != AS_OK) return st;
+    return csr2csc_launch(c, M, N, nnz, rowptr, colind, val, colptr, rowind, cscval, w,
+                          static_cast<cudaStream_t>(stream));
+}
+
+as_status as_f32_to_bf16(as_ctx *c, long n, const float *src, uint16_t *dst, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_f32_to_bf16: ctx is NULL");
+    if (n < 0) return fail(AS_ERR_INVALID_VALUE, "as_f32_to_bf16: negative size");
+    if (n == 0) return AS_OK;
+    if (!src || !dst) return fail(AS_ERR_INVALID_VALUE, "as_f32_to_bf16: NULL pointer");
+    DeviceGuard g(c->device);
+    return f32_to_bf16_launch(c, n, src, dst, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

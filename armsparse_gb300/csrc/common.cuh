@@ -1,0 +1,57 @@
+// Shared device helpers for the sm_103a sparse kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "armsparse_gpu.h"
+
+namespace as {
+
+// Bits of the device status word (the context's error flag). Kernels OR them in and keep
+// going on a memory-safe path; the host maps them to as_status.
+enum : unsigned {
+    kFlagBadRowptr = 1u,
+    kFlagBadColind = 2u,
+    kFlagTimeout = 4u,
+};
+
+__device__ __forceinline__ void flag(unsigned *status, unsigned bit) {
+    if (status) atomicOr(status, bit);
+}
+
+// Read-only, no-allocate-in-L1 loads for streamed index/value arrays.
+__device__ __forceinline__ int ld_stream(const int *p) { return __ldcs(p); }
+__device__ __forceinline__ float ld_stream(const float *p) { return __ldcs(p); }
+__device__ __forceinline__ uint16_t ld_stream(const uint16_t *p) {
+    return __ldcs(reinterpret_cast<const unsigned short *>(p));
+}
+
+__device__ __forceinline__ float bf16_to_f32(uint16_t h) {
+    return __uint_as_float(static_cast<unsigned>(h) << 16);
+}
+
+// Round to nearest even; NaN stays a quiet NaN.
+__device__ __forceinline__ uint16_t f32_to_bf16(float f) {
+    unsigned u = __float_as_uint(f);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return static_cast<uint16_t>((u >> 16) | 0x40u);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return static_cast<uint16_t>(u >> 16);
+}
+
+// Valid row range [lo, hi) of row r; rows with malformed pointers become empty and flag.
+__device__ __forceinline__ void row_range(const int *rowptr, int r, int nnz, unsigned *status,
+                                          int &lo, int &hi) {
+    lo = __ldg(rowptr + r);
+    hi = __ldg(rowptr + r + 1);
+    if (lo < 0 || hi < lo || hi > nnz) {
+        flag(status, kFlagBadRowptr);
+        lo = hi = 0;
+    }
+}
+
+__host__ __device__ __forceinline__ long long ceil_div(long long a, long long b) {
+    return (a + b - 1) / b;
+}
+
+}  // namespace as

@@ -1,0 +1,265 @@
+// Host-pointer shims with the reference drivers' signatures (include/armsparse_drivers.h).
+// Each call: copy the host arrays to cached device buffers, run the kernel through the C
+// ABI, copy the result back, wait. The process-wide state is guarded by one mutex.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "armsparse_drivers.h"
+
+namespace {
+
+struct State {
+    std::mutex mu;
+    as_ctx *ctx = nullptr;
+    cudaStream_t stream = nullptr;
+    void *buf = nullptr;
+    size_t cap = 0;
+    as_status last = AS_OK;
+};
+
+State &state() {
+    static State s;
+    return s;
+}
+
+as_status report(State &s, as_status st, const char *fn) {
+    s.last = st;
+    if (st != AS_OK) fprintf(stderr, "armsparse %s: %s: %s\n", fn, as_status_string(st), as_last_error());
+    return st;
+}
+
+// Lazily creates the context/stream on the current device and grows the device arena.
+as_status prepare(State &s, size_t bytes, char **base) {
+    if (!s.ctx) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        as_status st = as_ctx_create(&s.ctx, dev);
+        if (st != AS_OK) return st;
+        if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess)
+            return AS_ERR_CUDA;
+    }
+    if (bytes > s.cap) {
+        if (s.buf) cudaFree(s.buf);
+        s.buf = nullptr;
+        s.cap = 0;
+        if (cudaMalloc(&s.buf, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return AS_ERR_ALLOC;
+        }
+        s.cap = bytes;
+    }
+    *base = static_cast<char *>(s.buf);
+    return AS_OK;
+}
+
+size_t al(size_t b) { return (b + 255) & ~size_t(255); }
+
+struct Arena {
+    char *p;
+    template <typename T>
+    T *take(size_t n) {
+        T *q = reinterpret_cast<T *>(p);
+        p += al(n * sizeof(T));
+        return q;
+    }
+};
+
+as_status h2d(State &s, void *d, const void *h, size_t bytes) {
+    if (bytes == 0) return AS_OK;
+    return cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s.stream) == cudaSuccess ? AS_OK
+                                                                                           : AS_ERR_CUDA;
+}
+
+as_status finish(State &s, void *h, const void *d, size_t bytes) {
+    if (bytes && cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, s.stream) != cudaSuccess)
+        return AS_ERR_CUDA;
+    if (cudaStreamSynchronize(s.stream) != cudaSuccess) return AS_ERR_CUDA;
+    return as_ctx_sync_status(s.ctx, s.stream);
+}
+
+as_status spmm_host(const int *rowPtr, const int *colInd, const float *val, const float *B,
+                    float *C, int M, int K, int N, float beta) {
+    State &s = state();
+    if (M < 0 || K < 0 || N < 0 || !rowPtr) return AS_ERR_INVALID_VALUE;
+    const int nnz = rowPtr[M];
+    if (nnz < 0) return AS_ERR_INVALID_CSR;
+    const size_t bytes = al(sizeof(int) * (M + 1)) + 2 * al(sizeof(int) * nnz) +
+                         al(sizeof(float) * size_t(K) * N) + al(sizeof(float) * size_t(M) * N);
+    char *base = nullptr;
+    as_status st = prepare(s, bytes, &base);
+    if (st != AS_OK) return st;
+    Arena a{base};
+    int *drp = a.take<int>(M + 1);
+    int *dci = a.take<int>(nnz);
+    float *dv = a.take<float>(nnz);
+    float *dB = a.take<float>(size_t(K) * N);
+    float *dC = a.take<float>(size_t(M) * N);
+    if ((st = h2d(s, drp, rowPtr, sizeof(int) * (M + 1))) != AS_OK) return st;
+    if ((st = h2d(s, dci, colInd, sizeof(int) * nnz)) != AS_OK) return st;
+    if ((st = h2d(s, dv, val, sizeof(float) * nnz)) != AS_OK) return st;
+    if ((st = h2d(s, dB, B, sizeof(float) * size_t(K) * N)) != AS_OK) return st;
+    if (beta != 0.0f && (st = h2d(s, dC, C, sizeof(float) * size_t(M) * N)) != AS_OK) return st;
+    st = as_spmm_csr_f32(s.ctx, M, K, N, nnz, drp, dci, dv, dB, N, dC, N, beta, 0, s.stream);
+    if (st != AS_OK) return st;
+    return finish(s, C, dC, sizeof(float) * size_t(M) * N);
+}
+
+}  // namespace
+
+void rowBaseSpmm3(int rowPtr[], int colInd[], float val[], float B[], float C[], int M, int K,
+                  int N, int threads) {
+    (void)threads;
+    State &s = state();
+    std::lock_guard<std::mutex> g(s.mu);
+    report(s, spmm_host(rowPtr, colInd, val, B, C, M, K, N, 1.0f), "rowBaseSpmm3");
+}
+
+void rowBaseSpmm2(int rowPtr[], int colInd[], float val[], float B[], float C[], int M, int K,
+                  int N, int threads) {
+    (void)threads;
+    State &s = state();
+    std::lock_guard<std::mutex> g(s.mu);
+    report(s, spmm_host(rowPtr, colInd, val, B, C, M, K, N, 1.0f), "rowBaseSpmm2");
+}
+
+void origin(int rowPtr[], int colInd[], float val[], float B[], float C[], int M, int K, int N,
+            int threads) {
+    (void)threads;
+    State &s = state();
+    std::lock_guard<std::mutex> g(s.mu);
+    report(s, spmm_host(rowPtr, colInd, val, B, C, M, K, N, 0.0f), "origin");
+}
+
+void csr_spmm_kernel(int A_nrows, int B_ncols, int *A_csrRowPtr, int *A_csrColInd,
+                     float *A_csrVal, float *B_dnVal, float *C_dnVal) {
+    State &s = state();
+    std::lock_guard<std::mutex> g(s.mu);
+    int K = 0;
+    if (A_csrRowPtr && A_nrows > 0) {
+        const int nnz = A_csrRowPtr[A_nrows];
+        for (int e = 0; e < nnz; ++e) K = std::max(K, A_csrColInd[e] + 1);
+    }
+    report(s, spmm_host(A_csrRowPtr, A_csrColInd, A_csrVal, B_dnVal, C_dnVal, A_nrows, K, B_ncols,
+                        1.0f),
+           "csr_spmm_kernel");
+}
+
+void sparse_dense_vector(float *B, float *C, int rowPtr[], int colInd[], float val[], int M,
+                         int threads) {
+    (void)threads;
+    State &s = state();
+    std::lock_guard<std::mutex> g(s.mu);
+    auto run = [&]() -> as_status {
+        if (M < 0 || !rowPtr) return AS_ERR_INVALID_VALUE;
+        const int ns = rowPtr[M];
+        int K = 0;
+        for (int e = 0; e < ns; e += 4) K = std::max(K, colInd[e] + 4);
+        const size_t bytes = al(sizeof(int) * (M + 1)) + 2 * al(sizeof(int) * ns) +
+                             al(sizeof(float) * K) + al(sizeof(float) * M);
+        char *base = nullptr;
+        as_status st = prepare(s, bytes, &base);
+        if (st != AS_OK) return st;
+        Arena a{base};
+        int *drp = a.take<int>(M + 1);
+        int *dci = a.take<int>(ns);
+        float *dv = a.take<float>(ns);
+        float *dx = a.take<float>(K);
+        float *dy = a.take<float>(M);
+        if ((st = h2d(s, drp, rowPtr, sizeof(int) * (M + 1))) != AS_OK) return st;
+        if ((st = h2d(s, dci, colInd, sizeof(int) * ns)) != AS_OK) return st;
+        if ((st = h2d(s, dv, val, sizeof(float) * ns)) != AS_OK) return st;
+        if ((st = h2d(s, dx, B, sizeof(float) * K)) != AS_OK) return st;
+        if ((st = h2d(s, dy, C, sizeof(float) * M)) != AS_OK) return st;
+        st = as_spmv_vcsr4_f32(s.ctx, M, K, ns, drp, dci, dv, dx, dy, 1.0f, s.stream);
+        if (st != AS_OK) return st;
+        return finish(s, C, dy, sizeof(float) * M);
+    };
+    report(s, run(), "sparse_dense_vector");
+}
+
+static as_status transpose_host(int *sm, int *res) {
+    State &s = state();
+    if (!sm || !res) return AS_ERR_INVALID_VALUE;
+    const int M = sm[0], N = sm[1], nnz = sm[2];
+    if (M < 0 || N < 0 || nnz < 0) return AS_ERR_INVALID_VALUE;
+    std::vector<int> rowptr(M + 1, 0), colind(nnz);
+    std::vector<float> val(nnz);
+    int prev_r = -1, prev_c = -1;
+    for (int e = 0; e < nnz; ++e) {
+        const int r = sm[3 * (e + 1)], c = sm[3 * (e + 1) + 1];
+        if (r < 0 || r >= M || c < 0 || c >= N) return AS_ERR_INVALID_CSR;
+        if (r < prev_r || (r == prev_r && c <= prev_c)) return AS_ERR_INVALID_VALUE;  // not row-major
+        prev_r = r;
+        prev_c = c;
+        rowptr[r + 1]++;
+        colind[e] = c;
+        memcpy(&val[e], &sm[3 * (e + 1) + 2], sizeof(float));  // int payload moves bit-exactly
+    }
+    for (int r = 0; r < M; ++r) rowptr[r + 1] += rowptr[r];
+    const size_t bytes = al(sizeof(int) * (M + 1)) + al(sizeof(int) * nnz) + al(sizeof(float) * nnz) +
+                         al(sizeof(int) * (N + 1)) + al(sizeof(int) * nnz) + al(sizeof(float) * nnz);
+    char *base = nullptr;
+    as_status st = prepare(s, bytes, &base);
+    if (st != AS_OK) return st;
+    Arena a{base};
+    int *drp = a.take<int>(M + 1);
+    int *dci = a.take<int>(nnz);
+    float *dv = a.take<float>(nnz);
+    int *dcp = a.take<int>(N + 1);
+    int *dri = a.take<int>(nnz);
+    float *dcv = a.take<float>(nnz);
+    if ((st = h2d(s, drp, rowptr.data(), sizeof(int) * (M + 1))) != AS_OK) return st;
+    if ((st = h2d(s, dci, colind.data(), sizeof(int) * nnz)) != AS_OK) return st;
+    if ((st = h2d(s, dv, val.data(), sizeof(float) * nnz)) != AS_OK) return st;
+    st = as_csr2csc(s.ctx, M, N, nnz, drp, dci, dv, dcp, dri, dcv, s.stream);
+    if (st != AS_OK) return st;
+    std::vector<int> colptr(N + 1), rowind(nnz);
+    std::vector<float> cval(nnz);
+    if (cudaMemcpyAsync(colptr.data(), dcp, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost, s.stream) != cudaSuccess ||
+        cudaMemcpyAsync(rowind.data(), dri, sizeof(int) * nnz, cudaMemcpyDeviceToHost, s.stream) != cudaSuccess)
+        return AS_ERR_CUDA;
+    if ((st = finish(s, cval.data(), dcv, sizeof(float) * nnz)) != AS_OK) return st;
+    res[0] = N;
+    res[1] = M;
+    res[2] = nnz;
+    for (int c = 0; c < N; ++c)
+        for (int p = colptr[c]; p < colptr[c + 1]; ++p) {
+            res[3 * (p + 1)] = c;
+            res[3 * (p + 1) + 1] = rowind[p];
+            memcpy(&res[3 * (p + 1) + 2], &cval[p], sizeof(int));
+        }
+    return AS_OK;
+}
+
+void fast_transpose(int *sm, int *res, std::mutex mtx[]) {
+    (void)mtx;
+    State &s = state();
+    std::lock_guard<std::mutex> g(s.mu);
+    report(s, transpose_host(sm, res), "fast_transpose");
+}
+
+extern "C" {
+void as_drv_rowBaseSpmm3(int *rowPtr, int *colInd, float *val, float *B, float *C, int M, int K,
+                         int N, int threads) {
+    rowBaseSpmm3(rowPtr, colInd, val, B, C, M, K, N, threads);
+}
+void as_drv_origin(int *rowPtr, int *colInd, float *val, float *B, float *C, int M, int K, int N,
+                   int threads) {
+    origin(rowPtr, colInd, val, B, C, M, K, N, threads);
+}
+void as_drv_sparse_dense_vector(float *B, float *C, int *rowPtr, int *colInd, float *val, int M,
+                                int threads) {
+    sparse_dense_vector(B, C, rowPtr, colInd, val, M, threads);
+}
+void as_drv_csr_spmm_kernel(int A_nrows, int B_ncols, int *rowptr, int *colind, float *val,
+                            float *B, float *C) {
+    csr_spmm_kernel(A_nrows, B_ncols, rowptr, colind, val, B, C);
+}
+void as_drv_fast_transpose(int *sm, int *res) { fast_transpose(sm, res, nullptr); }
+as_status as_drv_last_status(void) { return state().last; }
+}

@@ -1,0 +1,72 @@
+// Host-side declarations shared between the C-ABI layer (api.cu) and the kernel files.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "armsparse_gpu.h"
+
+struct as_ctx {
+    int device = 0;
+    unsigned *d_status = nullptr;  // device status word (bit flags from common.cuh)
+    void *scratch = nullptr;       // scratch arena
+    size_t scratch_bytes = 0;
+    uint64_t launches = 0;         // kernels this library launched through the context
+};
+
+namespace as {
+
+// Records the message for as_last_error() and returns s.
+as_status fail(as_status s, const std::string &msg);
+// Maps a CUDA error (from the last launch or a runtime call) to AS_ERR_CUDA with its text.
+as_status check_cuda(cudaError_t e, const char *what);
+// Scratch arena of at least `bytes` (256-byte aligned); grows by reallocation.
+as_status scratch(as_ctx *ctx, size_t bytes, void **out);
+
+// ---- launchers (return AS_OK or an error; count launches in ctx) ----
+struct SpmmArgs {
+    int M, K, N, nnz;
+    const int *rowptr, *colind;
+    const void *val, *B;
+    long ldb;
+    float *C;
+    long ldc;
+    float beta;
+    unsigned *status;
+};
+as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cudaStream_t s);
+int spmm_variant_count(int dtype);
+const char *spmm_variant_name(int dtype, int variant);
+int spmm_default_variant(int dtype, int M, int K, int N, int nnz, long ldb, long ldc,
+                         const void *B, const void *C);
+
+as_status spmv_csr_launch(as_ctx *ctx, int M, int K, int nnz, const int *rowptr,
+                          const int *colind, const float *val, const float *x, float *y,
+                          float beta, cudaStream_t s);
+as_status spmv_vcsr4_launch(as_ctx *ctx, int M, int K, int nslots, const int *rowptr,
+                            const int *colind, const float *val, const float *x, float *y,
+                            float beta, cudaStream_t s);
+
+as_status sddmm_f32_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
+                           const int *colind, const float *aval, const float *X, long ldx,
+                           const float *Y, long ldy, float *out, cudaStream_t s);
+as_status sddmm_bf16x3_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
+                              const int *colind, const float *aval, const float *X, long ldx,
+                              const float *Y, long ldy, float *out, cudaStream_t s);
+
+// Transpose; `work` is caller-provided scratch of csr2csc_scratch_bytes(nnz, N) bytes.
+size_t csr2csc_scratch_bytes(int nnz, int N, bool with_val);
+as_status csr2csc_launch(as_ctx *ctx, int M, int N, int nnz, const int *rowptr,
+                         const int *colind, const float *val, int *colptr, int *rowind,
+                         float *cscval, void *work, cudaStream_t s);
+
+as_status csr_validate_launch(as_ctx *ctx, int n_rows, int n_cols, int nnz, const int *rowptr,
+                              const int *colind, int require_sorted, unsigned *result,
+                              cudaStream_t s);
+as_status f32_to_bf16_launch(as_ctx *ctx, long n, const float *src, uint16_t *dst,
+                             cudaStream_t s);
+
+}  // namespace as

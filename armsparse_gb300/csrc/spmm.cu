@@ -1,0 +1,356 @@
+// CSR SpMM, C = A*B + beta*C, fp32 or bf16 storage with fp32 accumulation (sm_103a).
+//
+// Row-split family (bit-identical to the reference's rowBaseSpmm3, SDMM.cpp:90-114):
+//   A group of GROUP lanes (1..32, a power of two) owns one row of A and a tile of
+//   GROUP*ELEMS*CPL output columns. Lane g of the group holds CPL vectors of ELEMS
+//   consecutive columns (16/8/4/2-byte loads of B rows: 128-bit when the layout allows).
+//   The group fetches GROUP (colind, val) pairs of its row per step with one coalesced
+//   load and broadcasts them with width-GROUP shuffles; every lane then walks the entries
+//   in CSR order and updates its accumulators with fmaf(b, v, acc). Each output element is
+//   therefore exactly the reference's fused-FMA chain. Blocks are 256 threads; blockIdx.x
+//   runs over row blocks and blockIdx.y over column tiles, so the CTAs resident at any
+//   moment share one column tile of B, which stays in L2.
+//
+// NNZ-split family (skewed rows): fixed-size chunks of nnz, see spmm_nnzsplit below.
+#include <stdio.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace as {
+namespace {
+
+template <typename T, int VB>
+struct Vec;
+template <>
+struct Vec<float, 16> {
+    static constexpr int E = 4;
+    __device__ static void load(const float *p, float *o) {
+        float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+        o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+    }
+};
+template <>
+struct Vec<float, 8> {
+    static constexpr int E = 2;
+    __device__ static void load(const float *p, float *o) {
+        float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+        o[0] = v.x; o[1] = v.y;
+    }
+};
+template <>
+struct Vec<float, 4> {
+    static constexpr int E = 1;
+    __device__ static void load(const float *p, float *o) { o[0] = __ldg(p); }
+};
+template <>
+struct Vec<uint16_t, 16> {
+    static constexpr int E = 8;
+    __device__ static void load(const uint16_t *p, float *o) {
+        uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
+        unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            o[2 * i] = __uint_as_float(w[i] << 16);
+            o[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+        }
+    }
+};
+template <>
+struct Vec<uint16_t, 8> {
+    static constexpr int E = 4;
+    __device__ static void load(const uint16_t *p, float *o) {
+        uint2 v = __ldg(reinterpret_cast<const uint2 *>(p));
+        o[0] = __uint_as_float(v.x << 16); o[1] = __uint_as_float(v.x & 0xffff0000u);
+        o[2] = __uint_as_float(v.y << 16); o[3] = __uint_as_float(v.y & 0xffff0000u);
+    }
+};
+template <>
+struct Vec<uint16_t, 4> {
+    static constexpr int E = 2;
+    __device__ static void load(const uint16_t *p, float *o) {
+        unsigned v = __ldg(reinterpret_cast<const unsigned *>(p));
+        o[0] = __uint_as_float(v << 16); o[1] = __uint_as_float(v & 0xffff0000u);
+    }
+};
+template <>
+struct Vec<uint16_t, 2> {
+    static constexpr int E = 1;
+    __device__ static void load(const uint16_t *p, float *o) {
+        o[0] = bf16_to_f32(__ldg(reinterpret_cast<const unsigned short *>(p)));
+    }
+};
+
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(uint16_t v) { return bf16_to_f32(v); }
+
+template <int E>
+__device__ __forceinline__ void store_c(float *p, const float *v) {
+    if constexpr (E % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < E; i += 4)
+            __stcs(reinterpret_cast<float4 *>(p + i), make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]));
+    } else if constexpr (E == 2) {
+        __stcs(reinterpret_cast<float2 *>(p), make_float2(v[0], v[1]));
+    } else {
+#pragma unroll
+        for (int i = 0; i < E; ++i) __stcs(p + i, v[i]);
+    }
+}
+
+template <int E>
+__device__ __forceinline__ void load_c(const float *p, float *v) {
+    if constexpr (E % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < E; i += 4) {
+            float4 t = *reinterpret_cast<const float4 *>(p + i);
+            v[i] = t.x; v[i + 1] = t.y; v[i + 2] = t.z; v[i + 3] = t.w;
+        }
+    } else if constexpr (E == 2) {
+        float2 t = *reinterpret_cast<const float2 *>(p);
+        v[0] = t.x; v[1] = t.y;
+    } else {
+#pragma unroll
+        for (int i = 0; i < E; ++i) v[i] = p[i];
+    }
+}
+
+constexpr int kThreads = 256;
+
+template <typename T, int VB, int GROUP, int CPL>
+__global__ void __launch_bounds__(kThreads)
+spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
+              const int *__restrict__ colind, const T *__restrict__ val,
+              const T *__restrict__ B, long ldb, float *__restrict__ C, long ldc, float beta,
+              unsigned *status) {
+    using V = Vec<T, VB>;
+    constexpr int E = V::E;
+    constexpr int TILE = GROUP * E * CPL;
+    const int lane = threadIdx.x & 31;
+    const int g = threadIdx.x % GROUP;
+    const unsigned gmask =
+        GROUP == 32 ? 0xffffffffu : (((1u << GROUP) - 1u) << (lane & ~(GROUP - 1)));
+    const long row = static_cast<long>(blockIdx.x) * (kThreads / GROUP) + threadIdx.x / GROUP;
+    if (row >= M) return;  // the whole group leaves together
+    int lo, hi;
+    row_range(rowptr, static_cast<int>(row), nnz, status, lo, hi);
+
+    const int tile0 = blockIdx.y * TILE;
+    float acc[CPL][E];
+    float *crow = C + row * ldc;
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) {
+        const int c = tile0 + (j * GROUP + g) * E;
+        if (beta != 0.0f && c < N) {
+            load_c<E>(crow + c, acc[j]);
+#pragma unroll
+            for (int i = 0; i < E; ++i) acc[j][i] *= beta;
+        } else {
+#pragma unroll
+            for (int i = 0; i < E; ++i) acc[j][i] = 0.0f;
+        }
+    }
+
+    for (int base = lo; base < hi; base += GROUP) {
+        const int e = base + g;
+        int k = -1;
+        float v = 0.0f;
+        if (e < hi) {
+            k = ld_stream(colind + e);
+            v = to_f32(ld_stream(val + e));
+            if (static_cast<unsigned>(k) >= static_cast<unsigned>(K)) {
+                flag(status, kFlagBadColind);
+                k = -1;
+            }
+        }
+        const int cnt = min(GROUP, hi - base);
+        int t = 0;
+        for (; t + 4 <= cnt; t += 4) {
+            int kk[4];
+            float vv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                kk[u] = __shfl_sync(gmask, k, t + u, GROUP);
+                vv[u] = __shfl_sync(gmask, v, t + u, GROUP);
+            }
+            float b[4][CPL][E];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const T *brow = B + static_cast<long>(kk[u] < 0 ? 0 : kk[u]) * ldb;
+#pragma unroll
+                for (int j = 0; j < CPL; ++j) {
+                    const int c = tile0 + (j * GROUP + g) * E;
+                    if (c < N && kk[u] >= 0) {
+                        V::load(brow + c, b[u][j]);
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < E; ++i) b[u][j][i] = 0.0f;
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int j = 0; j < CPL; ++j)
+#pragma unroll
+                    for (int i = 0; i < E; ++i) acc[j][i] = fmaf(b[u][j][i], vv[u], acc[j][i]);
+        }
+        for (; t < cnt; ++t) {
+            const int kk = __shfl_sync(gmask, k, t, GROUP);
+            const float vv = __shfl_sync(gmask, v, t, GROUP);
+            if (kk < 0) continue;
+            const T *brow = B + static_cast<long>(kk) * ldb;
+#pragma unroll
+            for (int j = 0; j < CPL; ++j) {
+                const int c = tile0 + (j * GROUP + g) * E;
+                if (c < N) {
+                    float b[E];
+                    V::load(brow + c, b);
+#pragma unroll
+                    for (int i = 0; i < E; ++i) acc[j][i] = fmaf(b[i], vv, acc[j][i]);
+                }
+            }
+        }
+    }
+
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) {
+        const int c = tile0 + (j * GROUP + g) * E;
+        if (c < N) store_c<E>(crow + c, acc[j]);
+    }
+}
+
+// ---- variant table --------------------------------------------------------------------------
+struct Variant {
+    int vb, group, cpl;
+    const char *name;
+};
+
+#define AS_V(vb, g, c) {vb, g, c, "rowsplit_v" #vb "_g" #g "_c" #c}
+#define AS_VROW(vb) \
+    AS_V(vb, 1, 1), AS_V(vb, 1, 2), AS_V(vb, 1, 4), AS_V(vb, 2, 1), AS_V(vb, 2, 2), \
+    AS_V(vb, 2, 4), AS_V(vb, 4, 1), AS_V(vb, 4, 2), AS_V(vb, 4, 4), AS_V(vb, 8, 1), \
+    AS_V(vb, 8, 2), AS_V(vb, 8, 4), AS_V(vb, 16, 1), AS_V(vb, 16, 2), AS_V(vb, 16, 4), \
+    AS_V(vb, 32, 1), AS_V(vb, 32, 2), AS_V(vb, 32, 4)
+
+const Variant kF32[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4)};
+const Variant kBF16[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_VROW(2)};
+constexpr int kNF32 = sizeof(kF32) / sizeof(kF32[0]);
+constexpr int kNBF16 = sizeof(kBF16) / sizeof(kBF16[0]);
+
+template <typename T, int VB, int G, int CPL>
+void launch_one(const SpmmArgs &a, cudaStream_t s) {
+    constexpr int E = Vec<T, VB>::E;
+    constexpr int TILE = G * E * CPL;
+    dim3 grid(static_cast<unsigned>(ceil_div(a.M, kThreads / G)),
+              static_cast<unsigned>(ceil_div(a.N, TILE)));
+    spmm_rowsplit<T, VB, G, CPL><<<grid, kThreads, 0, s>>>(
+        a.M, a.K, a.N, a.nnz, a.rowptr, a.colind, static_cast<const T *>(a.val),
+        static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, a.status);
+}
+
+template <typename T, int VB, int G>
+bool dispatch_cpl(int cpl, const SpmmArgs &a, cudaStream_t s) {
+    switch (cpl) {
+        case 1: launch_one<T, VB, G, 1>(a, s); return true;
+        case 2: launch_one<T, VB, G, 2>(a, s); return true;
+        case 4: launch_one<T, VB, G, 4>(a, s); return true;
+    }
+    return false;
+}
+
+template <typename T, int VB>
+bool dispatch_group(int g, int cpl, const SpmmArgs &a, cudaStream_t s) {
+    switch (g) {
+        case 1: return dispatch_cpl<T, VB, 1>(cpl, a, s);
+        case 2: return dispatch_cpl<T, VB, 2>(cpl, a, s);
+        case 4: return dispatch_cpl<T, VB, 4>(cpl, a, s);
+        case 8: return dispatch_cpl<T, VB, 8>(cpl, a, s);
+        case 16: return dispatch_cpl<T, VB, 16>(cpl, a, s);
+        case 32: return dispatch_cpl<T, VB, 32>(cpl, a, s);
+    }
+    return false;
+}
+
+bool aligned(const void *p, int bytes) { return reinterpret_cast<uintptr_t>(p) % bytes == 0; }
+
+// Can vector width `vb` bytes serve these arguments?
+bool vb_ok(int dtype, int vb, int N, long ldb, long ldc, const void *B, const void *C) {
+    const int esz = dtype == 0 ? 4 : 2;
+    const int e = vb / esz;
+    if (e < 1) return false;
+    if (N % e || ldb % e || ldc % e) return false;
+    if (!aligned(B, vb)) return false;
+    // C is fp32: its vectors hold e floats
+    if (!aligned(C, 4 * e > 16 ? 16 : 4 * e)) return false;
+    return true;
+}
+
+}  // namespace
+
+int spmm_variant_count(int dtype) { return dtype == 0 ? kNF32 : kNBF16; }
+
+const char *spmm_variant_name(int dtype, int variant) {
+    const int n = spmm_variant_count(dtype);
+    if (variant < 1 || variant > n) return "unknown";
+    return dtype == 0 ? kF32[variant - 1].name : kBF16[variant - 1].name;
+}
+
+static int find_variant(int dtype, int vb, int g, int cpl) {
+    const Variant *t = dtype == 0 ? kF32 : kBF16;
+    const int n = spmm_variant_count(dtype);
+    for (int i = 0; i < n; ++i)
+        if (t[i].vb == vb && t[i].group == g && t[i].cpl == cpl) return i + 1;
+    return 0;
+}
+
+int spmm_default_variant(int dtype, int M, int K, int N, int nnz, long ldb, long ldc,
+                         const void *B, const void *C) {
+    (void)M; (void)K; (void)nnz;
+    const int esz = dtype == 0 ? 4 : 2;
+    // bf16 keeps 8-element (16-byte) loads only while C's matching 32-byte vectors split
+    // into two aligned float4 stores; widest load that divides the layout wins.
+    const int vbs_f32[] = {16, 8, 4};
+    const int vbs_bf16[] = {16, 8, 4, 2};
+    const int *vbs = dtype == 0 ? vbs_f32 : vbs_bf16;
+    const int nvb = dtype == 0 ? 3 : 4;
+    int vb = dtype == 0 ? 4 : 2;
+    for (int i = 0; i < nvb; ++i)
+        if (vb_ok(dtype, vbs[i], N, ldb, ldc, B, C)) { vb = vbs[i]; break; }
+    const int e = vb / esz;
+    const int lanes = static_cast<int>(ceil_div(N, e));
+    int g = 1;
+    while (g < lanes && g < 32) g <<= 1;
+    int cpl = 1;
+    if (lanes > 32) cpl = lanes >= 128 ? 4 : 2;
+    return find_variant(dtype, vb, g, cpl);
+}
+
+as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cudaStream_t s) {
+    const Variant &v = dtype == 0 ? kF32[variant - 1] : kBF16[variant - 1];
+    if (!vb_ok(dtype, v.vb, a.N, a.ldb, a.ldc, a.B, a.C))
+        return fail(AS_ERR_UNSUPPORTED, std::string("spmm: variant ") + v.name +
+                                            " needs N, ldb, ldc and pointer alignment to match its vector width");
+    if (ceil_div(a.N, (v.vb / (dtype == 0 ? 4 : 2)) * v.group * v.cpl) > 65535)
+        return fail(AS_ERR_UNSUPPORTED, "spmm: N too large for this variant's column tile");
+    bool ok = false;
+    if (dtype == 0) {
+        switch (v.vb) {
+            case 16: ok = dispatch_group<float, 16>(v.group, v.cpl, a, s); break;
+            case 8: ok = dispatch_group<float, 8>(v.group, v.cpl, a, s); break;
+            case 4: ok = dispatch_group<float, 4>(v.group, v.cpl, a, s); break;
+        }
+    } else {
+        switch (v.vb) {
+            case 16: ok = dispatch_group<uint16_t, 16>(v.group, v.cpl, a, s); break;
+            case 8: ok = dispatch_group<uint16_t, 8>(v.group, v.cpl, a, s); break;
+            case 4: ok = dispatch_group<uint16_t, 4>(v.group, v.cpl, a, s); break;
+            case 2: ok = dispatch_group<uint16_t, 2>(v.group, v.cpl, a, s); break;
+        }
+    }
+    if (!ok) return fail(AS_ERR_UNSUPPORTED, "spmm: variant not instantiated");
+    ctx->launches++;
+    return check_cuda(cudaGetLastError(), "spmm launch");
+}
+
+}  // namespace as

@@ -1,0 +1,374 @@
+// CSR -> CSC transpose, CSR validation and small conversion kernels (sm_103a).
+//
+// Transpose = stable sort of the CSR entries by column. The CSR order is already
+// row-ascending, so a stable sort by column leaves rows ascending inside every column:
+// exactly the canonical CSC that scipy's tocsc() builds on the reference's GCN path
+// (gcn/pytorch-custom/gcn_custom.py:52), and the order the reference's counting transpose
+// (sparseTranspose.cpp:95-142) gives when its scatter runs in order. The sort is an LSD
+// radix sort over 8-bit digits of the column id, ceil(log2 N / 8) passes, each pass:
+//   1. tile histogram   -- each CTA counts the digits of its tile of kTile entries into
+//                          hist[digit * tiles + tile] (shared-memory atomics on counts:
+//                          the counts, unlike positions, do not depend on ordering);
+//   2. exclusive scan   -- over hist in (digit, tile) order, giving every (digit, tile) its
+//                          first output slot;
+//   3. stable scatter   -- each CTA re-reads its tile in rounds of 256 entries and ranks
+//                          every entry among equal digits that precede it (warp
+//                          __match_any_sync + per-warp counts + a running per-digit count),
+//                          then writes key, row and value to their slots.
+// No position depends on timing, so the output is identical run to run. colptr comes
+// from the sorted keys (first slot of every column). All indices stay inside their
+// buffers for any input; malformed input sets the status word instead of faulting.
+#include "common.cuh"
+#include "internal.h"
+
+namespace as {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kRounds = 16;
+constexpr int kTile = kThreads * kRounds;  // entries per tile
+constexpr int kBins = 256;
+constexpr int kWarps = kThreads / 32;
+
+// ---- exclusive scan of int32 (three phases, no cross-CTA waits) ---------------------------
+constexpr int kScanItems = 8;
+constexpr int kScanChunk = kThreads * kScanItems;  // 2048 per CTA
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *smem_warp, int &total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) smem_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < kWarps ? smem_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < kWarps) smem_warp[lane] = w;  // inclusive warp totals
+    }
+    __syncthreads();
+    total = smem_warp[kWarps - 1];
+    const int before = warp ? smem_warp[warp - 1] : 0;
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void __launch_bounds__(kThreads)
+scan_reduce(const int *__restrict__ in, long n, int *__restrict__ block_sums) {
+    __shared__ int sw[kWarps];
+    const long base = static_cast<long>(blockIdx.x) * kScanChunk;
+    int s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        const long idx = base + static_cast<long>(i) * kThreads + threadIdx.x;
+        if (idx < n) s += in[idx];
+    }
+    int total;
+    block_exclusive_scan(s, sw, total);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// Single CTA: exclusive scan of the block sums in place (any count, chunked).
+__global__ void __launch_bounds__(kThreads) scan_block_sums(int *sums, int nb) {
+    __shared__ int sw[kWarps];
+    int carry = 0;
+    for (int base = 0; base < nb; base += kThreads) {
+        const int idx = base + threadIdx.x;
+        const int v = idx < nb ? sums[idx] : 0;
+        int total;
+        const int ex = block_exclusive_scan(v, sw, total);
+        if (idx < nb) sums[idx] = carry + ex;
+        carry += total;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads)
+scan_downsweep(const int *__restrict__ in, long n, const int *__restrict__ block_sums,
+               int *__restrict__ out) {
+    __shared__ int sw[kWarps];
+    const long base = static_cast<long>(blockIdx.x) * kScanChunk;
+    // blocked layout: thread t owns items [t*kScanItems, (t+1)*kScanItems)
+    int v[kScanItems];
+    int s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        const long idx = base + static_cast<long>(threadIdx.x) * kScanItems + i;
+        v[i] = idx < n ? in[idx] : 0;
+        s += v[i];
+    }
+    int total;
+    int run = block_exclusive_scan(s, sw, total) + block_sums[blockIdx.x];
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        const long idx = base + static_cast<long>(threadIdx.x) * kScanItems + i;
+        if (idx < n) out[idx] = run;
+        run += v[i];
+    }
+}
+
+// ---- transpose kernels -----------------------------------------------------------------
+// rowidx[e] = row of entry e (one warp per row); malformed rows flag and write nothing.
+__global__ void __launch_bounds__(kThreads)
+expand_rows(int M, int nnz, const int *__restrict__ rowptr, int *__restrict__ rowidx,
+            unsigned *status) {
+    const long warp = (static_cast<long>(blockIdx.x) * kThreads + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= M) return;
+    int lo, hi;
+    row_range(rowptr, static_cast<int>(warp), nnz, status, lo, hi);
+    for (int e = lo + lane; e < hi; e += 32) rowidx[e] = static_cast<int>(warp);
+}
+
+__global__ void __launch_bounds__(kThreads)
+check_rowptr_ends(int M, int nnz, const int *__restrict__ rowptr, int *__restrict__ rowidx,
+                  unsigned *status) {
+    // rowptr[0] must be 0 and rowptr[M] == nnz; otherwise some rowidx slots would be stale:
+    // zero them so the sort reads defined data, and flag.
+    const int first = __ldg(rowptr), last = __ldg(rowptr + M);
+    if (first != 0 || last != nnz) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) flag(status, kFlagBadRowptr);
+        for (long e = static_cast<long>(blockIdx.x) * kThreads + threadIdx.x; e < nnz;
+             e += static_cast<long>(gridDim.x) * kThreads)
+            rowidx[e] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads)
+radix_histogram(const int *__restrict__ keys, int nnz, int shift, int tiles, int N,
+                int *__restrict__ hist, unsigned *status, int check_range) {
+    __shared__ int h[kBins];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const long base = static_cast<long>(blockIdx.x) * kTile;
+    for (int i = 0; i < kRounds; ++i) {
+        const long idx = base + static_cast<long>(i) * kThreads + threadIdx.x;
+        if (idx < nnz) {
+            const int k = keys[idx];
+            if (check_range && static_cast<unsigned>(k) >= static_cast<unsigned>(N))
+                flag(status, kFlagBadColind);
+            atomicAdd(&h[(static_cast<unsigned>(k) >> shift) & (kBins - 1)], 1);
+        }
+    }
+    __syncthreads();
+    hist[static_cast<long>(threadIdx.x) * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kThreads)
+radix_scatter(const int *__restrict__ keys, const int *__restrict__ rows,
+              const float *__restrict__ vals, int nnz, int shift, int tiles,
+              const int *__restrict__ offsets, int *__restrict__ okeys, int *__restrict__ orows,
+              float *__restrict__ ovals) {
+    __shared__ int run[kBins];            // running count per digit inside this tile
+    __shared__ int wcnt[kWarps][kBins];   // per-warp counts of the current round
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    run[threadIdx.x] = offsets[static_cast<long>(threadIdx.x) * tiles + blockIdx.x];
+    const long base = static_cast<long>(blockIdx.x) * kTile;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    for (int i = 0; i < kRounds; ++i) {
+        const long idx = base + static_cast<long>(i) * kThreads + threadIdx.x;
+        const bool valid = idx < nnz;
+        int k = 0, r = 0;
+        float v = 0.0f;
+        if (valid) {
+            k = keys[idx];
+            r = rows[idx];
+            if (vals) v = vals[idx];
+        }
+        const int d = valid ? static_cast<int>((static_cast<unsigned>(k) >> shift) & (kBins - 1))
+                            : kBins;  // invalid lanes get a digit of their own
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) wcnt[w][threadIdx.x] = 0;
+        __syncthreads();
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int rank = __popc(peers & lt_mask);
+        if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        {   // per digit: exclusive prefix over warps, then advance the running count
+            const int dd = threadIdx.x;
+            int acc = run[dd];
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) {
+                const int c = wcnt[w][dd];
+                wcnt[w][dd] = acc;
+                acc += c;
+            }
+            run[dd] = acc;
+        }
+        __syncthreads();
+        if (valid) {
+            const int pos = wcnt[warp][d] + rank;
+            okeys[pos] = k;
+            orows[pos] = r;
+            if (vals) ovals[pos] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// colptr[c] = first slot whose key >= c, from the sorted keys.
+__global__ void __launch_bounds__(kThreads)
+colptr_from_keys(const int *__restrict__ skeys, int nnz, int N, int *__restrict__ colptr) {
+    const long p = static_cast<long>(blockIdx.x) * kThreads + threadIdx.x;
+    if (p > nnz) return;
+    long kprev = p == 0 ? -1 : skeys[p - 1];
+    long kcur = p == nnz ? N : skeys[p];
+    if (kprev < -1) kprev = -1;
+    if (kcur > N) kcur = N;
+    for (long c = kprev + 1; c <= kcur; ++c) colptr[c] = static_cast<int>(p);
+}
+
+// ---- validation --------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads)
+csr_validate(int n_rows, int n_cols, int nnz, const int *__restrict__ rowptr,
+             const int *__restrict__ colind, int require_sorted, unsigned *result) {
+    const long r = static_cast<long>(blockIdx.x) * kThreads + threadIdx.x;
+    if (r == 0 && (__ldg(rowptr) != 0 || __ldg(rowptr + n_rows) != nnz)) atomicOr(result, 1u);
+    if (r >= n_rows) return;
+    int lo = __ldg(rowptr + r), hi = __ldg(rowptr + r + 1);
+    if (hi < lo || lo < 0 || hi > nnz) {
+        atomicOr(result, 2u);
+        return;
+    }
+    int prev = -1;
+    for (int e = lo; e < hi; ++e) {
+        const int c = __ldg(colind + e);
+        if (static_cast<unsigned>(c) >= static_cast<unsigned>(n_cols)) atomicOr(result, 4u);
+        if (require_sorted && c <= prev) atomicOr(result, 8u);
+        prev = c;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads)
+f32_to_bf16_kernel(long n, const float *__restrict__ src, uint16_t *__restrict__ dst) {
+    for (long i = static_cast<long>(blockIdx.x) * kThreads + threadIdx.x; i < n;
+         i += static_cast<long>(gridDim.x) * kThreads)
+        dst[i] = f32_to_bf16(src[i]);
+}
+
+__global__ void zero_u32(unsigned *p) { *p = 0u; }
+
+int radix_passes(int N) {
+    int bits = 0;
+    while (bits < 31 && (1L << bits) < N) ++bits;
+    return bits <= 8 ? 1 : (bits + 7) / 8;
+}
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+}  // namespace
+
+// Exclusive scan of n ints (in may equal out); `work` holds ceil(n / 2048) ints.
+static as_status exclusive_scan(as_ctx *ctx, const int *in, int *out, long n, int *work,
+                                cudaStream_t s) {
+    const long nb = ceil_div(n, kScanChunk);
+    if (nb == 0) return AS_OK;
+    scan_reduce<<<static_cast<unsigned>(nb), kThreads, 0, s>>>(in, n, work);
+    scan_block_sums<<<1, kThreads, 0, s>>>(work, static_cast<int>(nb));
+    scan_downsweep<<<static_cast<unsigned>(nb), kThreads, 0, s>>>(in, n, work, out);
+    ctx->launches += 3;
+    return check_cuda(cudaGetLastError(), "scan launch");
+}
+
+size_t csr2csc_scratch_bytes(int nnz, int N, bool with_val) {
+    const long tiles = ceil_div(nnz, kTile);
+    const long hist = tiles * kBins;
+    size_t b = 0;
+    b += align256(sizeof(int) * static_cast<size_t>(nnz));        // rowidx
+    b += 2 * align256(sizeof(int) * static_cast<size_t>(nnz));    // keys ping-pong
+    b += align256(sizeof(int) * static_cast<size_t>(nnz));        // rows (intermediate)
+    if (with_val) b += align256(sizeof(float) * static_cast<size_t>(nnz));
+    b += align256(sizeof(int) * static_cast<size_t>(hist));       // histogram / offsets
+    b += align256(sizeof(int) * static_cast<size_t>(ceil_div(hist, kScanChunk) + 1));
+    (void)N;
+    return b;
+}
+
+as_status csr2csc_launch(as_ctx *ctx, int M, int N, int nnz, const int *rowptr,
+                         const int *colind, const float *val, int *colptr, int *rowind,
+                         float *cscval, void *work, cudaStream_t s) {
+    if (nnz == 0) {
+        if (cudaMemsetAsync(colptr, 0, sizeof(int) * (static_cast<size_t>(N) + 1), s) != cudaSuccess)
+            return check_cuda(cudaGetLastError(), "csr2csc memset");
+        return AS_OK;
+    }
+    if (M == 0) return fail(AS_ERR_INVALID_CSR, "csr2csc: nnz > 0 with zero rows");
+    if (N == 0) return fail(AS_ERR_INVALID_CSR, "csr2csc: nnz > 0 with zero columns");
+    const bool wv = val != nullptr;
+    const int tiles = static_cast<int>(ceil_div(nnz, kTile));
+    const long hist_n = static_cast<long>(tiles) * kBins;
+    char *p = static_cast<char *>(work);
+    auto take = [&](size_t bytes) { char *q = p; p += align256(bytes); return q; };
+    int *rowidx = reinterpret_cast<int *>(take(sizeof(int) * static_cast<size_t>(nnz)));
+    int *keysA = reinterpret_cast<int *>(take(sizeof(int) * static_cast<size_t>(nnz)));
+    int *keysB = reinterpret_cast<int *>(take(sizeof(int) * static_cast<size_t>(nnz)));
+    int *rowsT = reinterpret_cast<int *>(take(sizeof(int) * static_cast<size_t>(nnz)));
+    float *valsT = wv ? reinterpret_cast<float *>(take(sizeof(float) * static_cast<size_t>(nnz))) : nullptr;
+    int *hist = reinterpret_cast<int *>(take(sizeof(int) * static_cast<size_t>(hist_n)));
+    int *sums = reinterpret_cast<int *>(take(sizeof(int) * static_cast<size_t>(ceil_div(hist_n, kScanChunk) + 1)));
+
+    const unsigned gw = static_cast<unsigned>(ceil_div(static_cast<long>(M) * 32, kThreads));
+    expand_rows<<<gw, kThreads, 0, s>>>(M, nnz, rowptr, rowidx, ctx->d_status);
+    check_rowptr_ends<<<static_cast<unsigned>(ceil_div(nnz, kThreads) < 4096 ? ceil_div(nnz, kThreads) : 4096),
+                        kThreads, 0, s>>>(M, nnz, rowptr, rowidx, ctx->d_status);
+    ctx->launches += 2;
+
+    // Keys alternate between keysA and keysB. Rows and values of a non-last pass go to
+    // either the scratch buffer or the caller's output (free until the last pass), chosen
+    // backwards from the last pass so that no pass reads and writes the same buffer and
+    // the last pass reads scratch and writes rowind / cscval.
+    const int passes = radix_passes(N);
+    const int *src_k = colind;
+    const int *src_r = rowidx;
+    const float *src_v = val;
+    for (int pass = 0; pass < passes; ++pass) {
+        const bool last = pass == passes - 1;
+        const bool to_scratch = ((passes - 1 - pass) & 1) != 0;
+        int *dk = (pass & 1) ? keysB : keysA;
+        int *dr = (last || !to_scratch) ? rowind : rowsT;
+        float *dv = wv ? ((last || !to_scratch) ? cscval : valsT) : nullptr;
+        const int shift = 8 * pass;
+        radix_histogram<<<tiles, kThreads, 0, s>>>(src_k, nnz, shift, tiles, N, hist,
+                                                   ctx->d_status, pass == 0);
+        ctx->launches++;
+        as_status st = exclusive_scan(ctx, hist, hist, hist_n, sums, s);
+        if (st != AS_OK) return st;
+        radix_scatter<<<tiles, kThreads, 0, s>>>(src_k, src_r, src_v, nnz, shift, tiles, hist,
+                                                 dk, dr, dv);
+        ctx->launches++;
+        src_k = dk;
+        src_r = dr;
+        src_v = dv;
+    }
+    colptr_from_keys<<<static_cast<unsigned>(ceil_div(static_cast<long>(nnz) + 1, kThreads)),
+                       kThreads, 0, s>>>(src_k, nnz, N, colptr);
+    ctx->launches++;
+    return check_cuda(cudaGetLastError(), "csr2csc launch");
+}
+
+as_status csr_validate_launch(as_ctx *ctx, int n_rows, int n_cols, int nnz, const int *rowptr,
+                              const int *colind, int require_sorted, unsigned *result,
+                              cudaStream_t s) {
+    zero_u32<<<1, 1, 0, s>>>(result);
+    csr_validate<<<static_cast<unsigned>(ceil_div(static_cast<long>(n_rows) + 1, kThreads)),
+                   kThreads, 0, s>>>(n_rows, n_cols, nnz, rowptr, colind, require_sorted, result);
+    ctx->launches += 2;
+    return check_cuda(cudaGetLastError(), "csr_validate launch");
+}
+
+as_status f32_to_bf16_launch(as_ctx *ctx, long n, const float *src, uint16_t *dst,
+                             cudaStream_t s) {
+    long blocks = ceil_div(n, kThreads);
+    if (blocks > 152L * 16) blocks = 152L * 16;
+    f32_to_bf16_kernel<<<static_cast<unsigned>(blocks), kThreads, 0, s>>>(n, src, dst);
+    ctx->launches++;
+    return check_cuda(cudaGetLastError(), "f32_to_bf16 launch");
+}
+
+}  // namespace as

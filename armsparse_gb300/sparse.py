@@ -1,0 +1,207 @@
+"""Tensor-level API over the C ABI: CUDA tensors in, CUDA tensors out, on torch's current
+stream. Every function checks dtypes, devices and contiguity and raises on anything else;
+nothing here computes on the CPU.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _native as N
+
+
+def _ptr(t: torch.Tensor | None):
+    return None if t is None else t.data_ptr()
+
+
+def _stream(device: torch.device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def _dev(*ts) -> torch.device:
+    dev = None
+    for t in ts:
+        if t is None:
+            continue
+        if not t.is_cuda:
+            raise ValueError("armsparse_gb300 works on CUDA tensors only (no CPU path)")
+        if dev is None:
+            dev = t.device
+        elif t.device != dev:
+            raise ValueError("all tensors must be on the same device")
+    if dev is None:
+        raise ValueError("no tensor given")
+    return dev
+
+
+def _need(t: torch.Tensor, dtype, name: str, ndim: int | None = None):
+    if t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {t.dtype}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    if ndim is not None and t.dim() != ndim:
+        raise ValueError(f"{name} must have {ndim} dims")
+
+
+def _csr(rowptr, colind):
+    _need(rowptr, torch.int32, "rowptr", 1)
+    _need(colind, torch.int32, "colind", 1)
+    return rowptr.numel() - 1, colind.numel()
+
+
+def validate_csr(rowptr, colind, n_cols: int, require_sorted: bool = False) -> None:
+    """Synchronous device-side CSR check; raises NativeError(AS_ERR_INVALID_CSR) if bad."""
+    dev = _dev(rowptr, colind)
+    M, nnz = _csr(rowptr, colind)
+    ctx = N.context(dev.index)
+    N.check(N.load().as_csr_validate(ctx.handle, M, n_cols, nnz, _ptr(rowptr), _ptr(colind),
+                                     int(require_sorted), _stream(dev)), "as_csr_validate")
+
+
+def sync_status(device=None) -> None:
+    """Wait for the current stream and raise if a kernel saw malformed input since the last
+    check."""
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+    N.context(dev.index).sync_status(_stream(dev))
+
+
+def spmm(rowptr, colind, val, B, C=None, beta: float = 0.0, variant: int = 0):
+    """C = A*B + beta*C with A (M x K) in CSR. fp32 val/B -> fp32 path (bit-identical to the
+    reference's rowBaseSpmm3 for row-split variants); bf16 val/B -> bf16 storage with fp32
+    accumulation. C is fp32 (allocated when None)."""
+    dev = _dev(rowptr, colind, val, B, C)
+    M, nnz = _csr(rowptr, colind)
+    if B.dim() != 2:
+        raise ValueError("B must be 2-D")
+    if B.stride(1) != 1:
+        raise ValueError("B must be row-major with unit column stride")
+    K, Ncols = B.shape
+    ldb = B.stride(0) if K > 1 else Ncols
+    if val.dtype == torch.float32 and B.dtype == torch.float32:
+        fn, dname = N.load().as_spmm_csr_f32, "as_spmm_csr_f32"
+    elif val.dtype == torch.bfloat16 and B.dtype == torch.bfloat16:
+        fn, dname = N.load().as_spmm_csr_bf16, "as_spmm_csr_bf16"
+    else:
+        raise TypeError("val and B must both be float32 or both bfloat16")
+    _need(val, val.dtype, "val", 1)
+    if val.numel() != nnz:
+        raise ValueError("val and colind lengths differ")
+    if C is None:
+        if beta != 0.0:
+            raise ValueError("beta != 0 needs C")
+        C = torch.empty((M, Ncols), dtype=torch.float32, device=dev)
+    else:
+        if C.dtype != torch.float32 or C.dim() != 2 or C.shape != (M, Ncols) or C.stride(1) != 1:
+            raise ValueError("C must be float32 (M, N) row-major")
+    ldc = C.stride(0) if M > 1 else Ncols
+    ctx = N.context(dev.index)
+    N.check(fn(ctx.handle, M, K, Ncols, nnz, _ptr(rowptr), _ptr(colind), _ptr(val), _ptr(B),
+               ldb, _ptr(C), ldc, float(beta), int(variant), _stream(dev)), dname)
+    return C
+
+
+def spmm_variants(dtype: torch.dtype = torch.float32) -> list[str]:
+    d = 0 if dtype == torch.float32 else 1
+    L = N.load()
+    return [L.as_spmm_variant_name(d, i).decode() for i in range(1, L.as_spmm_variant_count(d) + 1)]
+
+
+def spmm_default_variant(B: torch.Tensor, C: torch.Tensor | None, M: int, nnz: int) -> int:
+    d = 0 if B.dtype == torch.float32 else 1
+    K, Ncols = B.shape
+    ldb = B.stride(0)
+    ldc = C.stride(0) if C is not None else Ncols
+    return int(N.load().as_spmm_default_variant(d, M, K, Ncols, nnz, ldb, ldc, _ptr(B),
+                                                _ptr(C) if C is not None else 256))
+
+
+def spmv(rowptr, colind, val, x, y=None, beta: float = 0.0):
+    """y = A*x + beta*y, plain CSR, fp32."""
+    dev = _dev(rowptr, colind, val, x, y)
+    M, nnz = _csr(rowptr, colind)
+    _need(val, torch.float32, "val", 1)
+    _need(x, torch.float32, "x", 1)
+    if y is None:
+        if beta != 0.0:
+            raise ValueError("beta != 0 needs y")
+        y = torch.empty(M, dtype=torch.float32, device=dev)
+    _need(y, torch.float32, "y", 1)
+    ctx = N.context(dev.index)
+    N.check(N.load().as_spmv_csr_f32(ctx.handle, M, x.numel(), nnz, _ptr(rowptr), _ptr(colind),
+                                     _ptr(val), _ptr(x), _ptr(y), float(beta), _stream(dev)),
+            "as_spmv_csr_f32")
+    return y
+
+
+def spmv_vcsr4(vrowptr, vcolind, vval, x, y=None, beta: float = 0.0):
+    """y = A*x + beta*y over the reference's 1x4-blocked layout (SpMV.cpp:15-38)."""
+    dev = _dev(vrowptr, vcolind, vval, x, y)
+    M, nslots = _csr(vrowptr, vcolind)
+    _need(vval, torch.float32, "val", 1)
+    _need(x, torch.float32, "x", 1)
+    if y is None:
+        if beta != 0.0:
+            raise ValueError("beta != 0 needs y")
+        y = torch.empty(M, dtype=torch.float32, device=dev)
+    _need(y, torch.float32, "y", 1)
+    ctx = N.context(dev.index)
+    N.check(N.load().as_spmv_vcsr4_f32(ctx.handle, M, x.numel(), nslots, _ptr(vrowptr),
+                                       _ptr(vcolind), _ptr(vval), _ptr(x), _ptr(y), float(beta),
+                                       _stream(dev)), "as_spmv_vcsr4_f32")
+    return y
+
+
+def sddmm(rowptr, colind, X, Y, aval=None, out=None, tensor_cores: bool = False):
+    """out[e] = aval[e] * <X[row(e)], Y[col(e)]> (aval None -> unscaled, the reference's
+    sddmm_cuda_csr). X: M x K, Y: N x K, fp32. tensor_cores selects the tcgen05 split-bf16
+    path."""
+    dev = _dev(rowptr, colind, X, Y, aval, out)
+    M, nnz = _csr(rowptr, colind)
+    for t, n in ((X, "X"), (Y, "Y")):
+        if t.dtype != torch.float32 or t.dim() != 2 or t.stride(1) != 1:
+            raise ValueError(f"{n} must be float32, 2-D, row-major")
+    if X.shape[0] != M:
+        raise ValueError("X must have one row per pattern row")
+    if X.shape[1] != Y.shape[1]:
+        raise ValueError("X and Y need the same K")
+    if aval is not None:
+        _need(aval, torch.float32, "aval", 1)
+    if out is None:
+        out = torch.empty(nnz, dtype=torch.float32, device=dev)
+    _need(out, torch.float32, "out", 1)
+    K = X.shape[1]
+    ldx = X.stride(0) if M > 1 else K
+    ldy = Y.stride(0) if Y.shape[0] > 1 else K
+    fn = N.load().as_sddmm_csr_bf16x3 if tensor_cores else N.load().as_sddmm_csr_f32
+    ctx = N.context(dev.index)
+    N.check(fn(ctx.handle, M, Y.shape[0], K, nnz, _ptr(rowptr), _ptr(colind), _ptr(aval),
+               _ptr(X), ldx, _ptr(Y), ldy, _ptr(out), _stream(dev)),
+            "as_sddmm_csr_bf16x3" if tensor_cores else "as_sddmm_csr_f32")
+    return out
+
+
+def csr2csc(rowptr, colind, val, n_cols: int):
+    """(colptr, rowind, cscval): rows ascending within each column (bit-exact, deterministic).
+    val may be None for a pattern-only transpose (cscval is then None)."""
+    dev = _dev(rowptr, colind, val)
+    M, nnz = _csr(rowptr, colind)
+    if val is not None:
+        _need(val, torch.float32, "val", 1)
+    colptr = torch.empty(n_cols + 1, dtype=torch.int32, device=dev)
+    rowind = torch.empty(nnz, dtype=torch.int32, device=dev)
+    cscval = torch.empty(nnz, dtype=torch.float32, device=dev) if val is not None else None
+    ctx = N.context(dev.index)
+    N.check(N.load().as_csr2csc(ctx.handle, M, n_cols, nnz, _ptr(rowptr), _ptr(colind), _ptr(val),
+                                _ptr(colptr), _ptr(rowind), _ptr(cscval), _stream(dev)),
+            "as_csr2csc")
+    return colptr, rowind, cscval
+
+
+def to_bf16(x: torch.Tensor) -> torch.Tensor:
+    """fp32 -> bf16 (round to nearest even) with this library's kernel."""
+    dev = _dev(x)
+    _need(x, torch.float32, "x")
+    out = torch.empty(x.shape, dtype=torch.bfloat16, device=dev)
+    ctx = N.context(dev.index)
+    N.check(N.load().as_f32_to_bf16(ctx.handle, x.numel(), _ptr(x), _ptr(out), _stream(dev)),
+            "as_f32_to_bf16")
+    return out

@@ -1,0 +1,131 @@
+/*
+ * armsparse_gpu.h -- C ABI of the GB300 (sm_103a) sparse kernels.
+ *
+ * Every entry point takes plain device pointers and sizes, is asynchronous on the given
+ * stream (a cudaStream_t passed as void*, NULL = legacy default stream) and returns an
+ * as_status. The caller owns every input and output buffer; the library allocates only
+ * scratch memory, which lives in the as_ctx. Nothing here calls exit(), traps or asserts
+ * on the device: malformed CSR arrays are detected on the device, recorded in the
+ * context's status word, and reported by as_ctx_sync_status() (or synchronously by
+ * as_csr_validate()).
+ *
+ * Index arrays are int32, CSR row pointers are zero-based, dense matrices are row-major
+ * with a leading dimension in elements. bf16 data is passed as uint16_t bit patterns.
+ */
+#ifndef ARMSPARSE_GPU_H
+#define ARMSPARSE_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum as_status {
+    AS_OK = 0,
+    AS_ERR_INVALID_VALUE = 1, /* a size, pointer, leading dimension or alignment is wrong  */
+    AS_ERR_INVALID_CSR = 2,   /* rowptr not monotone / out of [0,nnz], colind out of range */
+    AS_ERR_UNSUPPORTED = 3,   /* the requested variant cannot run these arguments          */
+    AS_ERR_CUDA = 4,          /* a CUDA runtime call failed (as_last_error() has the text) */
+    AS_ERR_TIMEOUT = 5,       /* a bounded device-side wait gave up                        */
+    AS_ERR_ALLOC = 6          /* scratch allocation failed                                 */
+} as_status;
+
+typedef struct as_ctx as_ctx;
+
+/* ---- context ---------------------------------------------------------------------------
+ * One context per host thread and device. It owns the device status word and the scratch
+ * arena (grown on demand; growth synchronises the device). */
+as_status as_ctx_create(as_ctx **ctx, int device);
+as_status as_ctx_destroy(as_ctx *ctx);
+/* Waits for `stream`, returns and clears the device status word (AS_OK if no kernel since
+ * the last call found malformed input). */
+as_status as_ctx_sync_status(as_ctx *ctx, void *stream);
+/* Text of the last error raised on this host thread (never NULL). */
+const char *as_last_error(void);
+const char *as_status_string(as_status s);
+/* Number of this library's kernels launched through `ctx` since creation. */
+uint64_t as_ctx_launch_count(const as_ctx *ctx);
+
+/* ---- CSR validation (synchronous) --------------------------------------------------------
+ * rowptr[0] == 0, rowptr non-decreasing, rowptr[n_rows] == nnz, 0 <= colind < n_cols.
+ * With require_sorted != 0 also checks strictly ascending columns within each row. */
+as_status as_csr_validate(as_ctx *ctx, int n_rows, int n_cols, int nnz, const int *rowptr,
+                          const int *colind, int require_sorted, void *stream);
+
+/* ---- SpMM: C = A * B + beta * C ------------------------------------------------------------
+ * A: M x K CSR (rowptr[M+1], colind[nnz], val[nnz]); B: K x N (ldb >= N); C: M x N (ldc >= N).
+ * beta == 0 overwrites C without reading it; beta == 1 accumulates, which is the reference
+ * driver's C += A*B.
+ * variant: 0 = library choice; otherwise an id from as_spmm_variant_*().
+ * Replaces: rowBaseSpmm3 / rowBaseSpmm2 / origin (SDMM.cpp:90, :65, :422), the GCN op's
+ * csr_spmm_kernel (gcn/pytorch-custom/spmm.cpp:49-71) and spmm_cuda
+ * (gcn/pytorch-custom/spmm_kernel.cu:425-458).
+ * Row-split variants are bit-identical to rowBaseSpmm3: every output is one fused
+ * multiply-add chain over the row's entries in CSR order. NNZ-split variants balance
+ * skewed rows and add the partial sums of a split row in a fixed order (deterministic,
+ * not bit-identical). */
+as_status as_spmm_csr_f32(as_ctx *ctx, int M, int K, int N, int nnz, const int *rowptr,
+                          const int *colind, const float *val, const float *B, long ldb,
+                          float *C, long ldc, float beta, int variant, void *stream);
+
+/* Same with A's values and B stored as bf16, products accumulated in fp32, C fp32. */
+as_status as_spmm_csr_bf16(as_ctx *ctx, int M, int K, int N, int nnz, const int *rowptr,
+                           const int *colind, const uint16_t *val, const uint16_t *B,
+                           long ldb, float *C, long ldc, float beta, int variant,
+                           void *stream);
+
+/* Variant table for tuning: ids are 1..count. dtype 0 = f32, 1 = bf16. */
+int as_spmm_variant_count(int dtype);
+const char *as_spmm_variant_name(int dtype, int variant);
+/* The variant the library picks for these arguments (what variant 0 runs). */
+int as_spmm_default_variant(int dtype, int M, int K, int N, int nnz, long ldb, long ldc,
+                            const void *B, const void *C);
+
+/* ---- SpMV: y = A * x + beta * y ------------------------------------------------------------
+ * Plain CSR. Replaces sparse_dense_vector (SpMV.cpp:155-179) for callers holding CSR. */
+as_status as_spmv_csr_f32(as_ctx *ctx, int M, int K, int nnz, const int *rowptr,
+                          const int *colind, const float *val, const float *x, float *y,
+                          float beta, void *stream);
+
+/* The reference's 1x4-blocked layout unchanged (SpMV.cpp:15-38): each stored block is four
+ * consecutive slots whose first colind is the block's first column; nslots = rowptr[M] is a
+ * multiple of 4 and the block's columns must lie in [0, K). Each row's four lane sums are
+ * combined as (s2 + s0) + (s3 + s1), as the reference does (SpMV.cpp:175-176).
+ * Replaces sparse_dense_vector (SpMV.cpp:155). */
+as_status as_spmv_vcsr4_f32(as_ctx *ctx, int M, int K, int nslots, const int *rowptr,
+                            const int *colind, const float *val, const float *x, float *y,
+                            float beta, void *stream);
+
+/* ---- SDDMM: out[e] = s_e * <X[row(e), :], Y[col(e), :]> ---------------------------------------
+ * Pattern: M x N CSR; X: M x K (ldx >= K); Y: N x K (ldy >= K); out: nnz values in CSR
+ * order. s_e = aval[e], or 1 when aval is NULL (exactly the reference's sddmm_cuda_csr,
+ * gcn/pytorch-custom/sddmm.cu:459-483, which never scales).
+ * as_sddmm_csr_f32: FP32 CUDA-core dot products.
+ * as_sddmm_csr_bf16x3: tensor cores (tcgen05), operands split as x = hi + lo in bf16 and
+ * x.y ~ hi.hi + hi.lo + lo.hi accumulated in FP32 (relative error near FP32's). */
+as_status as_sddmm_csr_f32(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
+                           const int *colind, const float *aval, const float *X, long ldx,
+                           const float *Y, long ldy, float *out, void *stream);
+as_status as_sddmm_csr_bf16x3(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
+                              const int *colind, const float *aval, const float *X, long ldx,
+                              const float *Y, long ldy, float *out, void *stream);
+
+/* ---- CSR -> CSC (transpose) ------------------------------------------------------------------
+ * A: M x N CSR. Outputs colptr[N+1], rowind[nnz], cscval[nnz] (val / cscval may be NULL
+ * for a pattern-only transpose). Rows are ascending within every column, so the result is
+ * unique and bit-exact (a stable counting sort by column; deterministic run to run).
+ * Replaces csr2csc_cuda (gcn/pytorch-custom/spmm_kernel.cu:460-476) and the CPU
+ * fast_transpose (sparseTranspose.cpp:95-142). */
+as_status as_csr2csc(as_ctx *ctx, int M, int N, int nnz, const int *rowptr, const int *colind,
+                     const float *val, int *colptr, int *rowind, float *cscval, void *stream);
+
+/* ---- small dense helpers used around the hot path ---------------------------------------- */
+/* dst[i] = bf16(src[i]) (round to nearest even). */
+as_status as_f32_to_bf16(as_ctx *ctx, long n, const float *src, uint16_t *dst, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ARMSPARSE_GPU_H */

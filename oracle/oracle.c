@@ -1,0 +1,229 @@
+/*
+ * CPU oracle for the sparse hot path: a plain-C restatement of the reference's algorithms.
+ *
+ * TEST INFRASTRUCTURE. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg (and its reference arm) may load this library, and only as the checker or as the
+ * timed CPU baseline. The product path (armsparse_gb300) never calls it.
+ *
+ * Pinning: tests/test_oracle_pins.py checks every function here that restates a reference
+ * kernel against the reference's own code compiled from its sources by oracle/Makefile
+ * (target `ref`, x86 build through a scalar NEON shim) and against the committed golden
+ * vectors in tests/golden/ that tests/golden/make_golden.py produced from that build.
+ *
+ * Floating-point rules: this file is compiled with -ffp-contract=off, so every fused
+ * multiply-add below is an explicit fmaf()/fma() and every other expression rounds after
+ * each operation.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ----------------------------------------------------------------------------------------
+ * SpMM, C (+)= A*B with A in CSR and B, C dense row-major.
+ * Restates rowBaseSpmm3 (SDMM.cpp:90-114) with num_vector_neon (SDMM.cpp:449-469): for
+ * each row m and each stored entry idx of that row in CSR order, C[m,:] = fma(B[k,:],
+ * val[idx], C[m,:]). Every output element is therefore one fused-FMA chain over the row's
+ * entries in CSR order, starting from C's initial value (0 when accumulate == 0, which is
+ * what a caller that zeroes C gets from the reference). The reference's scalar tail
+ * (SDMM.cpp:465-467, C[i] = C[i] + A[i]*b) is fused by the compiler when FMA is available
+ * (-ffp-contract=fast on AArch64), so it is a fused step here too.
+ * ------------------------------------------------------------------------------------- */
+void or_spmm_fma_chain_f32(int M, int N, const int *rowptr, const int *colind,
+                           const float *val, const float *B, long ldb, float *C, long ldc,
+                           int accumulate, int threads) {
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int m = 0; m < M; ++m) {
+        float *c = C + (long)m * ldc;
+        if (!accumulate)
+            for (int j = 0; j < N; ++j) c[j] = 0.0f;
+        for (int idx = rowptr[m]; idx < rowptr[m + 1]; ++idx) {
+            const float v = val[idx];
+            const float *b = B + (long)colind[idx] * ldb;
+            for (int j = 0; j < N; ++j) c[j] = fmaf(b[j], v, c[j]);
+        }
+    }
+}
+
+/* SpMM in double precision with the per-output absolute sum sum_k |a_mk * b_kj|, used as
+ * the FP64 oracle and as the scale of the relative-error metric. Inputs are double so that
+ * callers can pass bf16-rounded values exactly. */
+void or_spmm_f64(int M, int N, const int *rowptr, const int *colind, const double *val,
+                 const double *B, long ldb, double *C, double *absC, int threads) {
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int m = 0; m < M; ++m) {
+        double *c = C + (long)m * N;
+        double *a = absC + (long)m * N;
+        for (int j = 0; j < N; ++j) { c[j] = 0.0; a[j] = 0.0; }
+        for (int idx = rowptr[m]; idx < rowptr[m + 1]; ++idx) {
+            const double v = val[idx];
+            const double *b = B + (long)colind[idx] * ldb;
+            for (int j = 0; j < N; ++j) {
+                c[j] += v * b[j];
+                a[j] += fabs(v * b[j]);
+            }
+        }
+    }
+}
+
+/* ----------------------------------------------------------------------------------------
+ * SpMV over the reference's 1x4-blocked "vector-aware CSR" (SpMV.cpp:15-38 builds it,
+ * SpMV.cpp:155-179 consumes it): every stored block is 4 consecutive values whose first
+ * column id is colInd[idx]; lane l of a 4-lane accumulator takes val[idx+l]*x[k+l]
+ * (vmlaq_f32), and the row result is (s2+s0) + (s3+s1), added to y[m].
+ * fused selects whether the lane update is one fused step (what GCC emits for vmlaq_f32
+ * under -ffp-contract=fast) or a multiply then an add.
+ * ------------------------------------------------------------------------------------- */
+void or_spmv_vcsr4_f32(int M, const int *rowptr, const int *colind, const float *val,
+                       const float *x, float *y, int fused, int threads) {
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int m = 0; m < M; ++m) {
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+        for (int idx = rowptr[m]; idx < rowptr[m + 1]; idx += 4) {
+            const int k = colind[idx];
+            if (fused) {
+                s0 = fmaf(val[idx + 0], x[k + 0], s0);
+                s1 = fmaf(val[idx + 1], x[k + 1], s1);
+                s2 = fmaf(val[idx + 2], x[k + 2], s2);
+                s3 = fmaf(val[idx + 3], x[k + 3], s3);
+            } else {
+                float p0 = val[idx + 0] * x[k + 0], p1 = val[idx + 1] * x[k + 1];
+                float p2 = val[idx + 2] * x[k + 2], p3 = val[idx + 3] * x[k + 3];
+                s0 = s0 + p0; s1 = s1 + p1; s2 = s2 + p2; s3 = s3 + p3;
+            }
+        }
+        const float r0 = s2 + s0, r1 = s3 + s1;
+        y[m] = y[m] + (r0 + r1);
+    }
+}
+
+/* Build the 1x4-blocked layout from a CSR matrix with K % 4 == 0: one block per aligned
+ * 4-column group that holds at least one entry, zeros filling the empty lanes, colind of
+ * lane l = 4*group + l (same layout toVectorAwareCSR produces from the dense matrix,
+ * SpMV.cpp:15-38). Returns the number of stored slots (4 * blocks); call with null outputs
+ * to size them. */
+long or_csr_to_vcsr4(int M, const int *rowptr, const int *colind, const float *val,
+                     int *vrowptr, int *vcolind, float *vval) {
+    long size = 0;
+    for (int m = 0; m < M; ++m) {
+        if (vrowptr) vrowptr[m] = (int)size;
+        int idx = rowptr[m];
+        while (idx < rowptr[m + 1]) {
+            const int g = colind[idx] >> 2;
+            if (vcolind) {
+                for (int l = 0; l < 4; ++l) { vcolind[size + l] = 4 * g + l; vval[size + l] = 0.f; }
+            }
+            while (idx < rowptr[m + 1] && (colind[idx] >> 2) == g) {
+                if (vval) vval[size + (colind[idx] & 3)] = val[idx];
+                ++idx;
+            }
+            size += 4;
+        }
+    }
+    if (vrowptr) vrowptr[M] = (int)size;
+    return size;
+}
+
+/* y = A*x in double with the per-row absolute sum. */
+void or_spmv_f64(int M, const int *rowptr, const int *colind, const double *val,
+                 const double *x, double *y, double *absy) {
+    for (int m = 0; m < M; ++m) {
+        double s = 0.0, a = 0.0;
+        for (int idx = rowptr[m]; idx < rowptr[m + 1]; ++idx) {
+            s += val[idx] * x[colind[idx]];
+            a += fabs(val[idx] * x[colind[idx]]);
+        }
+        y[m] = s;
+        absy[m] = a;
+    }
+}
+
+/* ----------------------------------------------------------------------------------------
+ * SDDMM over a CSR pattern: out[e] = (aval ? aval[e] : 1) * <X[row(e),:], Y[col(e),:]>,
+ * X is M x K and Y is N x K, both row-major (the reference's D1 and D2,
+ * gcn/pytorch-custom/sddmm.cu:459-483; the reference never scales, aval == NULL
+ * reproduces it). Output in CSR order.
+ * or_sddmm_csr_f64: double accumulation plus the absolute sum for the error metric.
+ * or_sddmm_csr_f32_lanes: the CPU baseline -- float accumulation in 8 interleaved partial
+ * sums (k mod 8), combined pairwise, so that the compiler can vectorise it the way the
+ * reference vectorises its own dot products (SpMV.cpp:139-154).
+ * ------------------------------------------------------------------------------------- */
+void or_sddmm_csr_f64(int M, int K, const int *rowptr, const int *colind, const double *aval,
+                      const double *X, long ldx, const double *Y, long ldy, double *out,
+                      double *absout, int threads) {
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 16)
+    for (int m = 0; m < M; ++m) {
+        const double *x = X + (long)m * ldx;
+        for (int e = rowptr[m]; e < rowptr[m + 1]; ++e) {
+            const double *y = Y + (long)colind[e] * ldy;
+            double s = 0.0, a = 0.0;
+            for (int k = 0; k < K; ++k) { s += x[k] * y[k]; a += fabs(x[k] * y[k]); }
+            const double sc = aval ? aval[e] : 1.0;
+            out[e] = sc * s;
+            absout[e] = fabs(sc) * a;
+        }
+    }
+}
+
+void or_sddmm_csr_f32_lanes(int M, int K, const int *rowptr, const int *colind,
+                            const float *aval, const float *X, long ldx, const float *Y,
+                            long ldy, float *out, int threads) {
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 16)
+    for (int m = 0; m < M; ++m) {
+        const float *x = X + (long)m * ldx;
+        for (int e = rowptr[m]; e < rowptr[m + 1]; ++e) {
+            const float *y = Y + (long)colind[e] * ldy;
+            float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            int k = 0;
+            for (; k + 8 <= K; k += 8)
+                for (int l = 0; l < 8; ++l) s[l] = fmaf(x[k + l], y[k + l], s[l]);
+            for (; k < K; ++k) s[k & 7] = fmaf(x[k], y[k], s[k & 7]);
+            const float t = ((s[0] + s[4]) + (s[1] + s[5])) + ((s[2] + s[6]) + (s[3] + s[7]));
+            out[e] = aval ? aval[e] * t : t;
+        }
+    }
+}
+
+/* ----------------------------------------------------------------------------------------
+ * CSR -> CSC, stable: within each column the entries keep ascending row order. This is
+ * the ordering scipy's tocsc() gives on the GCN path (gcn/pytorch-custom/gcn_custom.py:52)
+ * and what the reference's counting transpose (sparseTranspose.cpp:95-142: column counts,
+ * prefix, scatter) produces when its scatter loop runs in order. Values move bit-exactly.
+ * ------------------------------------------------------------------------------------- */
+void or_csr2csc(int M, int N, const int *rowptr, const int *colind, const float *val,
+                int *colptr, int *rowind, float *cscval) {
+    int *cursor = (int *)calloc((size_t)N + 1, sizeof(int));
+    for (int c = 0; c <= N; ++c) colptr[c] = 0;
+    for (int e = 0; e < rowptr[M]; ++e) colptr[colind[e] + 1]++;
+    for (int c = 0; c < N; ++c) colptr[c + 1] += colptr[c];
+    for (int c = 0; c < N; ++c) cursor[c] = colptr[c];
+    for (int m = 0; m < M; ++m)
+        for (int e = rowptr[m]; e < rowptr[m + 1]; ++e) {
+            const int p = cursor[colind[e]]++;
+            rowind[p] = m;
+            if (val) cscval[p] = val[e];
+        }
+    free(cursor);
+}
+
+/* Rounding of float to bfloat16 (round to nearest even; NaN kept quiet), returned as the
+ * upper 16 bits. Used to build bf16 inputs and the split-bf16 operands on the CPU side. */
+uint16_t or_f32_to_bf16(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40u);
+    const uint32_t lsb = (u >> 16) & 1u;
+    u += 0x7fffu + lsb;
+    return (uint16_t)(u >> 16);
+}
+
+int or_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

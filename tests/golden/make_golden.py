@@ -1,0 +1,138 @@
+"""Generate the golden vectors in this folder from the reference's own kernels.
+
+Run in a checkout that has the reference sources (REF, default /root/reference):
+
+    python tests/golden/make_golden.py [REF]
+
+It compiles the reference's SDMM.cpp, SpMV.cpp and sparseTranspose.cpp unmodified through
+oracle/Makefile (target ``ref``; on x86_64 a scalar NEON shim stands in for <arm_neon.h>),
+runs them on small seeded inputs and saves inputs and outputs as .npz files:
+
+* spmm_rowbasespmm3.npz -- rowBaseSpmm3 (SDMM.cpp:90-114) from a zeroed C, and after a
+  second call (the driver's accumulate pattern, SDMM.cpp:277-283), plus origin
+  (SDMM.cpp:422-448); A built by the reference's toCSR (SDMM.cpp:355-370) from a dense
+  matrix;
+* spmv_vcsr4.npz -- toVectorAwareCSR (SpMV.cpp:15-38) and sparse_dense_vector
+  (SpMV.cpp:155-179);
+* transpose_triplets.npz -- convert (sparseTranspose.cpp:71-92) and fast_transpose
+  (sparseTranspose.cpp:95-142) run on one thread (stable order).
+
+The fixtures are small (a few hundred KB in total) and the GPU tests read only them, never
+the reference.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def dense_sparse(rng, rows, cols, density, kind="ref_int"):
+    d = np.zeros((rows, cols), np.float32)
+    nnz = int(density * rows * cols)
+    pos = rng.choice(rows * cols, nnz, replace=False)
+    if kind == "ref_int":
+        v = ((rng.integers(0, 20000, nnz) - 10000) / 1000.0).astype(np.float32)
+    else:
+        v = rng.uniform(-1, 1, nnz).astype(np.float32)
+    v[v == 0] = 0.5
+    d.flat[pos] = v
+    return d
+
+
+def spmm_cases(ref):
+    cases = [(64, 48, 32, 0.08, 1), (50, 40, 7, 0.2, 2), (33, 33, 3, 0.1, 3),
+             (40, 64, 130, 0.15, 4), (16, 16, 1, 0.3, 5), (8, 7, 6, 0.45, 6)]
+    out = {}
+    for i, (M, K, N, dens, seed) in enumerate(cases):
+        rng = np.random.default_rng(1000 + seed)
+        dense = dense_sparse(rng, M, K, dens)
+        if i == 0:
+            dense[5, :] = 0  # an empty row
+        nnz = int((dense != 0).sum())
+        rowptr = np.zeros(M + 1, np.int32)
+        colind = np.zeros(max(nnz, 1), np.int32)
+        val = np.zeros(max(nnz, 1), np.float32)
+        ref.ref_toCSR(_p(dense), M, K, _p(rowptr), _p(colind), _p(val))
+        B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+        C1 = np.zeros((M, N), np.float32)
+        ref.ref_rowBaseSpmm3(_p(rowptr), _p(colind), _p(val), _p(B), _p(C1), M, K, N, 4)
+        C2 = C1.copy()
+        ref.ref_rowBaseSpmm3(_p(rowptr), _p(colind), _p(val), _p(B), _p(C2), M, K, N, 4)
+        Co = np.zeros((M, N), np.float32)
+        ref.ref_origin(_p(rowptr), _p(colind), _p(val), _p(B), _p(Co), M, K, N, 4)
+        out.update({f"c{i}_shape": np.array([M, K, N], np.int32), f"c{i}_rowptr": rowptr,
+                    f"c{i}_colind": colind[:nnz], f"c{i}_val": val[:nnz], f"c{i}_B": B,
+                    f"c{i}_C": C1, f"c{i}_C_twice": C2, f"c{i}_C_origin": Co})
+    out["n_cases"] = np.array(len(cases), np.int32)
+    np.savez_compressed(os.path.join(HERE, "spmm_rowbasespmm3.npz"), **out)
+
+
+def spmv_cases(ref):
+    cases = [(37, 64, 0.1, 11), (64, 128, 0.03, 12), (5, 8, 0.5, 13)]
+    out = {}
+    for i, (M, K, dens, seed) in enumerate(cases):
+        rng = np.random.default_rng(2000 + seed)
+        dense = dense_sparse(rng, M, K, dens, kind="u11")
+        cap = 4 * M * K
+        rowptr = np.zeros(M + 1, np.int32)
+        colind = np.zeros(cap, np.int32)
+        val = np.zeros(cap, np.float32)
+        ref.ref_toVectorAwareCSR(_p(dense), M, K, _p(rowptr), _p(colind), _p(val))
+        n = int(rowptr[M])
+        x = rng.uniform(-1, 1, K).astype(np.float32)
+        y = np.zeros(M, np.float32)
+        ref.ref_sparse_dense_vector(_p(x), _p(y), _p(rowptr), _p(colind), _p(val), M, 1)
+        # the same matrix in plain CSR, for the layout converter
+        rows, cols = np.nonzero(dense)
+        crow = np.zeros(M + 1, np.int32)
+        np.cumsum(np.bincount(rows, minlength=M), out=crow[1:])
+        out.update({f"c{i}_shape": np.array([M, K], np.int32), f"c{i}_vrowptr": rowptr,
+                    f"c{i}_vcolind": colind[:n], f"c{i}_vval": val[:n], f"c{i}_x": x,
+                    f"c{i}_y": y, f"c{i}_rowptr": crow, f"c{i}_colind": cols.astype(np.int32),
+                    f"c{i}_val": dense[rows, cols].astype(np.float32)})
+    out["n_cases"] = np.array(len(cases), np.int32)
+    np.savez_compressed(os.path.join(HERE, "spmv_vcsr4.npz"), **out)
+
+
+def transpose_cases(ref):
+    cases = [(30, 20, 0.1, 21), (7, 40, 0.3, 22), (64, 64, 0.05, 23)]
+    out = {}
+    for i, (M, N, dens, seed) in enumerate(cases):
+        rng = np.random.default_rng(3000 + seed)
+        A = np.zeros((M, N), np.int32)
+        nnz = int(dens * M * N)
+        A.flat[rng.choice(M * N, nnz, replace=False)] = rng.integers(1, 100, nnz)
+        sm = np.zeros(((nnz + 1) * 3,), np.int32)
+        ref.ref_convert(_p(A), _p(sm), M, N)
+        res = np.zeros_like(sm)
+        ref.ref_fast_transpose(_p(sm), _p(res), 1)
+        out.update({f"c{i}_dense": A, f"c{i}_triplets": sm, f"c{i}_transposed": res})
+    out["n_cases"] = np.array(len(cases), np.int32)
+    np.savez_compressed(os.path.join(HERE, "transpose_triplets.npz"), **out)
+
+
+def main():
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if not O.build_ref(ref_dir):
+        raise SystemExit("could not build the reference kernels from " + ref_dir)
+    spmm_cases(O.ref_lib("sdmm"))
+    spmv_cases(O.ref_lib("spmv"))
+    transpose_cases(O.ref_lib("transpose"))
+    print("golden vectors written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

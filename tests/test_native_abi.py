@@ -1,0 +1,100 @@
+"""The C-ABI library loads and exports every entry point include/*.h declares; host-side
+argument checks work without a GPU (no compute calls here)."""
+import ctypes
+import os
+import re
+
+import pytest
+import torch
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols(header="armsparse_gpu.h"):
+    syms = set()
+    inc = os.path.join(ROOT, "include")
+    for name in [header]:
+        text = open(os.path.join(inc, name)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(as_[A-Za-z0-9_]+)\s*\(", text):
+            syms.add(m.group(1))
+    return sorted(syms)
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ["as_spmm_csr_f32", "as_spmm_csr_bf16", "as_spmv_csr_f32", "as_spmv_vcsr4_f32",
+              "as_sddmm_csr_f32", "as_sddmm_csr_bf16x3", "as_csr2csc", "as_ctx_create"]:
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    missing = [s for s in declared_symbols() if not hasattr(native_lib, s)]
+    assert not missing, missing
+
+
+def test_every_header_is_checked():
+    assert sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h")) == \
+        ["armsparse_drivers.h", "armsparse_gpu.h"]
+
+
+def test_drivers_library_exports_reference_signatures():
+    from armsparse_gb300 import build
+    lib = ctypes.CDLL(build.build_drivers())
+    missing = [s for s in declared_symbols("armsparse_drivers.h") if not hasattr(lib, s)]
+    assert not missing, missing
+    # the C++ entry points keep the reference's exact (mangled) signatures
+    out = os.popen("nm -D --defined-only " + build.os.path.join(build.PKG, build.DRIVERS_NAME)).read()
+    for mangled in ["_Z12rowBaseSpmm3PiS_PfS0_S0_iiii", "_Z12rowBaseSpmm2PiS_PfS0_S0_iiii",
+                    "_Z6originPiS_PfS0_S0_iiii", "_Z19sparse_dense_vectorPfS_PiS0_S_ii",
+                    "_Z15csr_spmm_kerneliiPiS_PfS0_S0_", "_Z14fast_transposePiS_PSt5mutex"]:
+        assert mangled in out, mangled
+
+
+def test_binding_covers_every_declared_symbol():
+    from armsparse_gb300 import _native
+    assert set(declared_symbols()) <= set(_native.SIGNATURES)
+
+
+def test_null_context_is_rejected_on_the_host(native_lib):
+    from armsparse_gb300 import _native as N
+    st = native_lib.as_spmm_csr_f32(None, 4, 4, 4, 0, None, None, None, None, 4, None, 4,
+                                    0.0, 0, None)
+    assert st == 1  # AS_ERR_INVALID_VALUE
+    assert b"ctx is NULL" in native_lib.as_last_error()
+    assert native_lib.as_status_string(2) == b"AS_ERR_INVALID_CSR"
+    for name in ["as_spmv_csr_f32", "as_spmv_vcsr4_f32"]:
+        assert getattr(native_lib, name)(None, 1, 1, 0, None, None, None, None, None, 0.0,
+                                         None) == 1
+    assert native_lib.as_csr2csc(None, 1, 1, 0, None, None, None, None, None, None, None) == 1
+
+
+def test_variant_table(native_lib):
+    n32, n16 = native_lib.as_spmm_variant_count(0), native_lib.as_spmm_variant_count(1)
+    assert n32 >= 54 and n16 >= 72
+    names = [native_lib.as_spmm_variant_name(0, i).decode() for i in range(1, n32 + 1)]
+    assert len(set(names)) == n32
+    assert native_lib.as_spmm_variant_name(0, 0) == b"unknown"
+    # the default pick for the 4096-wide fp32 case uses 128-bit loads and full warps
+    v = native_lib.as_spmm_default_variant(0, 4096, 4096, 4096, 167772, 4096, 4096, 256, 256)
+    assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v16_g32_c4"
+    v = native_lib.as_spmm_default_variant(0, 100, 100, 3, 500, 3, 3, 256, 256)
+    assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v4_g4_c1"
+
+
+@pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU error path")
+def test_context_creation_fails_loudly_without_gpu(native_lib):
+    from armsparse_gb300 import _native as N
+    with pytest.raises(N.NativeError):
+        N.Context(0)
+
+
+def test_ops_refuse_cpu_tensors(native_lib):
+    import armsparse_gb300 as A
+    rp = torch.tensor([0, 1], dtype=torch.int32)
+    ci = torch.tensor([0], dtype=torch.int32)
+    v = torch.ones(1)
+    with pytest.raises(ValueError, match="CUDA"):
+        A.spmm(rp, ci, v, torch.ones(1, 4))
+    with pytest.raises(ValueError, match="CUDA"):
+        A.csr2csc(rp, ci, v, 1)

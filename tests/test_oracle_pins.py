@@ -1,0 +1,142 @@
+"""The CPU oracle against the reference: golden vectors made from the reference's own
+kernels (always), and the reference compiled here from its sources (when present)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from armsparse_gb300 import synthetic as S
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def test_spmm_chain_matches_rowbasespmm3_golden(oracle, golden):
+    g = golden["spmm_rowbasespmm3"]
+    for i in range(int(g["n_cases"])):
+        M, K, N = g[f"c{i}_shape"]
+        rp, ci, v, B = g[f"c{i}_rowptr"], g[f"c{i}_colind"], g[f"c{i}_val"], g[f"c{i}_B"]
+        C = oracle.spmm_fma_chain_f32(rp, ci, v, B, threads=2)
+        assert np.array_equal(C.view(np.uint32), g[f"c{i}_C"].view(np.uint32)), i
+        C2 = oracle.spmm_fma_chain_f32(rp, ci, v, B, C=C, threads=2)
+        assert np.array_equal(C2.view(np.uint32), g[f"c{i}_C_twice"].view(np.uint32)), i
+        # origin() (SDMM.cpp:422-448): same terms, its own compiled summation; agrees to
+        # FP32 rounding
+        C64, A64 = oracle.spmm_f64(rp, ci, v, B, threads=1)
+        assert oracle.scaled_err(g[f"c{i}_C_origin"], C64, A64).max() < 1e-5
+
+
+def test_spmm_f64_close_to_golden(oracle, golden):
+    g = golden["spmm_rowbasespmm3"]
+    for i in range(int(g["n_cases"])):
+        rp, ci, v, B = g[f"c{i}_rowptr"], g[f"c{i}_colind"], g[f"c{i}_val"], g[f"c{i}_B"]
+        C64, A64 = oracle.spmm_f64(rp, ci, v, B, threads=1)
+        assert oracle.scaled_err(g[f"c{i}_C"], C64, A64).max() < 1e-5
+
+
+def test_vcsr4_layout_and_spmv_golden(oracle, golden):
+    g = golden["spmv_vcsr4"]
+    for i in range(int(g["n_cases"])):
+        vr, vc, vv = oracle.csr_to_vcsr4(g[f"c{i}_rowptr"], g[f"c{i}_colind"], g[f"c{i}_val"])
+        assert np.array_equal(vr, g[f"c{i}_vrowptr"])
+        assert np.array_equal(vc, g[f"c{i}_vcolind"])
+        assert np.array_equal(vv.view(np.uint32), g[f"c{i}_vval"].view(np.uint32))
+        y = oracle.spmv_vcsr4_f32(vr, vc, vv, g[f"c{i}_x"], fused=True, threads=1)
+        # the reference build here fuses vmlaq_f32 (-ffp-contract=fast with FMA available)
+        assert np.array_equal(y.view(np.uint32), g[f"c{i}_y"].view(np.uint32)), i
+
+
+def test_csr2csc_matches_fast_transpose_golden(oracle, golden):
+    g = golden["transpose_triplets"]
+    for i in range(int(g["n_cases"])):
+        dense = g[f"c{i}_dense"]
+        M, N = dense.shape
+        trip = g[f"c{i}_triplets"].reshape(-1, 3)
+        nnz = trip[0, 2]
+        rows, cols, vals = trip[1:nnz + 1, 0], trip[1:nnz + 1, 1], trip[1:nnz + 1, 2]
+        rp = np.zeros(M + 1, np.int32)
+        np.cumsum(np.bincount(rows, minlength=M), out=rp[1:])
+        cp, ri, cv = oracle.csr2csc(rp, cols, vals.astype(np.float32), N)
+        res = g[f"c{i}_transposed"].reshape(-1, 3)
+        assert res[0].tolist() == [N, M, nnz]
+        # transposed triplets: (col, row, value) in column-major order
+        assert np.array_equal(res[1:nnz + 1, 0], np.repeat(np.arange(N), np.diff(cp)))
+        assert np.array_equal(res[1:nnz + 1, 1], ri)
+        assert np.array_equal(res[1:nnz + 1, 2], cv.astype(np.int32))
+
+
+def test_csr2csc_matches_scipy(oracle):
+    sp = pytest.importorskip("scipy.sparse")
+    a = S.powerlaw_csr(500, 2.0, 6.0, seed=3, n_cols=300)
+    cp, ri, cv = oracle.csr2csc(a.rowptr, a.colind, a.val, a.n_cols)
+    m = sp.csr_matrix((a.val, a.colind, a.rowptr), shape=a.shape).tocsc()
+    assert np.array_equal(cp, m.indptr) and np.array_equal(ri, m.indices)
+    assert np.array_equal(cv.view(np.uint32), m.data.astype(np.float32).view(np.uint32))
+
+
+@pytest.mark.parametrize("M,K,N,nnz,seed", [(300, 200, 64, 3000, 0), (100, 80, 7, 900, 1),
+                                             (33, 40, 3, 200, 2), (128, 128, 130, 2000, 3)])
+def test_spmm_chain_against_compiled_reference(oracle, M, K, N, nnz, seed):
+    ref = oracle.ref_lib("sdmm")
+    if ref is None:
+        pytest.skip("reference sources not compiled here")
+    a = S.uniform_csr(M, K, nnz, seed, values="ref_int")
+    B = S.dense_uniform((K, N), seed + 10)
+    mine = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, B, threads=2)
+    C = np.zeros((M, N), np.float32)
+    rp, ci, v, Bc = a.rowptr.copy(), a.colind.copy(), a.val.copy(), B.copy()
+    ref.ref_rowBaseSpmm3(_p(rp), _p(ci), _p(v), _p(Bc), _p(C), M, K, N, 2)
+    assert np.array_equal(mine.view(np.uint32), C.view(np.uint32))
+
+
+def test_spmv_against_compiled_reference(oracle):
+    ref = oracle.ref_lib("spmv")
+    if ref is None:
+        pytest.skip("reference sources not compiled here")
+    a = S.uniform_csr(200, 256, 3000, 5)
+    vr, vc, vv = oracle.csr_to_vcsr4(a.rowptr, a.colind, a.val)
+    x = S.dense_uniform(256, 6)
+    y = np.zeros(200, np.float32)
+    ref.ref_sparse_dense_vector(_p(x.copy()), _p(y), _p(vr.copy()), _p(vc.copy()),
+                                _p(vv.copy()), 200, 2)
+    mine = oracle.spmv_vcsr4_f32(vr, vc, vv, x, fused=True, threads=2)
+    assert np.array_equal(mine.view(np.uint32), y.view(np.uint32))
+
+
+def test_sddmm_oracles_agree(oracle):
+    a = S.uniform_csr(64, 48, 600, 7, values="u0515")
+    X = S.dense_normal((64, 40), 8)
+    Y = S.dense_normal((48, 40), 9)
+    o64, ab = oracle.sddmm_f64(a.rowptr, a.colind, X, Y, aval=a.val)
+    o32 = oracle.sddmm_f32_lanes(a.rowptr, a.colind, X, Y, aval=a.val)
+    assert oracle.scaled_err(o32, o64, ab).max() < 1e-5
+    # against a dense formula
+    rows = np.repeat(np.arange(64), np.diff(a.rowptr))
+    dense = (X.astype(np.float64) @ Y.astype(np.float64).T)[rows, a.colind] * a.val
+    assert np.allclose(o64, dense, rtol=1e-12, atol=1e-12)
+
+
+def test_scaled_err_metric(oracle):
+    ref = np.array([1.0, 0.0, -2.0])
+    ab = np.array([1.0, 4.0, 2.0])
+    e = oracle.scaled_err(ref + np.array([1e-6, 1e-6, 0.0]), ref, ab)
+    assert e[0] == pytest.approx(1e-6) and e[1] == pytest.approx(2.5e-7) and e[2] == 0.0
+
+
+def test_rel_err_metric(oracle):
+    ref = np.array([1.0, 0.0, 1e-9, -2.0])
+    ab = np.array([1.0, 1.0, 1.0, 2.0])
+    got = ref + np.array([1e-6, 1e-7, 1e-7, 0.0])
+    e = oracle.rel_err(got, ref, ab)
+    assert e[0] == pytest.approx(1e-6)
+    assert e[1] == pytest.approx(1e-7 / 2 ** -20)
+    assert e[3] == 0.0
+
+
+def test_bf16_round(oracle):
+    x = np.array([1.0, 1.00390625, 1.005859375, -3.3, 65504.0], np.float32)
+    r = oracle.bf16_round(x)
+    # 1 + 2^-8 is a tie -> even (1.0); 1 + 1.5*2^-8 rounds up to 1 + 2^-7
+    assert r[0] == 1.0 and r[1] == 1.0 and r[2] == np.float32(1.0078125)
+    assert (r.view(np.uint32) & 0xFFFF).max() == 0

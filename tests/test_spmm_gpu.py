@@ -1,0 +1,154 @@
+"""SpMM on the GPU through the C ABI against the oracle (bit-exact for row-split variants,
+the reference's rowBaseSpmm3 per-output FMA chain) and against FP64 (bf16 path)."""
+import numpy as np
+import pytest
+import torch
+
+import armsparse_gb300 as A
+from armsparse_gb300 import _native as N
+from armsparse_gb300 import synthetic as S
+from gpu_util import bits, csr_dev, dev, to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def _variants(dtype):
+    return list(range(1, N.load().as_spmm_variant_count(0 if dtype == torch.float32 else 1) + 1))
+
+
+def _run_all_supported(rp, ci, v, B):
+    outs = {}
+    for var in _variants(B.dtype):
+        try:
+            outs[var] = A.spmm(rp, ci, v, B, variant=var)
+        except N.NativeError as e:
+            assert e.status == 3, e  # AS_ERR_UNSUPPORTED for layouts a vector width cannot serve
+    torch.cuda.synchronize()
+    return outs
+
+
+def test_golden_rowbasespmm3_every_variant(golden):
+    g = golden["spmm_rowbasespmm3"]
+    for i in range(int(g["n_cases"])):
+        rp, ci, v, B = (to_dev(g[f"c{i}_rowptr"]), to_dev(g[f"c{i}_colind"]),
+                        to_dev(g[f"c{i}_val"]), to_dev(g[f"c{i}_B"]))
+        outs = _run_all_supported(rp, ci, v, B)
+        assert len(outs) >= 18
+        for var, C in outs.items():
+            assert np.array_equal(bits(C), bits(g[f"c{i}_C"])), (i, A.spmm_variants()[var - 1])
+        # the driver's accumulate pattern: a second call with beta = 1
+        C = A.spmm(rp, ci, v, B)
+        A.spmm(rp, ci, v, B, C=C, beta=1.0)
+        assert np.array_equal(bits(C), bits(g[f"c{i}_C_twice"])), i
+    A.sync_status()
+
+
+@pytest.mark.parametrize("M,K,N,nnz,kind", [
+    (1, 1, 1, 1, "u"), (5, 3, 1, 7, "u"), (257, 300, 3, 2000, "u"), (1000, 800, 64, 20000, "u"),
+    (300, 500, 130, 6000, "u"), (64, 4096, 4096, 2600, "u"), (2000, 2000, 47, 0, "p"),
+    (3000, 3000, 256, 0, "p"), (500, 500, 16, 0, "b")])
+def test_bit_exact_against_oracle(oracle, M, K, N, nnz, kind):
+    if kind == "u":
+        a = S.uniform_csr(M, K, nnz, seed=M + N)
+    elif kind == "p":
+        a = S.powerlaw_csr(M, 2.0, 20.0, seed=N, n_cols=K)
+    else:
+        a = S.banded_csr(M, 33, seed=3)
+    B = S.dense_uniform((a.n_cols, N), seed=7)
+    ref = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, B)
+    rp, ci, v = csr_dev(a)
+    C = A.spmm(rp, ci, v, to_dev(B))
+    assert np.array_equal(bits(C), bits(ref))
+    A.sync_status()
+
+
+def test_full_size_4096_density_001(oracle):
+    """The SpMM driver's shape at full size: 4096^3, 167,772 entries: bit-exact."""
+    a = S.spmm_4096_d001(seed=0)
+    B = S.dense_uniform((4096, 4096), seed=1)
+    ref = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, B)
+    rp, ci, v = csr_dev(a)
+    Bd = to_dev(B)
+    C = A.spmm(rp, ci, v, Bd)
+    assert np.array_equal(bits(C), bits(ref))
+    # run to run identical, and accumulate == reference accumulate
+    C2 = A.spmm(rp, ci, v, Bd)
+    assert torch.equal(C, C2)
+    A.spmm(rp, ci, v, Bd, C=C2, beta=1.0)
+    ref2 = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, B, C=ref)
+    assert np.array_equal(bits(C2), bits(ref2))
+    A.sync_status()
+
+
+def test_strided_b_and_c(oracle):
+    a = S.uniform_csr(300, 200, 3000, seed=4)
+    Bw = S.dense_uniform((200, 96), seed=5)
+    ref = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, np.ascontiguousarray(Bw[:, :64]))
+    rp, ci, v = csr_dev(a)
+    Bd = to_dev(Bw)[:, :64]
+    Cw = torch.zeros((300, 80), device=dev())
+    C = Cw[:, 8:72]
+    A.spmm(rp, ci, v, Bd, C=C, beta=0.0)
+    assert np.array_equal(bits(C.contiguous()), bits(ref))
+    assert torch.count_nonzero(Cw[:, :8]) == 0
+
+
+def test_edge_cases(oracle):
+    # no entries: C = beta * C
+    rp = torch.zeros(11, dtype=torch.int32, device=dev())
+    ci = torch.zeros(0, dtype=torch.int32, device=dev())
+    v = torch.zeros(0, device=dev())
+    B = torch.randn(6, 8, device=dev())
+    C = A.spmm(rp, ci, v, B)
+    assert torch.count_nonzero(C) == 0
+    C0 = torch.randn(10, 8, device=dev())
+    C1 = C0.clone()
+    A.spmm(rp, ci, v, B, C=C1, beta=0.5)
+    assert torch.equal(C1, C0 * 0.5)
+    # zero rows / zero columns: nothing to do
+    A.spmm(torch.zeros(1, dtype=torch.int32, device=dev()), ci, v, B)
+    A.spmm(rp, ci, v, torch.zeros(6, 0, device=dev()))
+    A.sync_status()
+
+
+def test_malformed_csr_is_flagged_not_faulted():
+    a = S.uniform_csr(100, 50, 500, seed=1)
+    bad = a.colind.copy()
+    bad[17] = 50  # out of range
+    rp, v = to_dev(a.rowptr), to_dev(a.val)
+    B = torch.randn(50, 32, device=dev())
+    A.spmm(rp, to_dev(bad), v, B)
+    with pytest.raises(N.NativeError) as ei:
+        A.sync_status()
+    assert ei.value.status == 2
+    badrp = a.rowptr.copy()
+    badrp[40] = badrp[41] + 5  # not monotone
+    A.spmm(to_dev(badrp), to_dev(a.colind), v, B)
+    with pytest.raises(N.NativeError):
+        A.sync_status()
+    A.sync_status()  # cleared
+    with pytest.raises(N.NativeError):
+        A.validate_csr(to_dev(badrp), to_dev(a.colind), 50)
+    A.validate_csr(rp, to_dev(a.colind), 50, require_sorted=True)
+
+
+@pytest.mark.parametrize("N_", [3, 64, 256, 4096])
+def test_bf16_storage_fp32_accumulate(oracle, N_):
+    M = K = 4096 if N_ == 4096 else 2000
+    a = S.uniform_csr(M, K, int(0.01 * M * K), seed=N_)
+    B = S.dense_uniform((K, N_), seed=2)
+    vb, Bb = oracle.bf16_round(a.val), oracle.bf16_round(B)
+    rp, ci, _ = csr_dev(a)
+    C = A.spmm(rp, ci, to_dev(a.val).to(torch.bfloat16), to_dev(B).to(torch.bfloat16))
+    got = C.cpu().numpy()
+    # against FP64 of the bf16-rounded inputs: only FP32 accumulation error
+    R, Ab = oracle.spmm_f64(a.rowptr, a.colind, vb, Bb)
+    assert oracle.scaled_err(got, R, Ab).max() < 1e-5
+    # against FP64 of the original FP32 inputs: the bf16 storage error
+    R64, A64 = oracle.spmm_f64(a.rowptr, a.colind, a.val, B)
+    assert oracle.scaled_err(got, R64, A64).max() < 1e-2
+    A.sync_status()
+
+
+def test_native_kernels_ran():
+    assert N.total_launches() > 0
