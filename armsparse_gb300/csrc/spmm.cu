@@ -10,8 +10,6 @@
 //   therefore exactly the reference's fused-FMA chain. Blocks are 256 threads; blockIdx.x
 //   runs over row blocks and blockIdx.y over column tiles, so the CTAs resident at any
 //   moment share one column tile of B, which stays in L2.
-//
-// NNZ-split family (skewed rows): fixed-size chunks of nnz, see spmm_nnzsplit below.
 #include <stdio.h>
 
 #include "common.cuh"
@@ -117,7 +115,7 @@ __device__ __forceinline__ void load_c(const float *p, float *v) {
 
 constexpr int kThreads = 256;
 
-template <typename T, int VB, int GROUP, int CPL>
+template <typename T, int VB, int GROUP, int CPL, int U>
 __global__ void __launch_bounds__(kThreads)
 spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
               const int *__restrict__ colind, const T *__restrict__ val,
@@ -165,17 +163,18 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         }
         const int cnt = min(GROUP, hi - base);
         int t = 0;
-        for (; t + 4 <= cnt; t += 4) {
-            int kk[4];
-            float vv[4];
+        // U entries per step: all their B loads are issued before the FMAs, in CSR order
+        for (; t + U <= cnt; t += U) {
+            int kk[U];
+            float vv[U];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < U; ++u) {
                 kk[u] = __shfl_sync(gmask, k, t + u, GROUP);
                 vv[u] = __shfl_sync(gmask, v, t + u, GROUP);
             }
-            float b[4][CPL][E];
+            float b[U][CPL][E];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < U; ++u) {
                 const T *brow = B + static_cast<long>(kk[u] < 0 ? 0 : kk[u]) * ldb;
 #pragma unroll
                 for (int j = 0; j < CPL; ++j) {
@@ -189,7 +188,7 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 }
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
+            for (int u = 0; u < U; ++u)
 #pragma unroll
                 for (int j = 0; j < CPL; ++j)
 #pragma unroll
@@ -222,52 +221,57 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
 
 // ---- variant table --------------------------------------------------------------------------
 struct Variant {
-    int vb, group, cpl;
+    int vb, group, cpl, unroll;
     const char *name;
 };
 
-#define AS_V(vb, g, c) {vb, g, c, "rowsplit_v" #vb "_g" #g "_c" #c}
-#define AS_VROW(vb) \
-    AS_V(vb, 1, 1), AS_V(vb, 1, 2), AS_V(vb, 1, 4), AS_V(vb, 2, 1), AS_V(vb, 2, 2), \
-    AS_V(vb, 2, 4), AS_V(vb, 4, 1), AS_V(vb, 4, 2), AS_V(vb, 4, 4), AS_V(vb, 8, 1), \
-    AS_V(vb, 8, 2), AS_V(vb, 8, 4), AS_V(vb, 16, 1), AS_V(vb, 16, 2), AS_V(vb, 16, 4), \
-    AS_V(vb, 32, 1), AS_V(vb, 32, 2), AS_V(vb, 32, 4)
+#define AS_V(vb, g, c, u) {vb, g, c, u, "rowsplit_v" #vb "_g" #g "_c" #c "_u" #u}
+#define AS_VG(vb, g) AS_V(vb, g, 1, 4), AS_V(vb, g, 2, 4), AS_V(vb, g, 4, 4), AS_V(vb, g, 1, 8), \
+    AS_V(vb, g, 2, 8)
+#define AS_VROW(vb) AS_VG(vb, 1), AS_VG(vb, 2), AS_VG(vb, 4), AS_VG(vb, 8), AS_VG(vb, 16), AS_VG(vb, 32)
 
 const Variant kF32[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4)};
 const Variant kBF16[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_VROW(2)};
 constexpr int kNF32 = sizeof(kF32) / sizeof(kF32[0]);
 constexpr int kNBF16 = sizeof(kBF16) / sizeof(kBF16[0]);
 
-template <typename T, int VB, int G, int CPL>
+template <typename T, int VB, int G, int CPL, int U>
 void launch_one(const SpmmArgs &a, cudaStream_t s) {
     constexpr int E = Vec<T, VB>::E;
     constexpr int TILE = G * E * CPL;
     dim3 grid(static_cast<unsigned>(ceil_div(a.M, kThreads / G)),
               static_cast<unsigned>(ceil_div(a.N, TILE)));
-    spmm_rowsplit<T, VB, G, CPL><<<grid, kThreads, 0, s>>>(
+    spmm_rowsplit<T, VB, G, CPL, U><<<grid, kThreads, 0, s>>>(
         a.M, a.K, a.N, a.nnz, a.rowptr, a.colind, static_cast<const T *>(a.val),
         static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, a.status);
 }
 
 template <typename T, int VB, int G>
-bool dispatch_cpl(int cpl, const SpmmArgs &a, cudaStream_t s) {
-    switch (cpl) {
-        case 1: launch_one<T, VB, G, 1>(a, s); return true;
-        case 2: launch_one<T, VB, G, 2>(a, s); return true;
-        case 4: launch_one<T, VB, G, 4>(a, s); return true;
+bool dispatch_cpl(int cpl, int u, const SpmmArgs &a, cudaStream_t s) {
+    if (u == 4) {
+        switch (cpl) {
+            case 1: launch_one<T, VB, G, 1, 4>(a, s); return true;
+            case 2: launch_one<T, VB, G, 2, 4>(a, s); return true;
+            case 4: launch_one<T, VB, G, 4, 4>(a, s); return true;
+        }
+    } else if (u == 8) {
+        switch (cpl) {
+            case 1: launch_one<T, VB, G, 1, 8>(a, s); return true;
+            case 2: launch_one<T, VB, G, 2, 8>(a, s); return true;
+        }
     }
     return false;
 }
 
 template <typename T, int VB>
-bool dispatch_group(int g, int cpl, const SpmmArgs &a, cudaStream_t s) {
+bool dispatch_group(int g, int cpl, int u, const SpmmArgs &a, cudaStream_t s) {
     switch (g) {
-        case 1: return dispatch_cpl<T, VB, 1>(cpl, a, s);
-        case 2: return dispatch_cpl<T, VB, 2>(cpl, a, s);
-        case 4: return dispatch_cpl<T, VB, 4>(cpl, a, s);
-        case 8: return dispatch_cpl<T, VB, 8>(cpl, a, s);
-        case 16: return dispatch_cpl<T, VB, 16>(cpl, a, s);
-        case 32: return dispatch_cpl<T, VB, 32>(cpl, a, s);
+        case 1: return dispatch_cpl<T, VB, 1>(cpl, u, a, s);
+        case 2: return dispatch_cpl<T, VB, 2>(cpl, u, a, s);
+        case 4: return dispatch_cpl<T, VB, 4>(cpl, u, a, s);
+        case 8: return dispatch_cpl<T, VB, 8>(cpl, u, a, s);
+        case 16: return dispatch_cpl<T, VB, 16>(cpl, u, a, s);
+        case 32: return dispatch_cpl<T, VB, 32>(cpl, u, a, s);
     }
     return false;
 }
@@ -296,11 +300,11 @@ const char *spmm_variant_name(int dtype, int variant) {
     return dtype == 0 ? kF32[variant - 1].name : kBF16[variant - 1].name;
 }
 
-static int find_variant(int dtype, int vb, int g, int cpl) {
+static int find_variant(int dtype, int vb, int g, int cpl, int u) {
     const Variant *t = dtype == 0 ? kF32 : kBF16;
     const int n = spmm_variant_count(dtype);
     for (int i = 0; i < n; ++i)
-        if (t[i].vb == vb && t[i].group == g && t[i].cpl == cpl) return i + 1;
+        if (t[i].vb == vb && t[i].group == g && t[i].cpl == cpl && t[i].unroll == u) return i + 1;
     return 0;
 }
 
@@ -323,7 +327,7 @@ int spmm_default_variant(int dtype, int M, int K, int N, int nnz, long ldb, long
     while (g < lanes && g < 32) g <<= 1;
     int cpl = 1;
     if (lanes > 32) cpl = lanes >= 128 ? 4 : 2;
-    return find_variant(dtype, vb, g, cpl);
+    return find_variant(dtype, vb, g, cpl, 4);
 }
 
 as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cudaStream_t s) {
@@ -336,16 +340,16 @@ as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cu
     bool ok = false;
     if (dtype == 0) {
         switch (v.vb) {
-            case 16: ok = dispatch_group<float, 16>(v.group, v.cpl, a, s); break;
-            case 8: ok = dispatch_group<float, 8>(v.group, v.cpl, a, s); break;
-            case 4: ok = dispatch_group<float, 4>(v.group, v.cpl, a, s); break;
+            case 16: ok = dispatch_group<float, 16>(v.group, v.cpl, v.unroll, a, s); break;
+            case 8: ok = dispatch_group<float, 8>(v.group, v.cpl, v.unroll, a, s); break;
+            case 4: ok = dispatch_group<float, 4>(v.group, v.cpl, v.unroll, a, s); break;
         }
     } else {
         switch (v.vb) {
-            case 16: ok = dispatch_group<uint16_t, 16>(v.group, v.cpl, a, s); break;
-            case 8: ok = dispatch_group<uint16_t, 8>(v.group, v.cpl, a, s); break;
-            case 4: ok = dispatch_group<uint16_t, 4>(v.group, v.cpl, a, s); break;
-            case 2: ok = dispatch_group<uint16_t, 2>(v.group, v.cpl, a, s); break;
+            case 16: ok = dispatch_group<uint16_t, 16>(v.group, v.cpl, v.unroll, a, s); break;
+            case 8: ok = dispatch_group<uint16_t, 8>(v.group, v.cpl, v.unroll, a, s); break;
+            case 4: ok = dispatch_group<uint16_t, 4>(v.group, v.cpl, v.unroll, a, s); break;
+            case 2: ok = dispatch_group<uint16_t, 2>(v.group, v.cpl, v.unroll, a, s); break;
         }
     }
     if (!ok) return fail(AS_ERR_UNSUPPORTED, "spmm: variant not instantiated");

@@ -52,6 +52,7 @@ class SpmmF32:
     dtype = "f32"
     kernel = "spmm_rowsplit"
     profile = "spmm_rowsplit_f32_4096x4096x4096_d001"
+    e2e_api = "libarmsparse_drivers.so origin() (SDMM.cpp:422 signature) with host buffers"
 
     def __init__(self, seed=0):
         from armsparse_gb300 import synthetic as S
@@ -108,7 +109,101 @@ class SpmmF32:
         return 4 * (rows + 1) + 8 * nnz + 4 * self.K * self.N + 4 * rows * self.N
 
 
-WORKLOADS = {c.name: c for c in [SpmmF32]}
+class _Generic:
+    """End to end through the public Python API: pinned host inputs copied in, the op,
+    the output copied back to pinned host memory, all inside the timed region."""
+    bound = "hbm"
+
+    def e2e_setup(self):
+        import torch
+        self.h_in = {k: v.cpu().pin_memory() for k, v in self.inputs().items()}
+        self.h_out = torch.empty(self.output().shape, dtype=self.output().dtype).pin_memory()
+        self.h2d = sum(t.numel() * t.element_size() for t in self.h_in.values())
+        self.d2h = self.h_out.numel() * self.h_out.element_size()
+
+    def e2e_step(self):
+        import torch
+        for k, t in self.h_in.items():
+            self.inputs()[k].copy_(t, non_blocking=True)
+        self.step()
+        self.h_out.copy_(self.output(), non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+
+class SddmmTc(_Generic):
+    name = "sddmm_tc"
+    metric = "SDDMM GB/s (algorithmic bytes), tensor-core split-bf16 path"
+    unit = "GB/s"
+    dtype = "bf16x3 (fp32 in/out, fp32 accumulate)"
+    kernel = "sddmm_tc_kernel"
+    profile = "sddmm_tc_kernel_4096x4096x4096_d01"
+    bound = "tensor"
+    tensor_cores = True
+
+    def __init__(self, seed=0):
+        from armsparse_gb300 import synthetic as S
+        self.M = self.N = self.K = 4096
+        self.a = S.sddmm_4096_d01(seed)
+        self.X = S.dense_normal((self.M, self.K), seed + 1)
+        self.Y = S.dense_normal((self.N, self.K), seed + 2)
+        nnz = self.a.nnz
+        self.bytes = 4 * (self.M + 1) + 4 * nnz + 4 * nnz + 4 * nnz + 4 * self.M * self.K + \
+            4 * self.N * self.K
+        self.flops = 2 * nnz * self.K
+        self.exec_flops = 3 * 2 * self.M * self.N * self.K
+        self.config = {"workload": "sddmm_csr out[e]=val[e]*<X[r],Y[c]>, pattern 4096x4096 "
+                                   "uniform density 0.1 (1,677,721 nnz) val U(0.5,1.5), "
+                                   "X,Y 4096x4096 N(0,1), K=4096",
+                       "M": 4096, "N": 4096, "K": 4096, "nnz": nnz,
+                       "alg_bytes_per_step": self.bytes, "alg_flops_per_step": self.flops,
+                       "path": "tensor cores (tcgen05, split-bf16 x3)" if self.tensor_cores
+                       else "FP32 CUDA cores",
+                       "l2": "flushed between steps (256 MiB write, outside the timed events)"}
+
+    def to_device(self, dev):
+        import torch
+        self.rp = torch.from_numpy(self.a.rowptr).to(dev)
+        self.ci = torch.from_numpy(self.a.colind).to(dev)
+        self.v = torch.from_numpy(self.a.val).to(dev)
+        self.Xd = torch.from_numpy(self.X).to(dev)
+        self.Yd = torch.from_numpy(self.Y).to(dev)
+        self.out = torch.empty(self.a.nnz, device=dev)
+
+    def inputs(self):
+        return {"rp": self.rp, "ci": self.ci, "v": self.v, "X": self.Xd, "Y": self.Yd}
+
+    def output(self):
+        return self.out
+
+    def step(self):
+        import armsparse_gb300 as A
+        A.sddmm(self.rp, self.ci, self.Xd, self.Yd, aval=self.v, out=self.out,
+                tensor_cores=self.tensor_cores)
+
+    def cpu_step(self, threads, rows=None):
+        from oracle import oracle as O
+        a = self.a
+        if rows is None:
+            O.sddmm_f32_lanes(a.rowptr, a.colind, self.X, self.Y, aval=a.val, threads=threads)
+            return self.bytes
+        rp = a.rowptr[: rows + 1]
+        O.sddmm_f32_lanes(rp, a.colind, self.X[:rows], self.Y, aval=a.val, threads=threads)
+        nnz = int(rp[-1])
+        return 4 * (rows + 1) + 12 * nnz + 4 * rows * self.K + 4 * self.N * self.K
+
+
+class SddmmF32(SddmmTc):
+    name = "sddmm_f32"
+    metric = "SDDMM GB/s (algorithmic bytes), FP32 CUDA-core path"
+    dtype = "f32"
+    kernel = "sddmm_f32_lane"
+    profile = "sddmm_f32_lane_4096x4096x4096_d01"
+    bound = "hbm"
+    tensor_cores = False
+
+
+WORKLOADS = {c.name: c for c in [SpmmF32, SddmmTc, SddmmF32]}
+
 
 
 # ------------------------------------------------------------------------------------------
@@ -150,7 +245,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (OSError, ValueError):
             self.proc = None
@@ -313,21 +408,30 @@ def run_ours(args, wl_cls):
         e2e_s = float(t.item())
     e2e_value = ws * wl.bytes / e2e_s / 1e9
 
-    hbm, _, src = measured_peaks()
-    achieved = wl.bytes / (kernel_ms * 1e-3) / 1e9
+    hbm, bf16, src = measured_peaks()
+    if getattr(wl, "bound", "hbm") == "tensor":
+        achieved = wl.flops / (kernel_ms * 1e-3) / 1e12
+        roof = {"bound": "tensor", "achieved": round(achieved, 3), "peak": bf16,
+                "unit": "TFLOP/s", "frac": round(achieved / bf16, 5),
+                "traffic": profiled_traffic(wl.profile), "peak_source": src, "kernel": wl.kernel,
+                "achieved_is": "algorithmic (sampled) flops 2*nnz*K per step",
+                "executed_tflops": round(wl.exec_flops / (kernel_ms * 1e-3) / 1e12, 2),
+                "executed_frac": round(wl.exec_flops / (kernel_ms * 1e-3) / 1e12 / bf16, 4)}
+    else:
+        achieved = wl.bytes / (kernel_ms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "traffic": profiled_traffic(wl.profile),
+                "peak_source": src, "kernel": wl.kernel}
     line = {
         "metric": wl.metric, "value": round(value, 3), "unit": wl.unit, "n_gpus": ws,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(kernel_ms, 5),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": wl.dtype,
         "data": "synthetic (seeded)", "config": dict(wl.config, parallelism=f"replicas x{ws}"),
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm,
-                     "unit": "GB/s", "frac": round(achieved / hbm, 4),
-                     "traffic": profiled_traffic(wl.profile), "peak_source": src,
-                     "kernel": wl.kernel},
+        "roofline": roof,
         "e2e": {"value": round(e2e_value, 3), "unit": wl.unit,
                 "h2d_bytes_per_step": wl.h2d, "d2h_bytes_per_step": wl.d2h,
                 "ms_per_step": round(e2e_s * 1e3, 3),
-                "api": "libarmsparse_drivers.so origin() with host buffers"},
+                "api": getattr(wl, "e2e_api", "armsparse_gb300 Python API, pinned host buffers")},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "wall_s_timed_region": round(wall, 4),
@@ -344,7 +448,7 @@ def run_ours(args, wl_cls):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="spmm_f32")

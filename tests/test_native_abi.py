@@ -71,15 +71,15 @@ def test_null_context_is_rejected_on_the_host(native_lib):
 
 def test_variant_table(native_lib):
     n32, n16 = native_lib.as_spmm_variant_count(0), native_lib.as_spmm_variant_count(1)
-    assert n32 >= 54 and n16 >= 72
+    assert n32 >= 90 and n16 >= 120
     names = [native_lib.as_spmm_variant_name(0, i).decode() for i in range(1, n32 + 1)]
     assert len(set(names)) == n32
     assert native_lib.as_spmm_variant_name(0, 0) == b"unknown"
     # the default pick for the 4096-wide fp32 case uses 128-bit loads and full warps
     v = native_lib.as_spmm_default_variant(0, 4096, 4096, 4096, 167772, 4096, 4096, 256, 256)
-    assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v16_g32_c4"
+    assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v16_g32_c4_u4"
     v = native_lib.as_spmm_default_variant(0, 100, 100, 3, 500, 3, 3, 256, 256)
-    assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v4_g4_c1"
+    assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v4_g4_c1_u4"
 
 
 @pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU error path")

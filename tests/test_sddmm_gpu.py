@@ -52,3 +52,67 @@ def test_malformed_pattern_is_flagged():
     with pytest.raises(N.NativeError) as ei:
         A.sync_status()
     assert ei.value.status == 2
+
+
+# ---- tensor-core split-bf16 path -----------------------------------------------------------
+# Error budget per product: x = hi + lo + r with |lo| <= 2^-9 |x|, |r| <= 2^-18 |x|; the dropped
+# lo*lo and r terms are <= ~4 * 2^-18 |x y|, plus FP32 accumulation. Bar: scaled error
+# (relative to sum |x_k y_k|) below 3e-5 per output.
+TC_TOL = 3e-5
+
+
+@pytest.mark.parametrize("M,Ncol,K,nnz", [(128, 256, 64, 3000), (300, 500, 100, 15000),
+                                          (1000, 700, 4096, 35000), (129, 257, 8, 4000),
+                                          (64, 32, 1, 300)])
+def test_tc_against_fp64(oracle, M, Ncol, K, nnz):
+    a = S.uniform_csr(M, Ncol, nnz, seed=K + 1, values="u0515")
+    X = S.dense_normal((M, K), 11)
+    Y = S.dense_normal((Ncol, K), 12)
+    rp, ci, av = csr_dev(a)
+    for aval in (None, a.val):
+        out = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=None if aval is None else av,
+                      tensor_cores=True)
+        r64, ab = oracle.sddmm_f64(a.rowptr, a.colind, X, Y, aval=aval)
+        err = oracle.scaled_err(out.cpu().numpy(), r64, ab)
+        assert err.max() < TC_TOL, err.max()
+    A.sync_status()
+
+
+def test_tc_sparse_tiles_and_determinism(oracle):
+    a = S.banded_csr(3000, 16, seed=2, values="u0515")  # most 128x256 tiles are empty
+    X = S.dense_normal((3000, 256), 13)
+    Y = S.dense_normal((3000, 256), 14)
+    rp, ci, av = csr_dev(a)
+    o1 = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=av, tensor_cores=True)
+    o2 = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=av, tensor_cores=True)
+    assert torch.equal(o1, o2)
+    r64, ab = oracle.sddmm_f64(a.rowptr, a.colind, X, Y, aval=a.val)
+    assert oracle.scaled_err(o1.cpu().numpy(), r64, ab).max() < TC_TOL
+    A.sync_status()
+
+
+def test_tc_full_size_4096_density_01(oracle):
+    """The SDDMM workload at full size: 4096 x 4096 pattern, density 0.1, K = 4096."""
+    a = S.sddmm_4096_d01(seed=0)
+    X = S.dense_normal((4096, 4096), 1)
+    Y = S.dense_normal((4096, 4096), 2)
+    rp, ci, av = csr_dev(a)
+    out = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=av, tensor_cores=True)
+    out32 = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=av)
+    r64, ab = oracle.sddmm_f64(a.rowptr, a.colind, X, Y, aval=a.val)
+    e_tc = oracle.scaled_err(out.cpu().numpy(), r64, ab)
+    e_32 = oracle.scaled_err(out32.cpu().numpy(), r64, ab)
+    assert e_tc.max() < TC_TOL and e_32.max() < 1e-5
+    A.sync_status()
+
+
+def test_tc_unsorted_rows_flagged():
+    a = S.uniform_csr(200, 300, 3000, seed=3)
+    bad = a.colind.copy()
+    lo = a.rowptr[10]
+    bad[lo], bad[lo + 1] = bad[lo + 1], bad[lo]
+    A.sddmm(to_dev(a.rowptr), to_dev(bad), torch.randn(200, 64, device=dev()),
+            torch.randn(300, 64, device=dev()), tensor_cores=True)
+    with pytest.raises(N.NativeError) as ei:
+        A.sync_status()
+    assert ei.value.status == 2
