@@ -284,6 +284,23 @@ as_status as_sddmm_csr_bf16x3(as_ctx *c, int M, int N, int K, int nnz, const int
                         ldx, Y, ldy, out, stream);
 }
 
+as_status as_sddmm_coo_f32(as_ctx *c, int M, int N, int K, int nnz, const int *rowind,
+                           const int *colind, const float *aval, const float *X, long ldx,
+                           const float *Y, long ldy, float *out, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_sddmm_coo_f32: ctx is NULL");
+    if (M < 0 || N < 0 || K < 0 || nnz < 0)
+        return fail(AS_ERR_INVALID_VALUE, "as_sddmm_coo_f32: negative size");
+    if (nnz == 0) return AS_OK;
+    if (!rowind || !colind || !out)
+        return fail(AS_ERR_INVALID_VALUE, "as_sddmm_coo_f32: NULL index or output array");
+    if (K > 0 && (!X || !Y)) return fail(AS_ERR_INVALID_VALUE, "as_sddmm_coo_f32: X or Y is NULL");
+    if (ldx < K || ldy < K)
+        return fail(AS_ERR_INVALID_VALUE, "as_sddmm_coo_f32: leading dimension below K");
+    DeviceGuard g(c->device);
+    return sddmm_coo_f32_launch(c, M, N, K, nnz, rowind, colind, aval, X, ldx, Y, ldy, out,
+                                static_cast<cudaStream_t>(stream));
+}
+
 as_status as_csr2csc(as_ctx *c, int M, int N, int nnz, const int *rowptr, const int *colind,
                      const float *val, int *colptr, int *rowind, float *cscval, void *stream) {
     if (!c) return fail(AS_ERR_INVALID_VALUE, "as_csr2csc: ctx is NULL");
@@ -299,6 +316,40 @@ as_status as_csr2csc(as_ctx *c, int M, int N, int nnz, const int *rowptr, const 
     if (st != AS_OK) return st;
     return csr2csc_launch(c, M, N, nnz, rowptr, colind, val, colptr, rowind, cscval, w,
                           static_cast<cudaStream_t>(stream));
+}
+
+as_status as_spmm_csr_f64(as_ctx *c, int M, int K, int N, int nnz, const int *rowptr,
+                          const int *colind, const double *val, const double *B, long ldb,
+                          double *C, long ldc, double beta, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_spmm_csr_f64: ctx is NULL");
+    as_status st = check_csr_args("as_spmm_csr_f64", M, K, nnz, rowptr, colind, val, true);
+    if (st != AS_OK) return st;
+    if (N < 0) return fail(AS_ERR_INVALID_VALUE, "as_spmm_csr_f64: negative N");
+    if (M == 0 || N == 0) return AS_OK;
+    if (!C || (nnz > 0 && K > 0 && !B))
+        return fail(AS_ERR_INVALID_VALUE, "as_spmm_csr_f64: B or C is NULL");
+    if (ldb < N || ldc < N)
+        return fail(AS_ERR_INVALID_VALUE, "as_spmm_csr_f64: leading dimension below N");
+    DeviceGuard g(c->device);
+    return spmm_f64_launch(c, M, K, N, nnz, rowptr, colind, val, B, ldb, C, ldc, beta,
+                           static_cast<cudaStream_t>(stream));
+}
+
+as_status as_sddmm_csr_f64(as_ctx *c, int M, int N, int K, int nnz, const int *rowptr,
+                           const int *colind, const double *aval, const double *X, long ldx,
+                           const double *Y, long ldy, double *out, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_sddmm_csr_f64: ctx is NULL");
+    as_status st = check_csr_args("as_sddmm_csr_f64", M, N, nnz, rowptr, colind, nullptr, false);
+    if (st != AS_OK) return st;
+    if (K < 0) return fail(AS_ERR_INVALID_VALUE, "as_sddmm_csr_f64: negative K");
+    if (nnz == 0) return AS_OK;
+    if (!out || (K > 0 && (!X || !Y)))
+        return fail(AS_ERR_INVALID_VALUE, "as_sddmm_csr_f64: NULL operand");
+    if (ldx < K || ldy < K)
+        return fail(AS_ERR_INVALID_VALUE, "as_sddmm_csr_f64: leading dimension below K");
+    DeviceGuard g(c->device);
+    return sddmm_f64_launch(c, M, N, K, nnz, rowptr, colind, aval, X, ldx, Y, ldy, out,
+                            static_cast<cudaStream_t>(stream));
 }
 
 as_status as_f32_to_bf16(as_ctx *c, long n, const float *src, uint16_t *dst, void *stream) {

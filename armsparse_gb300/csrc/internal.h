@@ -53,9 +53,19 @@ as_status spmv_vcsr4_launch(as_ctx *ctx, int M, int K, int nslots, const int *ro
 as_status sddmm_f32_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
                            const int *colind, const float *aval, const float *X, long ldx,
                            const float *Y, long ldy, float *out, cudaStream_t s);
+as_status sddmm_coo_f32_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowind,
+                               const int *colind, const float *aval, const float *X, long ldx,
+                               const float *Y, long ldy, float *out, cudaStream_t s);
 as_status sddmm_bf16x3_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
                               const int *colind, const float *aval, const float *X, long ldx,
                               const float *Y, long ldy, float *out, cudaStream_t s);
+
+as_status spmm_f64_launch(as_ctx *ctx, int M, int K, int N, int nnz, const int *rowptr,
+                          const int *colind, const double *val, const double *B, long ldb,
+                          double *C, long ldc, double beta, cudaStream_t s);
+as_status sddmm_f64_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
+                           const int *colind, const double *aval, const double *X, long ldx,
+                           const double *Y, long ldy, double *out, cudaStream_t s);
 
 // Transpose; `work` is caller-provided scratch of csr2csc_scratch_bytes(nnz, N) bytes.
 size_t csr2csc_scratch_bytes(int nnz, int N, bool with_val);

@@ -2,7 +2,8 @@
 //
 // One lane per edge, edges in CSR order across the grid. A lane finds its row with one
 // binary search over rowptr (the reference searches per edge as well, findRow in
-// gcn/pytorch-custom/computeUtil.h:11-28) and then streams both operand rows with 32-byte
+// gcn/pytorch-custom/computeUtil.h:11-28), or reads it from the COO row array (the
+// reference's sddmm_cuda_coo, sddmm.cu:427-457), and then streams both operand rows with 32-byte
 // steps (two float4 loads per row per step when K and the leading dimensions are multiples
 // of 8 floats, else scalar). Lanes of a warp mostly share the row, so the X loads
 // broadcast; each lane's Y reads are full 32-byte sectors. Eight interleaved partial sums
@@ -29,20 +30,31 @@ __device__ __forceinline__ int find_row(const int *__restrict__ rowptr, int M, i
     return lo;
 }
 
-template <bool VEC>
+// COO: rows come per entry from `rows` (any order); CSR: `rows` is the row pointer.
+template <bool VEC, bool COO>
 __global__ void __launch_bounds__(kThreads)
-sddmm_f32_lane(int M, int N, int K, int nnz, const int *__restrict__ rowptr,
+sddmm_f32_lane(int M, int N, int K, int nnz, const int *__restrict__ rows,
                const int *__restrict__ colind, const float *__restrict__ aval,
                const float *__restrict__ X, long ldx, const float *__restrict__ Y, long ldy,
                float *__restrict__ out, unsigned *status) {
     const long e = static_cast<long>(blockIdx.x) * kThreads + threadIdx.x;
     if (e >= nnz) return;
-    const int r = find_row(rowptr, M, static_cast<int>(e));
     const int c = ld_stream(colind + e);
-    if (__ldg(rowptr + r) > e || __ldg(rowptr + r + 1) <= e) {
-        flag(status, kFlagBadRowptr);
-        out[e] = 0.0f;
-        return;
+    int r;
+    if (COO) {
+        r = ld_stream(rows + e);
+        if (static_cast<unsigned>(r) >= static_cast<unsigned>(M)) {
+            flag(status, kFlagBadRowptr);
+            out[e] = 0.0f;
+            return;
+        }
+    } else {
+        r = find_row(rows, M, static_cast<int>(e));
+        if (__ldg(rows + r) > e || __ldg(rows + r + 1) <= e) {
+            flag(status, kFlagBadRowptr);
+            out[e] = 0.0f;
+            return;
+        }
     }
     if (static_cast<unsigned>(c) >= static_cast<unsigned>(N)) {
         flag(status, kFlagBadColind);
@@ -72,9 +84,10 @@ sddmm_f32_lane(int M, int N, int K, int nnz, const int *__restrict__ rowptr,
 
 }  // namespace
 
-as_status sddmm_f32_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
-                           const int *colind, const float *aval, const float *X, long ldx,
-                           const float *Y, long ldy, float *out, cudaStream_t s) {
+static as_status sddmm_lane_launch(as_ctx *ctx, bool coo, int M, int N, int K, int nnz,
+                                   const int *rows, const int *colind, const float *aval,
+                                   const float *X, long ldx, const float *Y, long ldy,
+                                   float *out, cudaStream_t s) {
     if (M == 0) {
         // a pattern with entries but no rows is malformed
         return fail(AS_ERR_INVALID_CSR, "sddmm: nnz > 0 with zero rows");
@@ -83,14 +96,24 @@ as_status sddmm_f32_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int 
                      reinterpret_cast<uintptr_t>(X) % 16 == 0 &&
                      reinterpret_cast<uintptr_t>(Y) % 16 == 0;
     const unsigned grid = static_cast<unsigned>(ceil_div(nnz, kThreads));
-    if (vec)
-        sddmm_f32_lane<true><<<grid, kThreads, 0, s>>>(M, N, K, nnz, rowptr, colind, aval, X, ldx,
-                                                      Y, ldy, out, ctx->d_status);
-    else
-        sddmm_f32_lane<false><<<grid, kThreads, 0, s>>>(M, N, K, nnz, rowptr, colind, aval, X,
-                                                       ldx, Y, ldy, out, ctx->d_status);
+    auto k = vec ? (coo ? sddmm_f32_lane<true, true> : sddmm_f32_lane<true, false>)
+                 : (coo ? sddmm_f32_lane<false, true> : sddmm_f32_lane<false, false>);
+    k<<<grid, kThreads, 0, s>>>(M, N, K, nnz, rows, colind, aval, X, ldx, Y, ldy, out,
+                                ctx->d_status);
     ctx->launches++;
     return check_cuda(cudaGetLastError(), "sddmm_f32 launch");
+}
+
+as_status sddmm_f32_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
+                           const int *colind, const float *aval, const float *X, long ldx,
+                           const float *Y, long ldy, float *out, cudaStream_t s) {
+    return sddmm_lane_launch(ctx, false, M, N, K, nnz, rowptr, colind, aval, X, ldx, Y, ldy, out, s);
+}
+
+as_status sddmm_coo_f32_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowind,
+                               const int *colind, const float *aval, const float *X, long ldx,
+                               const float *Y, long ldy, float *out, cudaStream_t s) {
+    return sddmm_lane_launch(ctx, true, M, N, K, nnz, rowind, colind, aval, X, ldx, Y, ldy, out, s);
 }
 
 }  // namespace as

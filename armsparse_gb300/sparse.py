@@ -80,8 +80,10 @@ def spmm(rowptr, colind, val, B, C=None, beta: float = 0.0, variant: int = 0):
         fn, dname = N.load().as_spmm_csr_f32, "as_spmm_csr_f32"
     elif val.dtype == torch.bfloat16 and B.dtype == torch.bfloat16:
         fn, dname = N.load().as_spmm_csr_bf16, "as_spmm_csr_bf16"
+    elif val.dtype == torch.float64 and B.dtype == torch.float64:
+        return _spmm_f64(rowptr, colind, val, B, C, beta)
     else:
-        raise TypeError("val and B must both be float32 or both bfloat16")
+        raise TypeError("val and B must both be float32, both bfloat16 or both float64")
     _need(val, val.dtype, "val", 1)
     if val.numel() != nnz:
         raise ValueError("val and colind lengths differ")
@@ -96,6 +98,22 @@ def spmm(rowptr, colind, val, B, C=None, beta: float = 0.0, variant: int = 0):
     ctx = N.context(dev.index)
     N.check(fn(ctx.handle, M, K, Ncols, nnz, _ptr(rowptr), _ptr(colind), _ptr(val), _ptr(B),
                ldb, _ptr(C), ldc, float(beta), int(variant), _stream(dev)), dname)
+    return C
+
+
+def _spmm_f64(rowptr, colind, val, B, C, beta):
+    """float64 SpMM (gradient checks only)."""
+    dev = B.device
+    M, nnz = _csr(rowptr, colind)
+    K, Ncols = B.shape
+    _need(val, torch.float64, "val", 1)
+    if C is None:
+        C = torch.empty((M, Ncols), dtype=torch.float64, device=dev)
+    ctx = N.context(dev.index)
+    N.check(N.load().as_spmm_csr_f64(ctx.handle, M, K, Ncols, nnz, _ptr(rowptr), _ptr(colind),
+                                     _ptr(val), _ptr(B), B.stride(0) if K > 1 else Ncols,
+                                     _ptr(C), C.stride(0) if M > 1 else Ncols, float(beta),
+                                     _stream(dev)), "as_spmm_csr_f64")
     return C
 
 
@@ -156,6 +174,8 @@ def sddmm(rowptr, colind, X, Y, aval=None, out=None, tensor_cores: bool = False)
     path."""
     dev = _dev(rowptr, colind, X, Y, aval, out)
     M, nnz = _csr(rowptr, colind)
+    if X.dtype == torch.float64:
+        return _sddmm_f64(rowptr, colind, X, Y, aval, out)
     for t, n in ((X, "X"), (Y, "Y")):
         if t.dtype != torch.float32 or t.dim() != 2 or t.stride(1) != 1:
             raise ValueError(f"{n} must be float32, 2-D, row-major")
@@ -176,6 +196,52 @@ def sddmm(rowptr, colind, X, Y, aval=None, out=None, tensor_cores: bool = False)
     N.check(fn(ctx.handle, M, Y.shape[0], K, nnz, _ptr(rowptr), _ptr(colind), _ptr(aval),
                _ptr(X), ldx, _ptr(Y), ldy, _ptr(out), _stream(dev)),
             "as_sddmm_csr_bf16x3" if tensor_cores else "as_sddmm_csr_f32")
+    return out
+
+
+def _sddmm_f64(rowptr, colind, X, Y, aval, out):
+    """float64 SDDMM (gradient checks only)."""
+    dev = X.device
+    M, nnz = _csr(rowptr, colind)
+    for t, n in ((X, "X"), (Y, "Y")):
+        if t.dtype != torch.float64 or t.dim() != 2 or not t.is_contiguous():
+            raise ValueError(f"{n} must be float64, 2-D, contiguous")
+    if aval is not None:
+        _need(aval, torch.float64, "aval", 1)
+    if out is None:
+        out = torch.empty(nnz, dtype=torch.float64, device=dev)
+    K = X.shape[1]
+    ctx = N.context(dev.index)
+    N.check(N.load().as_sddmm_csr_f64(ctx.handle, M, Y.shape[0], K, nnz, _ptr(rowptr),
+                                      _ptr(colind), _ptr(aval), _ptr(X), K, _ptr(Y), K, _ptr(out),
+                                      _stream(dev)), "as_sddmm_csr_f64")
+    return out
+
+
+def sddmm_coo(rowind, colind, X, Y, aval=None, out=None):
+    """out[e] = aval[e] * <X[rowind[e]], Y[colind[e]]>, entries in any order (FP32)."""
+    dev = _dev(rowind, colind, X, Y, aval, out)
+    _need(rowind, torch.int32, "rowind", 1)
+    _need(colind, torch.int32, "colind", 1)
+    nnz = colind.numel()
+    if rowind.numel() != nnz:
+        raise ValueError("rowind and colind lengths differ")
+    for t, n in ((X, "X"), (Y, "Y")):
+        if t.dtype != torch.float32 or t.dim() != 2 or t.stride(1) != 1:
+            raise ValueError(f"{n} must be float32, 2-D, row-major")
+    if X.shape[1] != Y.shape[1]:
+        raise ValueError("X and Y need the same K")
+    if aval is not None:
+        _need(aval, torch.float32, "aval", 1)
+    if out is None:
+        out = torch.empty(nnz, dtype=torch.float32, device=dev)
+    K = X.shape[1]
+    ldx = X.stride(0) if X.shape[0] > 1 else K
+    ldy = Y.stride(0) if Y.shape[0] > 1 else K
+    ctx = N.context(dev.index)
+    N.check(N.load().as_sddmm_coo_f32(ctx.handle, X.shape[0], Y.shape[0], K, nnz, _ptr(rowind),
+                                      _ptr(colind), _ptr(aval), _ptr(X), ldx, _ptr(Y), ldy,
+                                      _ptr(out), _stream(dev)), "as_sddmm_coo_f32")
     return out
 
 

@@ -111,6 +111,12 @@ as_status as_sddmm_csr_bf16x3(as_ctx *ctx, int M, int N, int K, int nnz, const i
                               const int *colind, const float *aval, const float *X, long ldx,
                               const float *Y, long ldy, float *out, void *stream);
 
+/* COO form: entry e has row rowind[e] and column colind[e] (any order); X, Y, out as above.
+ * Replaces sddmm_cuda_coo (gcn/pytorch-custom/sddmm.cu:427-457). */
+as_status as_sddmm_coo_f32(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowind,
+                           const int *colind, const float *aval, const float *X, long ldx,
+                           const float *Y, long ldy, float *out, void *stream);
+
 /* ---- CSR -> CSC (transpose) ------------------------------------------------------------------
  * A: M x N CSR. Outputs colptr[N+1], rowind[nnz], cscval[nnz] (val / cscval may be NULL
  * for a pattern-only transpose). Rows are ascending within every column, so the result is
@@ -119,6 +125,17 @@ as_status as_sddmm_csr_bf16x3(as_ctx *ctx, int M, int N, int K, int nnz, const i
  * fast_transpose (sparseTranspose.cpp:95-142). */
 as_status as_csr2csc(as_ctx *ctx, int M, int N, int nnz, const int *rowptr, const int *colind,
                      const float *val, int *colptr, int *rowind, float *cscval, void *stream);
+
+/* ---- FP64 forms, for gradient checks only ---------------------------------------------------
+ * Same contracts as as_spmm_csr_f32 (row-split order, one output per thread) and
+ * as_sddmm_csr_f32, in double precision. Not tuned; they exist so that the autograd op can be
+ * checked against finite differences in float64. */
+as_status as_spmm_csr_f64(as_ctx *ctx, int M, int K, int N, int nnz, const int *rowptr,
+                          const int *colind, const double *val, const double *B, long ldb,
+                          double *C, long ldc, double beta, void *stream);
+as_status as_sddmm_csr_f64(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
+                           const int *colind, const double *aval, const double *X, long ldx,
+                           const double *Y, long ldy, double *out, void *stream);
 
 /* ---- small dense helpers used around the hot path ---------------------------------------- */
 /* dst[i] = bf16(src[i]) (round to nearest even). */

@@ -116,3 +116,16 @@ def test_tc_unsorted_rows_flagged():
     with pytest.raises(N.NativeError) as ei:
         A.sync_status()
     assert ei.value.status == 2
+
+
+def test_coo_any_order(oracle):
+    a = S.uniform_csr(300, 200, 5000, seed=21, values="u0515")
+    X = S.dense_normal((300, 40), 22)
+    Y = S.dense_normal((200, 40), 23)
+    rows = np.repeat(np.arange(300, dtype=np.int32), np.diff(a.rowptr))
+    perm = np.random.default_rng(24).permutation(a.nnz)
+    out = A.sddmm_coo(to_dev(rows[perm]), to_dev(a.colind[perm]), to_dev(X), to_dev(Y),
+                      aval=to_dev(a.val[perm]))
+    lanes = oracle.sddmm_f32_lanes(a.rowptr, a.colind, X, Y, aval=a.val)
+    assert np.array_equal(bits(out), bits(lanes[perm]))
+    A.sync_status()
