@@ -1,0 +1,201 @@
+"""GCN on the sparse hot path: the autograd SpMM op, GCNConv and the 2-layer network.
+
+Mirrors gcn/pytorch-custom/op.py (SPMMFunction :8-37, GCNConv :79-153) and the model/training
+of gcn_custom.py (:72-126), GPU-resident, with three changes the reference lacks:
+
+* backward computes dB = A^T * dY with the CSC arrays (as op.py:30 does) AND the gradient of
+  the edge values dA[e] = <dY[row(e)], B[col(e)]> as an SDDMM at A's pattern (op.py:31 returns
+  None);
+* the CSC arrays come from the GPU transpose, computed once per graph and cached
+  (``Graph.csc``), instead of a host scipy ``tocsc()`` (gcn_custom.py:52);
+* no hidden global state: the reference's backward returns a stale module-level ``grad_feat``
+  when called without edge weights (op.py:21, :33-35).
+
+Orientation is explicit: ``rowptr/colind`` is the CSR of A in out = A * x (the reference builds
+its "rowptr" from ``tocsc()``, gcn_custom.py:48-55, which only coincides for symmetric graphs).
+"""
+from __future__ import annotations
+
+import math
+
+import torch
+import torch.nn.functional as F
+from torch.nn import Parameter
+
+from . import sparse as S
+
+
+def _spmm(rowptr, colind, values, feat, variant=0):
+    """A * feat for fp32 / fp64 / bf16 features (bf16 values and features are multiplied in fp32;
+    the result is returned in the feature dtype)."""
+    if feat.dtype == torch.bfloat16:
+        return S.spmm(rowptr, colind, values.to(torch.bfloat16), feat.contiguous(),
+                      variant=variant).to(torch.bfloat16)
+    return S.spmm(rowptr, colind, values.to(feat.dtype), feat.contiguous(), variant=variant)
+
+
+class SPMMFunction(torch.autograd.Function):
+    """out = A * feat, A given as CSR (rowptr, colind, edge_weight_csr) and as CSC (colptr, rowind,
+    edge_weight_csc). Same ``apply`` signature as the reference (op.py:9)."""
+
+    @staticmethod
+    def forward(ctx, rowptr, colind, colptr, rowind, feat, edge_weight_csr=None,
+                edge_weight_csc=None):
+        if edge_weight_csr is None:
+            raise ValueError("SPMMFunction needs edge values (pass ones for an unweighted graph)")
+        out = _spmm(rowptr, colind, edge_weight_csr, feat)
+        ctx.save_for_backward(rowptr, colind, colptr, rowind, feat, edge_weight_csr,
+                              edge_weight_csc)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        rowptr, colind, colptr, rowind, feat, w_csr, w_csc = ctx.saved_tensors
+        grad_feat = grad_w = None
+        g = grad_out.contiguous()
+        if ctx.needs_input_grad[4]:
+            if w_csc is None or w_csc.numel() != w_csr.numel():
+                raise RuntimeError("backward of SPMMFunction needs the edge values in CSC order "
+                                   "(SPMMFunction.apply(rowptr, colind, colptr, rowind, feat, "
+                                   "values_csr, values_csc))")
+            grad_feat = _spmm(colptr, rowind, w_csc, g)
+        if ctx.needs_input_grad[5]:
+            gf = g if g.dtype in (torch.float32, torch.float64) else g.float()
+            ff = feat if feat.dtype == gf.dtype else feat.to(gf.dtype)
+            grad_w = S.sddmm(rowptr, colind, gf, ff.contiguous()).to(w_csr.dtype)
+        return None, None, None, None, grad_feat, grad_w, None
+
+
+class Graph:
+    """A sparse adjacency on the GPU with its transpose computed once (GPU, deterministic)."""
+
+    def __init__(self, rowptr: torch.Tensor, colind: torch.Tensor, values: torch.Tensor,
+                 n_cols: int | None = None):
+        self.rowptr, self.colind, self.values = rowptr, colind, values
+        self.n_rows = rowptr.numel() - 1
+        self.n_cols = self.n_rows if n_cols is None else n_cols
+        self._csc = None
+
+    @property
+    def csc(self):
+        if self._csc is None:
+            self._csc = S.csr2csc(self.rowptr, self.colind, self.values, self.n_cols)
+        return self._csc
+
+    @classmethod
+    def from_csr(cls, a, device) -> "Graph":
+        t = lambda x: torch.from_numpy(x).to(device)
+        return cls(t(a.rowptr), t(a.colind), t(a.val), a.n_cols)
+
+    def aggregate(self, feat: torch.Tensor) -> torch.Tensor:
+        colptr, rowind, vcsc = self.csc
+        return SPMMFunction.apply(self.rowptr, self.colind, colptr, rowind, feat, self.values,
+                                  vcsc)
+
+
+def glorot_(w: torch.Tensor) -> None:
+    """U(-a, a), a = sqrt(6 / (fan_in + fan_out)) (the init op.py:76 imports)."""
+    a = math.sqrt(6.0 / (w.size(-2) + w.size(-1)))
+    with torch.no_grad():
+        w.uniform_(-a, a)
+
+
+class GCNConv(torch.nn.Module):
+    """x -> D_in^-1/2 * A * D_out^-1/2 * (x W) + b, op for op as op.py:112-149: the dense
+    product, the pre-scale by 1/sqrt(out-degree) (from colptr), the SpMM, the post-scale by
+    1/sqrt(in-degree) (from rowptr), the bias."""
+
+    def __init__(self, in_channels, out_channels, bias=True, normalize=True, cached=True):
+        super().__init__()
+        self.in_channels, self.out_channels = in_channels, out_channels
+        self.normalize, self.cached = normalize, cached
+        self.weight = Parameter(torch.empty(in_channels, out_channels))
+        self.bias = Parameter(torch.empty(out_channels)) if bias else None
+        self.cached_result = None
+        self.reset_parameters()
+
+    def reset_parameters(self):
+        glorot_(self.weight)
+        if self.bias is not None:
+            with torch.no_grad():
+                self.bias.zero_()
+        self.cached_result = None
+
+    @staticmethod
+    def deg_inv_sqrt(indptr):
+        return (1 / torch.sqrt((indptr[1:] - indptr[:-1]).float())).unsqueeze(dim=1)
+
+    def forward(self, x, rowptr, colind, colptr, rowind, edge_weight_csr, edge_weight_csc):
+        x = torch.matmul(x, self.weight)
+        if not self.cached or self.cached_result is None:
+            if self.normalize:
+                in_norm, out_norm = self.deg_inv_sqrt(rowptr), self.deg_inv_sqrt(colptr)
+            else:
+                in_norm = out_norm = None
+            self.cached_result = (in_norm, out_norm)
+        in_norm, out_norm = self.cached_result
+        if self.normalize:
+            x = x * out_norm
+        out = SPMMFunction.apply(rowptr, colind, colptr, rowind, x, edge_weight_csr,
+                                 edge_weight_csc)
+        if self.normalize:
+            out = out * in_norm
+        if self.bias is not None:
+            out = out + self.bias
+        return out
+
+
+class Net(torch.nn.Module):
+    """2-layer GCN of gcn_custom.py:72-90: conv -> relu -> dropout -> conv -> log_softmax."""
+
+    def __init__(self, n_features, n_hidden, n_classes):
+        super().__init__()
+        self.conv1 = GCNConv(n_features, n_hidden)
+        self.conv2 = GCNConv(n_hidden, n_classes)
+
+    def forward(self, x, g: Graph):
+        colptr, rowind, vcsc = g.csc
+        args = (g.rowptr, g.colind, colptr, rowind, g.values, vcsc)
+        x = F.relu(self.conv1(x, *args))
+        x = F.dropout(x, training=self.training)
+        x = self.conv2(x, *args)
+        return F.log_softmax(x, dim=1)
+
+
+def make_optimizer(model: Net):
+    """Adam, lr 0.01, weight decay 5e-4 on the first layer only (gcn_custom.py:116-119)."""
+    return torch.optim.Adam([dict(params=model.conv1.parameters(), weight_decay=5e-4),
+                             dict(params=model.conv2.parameters(), weight_decay=0)], lr=0.01)
+
+
+def train_epoch(model, opt, x, g, y, train_mask) -> torch.Tensor:
+    """One full-batch step (gcn_custom.py:122-126); returns the loss (on the device)."""
+    model.train()
+    opt.zero_grad()
+    loss = F.nll_loss(model(x, g)[train_mask], y[train_mask])
+    loss.backward()
+    opt.step()
+    return loss.detach()
+
+
+def synthetic_task(n_nodes=19717, n_edges=88648, n_features=500, n_classes=3, seed=0,
+                   device="cuda"):
+    """PubMed-shaped stand-in: power-law undirected graph with self-loops, 10 % non-zero U(0,1)
+    features, random labels, 60 training nodes per class (the reference's Planetoid split)."""
+    import numpy as np
+
+    from . import synthetic as syn
+    a = syn.powerlaw_graph(n_nodes, n_edges, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    x = np.zeros((n_nodes, n_features), np.float32)
+    mask = rng.random(x.shape) < 0.1
+    x[mask] = rng.random(int(mask.sum())).astype(np.float32)
+    y = rng.integers(0, n_classes, n_nodes)
+    train = np.zeros(n_nodes, bool)
+    for c in range(n_classes):
+        idx = np.flatnonzero(y == c)[:60]
+        train[idx] = True
+    dev = torch.device(device)
+    g = Graph.from_csr(a, dev)
+    return (torch.from_numpy(x).to(dev), g, torch.from_numpy(y).to(dev),
+            torch.from_numpy(train).to(dev), a)

@@ -15,7 +15,13 @@ runs them on small seeded inputs and saves inputs and outputs as .npz files:
 * spmv_vcsr4.npz -- toVectorAwareCSR (SpMV.cpp:15-38) and sparse_dense_vector
   (SpMV.cpp:155-179);
 * transpose_triplets.npz -- convert (sparseTranspose.cpp:71-92) and fast_transpose
-  (sparseTranspose.cpp:95-142) run on one thread (stable order).
+  (sparseTranspose.cpp:95-142) run on one thread (stable order);
+* gcn_op.npz -- the reference's own gcn/pytorch-custom/op.py imported as is: its
+  SPMMFunction forward and backward and one GCNConv forward+backward on a small seeded graph.
+  The module's ``spmm = load(name='spmm', ...)`` (op.py:6) is served by the reference's
+  compiled csr_spmm_kernel (spmm.cpp:49-71, oracle target ``ref-gcn``) called with a zeroed
+  output (spmm.cpp:41 leaves it uninitialised), and ``torch_geometric.nn.inits`` -- not
+  installed -- by a stub whose glorot/zeros follow pytorch_geometric's inits.py:30-33, :58-59.
 
 The fixtures are small (a few hundred KB in total) and the GPU tests read only them, never
 the reference.
@@ -124,6 +130,77 @@ def transpose_cases(ref):
     np.savez_compressed(os.path.join(HERE, "transpose_triplets.npz"), **out)
 
 
+def gcn_cases(ref_dir):
+    import types
+
+    import torch
+    import torch.utils.cpp_extension as ce
+
+    lib = O.ref_lib("gcnspmm")
+    if lib is None:
+        raise SystemExit("oracle/_ref/libref_gcnspmm.so missing (make -C oracle ref-gcn)")
+
+    def csr_spmm(rowptr, colind, values, dense):
+        rp = np.ascontiguousarray(rowptr.numpy().astype(np.int32))
+        ci = np.ascontiguousarray(colind.numpy().astype(np.int32))
+        v = np.ascontiguousarray(values.detach().numpy().astype(np.float32))
+        B = np.ascontiguousarray(dense.detach().numpy().astype(np.float32))
+        C = np.zeros((rp.size - 1, B.shape[1]), np.float32)
+        lib.ref_csr_spmm_kernel(rp.size - 1, B.shape[1], _p(rp), _p(ci), _p(v), _p(B), _p(C))
+        return torch.from_numpy(C)
+
+    fake = types.SimpleNamespace(csr_spmm=csr_spmm)
+    saved_load = ce.load
+    ce.load = lambda *a, **k: fake
+    inits = types.ModuleType("torch_geometric.nn.inits")
+
+    def glorot(t):
+        a = (6.0 / (t.size(-2) + t.size(-1))) ** 0.5
+        t.data.uniform_(-a, a)
+
+    inits.glorot = glorot
+    inits.zeros = lambda t: t.data.fill_(0.0) if t is not None else None
+    for name in ["torch_geometric", "torch_geometric.nn"]:
+        sys.modules.setdefault(name, types.ModuleType(name))
+    sys.modules["torch_geometric.nn.inits"] = inits
+    sys.path.insert(0, os.path.join(ref_dir, "gcn", "pytorch-custom"))
+    try:
+        import op  # the reference's module, unmodified
+    finally:
+        ce.load = saved_load
+        sys.path.pop(0)
+
+    from armsparse_gb300 import synthetic as syn
+    a = syn.powerlaw_graph(300, 1600, seed=5)
+    n = a.n_rows
+    rng = np.random.default_rng(6)
+    w = rng.uniform(0.5, 1.5, a.nnz).astype(np.float32)  # weighted edges
+    cp, ri, cw = O.csr2csc(a.rowptr, a.colind, w, n)
+    t = lambda x: torch.from_numpy(np.ascontiguousarray(x))
+    feat = rng.standard_normal((n, 16)).astype(np.float32)
+    gout = rng.standard_normal((n, 16)).astype(np.float32)
+    f = t(feat).requires_grad_(True)
+    out = op.SPMMFunction.apply(t(a.rowptr), t(a.colind), t(cp), t(ri), f, t(w), t(cw))
+    out.backward(t(gout))
+    # GCNConv with fixed weights: forward and input gradient
+    conv = op.GCNConv(16, 8, cached=True, normalize=True)
+    W = rng.standard_normal((16, 8)).astype(np.float32) * 0.3
+    bvec = rng.standard_normal(8).astype(np.float32) * 0.1
+    with torch.no_grad():
+        conv.weight.copy_(t(W))
+        conv.bias.copy_(t(bvec))
+    x = t(feat).requires_grad_(True)
+    y = conv(x, t(a.rowptr), t(a.colind), t(cp), t(ri), t(w), t(cw))
+    gy = rng.standard_normal((n, 8)).astype(np.float32)
+    y.backward(t(gy))
+    np.savez_compressed(os.path.join(HERE, "gcn_op.npz"), rowptr=a.rowptr, colind=a.colind,
+                        val=w, colptr=cp, rowind=ri, val_csc=cw, feat=feat, grad_out=gout,
+                        out=out.detach().numpy(), grad_feat=f.grad.numpy(), W=W, b=bvec,
+                        conv_out=y.detach().numpy(), conv_grad_out=gy,
+                        conv_grad_x=x.grad.numpy(), conv_grad_W=conv.weight.grad.numpy(),
+                        conv_grad_b=conv.bias.grad.numpy())
+
+
 def main():
     ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     if not O.build_ref(ref_dir):
@@ -131,6 +208,8 @@ def main():
     spmm_cases(O.ref_lib("sdmm"))
     spmv_cases(O.ref_lib("spmv"))
     transpose_cases(O.ref_lib("transpose"))
+    if O.build_ref(ref_dir, gcn=True):
+        gcn_cases(ref_dir)
     print("golden vectors written to", HERE)
 
 

@@ -1,0 +1,125 @@
+"""The GCN op on the GPU: the torch extension `spmm`, the autograd SPMMFunction and GCNConv
+against golden vectors made by running the reference's own op.py (forward bit-exact, input
+gradient bit-exact), FP64 gradcheck on a 500-node subgraph, and run-to-run reproducibility
+of GCN training."""
+import numpy as np
+import pytest
+import torch
+
+import armsparse_gb300 as A
+from armsparse_gb300 import gcn
+from armsparse_gb300 import synthetic as S
+from gpu_util import bits, dev, to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def test_extension_ops(oracle):
+    from armsparse_gb300.torch_ops import spmm
+    a = S.uniform_csr(700, 500, 9000, seed=3)
+    B = S.dense_uniform((500, 64), 4)
+    rp, ci, v, Bd = to_dev(a.rowptr), to_dev(a.colind), to_dev(a.val), to_dev(B)
+    out = spmm.csr_spmm(rp, ci, v, Bd)
+    assert np.array_equal(bits(out), bits(oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, B)))
+    ob = spmm.csr_spmm(rp, ci, v.bfloat16(), Bd.bfloat16())
+    assert ob.dtype == torch.float32
+    X, Y = S.dense_normal((700, 32), 5), S.dense_normal((500, 32), 6)
+    s = spmm.csr_sddmm(rp, ci, to_dev(X), to_dev(Y))
+    assert np.array_equal(bits(s), bits(oracle.sddmm_f32_lanes(a.rowptr, a.colind, X, Y)))
+    rows = np.repeat(np.arange(700, dtype=np.int32), np.diff(a.rowptr))
+    s2 = spmm.coo_sddmm(to_dev(rows), ci, to_dev(X), to_dev(Y))
+    assert torch.equal(s, s2)
+    colptr = torch.empty(501, dtype=torch.int32, device=dev())
+    rowind = torch.empty(a.nnz, dtype=torch.int32, device=dev())
+    cv = spmm.csr2csc(rp, ci, colptr, rowind, v)
+    ocp, ori, ocv = oracle.csr2csc(a.rowptr, a.colind, a.val, 500)
+    assert np.array_equal(colptr.cpu().numpy(), ocp) and np.array_equal(rowind.cpu().numpy(), ori)
+    assert np.array_equal(bits(cv), bits(ocv))
+    with pytest.raises(RuntimeError):
+        spmm.csr_spmm(rp, ci, v, Bd.double())
+
+
+def test_spmm_function_matches_reference_op(golden):
+    g = golden["gcn_op"]
+    rp, ci, cp, ri = (to_dev(g[k]) for k in ("rowptr", "colind", "colptr", "rowind"))
+    w, wc = to_dev(g["val"]), to_dev(g["val_csc"])
+    f = to_dev(g["feat"]).requires_grad_(True)
+    out = gcn.SPMMFunction.apply(rp, ci, cp, ri, f, w, wc)
+    out.backward(to_dev(g["grad_out"]))
+    assert np.array_equal(bits(out), bits(g["out"]))
+    assert np.array_equal(bits(f.grad), bits(g["grad_feat"]))
+    # the same through the cached GPU transpose
+    G = gcn.Graph(rp, ci, w)
+    colptr, rowind, vcsc = G.csc
+    assert torch.equal(colptr, cp) and torch.equal(rowind, ri)
+    assert np.array_equal(bits(vcsc), bits(g["val_csc"]))
+
+
+def test_gcnconv_matches_reference_op(golden):
+    g = golden["gcn_op"]
+    rp, ci, cp, ri = (to_dev(g[k]) for k in ("rowptr", "colind", "colptr", "rowind"))
+    w, wc = to_dev(g["val"]), to_dev(g["val_csc"])
+    conv = gcn.GCNConv(16, 8).to(dev())
+    with torch.no_grad():
+        conv.weight.copy_(to_dev(g["W"]))
+        conv.bias.copy_(to_dev(g["b"]))
+    x = to_dev(g["feat"]).requires_grad_(True)
+    y = conv(x, rp, ci, cp, ri, w, wc)
+    y.backward(to_dev(g["conv_grad_out"]))
+    # the dense x @ W runs in cuBLAS here and in CPU torch in the reference: FP32 rounding only
+    for got, ref in ((y, g["conv_out"]), (x.grad, g["conv_grad_x"]),
+                     (conv.weight.grad, g["conv_grad_W"]), (conv.bias.grad, g["conv_grad_b"])):
+        got = got.detach().cpu().numpy()
+        assert np.allclose(got, ref, rtol=1e-5, atol=1e-5 * np.abs(ref).max()), np.abs(got - ref).max()
+
+
+def _subgraph(a, n):
+    """Induced subgraph on the first n nodes (keeps self-loops), CSR."""
+    rows = np.repeat(np.arange(a.n_rows), np.diff(a.rowptr))
+    keep = (rows < n) & (a.colind < n)
+    r, c = rows[keep], a.colind[keep]
+    rp = np.zeros(n + 1, np.int32)
+    np.cumsum(np.bincount(r, minlength=n), out=rp[1:])
+    return S.CSR(rp, c.astype(np.int32), a.val[keep], n, n)
+
+
+def test_gradcheck_fp64_500_node_subgraph():
+    a = _subgraph(S.powerlaw_graph(19717, 88648, seed=9), 500)
+    rng = np.random.default_rng(1)
+    w = rng.uniform(0.5, 1.5, a.nnz)
+    G = gcn.Graph(to_dev(a.rowptr), to_dev(a.colind), to_dev(w.astype(np.float32)))
+    colptr, rowind, _ = G.csc
+    # CSC values in float64: permute the CSR values the way the transpose does
+    perm = np.lexsort((np.repeat(np.arange(500), np.diff(a.rowptr)), a.colind))
+    wd = torch.tensor(w, dtype=torch.float64, device=dev(), requires_grad=True)
+    wcsc = torch.tensor(w[perm], dtype=torch.float64, device=dev())
+    feat = torch.randn(500, 3, dtype=torch.float64, device=dev(), requires_grad=True)
+    fn = lambda f, ww: gcn.SPMMFunction.apply(G.rowptr, G.colind, colptr, rowind, f, ww, wcsc)
+    assert torch.autograd.gradcheck(fn, (feat, wd), eps=1e-6, atol=1e-8, rtol=1e-6)
+
+
+def test_edge_value_gradient_is_sddmm(oracle):
+    a = S.powerlaw_graph(2000, 12000, seed=4)
+    G = gcn.Graph.from_csr(a, dev())
+    w = G.values.clone().requires_grad_(True)
+    colptr, rowind, vcsc = G.csc
+    f = torch.randn(2000, 24, device=dev())
+    out = gcn.SPMMFunction.apply(G.rowptr, G.colind, colptr, rowind, f, w, vcsc)
+    gy = torch.randn_like(out)
+    out.backward(gy)
+    ref = oracle.sddmm_f32_lanes(a.rowptr, a.colind, gy.cpu().numpy(), f.cpu().numpy())
+    assert np.array_equal(bits(w.grad), bits(ref))
+
+
+def test_gcn_training_is_reproducible():
+    x, g, y, train, _ = gcn.synthetic_task(seed=0)
+
+    def run():
+        torch.manual_seed(0)
+        model = gcn.Net(x.shape[1], 64, 3).to(dev())
+        opt = gcn.make_optimizer(model)
+        return torch.stack([gcn.train_epoch(model, opt, x, g, y, train) for _ in range(10)])
+
+    l1, l2 = run(), run()
+    assert torch.equal(l1, l2)
+    assert torch.isfinite(l1).all() and l1[-1] < l1[0]

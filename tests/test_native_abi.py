@@ -98,3 +98,14 @@ def test_ops_refuse_cpu_tensors(native_lib):
         A.spmm(rp, ci, v, torch.ones(1, 4))
     with pytest.raises(ValueError, match="CUDA"):
         A.csr2csc(rp, ci, v, 1)
+
+
+def test_torch_extension_loads_and_refuses_cpu_tensors():
+    from armsparse_gb300 import build
+    build.build_torch_extension()
+    from armsparse_gb300.torch_ops import spmm
+    for name in ["csr_spmm", "csr_sddmm", "coo_sddmm", "csr2csc"]:
+        assert hasattr(spmm, name)
+    rp = torch.tensor([0, 1], dtype=torch.int32)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        spmm.csr_spmm(rp, torch.tensor([0], dtype=torch.int32), torch.ones(1), torch.ones(1, 4))
