@@ -372,3 +372,138 @@ as_status f32_to_bf16_launch(as_ctx *ctx, long n, const float *src, uint16_t *ds
 }
 
 }  // namespace as
+
+// ---- no-allocation transpose -----------------------------------------------------------------
+// as_csr2csc_static: the same transpose with its scratch in a file-scope device array, for
+// callers that cannot allocate device memory. The array is sized for
+// AS_CSR2CSC_STATIC_MAX_NNZ entries; every GPU that loads this library holds it until the
+// process exits. Host code only knows the array through the address cudaGetSymbolAddress
+// returns for the current device (the symbol itself is a host-side stand-in), fetched once
+// per device by the first call on that device.
+#include <mutex>
+
+namespace as {
+namespace {
+
+constexpr size_t align256c(size_t b) { return (b + 255) & ~size_t(255); }
+constexpr long kStaticTiles = (AS_CSR2CSC_STATIC_MAX_NNZ + kTile - 1) / kTile;
+constexpr long kStaticHist = kStaticTiles * kBins;
+constexpr size_t kStaticScratchBytes =
+    5 * align256c(sizeof(int) * static_cast<size_t>(AS_CSR2CSC_STATIC_MAX_NNZ)) +
+    align256c(sizeof(int) * static_cast<size_t>(kStaticHist)) +
+    align256c(sizeof(int) * static_cast<size_t>((kStaticHist + kScanChunk - 1) / kScanChunk + 1));
+constexpr int kStaticMaxDevices = 64;
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_csr2csc_static_scratch[kStaticScratchBytes];
+static __device__ unsigned g_csr2csc_static_status;
+
+namespace {
+
+struct StaticSlot {
+    bool ready = false;
+    unsigned char *scratch = nullptr;
+    unsigned *status = nullptr;
+};
+std::mutex g_static_mu;
+StaticSlot g_static_slots[kStaticMaxDevices];
+
+// Device addresses of the static scratch and status word on the current device.
+cudaError_t static_slot(int dev, StaticSlot *out) {
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    StaticSlot &s = g_static_slots[dev];
+    if (!s.ready) {
+        void *p = nullptr, *q = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_csr2csc_static_scratch);
+        if (e != cudaSuccess) return e;
+        e = cudaGetSymbolAddress(&q, g_csr2csc_static_status);
+        if (e != cudaSuccess) return e;
+        s.scratch = static_cast<unsigned char *>(p);
+        s.status = static_cast<unsigned *>(q);
+        s.ready = true;
+    }
+    *out = s;
+    return cudaSuccess;
+}
+
+// The launch sequence of csr2csc_launch, reporting through cudaError_t only.
+cudaError_t csr2csc_static_run(int M, int N, int nnz, const int *rowptr, const int *colind,
+                               const float *val, int *colptr, int *rowind, float *cscval,
+                               unsigned char *work, unsigned *status, cudaStream_t s) {
+    const bool wv = val != nullptr;
+    const int tiles = static_cast<int>(ceil_div(nnz, kTile));
+    const long hist_n = static_cast<long>(tiles) * kBins;
+    const size_t cap = align256c(sizeof(int) * static_cast<size_t>(AS_CSR2CSC_STATIC_MAX_NNZ));
+    int *rowidx = reinterpret_cast<int *>(work);
+    int *keysA = reinterpret_cast<int *>(work + cap);
+    int *keysB = reinterpret_cast<int *>(work + 2 * cap);
+    int *rowsT = reinterpret_cast<int *>(work + 3 * cap);
+    float *valsT = reinterpret_cast<float *>(work + 4 * cap);
+    int *hist = reinterpret_cast<int *>(work + 5 * cap);
+    int *sums = reinterpret_cast<int *>(work + 5 * cap + align256c(sizeof(int) * kStaticHist));
+
+    const unsigned gw = static_cast<unsigned>(ceil_div(static_cast<long>(M) * 32, kThreads));
+    expand_rows<<<gw, kThreads, 0, s>>>(M, nnz, rowptr, rowidx, status);
+    const long cb = ceil_div(nnz, kThreads);
+    check_rowptr_ends<<<static_cast<unsigned>(cb < 4096 ? cb : 4096), kThreads, 0, s>>>(
+        M, nnz, rowptr, rowidx, status);
+    const int passes = radix_passes(N);
+    const int *src_k = colind;
+    const int *src_r = rowidx;
+    const float *src_v = val;
+    const long nb = ceil_div(hist_n, kScanChunk);
+    for (int pass = 0; pass < passes; ++pass) {
+        const bool last = pass == passes - 1;
+        const bool to_scratch = ((passes - 1 - pass) & 1) != 0;
+        int *dk = (pass & 1) ? keysB : keysA;
+        int *dr = (last || !to_scratch) ? rowind : rowsT;
+        float *dv = wv ? ((last || !to_scratch) ? cscval : valsT) : nullptr;
+        const int shift = 8 * pass;
+        radix_histogram<<<tiles, kThreads, 0, s>>>(src_k, nnz, shift, tiles, N, hist, status,
+                                                   pass == 0);
+        scan_reduce<<<static_cast<unsigned>(nb), kThreads, 0, s>>>(hist, hist_n, sums);
+        scan_block_sums<<<1, kThreads, 0, s>>>(sums, static_cast<int>(nb));
+        scan_downsweep<<<static_cast<unsigned>(nb), kThreads, 0, s>>>(hist, hist_n, sums, hist);
+        radix_scatter<<<tiles, kThreads, 0, s>>>(src_k, src_r, src_v, nnz, shift, tiles, hist,
+                                                 dk, dr, dv);
+        src_k = dk;
+        src_r = dr;
+        src_v = dv;
+    }
+    colptr_from_keys<<<static_cast<unsigned>(ceil_div(static_cast<long>(nnz) + 1, kThreads)),
+                       kThreads, 0, s>>>(src_k, nnz, N, colptr);
+    return cudaGetLastError();
+}
+
+}  // namespace
+}  // namespace as
+
+extern "C" as_status as_csr2csc_static(int M, int N, int nnz, const int *rowptr,
+                                       const int *colind, const float *val, int *colptr,
+                                       int *rowind, float *cscval, void *stream) {
+    using namespace as;
+    if (M < 0 || N < 0 || nnz < 0) return AS_ERR_INVALID_VALUE;
+    if (nnz > AS_CSR2CSC_STATIC_MAX_NNZ) return AS_ERR_UNSUPPORTED;
+    if (!rowptr || !colptr || (nnz > 0 && (!colind || !rowind))) return AS_ERR_INVALID_VALUE;
+    if ((val == nullptr) != (cscval == nullptr)) return AS_ERR_INVALID_VALUE;
+    if (nnz > 0 && (M == 0 || N == 0)) return AS_ERR_INVALID_CSR;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return AS_ERR_CUDA;
+    if (dev < 0 || dev >= kStaticMaxDevices) return AS_ERR_UNSUPPORTED;
+    StaticSlot slot;
+    if (static_slot(dev, &slot) != cudaSuccess) return AS_ERR_CUDA;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // the status word keeps the previous call's flags: start each call from zero
+    if (cudaMemsetAsync(slot.status, 0, sizeof(unsigned), s) != cudaSuccess) return AS_ERR_CUDA;
+    if (nnz == 0) {
+        return cudaMemsetAsync(colptr, 0, sizeof(int) * (static_cast<size_t>(N) + 1), s) ==
+                       cudaSuccess
+                   ? AS_OK
+                   : AS_ERR_CUDA;
+    }
+    return csr2csc_static_run(M, N, nnz, rowptr, colind, val, colptr, rowind, cscval,
+                              slot.scratch, slot.status, s) == cudaSuccess
+               ? AS_OK
+               : AS_ERR_CUDA;
+}

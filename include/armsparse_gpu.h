@@ -126,6 +126,30 @@ as_status as_sddmm_coo_f32(as_ctx *ctx, int M, int N, int K, int nnz, const int 
 as_status as_csr2csc(as_ctx *ctx, int M, int N, int nnz, const int *rowptr, const int *colind,
                      const float *val, int *colptr, int *rowind, float *cscval, void *stream);
 
+/* ---- CSR -> CSC without allocating ------------------------------------------------------------
+ * No counterpart in the reference. Some callers of this library cannot allocate device
+ * memory: a plugin inside a host framework that owns every device allocation through its own
+ * pool, or a serving loop that forbids allocation after start-up because cudaMalloc/cudaFree
+ * synchronise the device and fragment it. They cannot create an as_ctx (its status word and
+ * scratch arena are allocated). as_csr2csc_static is as_csr2csc for them: the caller passes
+ * the inputs and outputs, and the transpose's scratch is a fixed device array inside this
+ * library (about 5 MB, reserved on every GPU that loads the library until the process exits).
+ * It calls no cudaMalloc, cudaFree or other allocating routine.
+ *  - Limit: nnz <= AS_CSR2CSC_STATIC_MAX_NNZ; larger calls return AS_ERR_UNSUPPORTED and launch
+ *    nothing. Other argument errors return AS_ERR_INVALID_VALUE (AS_ERR_INVALID_CSR for entries
+ *    without rows or columns); these statuses are the whole report (as_last_error() is not set).
+ *  - The first call on a device looks up the array's device address (cudaGetSymbolAddress)
+ *    with that device current; make that first call before any stream capture.
+ *  - All calls share the one array: calls whose work overlaps on the GPU (different streams or
+ *    threads, no ordering between them) race and corrupt each other's results. Serialise them.
+ *  - Malformed CSR is handled memory-safely but not reported (there is no context to hold the
+ *    flag); validate with as_csr_validate beforehand where that matters.
+ * Same output contract as as_csr2csc (rows ascending within columns, bit-exact). */
+#define AS_CSR2CSC_STATIC_MAX_NNZ (1 << 18)
+as_status as_csr2csc_static(int M, int N, int nnz, const int *rowptr, const int *colind,
+                            const float *val, int *colptr, int *rowind, float *cscval,
+                            void *stream);
+
 /* ---- FP64 forms, for gradient checks only ---------------------------------------------------
  * Same contracts as as_spmm_csr_f32 (row-split order, one output per thread) and
  * as_sddmm_csr_f32, in double precision. Not tuned; they exist so that the autograd op can be
