@@ -38,6 +38,10 @@ struct SpmmArgs {
     unsigned *status;
 };
 as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cudaStream_t s);
+as_status spmm_nnz_launch(as_ctx *ctx, int dtype, int vb, int group, int cpl, int chunk,
+                          const SpmmArgs &a, cudaStream_t s);
+as_status spmm_bulk_launch(as_ctx *ctx, int dtype, int lane_bytes, int stages, const SpmmArgs &a,
+                           cudaStream_t s);
 int spmm_variant_count(int dtype);
 const char *spmm_variant_name(int dtype, int variant);
 int spmm_default_variant(int dtype, int M, int K, int N, int nnz, long ldb, long ldc,

@@ -223,15 +223,24 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
 struct Variant {
     int vb, group, cpl, unroll;
     const char *name;
+    int kind;  // 0 = row-split (registers), 1 = bulk-copy staged (spmm_bulk.cu: vb = bytes per
+               // lane, unroll = ring stages), 2 = nnz-split (spmm_nnz.cu: unroll = chunk size)
 };
 
-#define AS_V(vb, g, c, u) {vb, g, c, u, "rowsplit_v" #vb "_g" #g "_c" #c "_u" #u}
+#define AS_V(vb, g, c, u) {vb, g, c, u, "rowsplit_v" #vb "_g" #g "_c" #c "_u" #u, 0}
+#define AS_BULK(lb, st) {lb, 32, 1, st, "bulk_lb" #lb "_s" #st, 1}
+#define AS_BULKS AS_BULK(16, 8), AS_BULK(32, 8), AS_BULK(16, 16), AS_BULK(32, 4)
+#define AS_NNZ(vb, g, c, ch) {vb, g, c, ch, "nnzsplit_v" #vb "_g" #g "_c" #c "_ch" #ch, 2}
+#define AS_NNZS(ch) AS_NNZ(16, 8, 1, ch), AS_NNZ(16, 16, 1, ch), AS_NNZ(16, 32, 1, ch), \
+    AS_NNZ(16, 32, 2, ch), AS_NNZ(4, 32, 1, ch), AS_NNZ(4, 32, 2, ch)
 #define AS_VG(vb, g) AS_V(vb, g, 1, 4), AS_V(vb, g, 2, 4), AS_V(vb, g, 4, 4), AS_V(vb, g, 1, 8), \
     AS_V(vb, g, 2, 8)
 #define AS_VROW(vb) AS_VG(vb, 1), AS_VG(vb, 2), AS_VG(vb, 4), AS_VG(vb, 8), AS_VG(vb, 16), AS_VG(vb, 32)
 
-const Variant kF32[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4)};
-const Variant kBF16[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_VROW(2)};
+const Variant kF32[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_BULKS, AS_NNZS(128),
+                        AS_NNZS(1024)};
+const Variant kBF16[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_VROW(2), AS_BULKS,
+                         AS_NNZS(128), AS_NNZS(1024)};
 constexpr int kNF32 = sizeof(kF32) / sizeof(kF32[0]);
 constexpr int kNBF16 = sizeof(kBF16) / sizeof(kBF16[0]);
 
@@ -304,34 +313,48 @@ static int find_variant(int dtype, int vb, int g, int cpl, int u) {
     const Variant *t = dtype == 0 ? kF32 : kBF16;
     const int n = spmm_variant_count(dtype);
     for (int i = 0; i < n; ++i)
-        if (t[i].vb == vb && t[i].group == g && t[i].cpl == cpl && t[i].unroll == u) return i + 1;
+        if (t[i].kind == 0 && t[i].vb == vb && t[i].group == g && t[i].cpl == cpl &&
+            t[i].unroll == u)
+            return i + 1;
     return 0;
 }
 
+// Library choice among the bit-identical row-split kernels, from the variant sweep on GB300:
+// wide rows of B (N >= 512) want full warps with two or four vectors per lane (fp32:
+// float2 x 4, bf16: 8 x bf16 x 1); narrow B wants full warps of scalar lanes with 8 entries
+// per step (the batch of 32 (colind, val) pairs amortises the index loads). The entry-balanced
+// kernels, which win on skewed rows, are not picked here: they change the summation order of
+// rows that cross a chunk, and the library cannot see the row lengths without reading rowptr
+// (the learned selector does that on the host).
 int spmm_default_variant(int dtype, int M, int K, int N, int nnz, long ldb, long ldc,
                          const void *B, const void *C) {
     (void)M; (void)K; (void)nnz;
     const int esz = dtype == 0 ? 4 : 2;
-    // bf16 keeps 8-element (16-byte) loads only while C's matching 32-byte vectors split
-    // into two aligned float4 stores; widest load that divides the layout wins.
-    const int vbs_f32[] = {16, 8, 4};
-    const int vbs_bf16[] = {16, 8, 4, 2};
-    const int *vbs = dtype == 0 ? vbs_f32 : vbs_bf16;
-    const int nvb = dtype == 0 ? 3 : 4;
-    int vb = dtype == 0 ? 4 : 2;
-    for (int i = 0; i < nvb; ++i)
-        if (vb_ok(dtype, vbs[i], N, ldb, ldc, B, C)) { vb = vbs[i]; break; }
-    const int e = vb / esz;
-    const int lanes = static_cast<int>(ceil_div(N, e));
-    int g = 1;
-    while (g < lanes && g < 32) g <<= 1;
-    int cpl = 1;
-    if (lanes > 32) cpl = lanes >= 128 ? 4 : 2;
-    return find_variant(dtype, vb, g, cpl, 4);
+    struct Pick { int vb, g, cpl, u; };
+    const Pick wide_f32[] = {{8, 32, 4, 4}, {16, 32, 2, 4}, {4, 32, 2, 8}};
+    const Pick wide_bf16[] = {{16, 32, 1, 4}, {8, 32, 2, 4}, {4, 32, 4, 4}, {2, 32, 2, 8}};
+    const Pick narrow_f32[] = {{4, 32, 2, 8}};
+    const Pick narrow_bf16[] = {{4, 32, 2, 8}, {2, 32, 2, 8}};
+    const Pick *list;
+    int n;
+    if (N >= 512) {
+        list = dtype == 0 ? wide_f32 : wide_bf16;
+        n = dtype == 0 ? 3 : 4;
+    } else {
+        list = dtype == 0 ? narrow_f32 : narrow_bf16;
+        n = dtype == 0 ? 1 : 2;
+    }
+    for (int i = 0; i < n; ++i)
+        if (vb_ok(dtype, list[i].vb, N, ldb, ldc, B, C))
+            return find_variant(dtype, list[i].vb, list[i].g, list[i].cpl, list[i].u);
+    // any layout: scalar lanes
+    return find_variant(dtype, esz, 32, N > 32 ? 2 : 1, 8);
 }
 
 as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cudaStream_t s) {
     const Variant &v = dtype == 0 ? kF32[variant - 1] : kBF16[variant - 1];
+    if (v.kind == 1) return spmm_bulk_launch(ctx, dtype, v.vb, v.unroll, a, s);
+    if (v.kind == 2) return spmm_nnz_launch(ctx, dtype, v.vb, v.group, v.cpl, v.unroll, a, s);
     if (!vb_ok(dtype, v.vb, a.N, a.ldb, a.ldc, a.B, a.C))
         return fail(AS_ERR_UNSUPPORTED, std::string("spmm: variant ") + v.name +
                                             " needs N, ldb, ldc and pointer alignment to match its vector width");

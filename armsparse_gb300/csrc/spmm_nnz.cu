@@ -1,0 +1,270 @@
+// CSR SpMM balanced by entries (sm_103a): C = A*B + beta*C for matrices whose row lengths are
+// skewed (power-law graphs), where one long row would serialise a row-per-group kernel.
+//
+// Pass 1 (spmm_nnzsplit): the entries are cut into chunks of CH consecutive entries; a group
+//   of GROUP lanes takes one chunk and one column tile, walks the chunk's row segments in CSR
+//   order and accumulates each segment with fmaf like the row-split kernels. A row that lies
+//   entirely inside the chunk is written to C directly (bit-identical to rowBaseSpmm3,
+//   SDMM.cpp:90-114). A row that crosses a chunk boundary leaves its segment's partial sum in
+//   a carry slot: slot 0 when the segment starts the chunk, slot 1 otherwise.
+// Pass 2 (spmm_nnz_fixup): for every row that ends inside chunk c after starting in an earlier
+//   chunk, the group of chunk c adds that row's partial sums in chunk order (then beta * C):
+//   a fixed order, so the result is deterministic run to run (not bit-identical to a single
+//   chain for those rows).
+// Pass 3 (spmm_empty_rows): rows without entries get beta * C (zeros when beta == 0).
+#include "common.cuh"
+#include "internal.h"
+
+namespace as {
+namespace {
+
+constexpr int kThreads = 256;
+
+template <typename T, int VB>
+struct V;
+template <>
+struct V<float, 16> {
+    static constexpr int E = 4;
+    __device__ static void load(const float *p, float *o) {
+        const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+        o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+    }
+};
+template <>
+struct V<float, 4> {
+    static constexpr int E = 1;
+    __device__ static void load(const float *p, float *o) { o[0] = __ldg(p); }
+};
+template <>
+struct V<uint16_t, 16> {
+    static constexpr int E = 8;
+    __device__ static void load(const uint16_t *p, float *o) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
+        const unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            o[2 * i] = __uint_as_float(w[i] << 16);
+            o[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+        }
+    }
+};
+template <>
+struct V<uint16_t, 4> {
+    static constexpr int E = 2;
+    __device__ static void load(const uint16_t *p, float *o) {
+        const unsigned v = __ldg(reinterpret_cast<const unsigned *>(p));
+        o[0] = __uint_as_float(v << 16);
+        o[1] = __uint_as_float(v & 0xffff0000u);
+    }
+};
+
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(uint16_t v) { return bf16_to_f32(v); }
+
+__device__ __forceinline__ int find_row(const int *__restrict__ rowptr, int M, int e) {
+    int lo = 0, hi = M;  // largest r with rowptr[r] <= e
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(rowptr + mid) <= e)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+template <typename T, int VB, int GROUP, int CPL>
+__global__ void __launch_bounds__(kThreads)
+spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowptr,
+              const int *__restrict__ colind, const T *__restrict__ val,
+              const T *__restrict__ B, long ldb, float *__restrict__ C, long ldc, float beta,
+              float *__restrict__ carry, unsigned *status) {
+    constexpr int E = V<T, VB>::E;
+    constexpr int TILE = GROUP * E * CPL;
+    const int lane = threadIdx.x & 31;
+    const int g = threadIdx.x % GROUP;
+    const unsigned gmask =
+        GROUP == 32 ? 0xffffffffu : (((1u << GROUP) - 1u) << (lane & ~(GROUP - 1)));
+    const long chunk = static_cast<long>(blockIdx.x) * (kThreads / GROUP) + threadIdx.x / GROUP;
+    const long e0l = chunk * CH;
+    if (e0l >= nnz) return;
+    const int e0 = static_cast<int>(e0l);
+    const int e1 = static_cast<int>(e0l + CH < nnz ? e0l + CH : nnz);
+    const int tile0 = blockIdx.y * TILE;
+    int r = find_row(rowptr, M, e0);
+    int e = e0;
+    while (e < e1 && r < M) {
+        const int rs = __ldg(rowptr + r), re = __ldg(rowptr + r + 1);
+        if (re <= e || rs > e) {  // empty row before e, or malformed pointers
+            if (rs > e || re < rs) {
+                flag(status, kFlagBadRowptr);
+                break;
+            }
+            ++r;
+            continue;
+        }
+        const int se = re < e1 ? re : e1;
+        const bool split = rs < e0 || re > e1;
+        float acc[CPL][E];
+#pragma unroll
+        for (int j = 0; j < CPL; ++j) {
+            const int cc = tile0 + (j * GROUP + g) * E;
+#pragma unroll
+            for (int i = 0; i < E; ++i)
+                acc[j][i] = (!split && beta != 0.0f && cc < N) ? beta * C[r * ldc + cc + i] : 0.0f;
+        }
+        for (int base = e; base < se; base += GROUP) {
+            const int ee = base + g;
+            int k = -1;
+            float v = 0.0f;
+            if (ee < se) {
+                k = ld_stream(colind + ee);
+                v = to_f32(ld_stream(val + ee));
+                if (static_cast<unsigned>(k) >= static_cast<unsigned>(K)) {
+                    flag(status, kFlagBadColind);
+                    k = -1;
+                }
+            }
+            const int cnt = min(GROUP, se - base);
+            int t = 0;
+            for (; t + 4 <= cnt; t += 4) {
+                int kk[4];
+                float vv[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    kk[u] = __shfl_sync(gmask, k, t + u, GROUP);
+                    vv[u] = __shfl_sync(gmask, v, t + u, GROUP);
+                }
+                float b[4][CPL][E];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int j = 0; j < CPL; ++j) {
+                        const int cc = tile0 + (j * GROUP + g) * E;
+                        if (cc < N && kk[u] >= 0)
+                            V<T, VB>::load(B + static_cast<long>(kk[u]) * ldb + cc, b[u][j]);
+                        else
+#pragma unroll
+                            for (int i = 0; i < E; ++i) b[u][j][i] = 0.0f;
+                    }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (kk[u] >= 0)
+#pragma unroll
+                        for (int j = 0; j < CPL; ++j)
+#pragma unroll
+                            for (int i = 0; i < E; ++i) acc[j][i] = fmaf(b[u][j][i], vv[u], acc[j][i]);
+            }
+            for (; t < cnt; ++t) {
+                const int kk = __shfl_sync(gmask, k, t, GROUP);
+                const float vv = __shfl_sync(gmask, v, t, GROUP);
+                if (kk < 0) continue;
+#pragma unroll
+                for (int j = 0; j < CPL; ++j) {
+                    const int cc = tile0 + (j * GROUP + g) * E;
+                    if (cc < N) {
+                        float b[E];
+                        V<T, VB>::load(B + static_cast<long>(kk) * ldb + cc, b);
+#pragma unroll
+                        for (int i = 0; i < E; ++i) acc[j][i] = fmaf(b[i], vv, acc[j][i]);
+                    }
+                }
+            }
+        }
+        float *dst = split ? carry + (2 * chunk + (e == e0 ? 0 : 1)) * static_cast<long>(N)
+                           : C + r * ldc;
+#pragma unroll
+        for (int j = 0; j < CPL; ++j) {
+            const int cc = tile0 + (j * GROUP + g) * E;
+            if (cc < N)
+#pragma unroll
+                for (int i = 0; i < E; ++i) dst[cc + i] = acc[j][i];
+        }
+        e = se;
+        ++r;
+    }
+}
+
+// Rows that end in chunk c after starting in an earlier chunk: sum the partials in order.
+__global__ void __launch_bounds__(kThreads)
+spmm_nnz_fixup(int M, int N, int nnz, int CH, const int *__restrict__ rowptr,
+               const float *__restrict__ carry, float *__restrict__ C, long ldc, float beta) {
+    const long chunk = blockIdx.x;
+    const long e0l = chunk * CH;
+    if (e0l >= nnz) return;
+    const int e0 = static_cast<int>(e0l);
+    const int e1 = static_cast<int>(e0l + CH < nnz ? e0l + CH : nnz);
+    const int r = find_row(rowptr, M, e0);
+    const int rs = __ldg(rowptr + r), re = __ldg(rowptr + r + 1);
+    if (!(rs < e0 && re <= e1 && re > e0)) return;
+    const long c_first = rs / CH;
+    for (int col = blockIdx.y * kThreads + threadIdx.x; col < N; col += gridDim.y * kThreads) {
+        float acc = 0.0f;
+        for (long cc = c_first; cc <= chunk; ++cc) {
+            const int slot = (cc == c_first && static_cast<long>(rs) != cc * CH) ? 1 : 0;
+            acc += carry[(2 * cc + slot) * static_cast<long>(N) + col];
+        }
+        C[r * ldc + col] = beta == 0.0f ? acc : fmaf(beta, C[r * ldc + col], acc);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads)
+spmm_empty_rows(int M, int N, const int *__restrict__ rowptr, float *__restrict__ C, long ldc,
+                float beta) {
+    const long r = static_cast<long>(blockIdx.x) * (kThreads / 32) + (threadIdx.x >> 5);
+    if (r >= M) return;
+    if (__ldg(rowptr + r) != __ldg(rowptr + r + 1)) return;
+    for (int col = threadIdx.x & 31; col < N; col += 32)
+        C[r * ldc + col] = beta == 0.0f ? 0.0f : beta * C[r * ldc + col];
+}
+
+template <typename T, int VB, int G, int CPL>
+as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, cudaStream_t s) {
+    constexpr int E = V<T, VB>::E;
+    constexpr int TILE = G * E * CPL;
+    const int esz = sizeof(T);
+    if ((a.N % E) || (a.ldb % E) || (reinterpret_cast<uintptr_t>(a.B) % (E * esz)))
+        return fail(AS_ERR_UNSUPPORTED, "spmm nnz-split: layout does not fit the vector width");
+    if (ceil_div(a.N, TILE) > 65535) return fail(AS_ERR_UNSUPPORTED, "spmm nnz-split: N too large");
+    const long nchunks = ceil_div(a.nnz, CH);
+    void *w = nullptr;
+    as_status st = scratch(ctx, sizeof(float) * static_cast<size_t>(2 * nchunks) * a.N, &w);
+    if (st != AS_OK) return st;
+    float *carry = static_cast<float *>(w);
+    if (nchunks > 0) {
+        dim3 g1(static_cast<unsigned>(ceil_div(nchunks, kThreads / G)),
+                static_cast<unsigned>(ceil_div(a.N, TILE)));
+        spmm_nnzsplit<T, VB, G, CPL><<<g1, kThreads, 0, s>>>(
+            a.M, a.K, a.N, a.nnz, CH, a.rowptr, a.colind, static_cast<const T *>(a.val),
+            static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, carry, a.status);
+        dim3 g2(static_cast<unsigned>(nchunks),
+                static_cast<unsigned>(ceil_div(a.N, kThreads) < 64 ? ceil_div(a.N, kThreads) : 64));
+        spmm_nnz_fixup<<<g2, kThreads, 0, s>>>(a.M, a.N, a.nnz, CH, a.rowptr, carry, a.C, a.ldc,
+                                               a.beta);
+        ctx->launches += 2;
+    }
+    spmm_empty_rows<<<static_cast<unsigned>(ceil_div(a.M, kThreads / 32)), kThreads, 0, s>>>(
+        a.M, a.N, a.rowptr, a.C, a.ldc, a.beta);
+    ctx->launches++;
+    return check_cuda(cudaGetLastError(), "spmm nnz-split launch");
+}
+
+}  // namespace
+
+as_status spmm_nnz_launch(as_ctx *ctx, int dtype, int vb, int group, int cpl, int chunk,
+                          const SpmmArgs &a, cudaStream_t s) {
+#define AS_NNZ_CASE(T, VBV, G, C)                                      \
+    if (vb == VBV && group == G && cpl == C) return launch<T, VBV, G, C>(ctx, a, chunk, s);
+    if (dtype == 0) {
+        AS_NNZ_CASE(float, 16, 8, 1) AS_NNZ_CASE(float, 16, 16, 1) AS_NNZ_CASE(float, 16, 32, 1)
+        AS_NNZ_CASE(float, 16, 32, 2) AS_NNZ_CASE(float, 4, 32, 1) AS_NNZ_CASE(float, 4, 32, 2)
+    } else {
+        AS_NNZ_CASE(uint16_t, 16, 8, 1) AS_NNZ_CASE(uint16_t, 16, 16, 1)
+        AS_NNZ_CASE(uint16_t, 16, 32, 1) AS_NNZ_CASE(uint16_t, 16, 32, 2)
+        AS_NNZ_CASE(uint16_t, 4, 32, 1) AS_NNZ_CASE(uint16_t, 4, 32, 2)
+    }
+#undef AS_NNZ_CASE
+    return fail(AS_ERR_UNSUPPORTED, "spmm nnz-split: configuration not instantiated");
+}
+
+}  // namespace as

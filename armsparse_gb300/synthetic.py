@@ -190,3 +190,48 @@ def spmm_4096_d001(seed: int = 0) -> CSR:
 def sddmm_4096_d01(seed: int = 0) -> CSR:
     """SDDMM pattern: 4096 x 4096, density 0.1 (1,677,721 entries), values U(0.5,1.5)."""
     return uniform_csr(4096, 4096, int(0.1 * 4096 * 4096), seed, values="u0515")
+
+
+# ---- generators on the GPU (for the selector sweep: hundreds of matrices up to 1M rows) -------
+def _csr_from_sorted_keys_torch(keys, n_rows, n_cols):
+    import torch
+    rows = keys // n_cols
+    cols = (keys % n_cols).to(torch.int32)
+    counts = torch.bincount(rows, minlength=n_rows)
+    rowptr = torch.zeros(n_rows + 1, dtype=torch.int64, device=keys.device)
+    rowptr[1:] = torch.cumsum(counts, 0)
+    return rowptr.to(torch.int32), cols
+
+
+def powerlaw_csr_device(n, exponent, mean_nnz, seed, device, n_cols=None):
+    """Same distribution as powerlaw_csr (Pareto row lengths rescaled to the mean, uniform
+    column ids), drawn with a seeded torch generator on the device; duplicate column ids in a
+    row are merged, so rows may come out slightly shorter than drawn."""
+    import torch
+    n_cols = n if n_cols is None else n_cols
+    g = torch.Generator(device=device).manual_seed(seed)
+    u = torch.rand(n, generator=g, device=device, dtype=torch.float64)
+    raw = (1.0 - u) ** (-1.0 / (exponent - 1.0))
+    lengths = raw * (mean_nnz / raw.mean())
+    lengths = torch.clamp(torch.floor(lengths + torch.rand(n, generator=g, device=device,
+                                                           dtype=torch.float64)), 0, n_cols).long()
+    rows = torch.repeat_interleave(torch.arange(n, device=device), lengths)
+    cols = torch.randint(0, n_cols, (rows.numel(),), generator=g, device=device)
+    keys = torch.unique(rows * n_cols + cols)  # sorted
+    rowptr, colind = _csr_from_sorted_keys_torch(keys, n, n_cols)
+    val = torch.rand(colind.numel(), generator=g, device=device) * 2 - 1
+    return rowptr, colind, val
+
+
+def banded_csr_device(n, bandwidth, seed, device):
+    import torch
+    g = torch.Generator(device=device).manual_seed(seed)
+    half = bandwidth // 2
+    offs = torch.arange(-half, bandwidth - half, device=device)
+    rows = torch.arange(n, device=device).repeat_interleave(offs.numel())
+    cols = rows + offs.repeat(n)
+    keep = (cols >= 0) & (cols < n)
+    keys = rows[keep] * n + cols[keep]
+    rowptr, colind = _csr_from_sorted_keys_torch(keys, n, n)
+    val = torch.rand(colind.numel(), generator=g, device=device) * 2 - 1
+    return rowptr, colind, val

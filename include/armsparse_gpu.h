@@ -61,10 +61,11 @@ as_status as_csr_validate(as_ctx *ctx, int n_rows, int n_cols, int nnz, const in
  * Replaces: rowBaseSpmm3 / rowBaseSpmm2 / origin (SDMM.cpp:90, :65, :422), the GCN op's
  * csr_spmm_kernel (gcn/pytorch-custom/spmm.cpp:49-71) and spmm_cuda
  * (gcn/pytorch-custom/spmm_kernel.cu:425-458).
- * Row-split variants are bit-identical to rowBaseSpmm3: every output is one fused
- * multiply-add chain over the row's entries in CSR order. NNZ-split variants balance
- * skewed rows and add the partial sums of a split row in a fixed order (deterministic,
- * not bit-identical). */
+ * Row-split ("rowsplit_*") and shared-memory-staged ("bulk_*") variants are bit-identical to
+ * rowBaseSpmm3: every output is one fused multiply-add chain over the row's entries in CSR
+ * order. NNZ-split variants ("nnzsplit_*") balance skewed rows by cutting the entries into
+ * fixed chunks; a row that crosses a chunk boundary gets its partial sums added in chunk
+ * order (deterministic, not bit-identical for those rows; rows inside one chunk are). */
 as_status as_spmm_csr_f32(as_ctx *ctx, int M, int K, int N, int nnz, const int *rowptr,
                           const int *colind, const float *val, const float *B, long ldb,
                           float *C, long ldc, float beta, int variant, void *stream);

@@ -241,3 +241,39 @@ def bf16_round(a) -> np.ndarray:
     r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
     r = np.where(nan, (u | 0x400000) & 0xFFFF0000, r).astype(np.uint32)
     return r.view(np.float32).reshape(a.shape)
+
+
+# ------------------------------------------------------------------------------------------
+# Dense-network reference for the selector's kernels (float64 numpy)
+# ------------------------------------------------------------------------------------------
+def mlp_linear_fwd(X, W, b=None, relu=False):
+    Y = np.asarray(X, np.float64) @ np.asarray(W, np.float64).T
+    if b is not None:
+        Y = Y + np.asarray(b, np.float64)
+    return np.maximum(Y, 0.0) if relu else Y
+
+
+def mlp_linear_bwd(dY, X, W, relu_in=None):
+    dY = np.asarray(dY, np.float64)
+    dX = dY @ np.asarray(W, np.float64)
+    if relu_in is not None:
+        dX = np.where(np.asarray(relu_in) > 0, dX, 0.0)
+    return dX, dY.T @ np.asarray(X, np.float64), dY.sum(axis=0)
+
+
+def mlp_softmax_xent(Z, T, scale=1.0):
+    Z = np.asarray(Z, np.float64)
+    T = np.asarray(T, np.float64)
+    m = Z.max(axis=1, keepdims=True)
+    lse = m + np.log(np.exp(Z - m).sum(axis=1, keepdims=True))
+    P = np.exp(Z - lse)
+    return -(T * (Z - lse)).sum(axis=1), (P - T) * scale
+
+
+def mlp_adam(p, g, m, v, lr, b1, b2, eps, wd, step):
+    g = g + wd * p
+    m = b1 * m + (1 - b1) * g
+    v = b2 * v + (1 - b2) * g * g
+    mh = m / (1 - b1 ** step)
+    vh = v / (1 - b2 ** step)
+    return p - lr * mh / (np.sqrt(vh) + eps), m, v

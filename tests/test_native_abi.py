@@ -35,7 +35,14 @@ def test_library_exports_every_declared_symbol(native_lib):
 
 def test_every_header_is_checked():
     assert sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h")) == \
-        ["armsparse_drivers.h", "armsparse_gpu.h"]
+        ["armsparse_drivers.h", "armsparse_gpu.h", "armsparse_mlp.h"]
+
+
+def test_mlp_header_symbols_exported(native_lib):
+    from armsparse_gb300 import _native
+    syms = declared_symbols("armsparse_mlp.h")
+    assert len(syms) == 4
+    assert all(hasattr(native_lib, s) for s in syms) and set(syms) <= set(_native.SIGNATURES)
 
 
 def test_drivers_library_exports_reference_signatures():
@@ -77,9 +84,9 @@ def test_variant_table(native_lib):
     assert native_lib.as_spmm_variant_name(0, 0) == b"unknown"
     # the default pick for the 4096-wide fp32 case uses 128-bit loads and full warps
     v = native_lib.as_spmm_default_variant(0, 4096, 4096, 4096, 167772, 4096, 4096, 256, 256)
-    assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v16_g32_c4_u4"
+    assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v8_g32_c4_u4"
     v = native_lib.as_spmm_default_variant(0, 100, 100, 3, 500, 3, 3, 256, 256)
-    assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v4_g4_c1_u4"
+    assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v4_g32_c2_u8"
 
 
 @pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU error path")
