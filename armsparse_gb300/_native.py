@@ -39,6 +39,8 @@ SIGNATURES = {
     "as_sddmm_csr_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P, _P]),
     "as_sddmm_csr_bf16x3": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P, _P]),
     "as_csr2csc_static": (_I, [_I, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
+    "as_sddmm_csr_bf16x3_v": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P, _I, _P]),
+    "as_sddmm_bf16x3_variant_count": (_I, []),
     "as_sddmm_coo_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P, _P]),
     "as_csr2csc": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
     "as_spmm_csr_f64": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, ctypes.c_double, _P]),

@@ -254,7 +254,7 @@ as_status as_spmv_vcsr4_f32(as_ctx *c, int M, int K, int nslots, const int *rowp
 static as_status sddmm_common(const char *fn, bool tc, as_ctx *c, int M, int N, int K, int nnz,
                               const int *rowptr, const int *colind, const float *aval,
                               const float *X, long ldx, const float *Y, long ldy, float *out,
-                              void *stream) {
+                              void *stream, int variant = 0) {
     if (!c) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": ctx is NULL");
     as_status st = check_csr_args(fn, M, N, nnz, rowptr, colind, nullptr, false);
     if (st != AS_OK) return st;
@@ -266,7 +266,12 @@ static as_status sddmm_common(const char *fn, bool tc, as_ctx *c, int M, int N, 
         return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": leading dimension below K");
     DeviceGuard g(c->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (tc) return sddmm_bf16x3_launch(c, M, N, K, nnz, rowptr, colind, aval, X, ldx, Y, ldy, out, s);
+    if (tc) {
+        if (variant < 0 || variant > sddmm_tc_variant_count())
+            return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": unknown variant");
+        return sddmm_bf16x3_launch(c, M, N, K, nnz, rowptr, colind, aval, X, ldx, Y, ldy, out,
+                                   variant, s);
+    }
     return sddmm_f32_launch(c, M, N, K, nnz, rowptr, colind, aval, X, ldx, Y, ldy, out, s);
 }
 
@@ -283,6 +288,15 @@ as_status as_sddmm_csr_bf16x3(as_ctx *c, int M, int N, int K, int nnz, const int
     return sddmm_common("as_sddmm_csr_bf16x3", true, c, M, N, K, nnz, rowptr, colind, aval, X,
                         ldx, Y, ldy, out, stream);
 }
+
+as_status as_sddmm_csr_bf16x3_v(as_ctx *c, int M, int N, int K, int nnz, const int *rowptr,
+                                const int *colind, const float *aval, const float *X, long ldx,
+                                const float *Y, long ldy, float *out, int variant, void *stream) {
+    return sddmm_common("as_sddmm_csr_bf16x3_v", true, c, M, N, K, nnz, rowptr, colind, aval, X,
+                        ldx, Y, ldy, out, stream, variant);
+}
+
+int as_sddmm_bf16x3_variant_count(void) { return sddmm_tc_variant_count(); }
 
 as_status as_sddmm_coo_f32(as_ctx *c, int M, int N, int K, int nnz, const int *rowind,
                            const int *colind, const float *aval, const float *X, long ldx,

@@ -62,7 +62,8 @@ as_status sddmm_coo_f32_launch(as_ctx *ctx, int M, int N, int K, int nnz, const 
                                const float *Y, long ldy, float *out, cudaStream_t s);
 as_status sddmm_bf16x3_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
                               const int *colind, const float *aval, const float *X, long ldx,
-                              const float *Y, long ldy, float *out, cudaStream_t s);
+                              const float *Y, long ldy, float *out, int variant, cudaStream_t s);
+int sddmm_tc_variant_count();
 
 as_status spmm_f64_launch(as_ctx *ctx, int M, int K, int N, int nnz, const int *rowptr,
                           const int *colind, const double *val, const double *B, long ldb,

@@ -307,6 +307,243 @@ sddmm_tc_kernel(const __grid_constant__ CUtensorMap tmXhi, const __grid_constant
     }
 }
 
+// ---- persistent form --------------------------------------------------------------------
+// One CTA per SM walks the tiles (grouped order: 16 row tiles at a time across all column
+// tiles, for L2 reuse of the operand panels) and skips tiles without pattern entries (a
+// pre-pass marks them). Two accumulators in tensor memory (2 x BN columns): the epilogue
+// warps drain tile j from one while the MMA thread accumulates tile j+1 in the other. BK is
+// the K width of a pipeline stage: 64 (128-byte swizzle, 2 stages of 96 KB) or 32 (64-byte
+// swizzle, 4 stages of 48 KB).
+template <int BN, int BK>
+struct PSmem {
+    static constexpr int kTileA = kBM * BK * 2;
+    static constexpr int kTileB = BN * BK * 2;
+    static constexpr int kStage = 2 * kTileA + 2 * kTileB;
+    static constexpr int kStages = BK == 32 ? 4 : 2;
+    static constexpr int kStaging = 128 * 33 * 4;
+    static constexpr int kBytes = 1024 + kStages * kStage + kStaging + 512;
+    static constexpr int kLayout = BK == 32 ? 4 : 2;  // descriptor swizzle: 64B / 128B
+    static constexpr int kSBO = 8 * BK * 2;           // bytes between 8-row core groups
+};
+constexpr int kGroupM = 16;
+
+__device__ __forceinline__ uint64_t desc_kmajor(uint32_t saddr, int sbo, int layout) {
+    uint64_t d = 0;
+    d |= static_cast<uint64_t>((saddr >> 4) & 0x3FFFu);
+    d |= static_cast<uint64_t>(1) << 16;
+    d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFF) << 32;
+    d |= static_cast<uint64_t>(1) << 46;
+    d |= static_cast<uint64_t>(layout) << 61;
+    return d;
+}
+
+__device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int &tm, int &tn) {
+    const int per = kGroupM * tiles_n;
+    const int g = t / per, r = t - g * per;
+    const int rows = min(kGroupM, tiles_m - g * kGroupM);
+    tm = g * kGroupM + r % rows;
+    tn = r / rows;
+}
+
+template <int BN, int BK>
+__global__ void __launch_bounds__(kThreads, 1)
+sddmm_tc_persistent(const __grid_constant__ CUtensorMap tmXhi, const __grid_constant__ CUtensorMap tmXlo,
+                    const __grid_constant__ CUtensorMap tmYhi, const __grid_constant__ CUtensorMap tmYlo,
+                    int M, int N, int nkb, int nnz, const int *__restrict__ rowptr,
+                    const int *__restrict__ colind, const float *__restrict__ aval,
+                    float *__restrict__ out, const unsigned char *__restrict__ occ, int tiles_m,
+                    int tiles_n, unsigned *status) {
+    using L = PSmem<BN, BK>;
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    uint8_t *smem = smem_raw + ((1024 - (raw & 1023)) & 1023);
+    uint8_t *stages = smem;
+    float *staging = reinterpret_cast<float *>(smem + L::kStages * L::kStage);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + L::kStages * L::kStage + L::kStaging);
+    uint64_t *empty = full + L::kStages;
+    uint64_t *accf = empty + L::kStages;
+    uint64_t *acce = accf + 2;
+    uint64_t *done = acce + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ntiles = tiles_m * tiles_n;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < L::kStages; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        mbar_init(&accf[0], 1);
+        mbar_init(&accf[1], 1);
+        mbar_init(&acce[0], 128);
+        mbar_init(&acce[1], 128);
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmem_slot)),
+                     "r"(2 * BN)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int it = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                int tm, tn;
+                tile_coords(t, tiles_m, tiles_n, tm, tn);
+                if (!occ[static_cast<long>(tm) * tiles_n + tn]) continue;
+                for (int kb = 0; kb < nkb; ++kb, ++it) {
+                    const int s = it % L::kStages, r = it / L::kStages;
+                    if (r > 0 && !mbar_wait(&empty[s], (r - 1) & 1, abort_flag, status)) {
+                        ok = false;
+                        break;
+                    }
+                    uint8_t *st = stages + s * L::kStage;
+                    mbar_expect_tx(&full[s], L::kStage);
+                    tma_load_2d(st, &tmXhi, &full[s], kb * BK, tm * kBM);
+                    tma_load_2d(st + L::kTileA, &tmXlo, &full[s], kb * BK, tm * kBM);
+                    tma_load_2d(st + 2 * L::kTileA, &tmYhi, &full[s], kb * BK, tn * BN);
+                    tma_load_2d(st + 2 * L::kTileA + L::kTileB, &tmYlo, &full[s], kb * BK, tn * BN);
+                }
+            }
+            for (int d = it - L::kStages > 0 ? it - L::kStages : 0; d < it; ++d)
+                for (unsigned i = 0; i < kSpinLimit; ++i)
+                    if (mbar_try_wait(&full[d % L::kStages], (d / L::kStages) & 1)) break;
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_bf16(kBM, BN);
+            int it = 0, j = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                int tm, tn;
+                tile_coords(t, tiles_m, tiles_n, tm, tn);
+                if (!occ[static_cast<long>(tm) * tiles_n + tn]) continue;
+                const int buf = j & 1, use = j >> 1;
+                if (use > 0 && !mbar_wait(&acce[buf], (use - 1) & 1, abort_flag, status)) break;
+                tc_fence_after();
+                const uint32_t d = tmem + buf * BN;
+                for (int kb = 0; kb < nkb; ++kb, ++it) {
+                    const int s = it % L::kStages, r = it / L::kStages;
+                    if (!mbar_wait(&full[s], r & 1, abort_flag, status)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t base = smem_u32(stages + s * L::kStage);
+                    const uint64_t ahi = desc_kmajor(base, L::kSBO, L::kLayout);
+                    const uint64_t alo = desc_kmajor(base + L::kTileA, L::kSBO, L::kLayout);
+                    const uint64_t bhi = desc_kmajor(base + 2 * L::kTileA, L::kSBO, L::kLayout);
+                    const uint64_t blo = desc_kmajor(base + 2 * L::kTileA + L::kTileB, L::kSBO, L::kLayout);
+#pragma unroll
+                    for (int k = 0; k < BK / 16; ++k) {
+                        const uint64_t adv = static_cast<uint64_t>(k * 32 >> 4);
+                        mma_bf16(d, ahi + adv, bhi + adv, idesc, (kb | k) != 0);
+                        mma_bf16(d, ahi + adv, blo + adv, idesc, 1u);
+                        mma_bf16(d, alo + adv, bhi + adv, idesc, 1u);
+                    }
+                    mma_commit(&empty[s]);
+                }
+                if (!ok) break;
+                mma_commit(&accf[buf]);
+                ++j;
+            }
+            // every MMA this thread issued has completed once `done` flips
+            mma_commit(done);
+            for (unsigned i = 0; i < kSpinLimit; ++i)
+                if (mbar_try_wait(done, 0)) break;
+        }
+    } else {
+        const int q = warp & 3;
+        float *my = staging + (32 * q + lane) * 33;
+        const uint32_t lane_addr = tmem + (static_cast<uint32_t>(32 * q) << 16);
+        int j = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            int tm, tn;
+            tile_coords(t, tiles_m, tiles_n, tm, tn);
+            if (!occ[static_cast<long>(tm) * tiles_n + tn]) continue;
+            const int buf = j & 1, use = j >> 1;
+            const int c0 = tn * BN;
+            const int row = tm * kBM + 32 * q + lane;
+            int e = 0, hi = 0;
+            if (row < M) {
+                int lo;
+                row_range(rowptr, row, nnz, status, lo, hi);
+                int a = lo, b = hi;
+                while (a < b) {
+                    const int m = (a + b) >> 1;
+                    if (__ldg(colind + m) < c0) a = m + 1; else b = m;
+                }
+                e = a;
+            }
+            const bool ready = __all_sync(0xffffffffu, mbar_wait(&accf[buf], use & 1, abort_flag, status));
+            if (!ready) break;
+            tc_fence_after();
+            int prev = -1;
+#pragma unroll 1
+            for (int jj = 0; jj < BN / 32; ++jj) {
+                uint32_t v[32];
+                tmem_ld32(lane_addr + buf * BN + 32 * jj, v);
+                const int cend = c0 + 32 * (jj + 1);
+                if (e < hi && __ldg(colind + e) < cend) {
+#pragma unroll
+                    for (int u = 0; u < 32; ++u) my[u] = __uint_as_float(v[u]);
+                    while (e < hi) {
+                        const int c = __ldg(colind + e);
+                        if (c >= cend) break;
+                        if (c <= prev || c >= N) {
+                            flag(status, kFlagBadColind);
+                            out[e] = 0.0f;
+                        } else {
+                            const float dv = my[c - (cend - 32)];
+                            out[e] = aval ? __ldg(aval + e) * dv : dv;
+                        }
+                        prev = c;
+                        ++e;
+                    }
+                }
+            }
+            tc_fence_before();
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acce[buf])) : "memory");
+            ++j;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN)
+                     : "memory");
+    }
+}
+
+// occ[tm * tiles_n + tn] = 1 for every output tile holding a pattern entry (one warp per row;
+// concurrent stores of the same value).
+__global__ void __launch_bounds__(256)
+mark_tiles(int M, int N, int nnz, const int *__restrict__ rowptr, const int *__restrict__ colind,
+           int BN, int tiles_n, unsigned char *__restrict__ occ) {
+    const long w = (static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= M) return;
+    int lo = __ldg(rowptr + w), hi = __ldg(rowptr + w + 1);
+    if (lo < 0 || hi < lo || hi > nnz) return;
+    unsigned char *rowocc = occ + (w / kBM) * static_cast<long>(tiles_n);
+    for (int e = lo + lane; e < hi; e += 32) {
+        const int c = __ldg(colind + e);
+        if (c >= 0 && c < N) rowocc[c / BN] = 1;
+    }
+}
+
 // hi = bf16(x), lo = bf16(x - hi); columns [K, Kp) are zero. Blocks stride over rows,
 // threads over groups of four columns.
 template <bool VEC>
@@ -376,16 +613,18 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// 2-D bf16 tensor map: rows x Kp (row-major), box = box_rows x 64, 128-byte swizzle.
-bool make_map(CUtensorMap *m, const uint16_t *base, long rows, int Kp, int box_rows) {
+// 2-D bf16 tensor map: rows x Kp (row-major), box = box_rows x box_k, swizzle = box_k * 2 bytes.
+bool make_map(CUtensorMap *m, const uint16_t *base, long rows, int Kp, int box_rows,
+              int box_k = kBK) {
     auto enc = encode_fn();
     if (!enc) return false;
     cuuint64_t dims[2] = {static_cast<cuuint64_t>(Kp), static_cast<cuuint64_t>(rows)};
     cuuint64_t strides[1] = {static_cast<cuuint64_t>(Kp) * 2};
-    cuuint32_t box[2] = {static_cast<cuuint32_t>(kBK), static_cast<cuuint32_t>(box_rows)};
+    cuuint32_t box[2] = {static_cast<cuuint32_t>(box_k), static_cast<cuuint32_t>(box_rows)};
     cuuint32_t estr[2] = {1, 1};
     return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<uint16_t *>(base), dims, strides,
-               box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+               box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               box_k == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
                CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -410,11 +649,50 @@ as_status launch_tiles(as_ctx *ctx, int M, int N, int Kp, int nnz, const int *ro
     return check_cuda(cudaGetLastError(), "sddmm_bf16x3 launch");
 }
 
+int sm_count() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 148;
+}
+
+template <int BN, int BK>
+as_status launch_persistent(as_ctx *ctx, int M, int N, int Kp, int nnz, const int *rowptr,
+                            const int *colind, const float *aval, float *out, const uint16_t *xhi,
+                            const uint16_t *xlo, const uint16_t *yhi, const uint16_t *ylo,
+                            unsigned char *occ, cudaStream_t s) {
+    CUtensorMap mxh, mxl, myh, myl;
+    if (!make_map(&mxh, xhi, M, Kp, kBM, BK) || !make_map(&mxl, xlo, M, Kp, kBM, BK) ||
+        !make_map(&myh, yhi, N, Kp, BN, BK) || !make_map(&myl, ylo, N, Kp, BN, BK))
+        return fail(AS_ERR_CUDA, "sddmm_bf16x3: cuTensorMapEncodeTiled failed");
+    const int tiles_m = static_cast<int>(ceil_div(M, kBM)), tiles_n = static_cast<int>(ceil_div(N, BN));
+    cudaError_t e = cudaMemsetAsync(occ, 0, static_cast<size_t>(tiles_m) * tiles_n, s);
+    if (e != cudaSuccess) return check_cuda(e, "sddmm_bf16x3: occupancy clear");
+    mark_tiles<<<static_cast<unsigned>(ceil_div(static_cast<long>(M) * 32, 256)), 256, 0, s>>>(
+        M, N, nnz, rowptr, colind, BN, tiles_n, occ);
+    const int smem = PSmem<BN, BK>::kBytes;
+    e = cudaFuncSetAttribute(sddmm_tc_persistent<BN, BK>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return check_cuda(e, "sddmm_bf16x3: shared memory attribute");
+    const long ntiles = static_cast<long>(tiles_m) * tiles_n;
+    const int grid = static_cast<int>(ntiles < sm_count() ? ntiles : sm_count());
+    sddmm_tc_persistent<BN, BK><<<grid, kThreads, smem, s>>>(
+        mxh, mxl, myh, myl, M, N, Kp / BK, nnz, rowptr, colind, aval, out, occ, tiles_m, tiles_n,
+        ctx->d_status);
+    ctx->launches += 2;
+    return check_cuda(cudaGetLastError(), "sddmm_bf16x3 persistent launch");
+}
+
 }  // namespace
 
+int sddmm_tc_variant_count() { return 3; }
+
+// variant: 1 = one tile per CTA (K block 64), 2 = persistent, K block 64, 3 = persistent,
+// K block 32 (deeper pipeline); 0 = library choice.
 as_status sddmm_bf16x3_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
                               const int *colind, const float *aval, const float *X, long ldx,
-                              const float *Y, long ldy, float *out, cudaStream_t s) {
+                              const float *Y, long ldy, float *out, int variant, cudaStream_t s) {
+    if (variant == 0) variant = 1;
     if (M == 0) return fail(AS_ERR_INVALID_CSR, "sddmm: nnz > 0 with zero rows");
     check_sorted_rows<<<static_cast<unsigned>(ceil_div(static_cast<long>(M) * 32, 256)), 256, 0, s>>>(
         M, N, nnz, rowptr, colind, ctx->d_status);
@@ -427,8 +705,9 @@ as_status sddmm_bf16x3_launch(as_ctx *ctx, int M, int N, int K, int nnz, const i
     const int Kp = static_cast<int>(ceil_div(K, kBK) * kBK);
     const size_t xs = static_cast<size_t>(M) * Kp * 2, ys = static_cast<size_t>(N) * Kp * 2;
     auto al = [](size_t b) { return (b + 1023) & ~size_t(1023); };
+    const size_t occ_bytes = static_cast<size_t>(ceil_div(M, kBM)) * ceil_div(N, 256);
     void *w = nullptr;
-    as_status st = scratch(ctx, 2 * al(xs) + 2 * al(ys), &w);
+    as_status st = scratch(ctx, 2 * al(xs) + 2 * al(ys) + al(occ_bytes), &w);
     if (st != AS_OK) return st;
     uint8_t *p = static_cast<uint8_t *>(w);
     uint16_t *xhi = reinterpret_cast<uint16_t *>(p);
@@ -446,6 +725,13 @@ as_status sddmm_bf16x3_launch(as_ctx *ctx, int M, int N, int K, int nnz, const i
     ctx->launches += 2;
     st = check_cuda(cudaGetLastError(), "sddmm_bf16x3 split");
     if (st != AS_OK) return st;
+    unsigned char *occ = p + 2 * al(xs) + 2 * al(ys);
+    if (variant == 2)
+        return launch_persistent<256, 64>(ctx, M, N, Kp, nnz, rowptr, colind, aval, out, xhi, xlo,
+                                          yhi, ylo, occ, s);
+    if (variant == 3)
+        return launch_persistent<256, 32>(ctx, M, N, Kp, nnz, rowptr, colind, aval, out, xhi, xlo,
+                                          yhi, ylo, occ, s);
     return launch_tiles<256>(ctx, M, N, Kp, nnz, rowptr, colind, aval, out, xhi, xlo, yhi, ylo, s);
 }
 

@@ -36,16 +36,20 @@ def _spmm(rowptr, colind, values, feat, variant=0):
 
 class SPMMFunction(torch.autograd.Function):
     """out = A * feat, A given as CSR (rowptr, colind, edge_weight_csr) and as CSC (colptr, rowind,
-    edge_weight_csc). Same ``apply`` signature as the reference (op.py:9)."""
+    edge_weight_csc). Same ``apply`` signature as the reference (op.py:9), plus an optional
+    ``variants`` pair (kernel variant ids for the forward CSR product and the backward CSC
+    product; 0 = library choice)."""
 
     @staticmethod
     def forward(ctx, rowptr, colind, colptr, rowind, feat, edge_weight_csr=None,
-                edge_weight_csc=None):
+                edge_weight_csc=None, variants=None):
         if edge_weight_csr is None:
             raise ValueError("SPMMFunction needs edge values (pass ones for an unweighted graph)")
-        out = _spmm(rowptr, colind, edge_weight_csr, feat)
+        fwd_v, bwd_v = variants if variants is not None else (0, 0)
+        out = _spmm(rowptr, colind, edge_weight_csr, feat, fwd_v)
         ctx.save_for_backward(rowptr, colind, colptr, rowind, feat, edge_weight_csr,
                               edge_weight_csc)
+        ctx.bwd_variant = bwd_v
         return out
 
     @staticmethod
@@ -58,12 +62,12 @@ class SPMMFunction(torch.autograd.Function):
                 raise RuntimeError("backward of SPMMFunction needs the edge values in CSC order "
                                    "(SPMMFunction.apply(rowptr, colind, colptr, rowind, feat, "
                                    "values_csr, values_csc))")
-            grad_feat = _spmm(colptr, rowind, w_csc, g)
+            grad_feat = _spmm(colptr, rowind, w_csc, g, ctx.bwd_variant)
         if ctx.needs_input_grad[5]:
             gf = g if g.dtype in (torch.float32, torch.float64) else g.float()
             ff = feat if feat.dtype == gf.dtype else feat.to(gf.dtype)
             grad_w = S.sddmm(rowptr, colind, gf, ff.contiguous()).to(w_csr.dtype)
-        return None, None, None, None, grad_feat, grad_w, None
+        return None, None, None, None, grad_feat, grad_w, None, None
 
 
 class Graph:
@@ -75,12 +79,25 @@ class Graph:
         self.n_rows = rowptr.numel() - 1
         self.n_cols = self.n_rows if n_cols is None else n_cols
         self._csc = None
+        self.selector = None  # a selector.Selector: per-width kernel choice (None = library choice)
+        self._plans = {}
 
     @property
     def csc(self):
         if self._csc is None:
             self._csc = S.csr2csc(self.rowptr, self.colind, self.values, self.n_cols)
         return self._csc
+
+    def plan(self, N: int, dtype=torch.float32):
+        """(forward, backward) kernel variants for dense width N, from the selector."""
+        if self.selector is None or dtype == torch.float64:
+            return (0, 0)
+        key = (N, dtype)
+        if key not in self._plans:
+            colptr, _, _ = self.csc
+            self._plans[key] = (self.selector.choose(self.rowptr, self.n_cols, N, dtype),
+                                self.selector.choose(colptr, self.n_rows, N, dtype))
+        return self._plans[key]
 
     @classmethod
     def from_csr(cls, a, device) -> "Graph":
@@ -90,7 +107,7 @@ class Graph:
     def aggregate(self, feat: torch.Tensor) -> torch.Tensor:
         colptr, rowind, vcsc = self.csc
         return SPMMFunction.apply(self.rowptr, self.colind, colptr, rowind, feat, self.values,
-                                  vcsc)
+                                  vcsc, self.plan(feat.shape[1], feat.dtype))
 
 
 def glorot_(w: torch.Tensor) -> None:
@@ -125,7 +142,8 @@ class GCNConv(torch.nn.Module):
     def deg_inv_sqrt(indptr):
         return (1 / torch.sqrt((indptr[1:] - indptr[:-1]).float())).unsqueeze(dim=1)
 
-    def forward(self, x, rowptr, colind, colptr, rowind, edge_weight_csr, edge_weight_csc):
+    def forward(self, x, rowptr, colind, colptr, rowind, edge_weight_csr, edge_weight_csc,
+                variants=None):
         x = torch.matmul(x, self.weight)
         if not self.cached or self.cached_result is None:
             if self.normalize:
@@ -137,7 +155,7 @@ class GCNConv(torch.nn.Module):
         if self.normalize:
             x = x * out_norm
         out = SPMMFunction.apply(rowptr, colind, colptr, rowind, x, edge_weight_csr,
-                                 edge_weight_csc)
+                                 edge_weight_csc, variants)
         if self.normalize:
             out = out * in_norm
         if self.bias is not None:
@@ -156,9 +174,9 @@ class Net(torch.nn.Module):
     def forward(self, x, g: Graph):
         colptr, rowind, vcsc = g.csc
         args = (g.rowptr, g.colind, colptr, rowind, g.values, vcsc)
-        x = F.relu(self.conv1(x, *args))
+        x = F.relu(self.conv1(x, *args, variants=g.plan(self.conv1.out_channels, x.dtype)))
         x = F.dropout(x, training=self.training)
-        x = self.conv2(x, *args)
+        x = self.conv2(x, *args, variants=g.plan(self.conv2.out_channels, x.dtype))
         return F.log_softmax(x, dim=1)
 
 

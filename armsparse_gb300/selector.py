@@ -94,7 +94,8 @@ def sweep(configs, device=None, reps=3, log=None):
         g = torch.Generator(device=device).manual_seed(cfg["seed"] + 7)
         B = (torch.rand(cfg["n"], cfg["N"], generator=g, device=device) * 2 - 1).to(dt)
         ids = variant_ids(CANDIDATES, dt)
-        t = tuner.autotune_spmm(rowptr, colind, val.to(dt), B, variants=ids, reps=reps)
+        t = tuner.autotune_spmm(rowptr, colind, val.to(dt), B, variants=ids, reps=reps,
+                                max_ratio=4.0)
         feats = tuner.features(rowptr.cpu().numpy(), cfg["n"], cfg["N"], dt == torch.bfloat16)
         rec = {"cfg": cfg, "features": feats.tolist(), "nnz": int(colind.numel()),
                "times_ms": [x.ms for x in t]}

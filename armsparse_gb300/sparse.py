@@ -168,7 +168,8 @@ def spmv_vcsr4(vrowptr, vcolind, vval, x, y=None, beta: float = 0.0):
     return y
 
 
-def sddmm(rowptr, colind, X, Y, aval=None, out=None, tensor_cores: bool = False):
+def sddmm(rowptr, colind, X, Y, aval=None, out=None, tensor_cores: bool = False,
+          variant: int = 0):
     """out[e] = aval[e] * <X[row(e)], Y[col(e)]> (aval None -> unscaled, the reference's
     sddmm_cuda_csr). X: M x K, Y: N x K, fp32. tensor_cores selects the tcgen05 split-bf16
     path."""
@@ -191,11 +192,16 @@ def sddmm(rowptr, colind, X, Y, aval=None, out=None, tensor_cores: bool = False)
     K = X.shape[1]
     ldx = X.stride(0) if M > 1 else K
     ldy = Y.stride(0) if Y.shape[0] > 1 else K
-    fn = N.load().as_sddmm_csr_bf16x3 if tensor_cores else N.load().as_sddmm_csr_f32
     ctx = N.context(dev.index)
-    N.check(fn(ctx.handle, M, Y.shape[0], K, nnz, _ptr(rowptr), _ptr(colind), _ptr(aval),
-               _ptr(X), ldx, _ptr(Y), ldy, _ptr(out), _stream(dev)),
-            "as_sddmm_csr_bf16x3" if tensor_cores else "as_sddmm_csr_f32")
+    if tensor_cores:
+        N.check(N.load().as_sddmm_csr_bf16x3_v(ctx.handle, M, Y.shape[0], K, nnz, _ptr(rowptr),
+                                               _ptr(colind), _ptr(aval), _ptr(X), ldx, _ptr(Y),
+                                               ldy, _ptr(out), int(variant), _stream(dev)),
+                "as_sddmm_csr_bf16x3_v")
+    else:
+        N.check(N.load().as_sddmm_csr_f32(ctx.handle, M, Y.shape[0], K, nnz, _ptr(rowptr),
+                                          _ptr(colind), _ptr(aval), _ptr(X), ldx, _ptr(Y), ldy,
+                                          _ptr(out), _stream(dev)), "as_sddmm_csr_f32")
     return out
 
 

@@ -235,3 +235,26 @@ def banded_csr_device(n, bandwidth, seed, device):
     rowptr, colind = _csr_from_sorted_keys_torch(keys, n, n)
     val = torch.rand(colind.numel(), generator=g, device=device) * 2 - 1
     return rowptr, colind, val
+
+
+def powerlaw_graph_device(n_nodes, n_edges, exponent, seed, device, self_loops=True):
+    """Directed power-law graph on the device (Chung-Lu endpoint sampling with Pareto weights,
+    both endpoints drawn from the same weights), duplicates merged, self-loops added; CSR
+    (rowptr, colind) with values 1. For the large GCN layer: 2.4M nodes, 62M edges."""
+    import torch
+    g = torch.Generator(device=device).manual_seed(seed)
+    w = (1.0 - torch.rand(n_nodes, generator=g, device=device, dtype=torch.float64)) ** \
+        (-1.0 / (exponent - 1.0))
+    cdf = torch.cumsum(w / w.sum(), 0)
+    cdf[-1] = 1.0
+    u = torch.searchsorted(cdf, torch.rand(n_edges, generator=g, device=device, dtype=torch.float64))
+    v = torch.searchsorted(cdf, torch.rand(n_edges, generator=g, device=device, dtype=torch.float64))
+    u = u.clamp_(max=n_nodes - 1)
+    v = v.clamp_(max=n_nodes - 1)
+    keys = u * n_nodes + v
+    if self_loops:
+        ids = torch.arange(n_nodes, device=device)
+        keys = torch.cat([keys, ids * n_nodes + ids])
+    keys = torch.unique(keys)
+    rowptr, colind = _csr_from_sorted_keys_torch(keys, n_nodes, n_nodes)
+    return rowptr, colind, torch.ones(colind.numel(), device=device)

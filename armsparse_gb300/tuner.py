@@ -57,15 +57,17 @@ class Timing:
 
 
 def autotune_spmm(rowptr, colind, val, B, C=None, variants=None, reps: int = 5,
-                  flush: bool = True) -> list[Timing]:
-    """Time every SpMM variant (or the given ids) on these arguments."""
-    dtype = 0 if B.dtype == torch.float32 else 1
+                  flush: bool = True, max_ratio: float | None = None) -> list[Timing]:
+    """Time every SpMM variant (or the given ids) on these arguments. With max_ratio, a
+    variant whose first timed run is more than max_ratio x the best time so far keeps that
+    single measurement (it cannot be the pick; this bounds the sweep time)."""
     names = S.spmm_variants(B.dtype)
     ids = variants or list(range(1, len(names) + 1))
     M = rowptr.numel() - 1
     if C is None:
         C = torch.empty((M, B.shape[1]), dtype=torch.float32, device=B.device)
     out = []
+    best_ms = None
     for v in ids:
         try:
             S.spmm(rowptr, colind, val, B, C=C, variant=v)
@@ -74,10 +76,12 @@ def autotune_spmm(rowptr, colind, val, B, C=None, variants=None, reps: int = 5,
                 out.append(Timing(v, names[v - 1], None))
                 continue
             raise
-        ms = time_cuda(lambda: S.spmm(rowptr, colind, val, B, C=C, variant=v), reps=reps,
-                       flush=flush, device=B.device)
+        fn = lambda: S.spmm(rowptr, colind, val, B, C=C, variant=v)
+        ms = time_cuda(fn, reps=1, warmup=0, flush=flush, device=B.device)
+        if not (max_ratio and best_ms is not None and ms > max_ratio * best_ms):
+            ms = time_cuda(fn, reps=reps, warmup=0, flush=flush, device=B.device)
+        best_ms = ms if best_ms is None else min(best_ms, ms)
         out.append(Timing(v, names[v - 1], ms))
-    del dtype
     return out
 
 

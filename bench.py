@@ -45,7 +45,47 @@ FALLBACK_BF16_TFLOPS = 1900.0
 # ------------------------------------------------------------------------------------------
 # Workloads
 # ------------------------------------------------------------------------------------------
-class SpmmF32:
+class Workload:
+    """Throughput workloads: value = algorithmic bytes / time (GB/s), higher is better."""
+    higher_is_better = True
+    bound = "hbm"
+
+    def value(self, seconds: float, ws: int = 1) -> float:
+        return ws * self.bytes / seconds / 1e9
+
+    def roofline(self, kernel_ms, hbm, bf16, src):
+        if self.bound == "tensor":
+            achieved = self.flops / (kernel_ms * 1e-3) / 1e12
+            return {"bound": "tensor", "achieved": round(achieved, 3), "peak": bf16,
+                    "unit": "TFLOP/s", "frac": round(achieved / bf16, 5),
+                    "traffic": profiled_traffic(self.profile), "peak_source": src,
+                    "kernel": self.kernel,
+                    "achieved_is": "algorithmic (sampled) flops 2*nnz*K per step",
+                    "executed_tflops": round(self.exec_flops / (kernel_ms * 1e-3) / 1e12, 2),
+                    "executed_frac": round(self.exec_flops / (kernel_ms * 1e-3) / 1e12 / bf16, 4)}
+        achieved = self.bytes / (kernel_ms * 1e-3) / 1e9
+        return {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "traffic": profiled_traffic(self.profile),
+                "peak_source": src, "kernel": self.kernel}
+
+    def cpu_value(self, threads: int, budget_s: float):
+        """The reference algorithm on the host cores for about budget_s seconds."""
+        self.cpu_step(threads)  # warm
+        t0 = time.perf_counter()
+        total, calls = 0, 0
+        while True:
+            total += self.cpu_step(threads)
+            calls += 1
+            if time.perf_counter() - t0 >= budget_s:
+                break
+        dt = time.perf_counter() - t0
+        return total / dt / 1e9, f"{calls} full calls in {dt:.1f} s"
+
+    def flush_between_steps(self) -> bool:
+        return True
+
+
+class SpmmF32(Workload):
     name = "spmm_f32"
     metric = "SpMM GB/s (algorithmic bytes) and % HBM roofline"
     unit = "GB/s"
@@ -109,7 +149,7 @@ class SpmmF32:
         return 4 * (rows + 1) + 8 * nnz + 4 * self.K * self.N + 4 * rows * self.N
 
 
-class _Generic:
+class _Generic(Workload):
     """End to end through the public Python API: pinned host inputs copied in, the op,
     the output copied back to pinned host memory, all inside the timed region."""
     bound = "hbm"
@@ -175,10 +215,12 @@ class SddmmTc(_Generic):
     def output(self):
         return self.out
 
+    variant = 0  # tensor-core kernel variant (0 = library choice); set by --tc-variant
+
     def step(self):
         import armsparse_gb300 as A
         A.sddmm(self.rp, self.ci, self.Xd, self.Yd, aval=self.v, out=self.out,
-                tensor_cores=self.tensor_cores)
+                tensor_cores=self.tensor_cores, variant=self.variant)
 
     def cpu_step(self, threads, rows=None):
         from oracle import oracle as O
@@ -202,7 +244,318 @@ class SddmmF32(SddmmTc):
     tensor_cores = False
 
 
-WORKLOADS = {c.name: c for c in [SpmmF32, SddmmTc, SddmmF32]}
+class _CpuSpmm:
+    """out = A * feat on the host with the oracle's restatement of the GCN op's kernel
+    (csr_spmm_kernel, gcn/pytorch-custom/spmm.cpp:49-71) -- the reference arm of the GCN
+    workload; backward uses the CSC arrays as op.py:30 does."""
+
+    @staticmethod
+    def make(threads):
+        import torch
+        from oracle import oracle as O
+
+        class F(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, feat, csr, csc):
+                ctx.csc = csc
+                rp, ci, v = csr
+                return torch.from_numpy(O.spmm_fma_chain_f32(rp, ci, v, feat.detach().numpy(),
+                                                             threads=threads))
+
+            @staticmethod
+            def backward(ctx, g):
+                cp, ri, v = ctx.csc
+                return (torch.from_numpy(O.spmm_fma_chain_f32(cp, ri, v, g.contiguous().numpy(),
+                                                              threads=threads)), None, None)
+        return F
+
+
+class GcnEpoch(Workload):
+    """One full-batch training epoch of the 2-layer GCN (gcn_custom.py:122-126) on the
+    PubMed-shaped synthetic graph: 19,717 nodes, 88,648 directed edges + self-loops =
+    108,365 entries, 500 features (10 % non-zero), hidden 64, 3 classes, Adam."""
+    name = "gcn_epoch"
+    metric = "GCN training epoch time (ms), 2-layer, 19,717 nodes, 500->64->3"
+    unit = "ms/epoch"
+    dtype = "f32"
+    kernel = "SpMM of layer 1 (N = 64)"
+    profile = "gcn_spmm_19717_n64"
+    higher_is_better = False
+
+    def __init__(self, seed=0):
+        from armsparse_gb300 import synthetic as S
+        self.a = S.powerlaw_graph(19717, 88648, seed=seed)
+        rng = np.random.default_rng(seed + 1)
+        x = np.zeros((19717, 500), np.float32)
+        m = rng.random(x.shape) < 0.1
+        x[m] = rng.random(int(m.sum())).astype(np.float32)
+        self.x = x
+        self.y = rng.integers(0, 3, 19717)
+        train = np.zeros(19717, bool)
+        for c in range(3):
+            train[np.flatnonzero(self.y == c)[:60]] = True
+        self.train = train
+        nnz = self.a.nnz
+        self.spmm_bytes = 4 * (19717 + 1) + 8 * nnz + 2 * 19717 * 64 * 4
+        self.bytes = self.spmm_bytes
+        self.config = {"workload": "GCN 2-layer training epoch, synthetic power-law graph "
+                                   "19,717 nodes / 108,365 nnz (incl. self-loops), 500->64->3, "
+                                   "Adam lr 0.01, dropout 0.5",
+                       "nodes": 19717, "nnz": nnz, "features": 500, "hidden": 64, "classes": 3,
+                       "l2": "flushed between epochs (256 MiB write, outside the timed events)"}
+
+    def value(self, seconds, ws=1):
+        return seconds * 1e3
+
+    def to_device(self, dev):
+        import torch
+        from armsparse_gb300 import gcn
+        self.dev = dev
+        self.xd = torch.from_numpy(self.x).to(dev)
+        self.yd = torch.from_numpy(self.y).to(dev)
+        self.td = torch.from_numpy(self.train).to(dev)
+        self.g = gcn.Graph.from_csr(self.a, dev)
+        self.g_plain = gcn.Graph.from_csr(self.a, dev)
+        try:
+            from armsparse_gb300 import selector
+            self.g.selector = selector.Selector.load()
+            self.config["kernels"] = "learned selector (armsparse_gb300/selector_model.json)"
+        except (OSError, ValueError):
+            self.config["kernels"] = "library default (no selector model file)"
+        torch.manual_seed(0)
+        self.model = gcn.Net(500, 64, 3).to(dev)
+        self.opt = gcn.make_optimizer(self.model)
+        torch.manual_seed(0)
+        self.model_plain = gcn.Net(500, 64, 3).to(dev)
+        self.opt_plain = gcn.make_optimizer(self.model_plain)
+        self.plan = self.g.plan(64, torch.float32), self.g.plan(3, torch.float32)
+
+    def step(self):
+        from armsparse_gb300 import gcn
+        self.loss = gcn.train_epoch(self.model, self.opt, self.xd, self.g, self.yd, self.td)
+
+    def plain_step(self):
+        from armsparse_gb300 import gcn
+        return gcn.train_epoch(self.model_plain, self.opt_plain, self.xd, self.g_plain, self.yd,
+                               self.td)
+
+    def roofline_ms(self, epoch_ms):
+        """Time of the dominant kernel of this project in the epoch: the layer-1 aggregation
+        (SpMM, N = 64), timed alone with CUDA events."""
+        import torch
+        import armsparse_gb300 as A
+        from armsparse_gb300 import tuner
+        B = torch.rand(19717, 64, device=self.dev)
+        C = torch.empty_like(B)
+        v = self.plan[0][0]
+        return tuner.time_cuda(lambda: A.spmm(self.g.rowptr, self.g.colind, self.g.values, B,
+                                              C=C, variant=v), reps=20)
+
+    def e2e_setup(self):
+        import torch
+        self.hx = torch.from_numpy(self.x).pin_memory()
+        self.h2d = self.hx.numel() * 4
+        self.d2h = 4
+
+    def e2e_step(self):
+        self.xd.copy_(self.hx, non_blocking=True)
+        self.step()
+        float(self.loss)
+
+    # --- reference arm: the same network on the host cores ---
+    def _cpu_setup(self, threads):
+        if getattr(self, "_cpu", None) is not None:
+            return
+        import torch
+        from oracle import oracle as O
+        torch.set_num_threads(threads)
+        a = self.a
+        cp, ri, cv = O.csr2csc(a.rowptr, a.colind, a.val, a.n_cols)
+        self._csr = (a.rowptr, a.colind, a.val)
+        self._csc = (cp, ri, cv)
+        self._F = _CpuSpmm.make(threads)
+        g = torch.Generator().manual_seed(0)
+        glorot = lambda i, o: ((torch.rand(i, o, generator=g) * 2 - 1) *
+                               (6.0 / (i + o)) ** 0.5).requires_grad_(True)
+        self._W1, self._W2 = glorot(500, 64), glorot(64, 3)
+        self._b1 = torch.zeros(64, requires_grad=True)
+        self._b2 = torch.zeros(3, requires_grad=True)
+        deg_r = np.diff(a.rowptr).astype(np.float32)
+        deg_c = np.diff(cp).astype(np.float32)
+        self._in = torch.from_numpy(1 / np.sqrt(deg_r))[:, None]
+        self._out = torch.from_numpy(1 / np.sqrt(deg_c))[:, None]
+        self._x = torch.from_numpy(self.x)
+        self._y = torch.from_numpy(self.y)
+        self._t = torch.from_numpy(self.train)
+        self._opt = torch.optim.Adam([dict(params=[self._W1, self._b1], weight_decay=5e-4),
+                                      dict(params=[self._W2, self._b2], weight_decay=0)], lr=0.01)
+        self._cpu = True
+
+    def cpu_step(self, threads):
+        import torch
+        import torch.nn.functional as Fn
+        self._cpu_setup(threads)
+        conv = lambda x, W, b: self._F.apply((x @ W) * self._out, self._csr, self._csc) * self._in + b
+        self._opt.zero_grad()
+        h = Fn.dropout(Fn.relu(conv(self._x, self._W1, self._b1)), training=True)
+        out = Fn.log_softmax(conv(h, self._W2, self._b2), dim=1)
+        Fn.nll_loss(out[self._t], self._y[self._t]).backward()
+        self._opt.step()
+        return 1
+
+    def cpu_aggregate(self, total, seconds, steps):
+        return seconds / steps * 1e3
+
+    def cpu_value(self, threads, budget_s):
+        self.cpu_step(threads)
+        t0 = time.perf_counter()
+        n = 0
+        while True:
+            self.cpu_step(threads)
+            n += 1
+            if time.perf_counter() - t0 >= budget_s:
+                break
+        dt = time.perf_counter() - t0
+        return dt / n * 1e3, f"{n} training epochs in {dt:.1f} s (torch CPU + restated csr_spmm_kernel)"
+
+    def extra(self):
+        """Plain path (library default kernels) vs the tuned path: epoch time and losses over
+        20 epochs from the same initial weights."""
+        import torch
+        from armsparse_gb300 import gcn, tuner
+        plain_ms = tuner.time_cuda(self.plain_step, reps=20, warmup=2, flush=False)
+        tuned_ms = tuner.time_cuda(self.step, reps=20, warmup=2, flush=False)
+        torch.manual_seed(1)
+        m1 = gcn.Net(500, 64, 3).to(self.dev)
+        torch.manual_seed(1)
+        m2 = gcn.Net(500, 64, 3).to(self.dev)
+        o1, o2 = gcn.make_optimizer(m1), gcn.make_optimizer(m2)
+        l1, l2 = [], []
+        for _ in range(20):
+            torch.manual_seed(_)
+            l1.append(float(gcn.train_epoch(m1, o1, self.xd, self.g_plain, self.yd, self.td)))
+            torch.manual_seed(_)
+            l2.append(float(gcn.train_epoch(m2, o2, self.xd, self.g, self.yd, self.td)))
+        return {"plain_ms_per_epoch": round(plain_ms, 4), "tuned_ms_per_epoch": round(tuned_ms, 4),
+                "plan_layer1": self.plan[0], "plan_layer2": self.plan[1],
+                "loss_max_abs_diff_20_epochs": max(abs(a - b) for a, b in zip(l1, l2))}
+
+
+class GcnLarge(Workload):
+    """One full-batch forward + backward of a 2-layer GCN on a large power-law graph (2.4M
+    nodes, 62M directed edges, exponent 2.1, + self-loops), 100-dim features, hidden 256, 47
+    classes, with the edge values trainable (their gradient is an SDDMM at the pattern).
+    Tuned path: learned-selector kernels, bf16 storage of the SpMM operands with fp32
+    accumulation; plain path (reported in `extra`): fp32, library-default kernels."""
+    name = "gcn_large"
+    metric = "GCN forward+backward time (ms), 2.4M nodes / 62M edges, 100->256->47"
+    unit = "ms/step"
+    dtype = "bf16 storage, fp32 accumulate"
+    kernel = "SpMM of layer 1 (N = 256)"
+    profile = "gcn_large_spmm_n256"
+    higher_is_better = False
+
+    def __init__(self, seed=0):
+        self.seed = seed
+        self.config = {"workload": "GCN 2-layer forward+backward with trainable edge values, "
+                                   "power-law graph 2.4M nodes, 62M directed edges (exp. 2.1) + "
+                                   "self-loops, 100->256->47",
+                       "nodes": 2_400_000, "edges": 62_000_000, "features": 100, "hidden": 256,
+                       "classes": 47, "l2": "inputs far larger than L2 (B alone is 0.5-2.4 GB)"}
+
+    def value(self, seconds, ws=1):
+        return seconds * 1e3
+
+    def flush_between_steps(self):
+        return False
+
+    def to_device(self, dev):
+        import torch
+        from armsparse_gb300 import gcn
+        from armsparse_gb300 import synthetic as S
+        self.dev = dev
+        rp, ci, val = S.powerlaw_graph_device(2_400_000, 62_000_000, 2.1, self.seed, dev)
+        n = 2_400_000
+        self.nnz = ci.numel()
+        self.config["nnz"] = self.nnz
+        self.bytes = 4 * (n + 1) + 8 * self.nnz + 2 * n * 256 * 2
+        deg = (rp[1:] - rp[:-1]).float()
+        self.g = gcn.Graph(rp, ci, (val / deg.sqrt().repeat_interleave(rp[1:] - rp[:-1])).contiguous())
+        self.g_plain = gcn.Graph(rp, ci, self.g.values)
+        try:
+            from armsparse_gb300 import selector
+            self.g.selector = selector.Selector.load()
+        except (OSError, ValueError):
+            pass
+        gen = torch.Generator(device=dev).manual_seed(self.seed + 1)
+        self.x = torch.rand(n, 100, generator=gen, device=dev)
+        self.y = torch.randint(0, 47, (n,), generator=gen, device=dev)
+        torch.manual_seed(0)
+        self.W1 = (torch.randn(100, 256, device=dev) * 0.1).requires_grad_(True)
+        self.W2 = (torch.randn(256, 47, device=dev) * 0.1).requires_grad_(True)
+        self.w = self.g.values.clone().requires_grad_(True)
+
+    def _layer(self, g, x, W, dtype, plan):
+        from armsparse_gb300 import gcn
+        colptr, rowind, vcsc = g.csc
+        h = (x @ W).to(dtype)
+        return gcn.SPMMFunction.apply(g.rowptr, g.colind, colptr, rowind, h, self.w, vcsc, plan)
+
+    def _step(self, g, dtype, tuned):
+        import torch.nn.functional as Fn
+        p1 = g.plan(256, dtype) if tuned else None
+        p2 = g.plan(47, dtype) if tuned else None
+        h = Fn.relu(self._layer(g, self.x, self.W1, dtype, p1).float())
+        out = self._layer(g, h, self.W2, dtype, p2).float()
+        loss = Fn.cross_entropy(out, self.y)
+        loss.backward()
+        self.W1.grad = self.W2.grad = self.w.grad = None
+        return loss.detach()
+
+    def step(self):
+        import torch
+        self.loss = self._step(self.g, torch.bfloat16, True)
+
+    def roofline_ms(self, step_ms):
+        import torch
+        import armsparse_gb300 as A
+        from armsparse_gb300 import tuner
+        B = torch.rand(self.g.n_rows, 256, device=self.dev).to(torch.bfloat16)
+        C = torch.empty(self.g.n_rows, 256, device=self.dev)
+        v = self.g.plan(256, torch.bfloat16)[0]
+        vb = self.g.values.to(torch.bfloat16)
+        return tuner.time_cuda(lambda: A.spmm(self.g.rowptr, self.g.colind, vb, B, C=C,
+                                              variant=v), reps=5, flush=False)
+
+    def e2e_setup(self):
+        self.hx = self.x.cpu().pin_memory()
+        self.h2d = self.hx.numel() * 4
+        self.d2h = 4
+
+    def e2e_step(self):
+        self.x.copy_(self.hx, non_blocking=True)
+        self.step()
+        float(self.loss)
+
+    def cpu_step(self, threads):
+        raise NotImplementedError("no CPU arm at this size (hours on the host cores)")
+
+    def cpu_value(self, threads, budget_s):
+        return float("nan"), "not run: the reference's CPU path at 62M edges takes hours"
+
+    def extra(self):
+        import torch
+        from armsparse_gb300 import tuner
+        plain_ms = tuner.time_cuda(lambda: self._step(self.g_plain, torch.float32, False),
+                                   reps=3, warmup=1, flush=False)
+        tuned_ms = tuner.time_cuda(lambda: self._step(self.g, torch.bfloat16, True), reps=3,
+                                   warmup=1, flush=False)
+        return {"plain_fp32_ms": round(plain_ms, 3), "tuned_bf16_ms": round(tuned_ms, 3),
+                "speedup": round(plain_ms / tuned_ms, 3),
+                "plan_256": self.g.plan(256, torch.bfloat16), "plan_47": self.g.plan(47, torch.bfloat16)}
+
+
+WORKLOADS = {c.name: c for c in [SpmmF32, SddmmTc, SddmmF32, GcnEpoch, GcnLarge]}
 
 
 
@@ -308,11 +661,11 @@ def run_reference(args, wl_cls):
     for _ in range(args.steps):
         total += wl.cpu_step(threads)
     dt = time.perf_counter() - t0
-    value = total / dt / 1e9
+    value = wl.cpu_aggregate(total, dt, args.steps) if hasattr(wl, "cpu_aggregate") else total / dt / 1e9
     line = {
         "impl": "reference", "metric": wl.metric, "value": round(value, 3), "unit": wl.unit,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
+        "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": wl.higher_is_better,
         "scaling": "weak", "vs_baseline": None, "dtype": wl.dtype, "data": "synthetic (seeded)",
         "config": wl.config,
         "cpu_baseline": {"value": round(value, 3), "unit": wl.unit, "cores": threads,
@@ -328,19 +681,10 @@ def run_reference(args, wl_cls):
 
 def cpu_baseline(wl, budget_s=10.0):
     threads = os.cpu_count() or 1
-    wl.cpu_step(threads)  # warm
-    t0 = time.perf_counter()
-    total, calls = 0, 0
-    while True:
-        total += wl.cpu_step(threads)
-        calls += 1
-        if time.perf_counter() - t0 >= budget_s:
-            break
-    dt = time.perf_counter() - t0
-    return {"value": round(total / dt / 1e9, 3), "unit": wl.unit, "cores": threads,
-            "kind": "port",
-            "sample": f"{calls} full calls in {dt:.1f} s (oracle restatement of the reference "
-                      "kernel, OpenMP over all host cores)"}
+    v, sample = wl.cpu_value(threads, budget_s)
+    return {"value": round(v, 3), "unit": wl.unit, "cores": threads, "kind": "port",
+            "sample": sample + " (oracle restatement of the reference kernel, OpenMP over all "
+                               "host cores)"}
 
 
 def run_ours(args, wl_cls):
@@ -360,7 +704,8 @@ def run_ours(args, wl_cls):
     stream = torch.cuda.current_stream(dev)
 
     for _ in range(max(args.warmup, 3)):
-        flush.fill_(1)
+        if wl.flush_between_steps():
+            flush.fill_(1)
         wl.step()
     torch.cuda.synchronize(dev)
 
@@ -376,7 +721,8 @@ def run_ours(args, wl_cls):
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         for i in range(args.steps):
-            flush.fill_(i & 0xFF)
+            if wl.flush_between_steps():
+                flush.fill_(i & 0xFF)
             evs[i][0].record(stream)
             wl.step()
             evs[i][1].record(stream)
@@ -390,7 +736,7 @@ def run_ours(args, wl_cls):
         t = torch.tensor([kernel_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         kernel_ms = float(t.item())
-    value = ws * wl.bytes / (kernel_ms * 1e-3) / 1e9
+    value = wl.value(kernel_ms * 1e-3, ws)
 
     # end to end through the reference-facing host call
     wl.e2e_setup()
@@ -406,26 +752,16 @@ def run_ours(args, wl_cls):
         t = torch.tensor([e2e_s], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-    e2e_value = ws * wl.bytes / e2e_s / 1e9
+    e2e_value = wl.value(e2e_s, ws)
 
     hbm, bf16, src = measured_peaks()
-    if getattr(wl, "bound", "hbm") == "tensor":
-        achieved = wl.flops / (kernel_ms * 1e-3) / 1e12
-        roof = {"bound": "tensor", "achieved": round(achieved, 3), "peak": bf16,
-                "unit": "TFLOP/s", "frac": round(achieved / bf16, 5),
-                "traffic": profiled_traffic(wl.profile), "peak_source": src, "kernel": wl.kernel,
-                "achieved_is": "algorithmic (sampled) flops 2*nnz*K per step",
-                "executed_tflops": round(wl.exec_flops / (kernel_ms * 1e-3) / 1e12, 2),
-                "executed_frac": round(wl.exec_flops / (kernel_ms * 1e-3) / 1e12 / bf16, 4)}
-    else:
-        achieved = wl.bytes / (kernel_ms * 1e-3) / 1e9
-        roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 4), "traffic": profiled_traffic(wl.profile),
-                "peak_source": src, "kernel": wl.kernel}
+    roof = wl.roofline(wl.roofline_ms(kernel_ms) if hasattr(wl, "roofline_ms") else kernel_ms,
+                       hbm, bf16, src)
     line = {
         "metric": wl.metric, "value": round(value, 3), "unit": wl.unit, "n_gpus": ws,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(kernel_ms, 5),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": wl.dtype,
+        "higher_is_better": wl.higher_is_better, "scaling": "weak", "vs_baseline": None,
+        "dtype": wl.dtype,
         "data": "synthetic (seeded)", "config": dict(wl.config, parallelism=f"replicas x{ws}"),
         "roofline": roof,
         "e2e": {"value": round(e2e_value, 3), "unit": wl.unit,
@@ -436,6 +772,8 @@ def run_ours(args, wl_cls):
         "clocks": clk.summary(),
         "wall_s_timed_region": round(wall, 4),
     }
+    if hasattr(wl, "extra"):
+        line["extra"] = wl.extra()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
     if rank == 0:
@@ -454,8 +792,12 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="spmm_f32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--tc-variant", type=int, default=0,
+                    help="tensor-core SDDMM kernel variant (0 = library choice)")
     args = ap.parse_args()
     wl_cls = WORKLOADS[args.workload]
+    if hasattr(wl_cls, "variant"):
+        wl_cls.variant = args.tc_variant
     if args.impl == "reference":
         return run_reference(args, wl_cls)
     return run_ours(args, wl_cls)

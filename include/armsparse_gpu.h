@@ -112,6 +112,16 @@ as_status as_sddmm_csr_bf16x3(as_ctx *ctx, int M, int N, int K, int nnz, const i
                               const int *colind, const float *aval, const float *X, long ldx,
                               const float *Y, long ldy, float *out, void *stream);
 
+/* as_sddmm_csr_bf16x3 with an explicit kernel variant (tuning): 0 = library choice,
+ * 1 = one 128 x 256 output tile per CTA, 2 = persistent CTAs with two tensor-memory
+ * accumulators (epilogue of one tile under the MMAs of the next), 64-wide K stages,
+ * 3 = persistent with 32-wide K stages (4-deep pipeline). Same results for every variant
+ * up to FP32 accumulation order. */
+as_status as_sddmm_csr_bf16x3_v(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
+                                const int *colind, const float *aval, const float *X, long ldx,
+                                const float *Y, long ldy, float *out, int variant, void *stream);
+int as_sddmm_bf16x3_variant_count(void);
+
 /* COO form: entry e has row rowind[e] and column colind[e] (any order); X, Y, out as above.
  * Replaces sddmm_cuda_coo (gcn/pytorch-custom/sddmm.cu:427-457). */
 as_status as_sddmm_coo_f32(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowind,

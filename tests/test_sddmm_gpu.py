@@ -59,6 +59,7 @@ def test_malformed_pattern_is_flagged():
 # lo*lo and r terms are <= ~4 * 2^-18 |x y|, plus FP32 accumulation. Bar: scaled error
 # (relative to sum |x_k y_k|) below 3e-5 per output.
 TC_TOL = 3e-5
+TC_VARIANTS = (1, 2, 3)  # one tile per CTA; persistent with 64-wide / 32-wide K stages
 
 
 @pytest.mark.parametrize("M,Ncol,K,nnz", [(128, 256, 64, 3000), (300, 500, 100, 15000),
@@ -69,12 +70,13 @@ def test_tc_against_fp64(oracle, M, Ncol, K, nnz):
     X = S.dense_normal((M, K), 11)
     Y = S.dense_normal((Ncol, K), 12)
     rp, ci, av = csr_dev(a)
-    for aval in (None, a.val):
-        out = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=None if aval is None else av,
-                      tensor_cores=True)
-        r64, ab = oracle.sddmm_f64(a.rowptr, a.colind, X, Y, aval=aval)
-        err = oracle.scaled_err(out.cpu().numpy(), r64, ab)
-        assert err.max() < TC_TOL, err.max()
+    for variant in TC_VARIANTS:
+        for aval in (None, a.val):
+            out = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=None if aval is None else av,
+                          tensor_cores=True, variant=variant)
+            r64, ab = oracle.sddmm_f64(a.rowptr, a.colind, X, Y, aval=aval)
+            err = oracle.scaled_err(out.cpu().numpy(), r64, ab)
+            assert err.max() < TC_TOL, (variant, err.max())
     A.sync_status()
 
 
@@ -83,11 +85,12 @@ def test_tc_sparse_tiles_and_determinism(oracle):
     X = S.dense_normal((3000, 256), 13)
     Y = S.dense_normal((3000, 256), 14)
     rp, ci, av = csr_dev(a)
-    o1 = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=av, tensor_cores=True)
-    o2 = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=av, tensor_cores=True)
-    assert torch.equal(o1, o2)
     r64, ab = oracle.sddmm_f64(a.rowptr, a.colind, X, Y, aval=a.val)
-    assert oracle.scaled_err(o1.cpu().numpy(), r64, ab).max() < TC_TOL
+    for variant in TC_VARIANTS:
+        o1 = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=av, tensor_cores=True, variant=variant)
+        o2 = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=av, tensor_cores=True, variant=variant)
+        assert torch.equal(o1, o2)
+        assert oracle.scaled_err(o1.cpu().numpy(), r64, ab).max() < TC_TOL, variant
     A.sync_status()
 
 
@@ -97,12 +100,14 @@ def test_tc_full_size_4096_density_01(oracle):
     X = S.dense_normal((4096, 4096), 1)
     Y = S.dense_normal((4096, 4096), 2)
     rp, ci, av = csr_dev(a)
-    out = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=av, tensor_cores=True)
     out32 = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=av)
     r64, ab = oracle.sddmm_f64(a.rowptr, a.colind, X, Y, aval=a.val)
-    e_tc = oracle.scaled_err(out.cpu().numpy(), r64, ab)
     e_32 = oracle.scaled_err(out32.cpu().numpy(), r64, ab)
-    assert e_tc.max() < TC_TOL and e_32.max() < 1e-5
+    assert e_32.max() < 1e-5
+    for variant in TC_VARIANTS:
+        out = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=av, tensor_cores=True, variant=variant)
+        e_tc = oracle.scaled_err(out.cpu().numpy(), r64, ab)
+        assert e_tc.max() < TC_TOL, variant
     A.sync_status()
 
 
