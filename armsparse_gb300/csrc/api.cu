@@ -214,6 +214,10 @@ as_status as_spmm_csr_bf16(as_ctx *c, int M, int K, int N, int nnz, const int *r
 }
 
 int as_spmm_variant_count(int dtype) { return spmm_variant_count(dtype); }
+int as_spmm_variant_supported(int dtype, int variant, int N, long ldb, long ldc, const void *B,
+                              const void *C) {
+    return spmm_variant_supported(dtype, variant, N, ldb, ldc, B, C) ? 1 : 0;
+}
 const char *as_spmm_variant_name(int dtype, int variant) {
     return spmm_variant_name(dtype, variant);
 }

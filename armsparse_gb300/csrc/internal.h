@@ -43,6 +43,8 @@ as_status spmm_nnz_launch(as_ctx *ctx, int dtype, int vb, int group, int cpl, in
 as_status spmm_bulk_launch(as_ctx *ctx, int dtype, int lane_bytes, int stages, const SpmmArgs &a,
                            cudaStream_t s);
 int spmm_variant_count(int dtype);
+bool spmm_variant_supported(int dtype, int variant, int N, long ldb, long ldc, const void *B,
+                            const void *C);
 const char *spmm_variant_name(int dtype, int variant);
 int spmm_default_variant(int dtype, int M, int K, int N, int nnz, long ldb, long ldc,
                          const void *B, const void *C);

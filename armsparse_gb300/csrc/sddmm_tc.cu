@@ -692,7 +692,7 @@ int sddmm_tc_variant_count() { return 3; }
 as_status sddmm_bf16x3_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
                               const int *colind, const float *aval, const float *X, long ldx,
                               const float *Y, long ldy, float *out, int variant, cudaStream_t s) {
-    if (variant == 0) variant = 1;
+    if (variant == 0) variant = 3;  // persistent, 4-stage pipeline: fastest on GB300
     if (M == 0) return fail(AS_ERR_INVALID_CSR, "sddmm: nnz > 0 with zero rows");
     check_sorted_rows<<<static_cast<unsigned>(ceil_div(static_cast<long>(M) * 32, 256)), 256, 0, s>>>(
         M, N, nnz, rowptr, colind, ctx->d_status);

@@ -18,65 +18,92 @@
 namespace as {
 namespace {
 
+// Vector loads of B: Raw is the register form a load lands in (bf16 stays packed until the
+// FMA that consumes it, so a deep unroll keeps more bytes in flight per register).
 template <typename T, int VB>
 struct Vec;
 template <>
 struct Vec<float, 16> {
     static constexpr int E = 4;
+    using Raw = float4;
+    __device__ static Raw raw(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
+    __device__ static float at(const Raw &r, int i) {
+        return i == 0 ? r.x : i == 1 ? r.y : i == 2 ? r.z : r.w;
+    }
     __device__ static void load(const float *p, float *o) {
-        float4 v = __ldg(reinterpret_cast<const float4 *>(p));
-        o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+        const Raw r = raw(p);
+        o[0] = r.x; o[1] = r.y; o[2] = r.z; o[3] = r.w;
     }
 };
 template <>
 struct Vec<float, 8> {
     static constexpr int E = 2;
+    using Raw = float2;
+    __device__ static Raw raw(const float *p) { return __ldg(reinterpret_cast<const float2 *>(p)); }
+    __device__ static float at(const Raw &r, int i) { return i == 0 ? r.x : r.y; }
     __device__ static void load(const float *p, float *o) {
-        float2 v = __ldg(reinterpret_cast<const float2 *>(p));
-        o[0] = v.x; o[1] = v.y;
+        const Raw r = raw(p);
+        o[0] = r.x; o[1] = r.y;
     }
 };
 template <>
 struct Vec<float, 4> {
     static constexpr int E = 1;
+    using Raw = float;
+    __device__ static Raw raw(const float *p) { return __ldg(p); }
+    __device__ static float at(const Raw &r, int) { return r; }
     __device__ static void load(const float *p, float *o) { o[0] = __ldg(p); }
 };
+__device__ __forceinline__ float bf16_lo(unsigned w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16_hi(unsigned w) { return __uint_as_float(w & 0xffff0000u); }
 template <>
 struct Vec<uint16_t, 16> {
     static constexpr int E = 8;
+    using Raw = uint4;
+    __device__ static Raw raw(const uint16_t *p) { return __ldg(reinterpret_cast<const uint4 *>(p)); }
+    __device__ static float at(const Raw &r, int i) {
+        const unsigned w = (i >> 1) == 0 ? r.x : (i >> 1) == 1 ? r.y : (i >> 1) == 2 ? r.z : r.w;
+        return (i & 1) ? bf16_hi(w) : bf16_lo(w);
+    }
     __device__ static void load(const uint16_t *p, float *o) {
-        uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
-        unsigned w[4] = {v.x, v.y, v.z, v.w};
+        const Raw r = raw(p);
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            o[2 * i] = __uint_as_float(w[i] << 16);
-            o[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
-        }
+        for (int i = 0; i < 8; ++i) o[i] = at(r, i);
     }
 };
 template <>
 struct Vec<uint16_t, 8> {
     static constexpr int E = 4;
+    using Raw = uint2;
+    __device__ static Raw raw(const uint16_t *p) { return __ldg(reinterpret_cast<const uint2 *>(p)); }
+    __device__ static float at(const Raw &r, int i) {
+        const unsigned w = (i >> 1) == 0 ? r.x : r.y;
+        return (i & 1) ? bf16_hi(w) : bf16_lo(w);
+    }
     __device__ static void load(const uint16_t *p, float *o) {
-        uint2 v = __ldg(reinterpret_cast<const uint2 *>(p));
-        o[0] = __uint_as_float(v.x << 16); o[1] = __uint_as_float(v.x & 0xffff0000u);
-        o[2] = __uint_as_float(v.y << 16); o[3] = __uint_as_float(v.y & 0xffff0000u);
+        const Raw r = raw(p);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) o[i] = at(r, i);
     }
 };
 template <>
 struct Vec<uint16_t, 4> {
     static constexpr int E = 2;
+    using Raw = unsigned;
+    __device__ static Raw raw(const uint16_t *p) { return __ldg(reinterpret_cast<const unsigned *>(p)); }
+    __device__ static float at(const Raw &r, int i) { return (i & 1) ? bf16_hi(r) : bf16_lo(r); }
     __device__ static void load(const uint16_t *p, float *o) {
-        unsigned v = __ldg(reinterpret_cast<const unsigned *>(p));
-        o[0] = __uint_as_float(v << 16); o[1] = __uint_as_float(v & 0xffff0000u);
+        const Raw r = raw(p);
+        o[0] = bf16_lo(r); o[1] = bf16_hi(r);
     }
 };
 template <>
 struct Vec<uint16_t, 2> {
     static constexpr int E = 1;
-    __device__ static void load(const uint16_t *p, float *o) {
-        o[0] = bf16_to_f32(__ldg(reinterpret_cast<const unsigned short *>(p)));
-    }
+    using Raw = unsigned short;
+    __device__ static Raw raw(const uint16_t *p) { return __ldg(reinterpret_cast<const unsigned short *>(p)); }
+    __device__ static float at(const Raw &r, int) { return __uint_as_float(static_cast<unsigned>(r) << 16); }
+    __device__ static void load(const uint16_t *p, float *o) { o[0] = at(raw(p), 0); }
 };
 
 __device__ __forceinline__ float to_f32(float v) { return v; }
@@ -163,7 +190,9 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         }
         const int cnt = min(GROUP, hi - base);
         int t = 0;
-        // U entries per step: all their B loads are issued before the FMAs, in CSR order
+        // U entries per step: all their B loads are issued before the FMAs (branch-free:
+        // idle lanes and flagged entries load an in-bounds element and contribute nothing),
+        // then the FMAs run in CSR order.
         for (; t + U <= cnt; t += U) {
             int kk[U];
             float vv[U];
@@ -172,27 +201,27 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 kk[u] = __shfl_sync(gmask, k, t + u, GROUP);
                 vv[u] = __shfl_sync(gmask, v, t + u, GROUP);
             }
-            float b[U][CPL][E];
+            typename V::Raw b[U][CPL];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const T *brow = B + static_cast<long>(kk[u] < 0 ? 0 : kk[u]) * ldb;
 #pragma unroll
                 for (int j = 0; j < CPL; ++j) {
                     const int c = tile0 + (j * GROUP + g) * E;
-                    if (c < N && kk[u] >= 0) {
-                        V::load(brow + c, b[u][j]);
-                    } else {
-#pragma unroll
-                        for (int i = 0; i < E; ++i) b[u][j][i] = 0.0f;
-                    }
+                    b[u][j] = V::raw(brow + (c < N ? c : 0));
                 }
             }
+            // keep the compiler from sinking loads into the FMA sequence: all U * CPL loads of
+            // the step are in flight before the first FMA waits on one
+            asm volatile("" ::: "memory");
 #pragma unroll
-            for (int u = 0; u < U; ++u)
+            for (int u = 0; u < U; ++u) {
+                const float vu = kk[u] < 0 ? 0.0f : vv[u];
 #pragma unroll
                 for (int j = 0; j < CPL; ++j)
 #pragma unroll
-                    for (int i = 0; i < E; ++i) acc[j][i] = fmaf(b[u][j][i], vv[u], acc[j][i]);
+                    for (int i = 0; i < E; ++i) acc[j][i] = fmaf(V::at(b[u][j], i), vu, acc[j][i]);
+            }
         }
         for (; t < cnt; ++t) {
             const int kk = __shfl_sync(gmask, k, t, GROUP);
@@ -349,6 +378,28 @@ int spmm_default_variant(int dtype, int M, int K, int N, int nnz, long ldb, long
             return find_variant(dtype, list[i].vb, list[i].g, list[i].cpl, list[i].u);
     // any layout: scalar lanes
     return find_variant(dtype, esz, 32, N > 32 ? 2 : 1, 8);
+}
+
+// Whether `variant` can serve this layout (the launch would not return AS_ERR_UNSUPPORTED).
+bool spmm_variant_supported(int dtype, int variant, int N, long ldb, long ldc, const void *B,
+                            const void *C) {
+    if (variant < 1 || variant > spmm_variant_count(dtype)) return false;
+    const Variant &v = dtype == 0 ? kF32[variant - 1] : kBF16[variant - 1];
+    const int esz = dtype == 0 ? 4 : 2;
+    const uintptr_t pb = reinterpret_cast<uintptr_t>(B), pc = reinterpret_cast<uintptr_t>(C);
+    if (v.kind == 0) {
+        const int tile = (v.vb / esz) * v.group * v.cpl;
+        return vb_ok(dtype, v.vb, N, ldb, ldc, B, C) && ceil_div(N, tile) <= 65535;
+    }
+    if (v.kind == 1) {  // bulk: E = lane bytes / esz, tile = 32 * E
+        const int E = v.vb / esz, tile = 32 * E;
+        return N % E == 0 && (ldb * esz) % 16 == 0 && ldc % 4 == 0 && pb % 16 == 0 &&
+               pc % 16 == 0 && (static_cast<long>(N % tile) * esz) % 16 == 0 &&
+               ceil_div(N, tile) <= 65535;
+    }
+    const int E = v.vb / esz;  // nnz-split
+    return N % E == 0 && ldb % E == 0 && pb % (E * esz) == 0 &&
+           ceil_div(N, E * v.group * v.cpl) <= 65535;
 }
 
 as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cudaStream_t s) {

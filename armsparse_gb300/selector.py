@@ -278,7 +278,12 @@ class Selector:
         feats = tuner.features(rp, n_cols, N, dtype == torch.bfloat16)
         order = np.argsort(-host_forward(self.model, feats))
         ids = variant_ids(self.model["candidates"], dtype)
-        v = ids[int(order[0])]
+        # best-scored candidate that can run this width (e.g. vector kernels need N % width)
+        v = 0
+        for i in order:
+            if S.spmm_variant_supported(ids[int(i)], N, dtype):
+                v = ids[int(i)]
+                break
         if key is not None:
             self._cache[(key, N, dtype)] = v
         return v

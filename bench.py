@@ -555,7 +555,133 @@ class GcnLarge(Workload):
                 "plan_256": self.g.plan(256, torch.bfloat16), "plan_47": self.g.plan(47, torch.bfloat16)}
 
 
-WORKLOADS = {c.name: c for c in [SpmmF32, SddmmTc, SddmmF32, GcnEpoch, GcnLarge]}
+class SpmvF32(_Generic):
+    """y = A*x on the SpMV driver's matrix (4096 x 4096, density 0.01, 167,772 entries): a
+    1.4 MB problem, bound by launch latency; `extra` reports the per-call time when 100 calls
+    are replayed from a CUDA graph, and the 1x4-blocked layout of the reference."""
+    name = "spmv"
+    metric = "SpMV GB/s (algorithmic bytes), CSR fp32"
+    unit = "GB/s"
+    dtype = "f32"
+    kernel = "spmv_csr"
+    profile = "spmv_csr_4096_d001"
+
+    def __init__(self, seed=0):
+        from armsparse_gb300 import synthetic as S
+        self.a = S.spmm_4096_d001(seed)
+        self.x = S.dense_uniform(4096, seed + 1)
+        nnz = self.a.nnz
+        self.bytes = 4 * 4097 + 8 * nnz + 4 * 4096 + 4 * 4096
+        self.config = {"workload": "spmv_csr y=A*x, A 4096x4096 uniform density 0.01 (167,772 nnz)",
+                       "M": 4096, "K": 4096, "nnz": nnz, "alg_bytes_per_step": self.bytes,
+                       "l2": "flushed between steps (256 MiB write, outside the timed events)"}
+
+    def to_device(self, dev):
+        import torch
+        self.dev = dev
+        t = lambda a: torch.from_numpy(a).to(dev)
+        self.rp, self.ci, self.v, self.xd = t(self.a.rowptr), t(self.a.colind), t(self.a.val), t(self.x)
+        self.y = torch.empty(4096, device=dev)
+
+    def inputs(self):
+        return {"rp": self.rp, "ci": self.ci, "v": self.v, "x": self.xd}
+
+    def output(self):
+        return self.y
+
+    def step(self):
+        import armsparse_gb300 as A
+        A.spmv(self.rp, self.ci, self.v, self.xd, y=self.y)
+
+    def cpu_step(self, threads, rows=None):
+        from oracle import oracle as O
+        if not hasattr(self, "_v4"):
+            self._v4 = O.csr_to_vcsr4(self.a.rowptr, self.a.colind, self.a.val)
+        vr, vc, vv = self._v4
+        O.spmv_vcsr4_f32(vr, vc, vv, self.x, threads=threads)
+        return self.bytes
+
+    def extra(self):
+        import torch
+        import armsparse_gb300 as A
+        from oracle import oracle as O
+        vr, vc, vv = O.csr_to_vcsr4(self.a.rowptr, self.a.colind, self.a.val)
+        t = lambda a: torch.from_numpy(a).to(self.dev)
+        vrd, vcd, vvd = t(vr), t(vc), t(vv)
+        yv = torch.empty(4096, device=self.dev)
+        s = torch.cuda.Stream(self.dev)
+        out = {}
+        for name, fn in (("csr", self.step),
+                         ("vcsr4", lambda: A.spmv_vcsr4(vrd, vcd, vvd, self.xd, y=yv))):
+            with torch.cuda.stream(s):
+                fn()
+                s.synchronize()
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g, stream=s):
+                    for _ in range(100):
+                        fn()
+            g.replay()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(10):
+                g.replay()
+            e1.record()
+            e1.synchronize()
+            us = e0.elapsed_time(e1) * 1e3 / 1000
+            out[f"{name}_graph_us_per_call"] = round(us, 3)
+            out[f"{name}_graph_gbs"] = round(self.bytes / (us * 1e-6) / 1e9, 1)
+        return out
+
+
+class Csr2Csc(_Generic):
+    """CSR -> CSC of a power-law matrix with 1M rows and ~20M entries (3 radix passes)."""
+    name = "csr2csc"
+    metric = "CSR->CSC GB/s (algorithmic bytes)"
+    unit = "GB/s"
+    dtype = "int32 + f32 payload"
+    kernel = "radix_scatter"
+    profile = "csr2csc_powerlaw_1m_20m"
+    cpu_threads_used = 1
+
+    def __init__(self, seed=0):
+        from armsparse_gb300 import synthetic as S
+        self.a = S.powerlaw_csr(1_000_000, 2.1, 20.0, seed=seed)
+        n, nnz = self.a.n_rows, self.a.nnz
+        self.bytes = 4 * (n + 1) + 8 * nnz + 4 * (n + 1) + 8 * nnz
+        self.config = {"workload": "csr2csc of a power-law matrix 1M x 1M (exp. 2.1, mean 20 "
+                                   "entries/row), fp32 values", "n": n, "nnz": nnz,
+                       "alg_bytes_per_step": self.bytes,
+                       "l2": "flushed between steps (256 MiB write, outside the timed events)"}
+
+    def to_device(self, dev):
+        import torch
+        t = lambda a: torch.from_numpy(a).to(dev)
+        self.rp, self.ci, self.v = t(self.a.rowptr), t(self.a.colind), t(self.a.val)
+        self.res = None
+
+    def inputs(self):
+        return {"rp": self.rp, "ci": self.ci, "v": self.v}
+
+    def output(self):
+        return self.res[1] if self.res is not None else self.ci
+
+    def step(self):
+        import armsparse_gb300 as A
+        self.res = A.csr2csc(self.rp, self.ci, self.v, self.a.n_cols)
+
+    def cpu_step(self, threads, rows=None):
+        from oracle import oracle as O
+        O.csr2csc(self.a.rowptr, self.a.colind, self.a.val, self.a.n_cols)
+        return self.bytes
+
+    def cpu_value(self, threads, budget_s):
+        v, sample = Workload.cpu_value(self, threads, budget_s)
+        return v, sample + " (single-threaded counting transpose)"
+
+
+WORKLOADS = {c.name: c for c in [SpmmF32, SddmmTc, SddmmF32, GcnEpoch, GcnLarge, SpmvF32,
+                                 Csr2Csc]}
 
 
 
@@ -682,7 +808,8 @@ def run_reference(args, wl_cls):
 def cpu_baseline(wl, budget_s=10.0):
     threads = os.cpu_count() or 1
     v, sample = wl.cpu_value(threads, budget_s)
-    return {"value": round(v, 3), "unit": wl.unit, "cores": threads, "kind": "port",
+    cores = getattr(wl, "cpu_threads_used", threads)
+    return {"value": round(v, 3), "unit": wl.unit, "cores": cores, "kind": "port",
             "sample": sample + " (oracle restatement of the reference kernel, OpenMP over all "
                                "host cores)"}
 

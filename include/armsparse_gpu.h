@@ -79,6 +79,10 @@ as_status as_spmm_csr_bf16(as_ctx *ctx, int M, int K, int N, int nnz, const int 
 /* Variant table for tuning: ids are 1..count. dtype 0 = f32, 1 = bf16. */
 int as_spmm_variant_count(int dtype);
 const char *as_spmm_variant_name(int dtype, int variant);
+/* 1 if `variant` can run this layout (N, leading dimensions, pointer alignment), else 0 -- the
+ * launch would return AS_ERR_UNSUPPORTED. */
+int as_spmm_variant_supported(int dtype, int variant, int N, long ldb, long ldc, const void *B,
+                              const void *C);
 /* The variant the library picks for these arguments (what variant 0 runs). */
 int as_spmm_default_variant(int dtype, int M, int K, int N, int nnz, long ldb, long ldc,
                             const void *B, const void *C);

@@ -116,3 +116,18 @@ def test_torch_extension_loads_and_refuses_cpu_tensors():
     rp = torch.tensor([0, 1], dtype=torch.int32)
     with pytest.raises(RuntimeError, match="CUDA"):
         spmm.csr_spmm(rp, torch.tensor([0], dtype=torch.int32), torch.ones(1), torch.ones(1, 4))
+
+
+def test_variant_feasibility_query(native_lib):
+    import armsparse_gb300 as A
+    names = A.spmm_variants()
+    idx = {n: i + 1 for i, n in enumerate(names)}
+    assert A.spmm_variant_supported(idx["nnzsplit_v16_g32_c1_ch128"], 64)
+    assert not A.spmm_variant_supported(idx["nnzsplit_v16_g32_c1_ch128"], 3)
+    assert A.spmm_variant_supported(idx["rowsplit_v4_g32_c2_u8"], 3)
+    assert not A.spmm_variant_supported(idx["rowsplit_v16_g32_c2_u4"], 6)
+    assert not A.spmm_variant_supported(idx["bulk_lb16_s8"], 6)
+    # every default pick is feasible
+    for N_ in (1, 3, 47, 64, 4096):
+        v = native_lib.as_spmm_default_variant(0, 100, 100, N_, 500, N_, N_, 256, 256)
+        assert A.spmm_variant_supported(v, N_)
