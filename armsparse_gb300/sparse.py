@@ -123,13 +123,13 @@ def spmm_variants(dtype: torch.dtype = torch.float32) -> list[str]:
     return [L.as_spmm_variant_name(d, i).decode() for i in range(1, L.as_spmm_variant_count(d) + 1)]
 
 
-def spmm_variant_supported(variant: int, N: int, dtype=torch.float32, ldb: int | None = None,
+def spmm_variant_supported(variant: int, width: int, dtype=torch.float32, ldb: int | None = None,
                            ldc: int | None = None, B_ptr: int = 256, C_ptr: int = 256) -> bool:
-    """Whether a variant can run dense width N (contiguous, 256-byte aligned operands unless
-    given otherwise)."""
+    """Whether a variant can run dense width `width` (contiguous, 256-byte aligned operands
+    unless given otherwise)."""
     d = 0 if dtype == torch.float32 else 1
-    return bool(N.load().as_spmm_variant_supported(d, int(variant), int(N), ldb or N, ldc or N,
-                                                   B_ptr, C_ptr))
+    return bool(N.load().as_spmm_variant_supported(d, int(variant), int(width), ldb or width,
+                                                   ldc or width, B_ptr, C_ptr))
 
 
 def spmm_default_variant(B: torch.Tensor, C: torch.Tensor | None, M: int, nnz: int) -> int:
