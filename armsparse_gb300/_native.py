@@ -47,6 +47,10 @@ SIGNATURES = {
     "as_spmm_csr_f64": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, ctypes.c_double, _P]),
     "as_sddmm_csr_f64": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P, _P]),
     "as_f32_to_bf16": (_I, [_P, _L, _P, _P, _P]),
+    "as_dense_to_csr_count": (_I, [_P, _I, _I, _P, _L, _P, _P]),
+    "as_dense_to_csr_fill": (_I, [_P, _I, _I, _P, _L, _P, _P, _P, _P]),
+    "as_csr_to_vcsr4_count": (_I, [_P, _I, _I, _P, _P, _P, _P]),
+    "as_csr_to_vcsr4_fill": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
     # include/armsparse_mlp.h
     "as_mlp_linear_fwd": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _I, _P]),
     "as_mlp_linear_bwd": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),

@@ -370,6 +370,51 @@ as_status as_sddmm_csr_f64(as_ctx *c, int M, int N, int K, int nnz, const int *r
                             static_cast<cudaStream_t>(stream));
 }
 
+as_status as_dense_to_csr_count(as_ctx *c, int M, int K, const float *D, long ld, int *rowptr,
+                                void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_dense_to_csr_count: ctx is NULL");
+    if (M < 0 || K < 0 || ld < K || !rowptr || (static_cast<long>(M) * K > 0 && !D))
+        return fail(AS_ERR_INVALID_VALUE, "as_dense_to_csr_count: bad arguments");
+    DeviceGuard g(c->device);
+    return dense_to_csr_count_launch(c, M, K, D, ld, rowptr, static_cast<cudaStream_t>(stream));
+}
+
+as_status as_dense_to_csr_fill(as_ctx *c, int M, int K, const float *D, long ld,
+                               const int *rowptr, int *colind, float *val, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_dense_to_csr_fill: ctx is NULL");
+    if (M < 0 || K < 0 || ld < K || !rowptr || (static_cast<long>(M) * K > 0 && (!D || !colind || !val)))
+        return fail(AS_ERR_INVALID_VALUE, "as_dense_to_csr_fill: bad arguments");
+    if (M == 0) return AS_OK;
+    DeviceGuard g(c->device);
+    return dense_to_csr_fill_launch(c, M, K, D, ld, rowptr, colind, val,
+                                    static_cast<cudaStream_t>(stream));
+}
+
+as_status as_csr_to_vcsr4_count(as_ctx *c, int M, int nnz, const int *rowptr, const int *colind,
+                                int *vrowptr, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_csr_to_vcsr4_count: ctx is NULL");
+    as_status st = check_csr_args("as_csr_to_vcsr4_count", M, 0, nnz, rowptr, colind, nullptr, false);
+    if (st != AS_OK) return st;
+    if (!vrowptr) return fail(AS_ERR_INVALID_VALUE, "as_csr_to_vcsr4_count: vrowptr is NULL");
+    DeviceGuard g(c->device);
+    return csr_to_vcsr4_count_launch(c, M, nnz, rowptr, colind, vrowptr,
+                                     static_cast<cudaStream_t>(stream));
+}
+
+as_status as_csr_to_vcsr4_fill(as_ctx *c, int M, int nnz, const int *rowptr, const int *colind,
+                               const float *val, const int *vrowptr, int *vcolind, float *vval,
+                               void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_csr_to_vcsr4_fill: ctx is NULL");
+    as_status st = check_csr_args("as_csr_to_vcsr4_fill", M, 0, nnz, rowptr, colind, val, true);
+    if (st != AS_OK) return st;
+    if (!vrowptr || (nnz > 0 && (!vcolind || !vval)))
+        return fail(AS_ERR_INVALID_VALUE, "as_csr_to_vcsr4_fill: NULL output");
+    if (M == 0) return AS_OK;
+    DeviceGuard g(c->device);
+    return csr_to_vcsr4_fill_launch(c, M, nnz, rowptr, colind, val, vrowptr, vcolind, vval,
+                                    static_cast<cudaStream_t>(stream));
+}
+
 as_status as_f32_to_bf16(as_ctx *c, long n, const float *src, uint16_t *dst, void *stream) {
     if (!c) return fail(AS_ERR_INVALID_VALUE, "as_f32_to_bf16: ctx is NULL");
     if (n < 0) return fail(AS_ERR_INVALID_VALUE, "as_f32_to_bf16: negative size");

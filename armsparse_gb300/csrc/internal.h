@@ -83,6 +83,17 @@ as_status csr2csc_launch(as_ctx *ctx, int M, int N, int nnz, const int *rowptr,
 as_status csr_validate_launch(as_ctx *ctx, int n_rows, int n_cols, int nnz, const int *rowptr,
                               const int *colind, int require_sorted, unsigned *result,
                               cudaStream_t s);
+// Exclusive scan of n ints (in may equal out); block sums live in the context's scratch.
+as_status exclusive_scan_i32(as_ctx *ctx, const int *in, int *out, long n, cudaStream_t s);
+as_status dense_to_csr_count_launch(as_ctx *ctx, int M, int K, const float *D, long ld,
+                                    int *rowptr, cudaStream_t s);
+as_status dense_to_csr_fill_launch(as_ctx *ctx, int M, int K, const float *D, long ld,
+                                   const int *rowptr, int *colind, float *val, cudaStream_t s);
+as_status csr_to_vcsr4_count_launch(as_ctx *ctx, int M, int nnz, const int *rowptr,
+                                    const int *colind, int *vrowptr, cudaStream_t s);
+as_status csr_to_vcsr4_fill_launch(as_ctx *ctx, int M, int nnz, const int *rowptr,
+                                   const int *colind, const float *val, const int *vrowptr,
+                                   int *vcolind, float *vval, cudaStream_t s);
 as_status f32_to_bf16_launch(as_ctx *ctx, long n, const float *src, uint16_t *dst,
                              cudaStream_t s);
 

@@ -276,6 +276,13 @@ static as_status exclusive_scan(as_ctx *ctx, const int *in, int *out, long n, in
     return check_cuda(cudaGetLastError(), "scan launch");
 }
 
+as_status exclusive_scan_i32(as_ctx *ctx, const int *in, int *out, long n, cudaStream_t s) {
+    void *w = nullptr;
+    as_status st = scratch(ctx, sizeof(int) * static_cast<size_t>(ceil_div(n, kScanChunk) + 1), &w);
+    if (st != AS_OK) return st;
+    return exclusive_scan(ctx, in, out, n, static_cast<int *>(w), s);
+}
+
 size_t csr2csc_scratch_bytes(int nnz, int N, bool with_val) {
     const long tiles = ceil_div(nnz, kTile);
     const long hist = tiles * kBins;

@@ -286,3 +286,43 @@ def to_bf16(x: torch.Tensor) -> torch.Tensor:
     N.check(N.load().as_f32_to_bf16(ctx.handle, x.numel(), _ptr(x), _ptr(out), _stream(dev)),
             "as_f32_to_bf16")
     return out
+
+
+def dense_to_csr(D: torch.Tensor):
+    """(rowptr, colind, val) of a dense fp32 matrix: entries != 0, row-major order (the
+    reference's toCSR). Synchronises once to size the outputs."""
+    dev = _dev(D)
+    if D.dtype != torch.float32 or D.dim() != 2 or D.stride(1) != 1:
+        raise ValueError("D must be float32, 2-D, row-major")
+    M, K = D.shape
+    ld = D.stride(0) if M > 1 else K
+    rowptr = torch.empty(M + 1, dtype=torch.int32, device=dev)
+    ctx = N.context(dev.index)
+    N.check(N.load().as_dense_to_csr_count(ctx.handle, M, K, _ptr(D), ld, _ptr(rowptr),
+                                           _stream(dev)), "as_dense_to_csr_count")
+    nnz = int(rowptr[M])
+    colind = torch.empty(nnz, dtype=torch.int32, device=dev)
+    val = torch.empty(nnz, dtype=torch.float32, device=dev)
+    N.check(N.load().as_dense_to_csr_fill(ctx.handle, M, K, _ptr(D), ld, _ptr(rowptr),
+                                          _ptr(colind), _ptr(val), _stream(dev)),
+            "as_dense_to_csr_fill")
+    return rowptr, colind, val
+
+
+def csr_to_vcsr4(rowptr, colind, val):
+    """The reference's 1x4-blocked layout (toVectorAwareCSR) from CSR with ascending columns.
+    Synchronises once to size the outputs."""
+    dev = _dev(rowptr, colind, val)
+    M, nnz = _csr(rowptr, colind)
+    _need(val, torch.float32, "val", 1)
+    vrowptr = torch.empty(M + 1, dtype=torch.int32, device=dev)
+    ctx = N.context(dev.index)
+    N.check(N.load().as_csr_to_vcsr4_count(ctx.handle, M, nnz, _ptr(rowptr), _ptr(colind),
+                                           _ptr(vrowptr), _stream(dev)), "as_csr_to_vcsr4_count")
+    ns = int(vrowptr[M])
+    vcolind = torch.empty(ns, dtype=torch.int32, device=dev)
+    vval = torch.empty(ns, dtype=torch.float32, device=dev)
+    N.check(N.load().as_csr_to_vcsr4_fill(ctx.handle, M, nnz, _ptr(rowptr), _ptr(colind),
+                                          _ptr(val), _ptr(vrowptr), _ptr(vcolind), _ptr(vval),
+                                          _stream(dev)), "as_csr_to_vcsr4_fill")
+    return vrowptr, vcolind, vval

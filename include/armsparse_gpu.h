@@ -176,6 +176,24 @@ as_status as_sddmm_csr_f64(as_ctx *ctx, int M, int N, int K, int nnz, const int 
                            const int *colind, const double *aval, const double *X, long ldx,
                            const double *Y, long ldy, double *out, void *stream);
 
+/* ---- format builders (two passes: count, then fill) -----------------------------------------
+ * Dense M x K (row-major, ld >= K) -> CSR, the reference's toCSR (SDMM.cpp:355-370): entries
+ * where value != 0 in row-major order, columns ascending. _count writes rowptr[0..M]
+ * (rowptr[M] = nnz, read it to size colind / val); _fill writes colind and val. */
+as_status as_dense_to_csr_count(as_ctx *ctx, int M, int K, const float *D, long ld, int *rowptr,
+                                void *stream);
+as_status as_dense_to_csr_fill(as_ctx *ctx, int M, int K, const float *D, long ld,
+                               const int *rowptr, int *colind, float *val, void *stream);
+/* CSR (columns ascending in rows) -> the reference's 1x4-blocked layout, toVectorAwareCSR
+ * (SpMV.cpp:15-38): one block of 4 slots per aligned 4-column group holding an entry, lane l
+ * of a block has column 4*group + l and the entry's value or 0. _count writes vrowptr[0..M]
+ * (vrowptr[M] = number of slots); _fill writes vcolind and vval. */
+as_status as_csr_to_vcsr4_count(as_ctx *ctx, int M, int nnz, const int *rowptr, const int *colind,
+                                int *vrowptr, void *stream);
+as_status as_csr_to_vcsr4_fill(as_ctx *ctx, int M, int nnz, const int *rowptr, const int *colind,
+                               const float *val, const int *vrowptr, int *vcolind, float *vval,
+                               void *stream);
+
 /* ---- small dense helpers used around the hot path ---------------------------------------- */
 /* dst[i] = bf16(src[i]) (round to nearest even). */
 as_status as_f32_to_bf16(as_ctx *ctx, long n, const float *src, uint16_t *dst, void *stream);

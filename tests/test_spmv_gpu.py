@@ -56,3 +56,37 @@ def test_csr_against_fp64(oracle, M, K, nnz, kind):
     A.spmv(rp, ci, v, to_dev(x), y=yb, beta=2.0)
     assert oracle.scaled_err(yb.cpu().numpy(), ref + 2.0, ab + 2.0).max() < 1e-5
     A.sync_status()
+
+
+def test_format_builders_match_reference_golden(golden):
+    """dense -> CSR equals the reference's toCSR output; CSR -> 1x4 blocks equals the
+    reference's toVectorAwareCSR output (both from its compiled code)."""
+    g = golden["spmm_rowbasespmm3"]
+    for i in range(int(g["n_cases"])):
+        M, K, _ = (int(x) for x in g[f"c{i}_shape"])
+        rp, ci, v = g[f"c{i}_rowptr"], g[f"c{i}_colind"], g[f"c{i}_val"]
+        dense = np.zeros((M, K), np.float32)
+        dense[np.repeat(np.arange(M), np.diff(rp)), ci] = v
+        r, c, vv = A.dense_to_csr(to_dev(dense))
+        assert np.array_equal(r.cpu().numpy(), rp) and np.array_equal(c.cpu().numpy(), ci)
+        assert np.array_equal(bits(vv), bits(v))
+    g = golden["spmv_vcsr4"]
+    for i in range(int(g["n_cases"])):
+        vr, vc, vv = A.csr_to_vcsr4(to_dev(g[f"c{i}_rowptr"]), to_dev(g[f"c{i}_colind"]),
+                                    to_dev(g[f"c{i}_val"]))
+        assert np.array_equal(vr.cpu().numpy(), g[f"c{i}_vrowptr"])
+        assert np.array_equal(vc.cpu().numpy(), g[f"c{i}_vcolind"])
+        assert np.array_equal(bits(vv), bits(g[f"c{i}_vval"]))
+
+
+def test_format_builders_large(oracle):
+    a = S.powerlaw_csr(20000, 2.0, 30.0, seed=9, n_cols=4096)  # rows longer than 32 entries
+    vr, vc, vv = A.csr_to_vcsr4(to_dev(a.rowptr), to_dev(a.colind), to_dev(a.val))
+    ovr, ovc, ovv = oracle.csr_to_vcsr4(a.rowptr, a.colind, a.val)
+    assert np.array_equal(vr.cpu().numpy(), ovr) and np.array_equal(vc.cpu().numpy(), ovc)
+    assert np.array_equal(bits(vv), bits(ovv))
+    d = S.to_dense(S.uniform_csr(500, 3000, 40000, seed=3))
+    d[7, 11] = -0.0
+    r, c, v = A.dense_to_csr(to_dev(d))
+    rows, cols = np.nonzero(d != 0)
+    assert np.array_equal(c.cpu().numpy(), cols) and int(r[-1]) == rows.size
