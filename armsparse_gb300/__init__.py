@@ -6,10 +6,10 @@ cores and tcgen05 split-bf16) and a deterministic CSR->CSC transpose, behind the
 include/armsparse_gpu.h. The ops need the CUDA library built in-tree and a GPU; there is no
 CPU fallback.
 """
-from .sparse import (csr2csc, csr_to_vcsr4, dense_to_csr, sddmm, sddmm_coo, spmm, spmm_default_variant, spmm_variant_supported, spmm_variants, spmv,
+from .sparse import (spmm_reduce, csr2csc, csr_to_vcsr4, dense_to_csr, sddmm, sddmm_coo, spmm, spmm_default_variant, spmm_variant_supported, spmm_variants, spmv,
                      spmv_vcsr4, sync_status, to_bf16, validate_csr)
 from ._native import NativeError, Context, context
 
-__all__ = ["csr_to_vcsr4", "dense_to_csr", "spmm", "spmv", "spmv_vcsr4", "sddmm", "sddmm_coo", "csr2csc", "validate_csr", "sync_status",
+__all__ = ["spmm_reduce", "csr_to_vcsr4", "dense_to_csr", "spmm", "spmv", "spmv_vcsr4", "sddmm", "sddmm_coo", "csr2csc", "validate_csr", "sync_status",
            "to_bf16", "spmm_variants", "spmm_default_variant", "spmm_variant_supported", "NativeError", "Context",
            "context"]

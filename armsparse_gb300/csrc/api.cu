@@ -213,6 +213,23 @@ as_status as_spmm_csr_bf16(as_ctx *c, int M, int K, int N, int nnz, const int *r
                        ldc, beta, variant, stream);
 }
 
+as_status as_spmm_csr_reduce_f32(as_ctx *c, int M, int K, int N, int nnz, const int *rowptr,
+                                 const int *colind, const float *val, const float *B, long ldb,
+                                 float *C, long ldc, int op, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_spmm_csr_reduce_f32: ctx is NULL");
+    as_status st = check_csr_args("as_spmm_csr_reduce_f32", M, K, nnz, rowptr, colind, nullptr, false);
+    if (st != AS_OK) return st;
+    if (op != AS_REDUCE_SUM && op != AS_REDUCE_MAX)
+        return fail(AS_ERR_INVALID_VALUE, "as_spmm_csr_reduce_f32: unknown reduction");
+    if (N < 0) return fail(AS_ERR_INVALID_VALUE, "as_spmm_csr_reduce_f32: negative N");
+    if (M == 0 || N == 0) return AS_OK;
+    if (!C || (nnz > 0 && K > 0 && !B) || ldb < N || ldc < N)
+        return fail(AS_ERR_INVALID_VALUE, "as_spmm_csr_reduce_f32: bad dense operand");
+    DeviceGuard g(c->device);
+    SpmmArgs a{M, K, N, nnz, rowptr, colind, val, B, ldb, C, ldc, 0.0f, c->d_status};
+    return spmm_reduce_launch(c, op, a, static_cast<cudaStream_t>(stream));
+}
+
 int as_spmm_variant_count(int dtype) { return spmm_variant_count(dtype); }
 int as_spmm_variant_supported(int dtype, int variant, int N, long ldb, long ldc, const void *B,
                               const void *C) {

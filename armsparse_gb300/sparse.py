@@ -117,6 +117,28 @@ def _spmm_f64(rowptr, colind, val, B, C, beta):
     return C
 
 
+def spmm_reduce(rowptr, colind, B, val=None, op: str = "sum", C=None):
+    """C[i,:] = reduce over row i of w_e * B[col(e),:], reduce in {"sum", "max"}, w_e = val or 1
+    (the unweighted copy-sum / copy-max aggregations); rows without entries give 0."""
+    dev = _dev(rowptr, colind, val, B, C)
+    M, nnz = _csr(rowptr, colind)
+    if B.dtype != torch.float32 or B.dim() != 2 or B.stride(1) != 1:
+        raise ValueError("B must be float32, 2-D, row-major")
+    if val is not None:
+        _need(val, torch.float32, "val", 1)
+    K, Ncols = B.shape
+    if C is None:
+        C = torch.empty((M, Ncols), dtype=torch.float32, device=dev)
+    ctx = N.context(dev.index)
+    N.check(N.load().as_spmm_csr_reduce_f32(ctx.handle, M, K, Ncols, nnz, _ptr(rowptr),
+                                            _ptr(colind), _ptr(val), _ptr(B),
+                                            B.stride(0) if K > 1 else Ncols, _ptr(C),
+                                            C.stride(0) if M > 1 else Ncols,
+                                            {"sum": 0, "max": 1}[op], _stream(dev)),
+            "as_spmm_csr_reduce_f32")
+    return C
+
+
 def spmm_variants(dtype: torch.dtype = torch.float32) -> list[str]:
     d = 0 if dtype == torch.float32 else 1
     L = N.load()

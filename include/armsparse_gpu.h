@@ -76,6 +76,17 @@ as_status as_spmm_csr_bf16(as_ctx *ctx, int M, int K, int N, int nnz, const int 
                            long ldb, float *C, long ldc, float beta, int variant,
                            void *stream);
 
+/* Other reductions: C[i,:] = reduce_{e in row i} w_e * B[col(e),:], reduce = sum or max,
+ * w_e = val[e] (val may be NULL: every w_e = 1, the unweighted "copy" aggregation). Rows
+ * without entries give 0. Unweighted sum adds in CSR order exactly as the reference's
+ * topo*SPMMKernel family (gcn/pytorch-custom/spmm_kernel.cu:31-207); max is the copy-max
+ * aggregation of its DGL kernels (binary_reduce_max.cu:26-168). Overwrites C. */
+#define AS_REDUCE_SUM 0
+#define AS_REDUCE_MAX 1
+as_status as_spmm_csr_reduce_f32(as_ctx *ctx, int M, int K, int N, int nnz, const int *rowptr,
+                                 const int *colind, const float *val, const float *B, long ldb,
+                                 float *C, long ldc, int op, void *stream);
+
 /* Variant table for tuning: ids are 1..count. dtype 0 = f32, 1 = bf16. */
 int as_spmm_variant_count(int dtype);
 const char *as_spmm_variant_name(int dtype, int variant);

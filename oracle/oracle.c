@@ -227,3 +227,27 @@ int or_max_threads(void) {
     return 1;
 #endif
 }
+
+/* Unweighted / weighted sum or max aggregation: C[i,:] = reduce over row i of w_e * B[col,:]
+ * (w_e = val[e] or 1 when val is NULL), in CSR order: the unweighted sum adds acc += B[...] as
+ * the reference's copy-sum kernels do (gcn/pytorch-custom/spmm_kernel.cu:156-173), the
+ * weighted sum is the fused chain of rowBaseSpmm3, max takes the rounded product. Rows without
+ * entries give 0. op: 0 = sum, 1 = max. */
+void or_spmm_reduce_f32(int M, int N, const int *rowptr, const int *colind, const float *val,
+                        const float *B, long ldb, float *C, int op) {
+    for (int m = 0; m < M; ++m) {
+        float *c = C + (long)m * N;
+        for (int j = 0; j < N; ++j) c[j] = op == 0 ? 0.0f : -INFINITY;
+        for (int e = rowptr[m]; e < rowptr[m + 1]; ++e) {
+            const float *b = B + (long)colind[e] * ldb;
+            for (int j = 0; j < N; ++j) {
+                if (op == 0)
+                    c[j] = val ? fmaf(b[j], val[e], c[j]) : c[j] + b[j];
+                else
+                    c[j] = fmaxf(c[j], val ? val[e] * b[j] : b[j]);
+            }
+        }
+        if (rowptr[m] == rowptr[m + 1])
+            for (int j = 0; j < N; ++j) c[j] = 0.0f;
+    }
+}

@@ -76,6 +76,8 @@ def lib():
                                                  _f32p, _c_long, _f32p, _c_long, _f32p, _c_int]
             L.or_csr2csc.argtypes = [_c_int, _c_int, _i32p, _i32p, _f32p, _i32p, _i32p, _f32p]
             L.or_max_threads.restype = _c_int
+            L.or_spmm_reduce_f32.argtypes = [_c_int, _c_int, _i32p, _i32p, ctypes.c_void_p, _f32p,
+                                             _c_long, _f32p, _c_int]
             _LIB = L
     return _LIB
 
@@ -112,6 +114,18 @@ def spmm_fma_chain_f32(rowptr, colind, val, B, C=None, threads=None):
     out = np.ascontiguousarray(C, dtype=np.float32).copy() if acc else np.empty((M, N), np.float32)
     lib().or_spmm_fma_chain_f32(M, N, rowptr, colind, np.ascontiguousarray(val, np.float32), B,
                                 N, out, N, int(acc), threads or max_threads())
+    return out
+
+
+def spmm_reduce_f32(rowptr, colind, B, val=None, op="sum"):
+    """Sum / max aggregation in CSR order (w_e = val or 1); empty rows give 0."""
+    rowptr, colind = _csr(rowptr, colind)
+    M = rowptr.size - 1
+    B = np.ascontiguousarray(B, np.float32)
+    out = np.empty((M, B.shape[1]), np.float32)
+    v = None if val is None else np.ascontiguousarray(val, np.float32)
+    lib().or_spmm_reduce_f32(M, B.shape[1], rowptr, colind, None if v is None else v.ctypes.data,
+                             B, B.shape[1], out, {"sum": 0, "max": 1}[op])
     return out
 
 

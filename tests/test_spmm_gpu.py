@@ -226,3 +226,18 @@ def test_nnzsplit_variants_skewed_rows(oracle):
             A.spmm(rpd, cid, vd, Bd, C=Cb, beta=0.5, variant=var)
             assert oracle.scaled_err(Cb.cpu().numpy(), C64 + 1.0, A64 + 1.0).max() < 1e-5
     A.sync_status()
+
+
+@pytest.mark.parametrize("op", ["sum", "max"])
+def test_reduce_aggregations(oracle, op):
+    """Unweighted copy-sum / copy-max and the weighted forms, bit-exact against the CSR-order
+    restatement (sum adds in order without fusing, as the reference's topo kernels do)."""
+    a = S.powerlaw_csr(3000, 2.0, 9.0, seed=51, n_cols=2500)
+    for N_ in (1, 47, 64, 300):
+        B = S.dense_uniform((2500, N_), 52)
+        rp, ci, v = csr_dev(a)
+        for val in (None, a.val):
+            got = A.spmm_reduce(rp, ci, to_dev(B), val=None if val is None else v, op=op)
+            ref = oracle.spmm_reduce_f32(a.rowptr, a.colind, B, val=val, op=op)
+            assert np.array_equal(bits(got), bits(ref)), (op, N_, val is None)
+    A.sync_status()
