@@ -190,9 +190,11 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         }
         const int cnt = min(GROUP, hi - base);
         int t = 0;
-        // U entries per step: all their B loads are issued before the FMAs (branch-free:
-        // idle lanes and flagged entries load an in-bounds element and contribute nothing),
-        // then the FMAs run in CSR order.
+        // U entries per step: their B loads are issued before the FMAs, which then run in
+        // CSR order. fp32 keeps per-load predicates (measured faster on GB300); bf16 loads
+        // branch-free into packed registers (an idle lane or a flagged entry reads an
+        // in-bounds element that contributes nothing) and unpacks at the FMA, which halves the
+        // registers held per load and lets more loads be in flight.
         for (; t + U <= cnt; t += U) {
             int kk[U];
             float vv[U];
@@ -201,26 +203,48 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 kk[u] = __shfl_sync(gmask, k, t + u, GROUP);
                 vv[u] = __shfl_sync(gmask, v, t + u, GROUP);
             }
-            typename V::Raw b[U][CPL];
+            if constexpr (sizeof(T) == 4) {
+                float b[U][CPL][E];
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const T *brow = B + static_cast<long>(kk[u] < 0 ? 0 : kk[u]) * ldb;
+                for (int u = 0; u < U; ++u) {
+                    const T *brow = B + static_cast<long>(kk[u] < 0 ? 0 : kk[u]) * ldb;
 #pragma unroll
-                for (int j = 0; j < CPL; ++j) {
-                    const int c = tile0 + (j * GROUP + g) * E;
-                    b[u][j] = V::raw(brow + (c < N ? c : 0));
+                    for (int j = 0; j < CPL; ++j) {
+                        const int c = tile0 + (j * GROUP + g) * E;
+                        if (c < N && kk[u] >= 0) {
+                            V::load(brow + c, b[u][j]);
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < E; ++i) b[u][j][i] = 0.0f;
+                        }
+                    }
                 }
-            }
-            // keep the compiler from sinking loads into the FMA sequence: all U * CPL loads of
-            // the step are in flight before the first FMA waits on one
-            asm volatile("" ::: "memory");
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const float vu = kk[u] < 0 ? 0.0f : vv[u];
+                for (int u = 0; u < U; ++u)
 #pragma unroll
-                for (int j = 0; j < CPL; ++j)
+                    for (int j = 0; j < CPL; ++j)
 #pragma unroll
-                    for (int i = 0; i < E; ++i) acc[j][i] = fmaf(V::at(b[u][j], i), vu, acc[j][i]);
+                        for (int i = 0; i < E; ++i) acc[j][i] = fmaf(b[u][j][i], vv[u], acc[j][i]);
+            } else {
+                typename V::Raw b[U][CPL];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const T *brow = B + static_cast<long>(kk[u] < 0 ? 0 : kk[u]) * ldb;
+#pragma unroll
+                    for (int j = 0; j < CPL; ++j) {
+                        const int c = tile0 + (j * GROUP + g) * E;
+                        b[u][j] = V::raw(brow + (c < N ? c : 0));
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const float vu = kk[u] < 0 ? 0.0f : vv[u];
+#pragma unroll
+                    for (int j = 0; j < CPL; ++j)
+#pragma unroll
+                        for (int i = 0; i < E; ++i)
+                            acc[j][i] = fmaf(V::at(b[u][j], i), vu, acc[j][i]);
+                }
             }
         }
         for (; t < cnt; ++t) {
@@ -262,6 +286,7 @@ struct Variant {
 #define AS_NNZ(vb, g, c, ch) {vb, g, c, ch, "nnzsplit_v" #vb "_g" #g "_c" #c "_ch" #ch, 2}
 #define AS_NNZS(ch) AS_NNZ(16, 8, 1, ch), AS_NNZ(16, 16, 1, ch), AS_NNZ(16, 32, 1, ch), \
     AS_NNZ(16, 32, 2, ch), AS_NNZ(4, 32, 1, ch), AS_NNZ(4, 32, 2, ch)
+#define AS_NNZS_BF16_SCALAR(ch) AS_NNZ(2, 32, 1, ch), AS_NNZ(2, 32, 2, ch)
 #define AS_VG(vb, g) AS_V(vb, g, 1, 4), AS_V(vb, g, 2, 4), AS_V(vb, g, 4, 4), AS_V(vb, g, 1, 8), \
     AS_V(vb, g, 2, 8)
 #define AS_VROW(vb) AS_VG(vb, 1), AS_VG(vb, 2), AS_VG(vb, 4), AS_VG(vb, 8), AS_VG(vb, 16), AS_VG(vb, 32)
@@ -269,7 +294,8 @@ struct Variant {
 const Variant kF32[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_BULKS, AS_NNZS(128),
                         AS_NNZS(1024)};
 const Variant kBF16[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_VROW(2), AS_BULKS,
-                         AS_NNZS(128), AS_NNZS(1024)};
+                         AS_NNZS(128), AS_NNZS(1024), AS_NNZS_BF16_SCALAR(128),
+                         AS_NNZS_BF16_SCALAR(1024)};
 constexpr int kNF32 = sizeof(kF32) / sizeof(kF32[0]);
 constexpr int kNBF16 = sizeof(kBF16) / sizeof(kBF16[0]);
 
@@ -350,7 +376,7 @@ static int find_variant(int dtype, int vb, int g, int cpl, int u) {
 
 // Library choice among the bit-identical row-split kernels, from the variant sweep on GB300:
 // wide rows of B (N >= 512) want full warps with two or four vectors per lane (fp32:
-// float2 x 4, bf16: 8 x bf16 x 1); narrow B wants full warps of scalar lanes with 8 entries
+// float2 x 4, bf16: 8 x bf16 x 2); narrow B wants full warps of scalar lanes with 8 entries
 // per step (the batch of 32 (colind, val) pairs amortises the index loads). The entry-balanced
 // kernels, which win on skewed rows, are not picked here: they change the summation order of
 // rows that cross a chunk, and the library cannot see the row lengths without reading rowptr
@@ -361,7 +387,7 @@ int spmm_default_variant(int dtype, int M, int K, int N, int nnz, long ldb, long
     const int esz = dtype == 0 ? 4 : 2;
     struct Pick { int vb, g, cpl, u; };
     const Pick wide_f32[] = {{8, 32, 4, 4}, {16, 32, 2, 4}, {4, 32, 2, 8}};
-    const Pick wide_bf16[] = {{16, 32, 1, 4}, {8, 32, 2, 4}, {4, 32, 4, 4}, {2, 32, 2, 8}};
+    const Pick wide_bf16[] = {{16, 32, 2, 4}, {8, 32, 2, 4}, {4, 32, 4, 4}, {2, 32, 2, 8}};
     const Pick narrow_f32[] = {{4, 32, 2, 8}};
     const Pick narrow_bf16[] = {{4, 32, 2, 8}, {2, 32, 2, 8}};
     const Pick *list;

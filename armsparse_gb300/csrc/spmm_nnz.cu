@@ -49,6 +49,13 @@ struct V<uint16_t, 16> {
     }
 };
 template <>
+struct V<uint16_t, 2> {
+    static constexpr int E = 1;
+    __device__ static void load(const uint16_t *p, float *o) {
+        o[0] = bf16_to_f32(__ldg(reinterpret_cast<const unsigned short *>(p)));
+    }
+};
+template <>
 struct V<uint16_t, 4> {
     static constexpr int E = 2;
     __device__ static void load(const uint16_t *p, float *o) {
@@ -262,6 +269,7 @@ as_status spmm_nnz_launch(as_ctx *ctx, int dtype, int vb, int group, int cpl, in
         AS_NNZ_CASE(uint16_t, 16, 8, 1) AS_NNZ_CASE(uint16_t, 16, 16, 1)
         AS_NNZ_CASE(uint16_t, 16, 32, 1) AS_NNZ_CASE(uint16_t, 16, 32, 2)
         AS_NNZ_CASE(uint16_t, 4, 32, 1) AS_NNZ_CASE(uint16_t, 4, 32, 2)
+        AS_NNZ_CASE(uint16_t, 2, 32, 1) AS_NNZ_CASE(uint16_t, 2, 32, 2)
     }
 #undef AS_NNZ_CASE
     return fail(AS_ERR_UNSUPPORTED, "spmm nnz-split: configuration not instantiated");

@@ -254,6 +254,21 @@ def width_rule(N):
     return "rowsplit_v4_g32_c2_u8" if N < 512 else "rowsplit_v8_g32_c4_u4"
 
 
+def narrower_feasible(names, name, N, dtype):
+    """The variant with `name`'s family, lane group, vectors per lane and unroll/chunk but the
+    narrowest vector width that can run width N, or 0."""
+    parts = name.split("_")
+    if parts[0] not in ("rowsplit", "nnzsplit"):
+        return 0
+    for vb in (4, 2):
+        alt = "_".join([parts[0], f"v{vb}"] + parts[2:])
+        if alt in names:
+            vid = names.index(alt) + 1
+            if S.spmm_variant_supported(vid, N, dtype):
+                return vid
+    return 0
+
+
 class Selector:
     def __init__(self, model: dict):
         if model.get("format") != FORMAT:
@@ -278,11 +293,18 @@ class Selector:
         feats = tuner.features(rp, n_cols, N, dtype == torch.bfloat16)
         order = np.argsort(-host_forward(self.model, feats))
         ids = variant_ids(self.model["candidates"], dtype)
-        # best-scored candidate that can run this width (e.g. vector kernels need N % width)
+        # best-scored candidate that can run this width (vector kernels need N % vector width);
+        # an infeasible pick falls back to the same kernel shape with narrower vectors
         v = 0
+        names = S.spmm_variants(dtype)
         for i in order:
-            if S.spmm_variant_supported(ids[int(i)], N, dtype):
-                v = ids[int(i)]
+            cand = ids[int(i)]
+            if S.spmm_variant_supported(cand, N, dtype):
+                v = cand
+                break
+            alt = narrower_feasible(names, names[cand - 1], N, dtype)
+            if alt:
+                v = alt
                 break
         if key is not None:
             self._cache[(key, N, dtype)] = v

@@ -170,6 +170,48 @@ class _Generic(Workload):
         torch.cuda.current_stream().synchronize()
 
 
+class SpmmBf16(_Generic, SpmmF32):
+    """The SpMM workload above with A's values and B stored as bf16 (fp32 products and
+    accumulation, fp32 C): the bf16-storage path of the GCN layers."""
+    name = "spmm_bf16"
+    metric = "SpMM GB/s (algorithmic bytes), bf16 storage / fp32 accumulate"
+    dtype = "bf16 storage, fp32 accumulate"
+    profile = "spmm_rowsplit_bf16_4096x4096x4096_d001"
+    e2e_api = "armsparse_gb300.spmm with pinned host inputs copied in and C copied back"
+
+    def __init__(self, seed=0):
+        super().__init__(seed)
+        nnz = self.a.nnz
+        self.bytes = 4 * (self.M + 1) + 6 * nnz + 2 * self.K * self.N + 4 * self.M * self.N
+        self.config.update(workload="spmm_csr_bf16 C=A*B, A 4096x4096 uniform density 0.01 "
+                                    "(167,772 nnz) U(-1,1), B 4096x4096 U(-1,1), values and B "
+                                    "rounded to bf16, C fp32", alg_bytes_per_step=self.bytes)
+
+    def to_device(self, dev):
+        import torch
+        super().to_device(dev)
+        self.v = self.v.to(torch.bfloat16)
+        self.Bd = self.Bd.to(torch.bfloat16)
+
+    def inputs(self):
+        return {"rp": self.rp, "ci": self.ci, "v": self.v, "B": self.Bd}
+
+    def output(self):
+        return self.C
+
+    def cpu_step(self, threads, rows=None):
+        from oracle import oracle as O
+        if not hasattr(self, "_bf"):
+            self._bf = (O.bf16_round(self.a.val), O.bf16_round(self.B))
+        v, B = self._bf
+        a = self.a
+        rp = a.rowptr if rows is None else a.rowptr[: rows + 1]
+        O.spmm_fma_chain_f32(rp, a.colind, v, B, threads=threads)
+        nnz = int(rp[-1])
+        m = a.n_rows if rows is None else rows
+        return 4 * (m + 1) + 6 * nnz + 2 * self.K * self.N + 4 * m * self.N
+
+
 class SddmmTc(_Generic):
     name = "sddmm_tc"
     metric = "SDDMM GB/s (algorithmic bytes), tensor-core split-bf16 path"
@@ -680,7 +722,7 @@ class Csr2Csc(_Generic):
         return v, sample + " (single-threaded counting transpose)"
 
 
-WORKLOADS = {c.name: c for c in [SpmmF32, SddmmTc, SddmmF32, GcnEpoch, GcnLarge, SpmvF32,
+WORKLOADS = {c.name: c for c in [SpmmF32, SpmmBf16, SddmmTc, SddmmF32, GcnEpoch, GcnLarge, SpmvF32,
                                  Csr2Csc]}
 
 
