@@ -109,12 +109,18 @@ as_status as_ctx_create(as_ctx **out, int device) {
     DeviceGuard g(device);
     as_ctx *c = new as_ctx();
     c->device = device;
-    e = cudaMalloc(&c->d_status, sizeof(unsigned));
+    e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) {
+        delete c;
+        return check_cuda(e, "as_ctx_create: multiprocessor count");
+    }
+    e = cudaMalloc(&c->d_status, 4 * sizeof(unsigned));
     if (e != cudaSuccess) {
         delete c;
         return check_cuda(e, "as_ctx_create: status word");
     }
-    e = cudaMemset(c->d_status, 0, sizeof(unsigned));
+    c->d_long = c->d_status + 1;
+    e = cudaMemset(c->d_status, 0, 4 * sizeof(unsigned));
     if (e != cudaSuccess) {
         cudaFree(c->d_status);
         delete c;
@@ -146,6 +152,9 @@ as_status as_ctx_sync_status(as_ctx *c, void *stream) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return check_cuda(e, "as_ctx_sync_status");
     if (h & kFlagTimeout) return fail(AS_ERR_TIMEOUT, "a bounded device wait gave up");
+    if (h & kFlagLongList)
+        return fail(AS_ERR_CUDA, "SpMM long-row list found non-empty at the start of a call "
+                                 "(an earlier call on this context failed part-way)");
     if (h & (kFlagBadRowptr | kFlagBadColind))
         return fail(AS_ERR_INVALID_CSR,
                     (h & kFlagBadRowptr) ? "malformed rowptr seen on the device"

@@ -14,6 +14,7 @@ enum : unsigned {
     kFlagBadRowptr = 1u,
     kFlagBadColind = 2u,
     kFlagTimeout = 4u,
+    kFlagLongList = 8u,  // the long-row list was not empty at the start of a call (internal)
 };
 
 __device__ __forceinline__ void flag(unsigned *status, unsigned bit) {

@@ -11,7 +11,10 @@
 
 struct as_ctx {
     int device = 0;
-    unsigned *d_status = nullptr;  // device status word (bit flags from common.cuh)
+    unsigned *d_status = nullptr;  // device words: [0] status (bit flags from common.cuh),
+                                   // [1..2] long-row list length and CTA-done count
+    unsigned *d_long = nullptr;    // = d_status + 1
+    int sms = 1;                   // multiprocessors of the device
     void *scratch = nullptr;       // scratch arena
     size_t scratch_bytes = 0;
     uint64_t launches = 0;         // kernels this library launched through the context
@@ -43,6 +46,11 @@ as_status spmm_nnz_launch(as_ctx *ctx, int dtype, int vb, int group, int cpl, in
                           const SpmmArgs &a, cudaStream_t s);
 as_status spmm_bulk_launch(as_ctx *ctx, int dtype, int lane_bytes, int stages, const SpmmArgs &a,
                            cudaStream_t s);
+// Long rows of the row-split kernels: the cp.async size (16 or 4 bytes) the layout allows,
+// 0 when none does; the launch of the kernel that takes the listed rows.
+int spmm_long_granule(int dtype, int N, long ldb, const void *B);
+as_status spmm_long_launch(as_ctx *ctx, int dtype, int granule, const SpmmArgs &a,
+                           const int *list, cudaStream_t s);
 int spmm_variant_count(int dtype);
 bool spmm_variant_supported(int dtype, int variant, int N, long ldb, long ldc, const void *B,
                             const void *C);

@@ -9,7 +9,10 @@
 //   in CSR order and updates its accumulators with fmaf(b, v, acc). Each output element is
 //   therefore exactly the reference's fused-FMA chain. Blocks are 256 threads; blockIdx.x
 //   runs over row blocks and blockIdx.y over column tiles, so the CTAs resident at any
-//   moment share one column tile of B, which stays in L2.
+//   moment share one column tile of B, which stays in L2. Rows with more than kLongRow
+//   entries are skipped here and computed by the long-row kernel (spmm_long.cu), which keeps
+//   the same chains.
+#include <limits.h>
 #include <stdio.h>
 
 #include "common.cuh"
@@ -141,13 +144,14 @@ __device__ __forceinline__ void load_c(const float *p, float *v) {
 }
 
 constexpr int kThreads = 256;
+constexpr int kLongRow = 256;  // entries; longer rows are handed to spmm_long.cu
 
 template <typename T, int VB, int GROUP, int CPL, int U>
 __global__ void __launch_bounds__(kThreads)
 spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
               const int *__restrict__ colind, const T *__restrict__ val,
               const T *__restrict__ B, long ldb, float *__restrict__ C, long ldc, float beta,
-              unsigned *status) {
+              unsigned *status, int long_thresh, int *long_list, unsigned *long_count) {
     using V = Vec<T, VB>;
     constexpr int E = V::E;
     constexpr int TILE = GROUP * E * CPL;
@@ -159,6 +163,16 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
     if (row >= M) return;  // the whole group leaves together
     int lo, hi;
     row_range(rowptr, static_cast<int>(row), nnz, status, lo, hi);
+    if (hi - lo > long_thresh) {  // left to the long-row kernel (spmm_long.cu)
+        if (blockIdx.y == 0 && g == 0) {
+            const unsigned idx = atomicAdd(long_count, 1u);
+            if (idx < static_cast<unsigned>(M))
+                long_list[idx] = static_cast<int>(row);
+            else
+                flag(status, kFlagLongList);
+        }
+        return;
+    }
 
     const int tile0 = blockIdx.y * TILE;
     float acc[CPL][E];
@@ -299,43 +313,51 @@ const Variant kBF16[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_VROW(2), AS_BUL
 constexpr int kNF32 = sizeof(kF32) / sizeof(kF32[0]);
 constexpr int kNBF16 = sizeof(kBF16) / sizeof(kBF16[0]);
 
+struct LongRows {
+    int thresh;       // rows with more entries go to the long-row kernel (INT_MAX: none)
+    int *list;        // their row numbers (scratch, M entries)
+    unsigned *count;  // list length (context device word)
+};
+
 template <typename T, int VB, int G, int CPL, int U>
-void launch_one(const SpmmArgs &a, cudaStream_t s) {
+void launch_one(const SpmmArgs &a, const LongRows &lr, cudaStream_t s) {
     constexpr int E = Vec<T, VB>::E;
     constexpr int TILE = G * E * CPL;
     dim3 grid(static_cast<unsigned>(ceil_div(a.M, kThreads / G)),
               static_cast<unsigned>(ceil_div(a.N, TILE)));
     spmm_rowsplit<T, VB, G, CPL, U><<<grid, kThreads, 0, s>>>(
         a.M, a.K, a.N, a.nnz, a.rowptr, a.colind, static_cast<const T *>(a.val),
-        static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, a.status);
+        static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, a.status, lr.thresh, lr.list,
+        lr.count);
 }
 
 template <typename T, int VB, int G>
-bool dispatch_cpl(int cpl, int u, const SpmmArgs &a, cudaStream_t s) {
+bool dispatch_cpl(int cpl, int u, const SpmmArgs &a, const LongRows &lr, cudaStream_t s) {
     if (u == 4) {
         switch (cpl) {
-            case 1: launch_one<T, VB, G, 1, 4>(a, s); return true;
-            case 2: launch_one<T, VB, G, 2, 4>(a, s); return true;
-            case 4: launch_one<T, VB, G, 4, 4>(a, s); return true;
+            case 1: launch_one<T, VB, G, 1, 4>(a, lr, s); return true;
+            case 2: launch_one<T, VB, G, 2, 4>(a, lr, s); return true;
+            case 4: launch_one<T, VB, G, 4, 4>(a, lr, s); return true;
         }
     } else if (u == 8) {
         switch (cpl) {
-            case 1: launch_one<T, VB, G, 1, 8>(a, s); return true;
-            case 2: launch_one<T, VB, G, 2, 8>(a, s); return true;
+            case 1: launch_one<T, VB, G, 1, 8>(a, lr, s); return true;
+            case 2: launch_one<T, VB, G, 2, 8>(a, lr, s); return true;
         }
     }
     return false;
 }
 
 template <typename T, int VB>
-bool dispatch_group(int g, int cpl, int u, const SpmmArgs &a, cudaStream_t s) {
+bool dispatch_group(int g, int cpl, int u, const SpmmArgs &a, const LongRows &lr,
+                    cudaStream_t s) {
     switch (g) {
-        case 1: return dispatch_cpl<T, VB, 1>(cpl, u, a, s);
-        case 2: return dispatch_cpl<T, VB, 2>(cpl, u, a, s);
-        case 4: return dispatch_cpl<T, VB, 4>(cpl, u, a, s);
-        case 8: return dispatch_cpl<T, VB, 8>(cpl, u, a, s);
-        case 16: return dispatch_cpl<T, VB, 16>(cpl, u, a, s);
-        case 32: return dispatch_cpl<T, VB, 32>(cpl, u, a, s);
+        case 1: return dispatch_cpl<T, VB, 1>(cpl, u, a, lr, s);
+        case 2: return dispatch_cpl<T, VB, 2>(cpl, u, a, lr, s);
+        case 4: return dispatch_cpl<T, VB, 4>(cpl, u, a, lr, s);
+        case 8: return dispatch_cpl<T, VB, 8>(cpl, u, a, lr, s);
+        case 16: return dispatch_cpl<T, VB, 16>(cpl, u, a, lr, s);
+        case 32: return dispatch_cpl<T, VB, 32>(cpl, u, a, lr, s);
     }
     return false;
 }
@@ -437,24 +459,39 @@ as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cu
                                             " needs N, ldb, ldc and pointer alignment to match its vector width");
     if (ceil_div(a.N, (v.vb / (dtype == 0 ? 4 : 2)) * v.group * v.cpl) > 65535)
         return fail(AS_ERR_UNSUPPORTED, "spmm: N too large for this variant's column tile");
+    // rows longer than kLongRow entries go to the long-row kernel when its copies can serve
+    // the layout (a matrix with nnz <= kLongRow has none)
+    LongRows lr{INT_MAX, nullptr, ctx->d_long};
+    const int granule = a.nnz > kLongRow && a.M > 0 ? spmm_long_granule(dtype, a.N, a.ldb, a.B) : 0;
+    if (granule) {
+        void *p = nullptr;
+        as_status st = scratch(ctx, static_cast<size_t>(a.M) * sizeof(int), &p);
+        if (st != AS_OK) return st;
+        lr.thresh = kLongRow;
+        lr.list = static_cast<int *>(p);
+    }
     bool ok = false;
     if (dtype == 0) {
         switch (v.vb) {
-            case 16: ok = dispatch_group<float, 16>(v.group, v.cpl, v.unroll, a, s); break;
-            case 8: ok = dispatch_group<float, 8>(v.group, v.cpl, v.unroll, a, s); break;
-            case 4: ok = dispatch_group<float, 4>(v.group, v.cpl, v.unroll, a, s); break;
+            case 16: ok = dispatch_group<float, 16>(v.group, v.cpl, v.unroll, a, lr, s); break;
+            case 8: ok = dispatch_group<float, 8>(v.group, v.cpl, v.unroll, a, lr, s); break;
+            case 4: ok = dispatch_group<float, 4>(v.group, v.cpl, v.unroll, a, lr, s); break;
         }
     } else {
         switch (v.vb) {
-            case 16: ok = dispatch_group<uint16_t, 16>(v.group, v.cpl, v.unroll, a, s); break;
-            case 8: ok = dispatch_group<uint16_t, 8>(v.group, v.cpl, v.unroll, a, s); break;
-            case 4: ok = dispatch_group<uint16_t, 4>(v.group, v.cpl, v.unroll, a, s); break;
-            case 2: ok = dispatch_group<uint16_t, 2>(v.group, v.cpl, v.unroll, a, s); break;
+            case 16: ok = dispatch_group<uint16_t, 16>(v.group, v.cpl, v.unroll, a, lr, s); break;
+            case 8: ok = dispatch_group<uint16_t, 8>(v.group, v.cpl, v.unroll, a, lr, s); break;
+            case 4: ok = dispatch_group<uint16_t, 4>(v.group, v.cpl, v.unroll, a, lr, s); break;
+            case 2: ok = dispatch_group<uint16_t, 2>(v.group, v.cpl, v.unroll, a, lr, s); break;
         }
     }
     if (!ok) return fail(AS_ERR_UNSUPPORTED, "spmm: variant not instantiated");
     ctx->launches++;
-    return check_cuda(cudaGetLastError(), "spmm launch");
+    as_status st = check_cuda(cudaGetLastError(), "spmm launch");
+    if (st != AS_OK || !granule) return st;
+    st = spmm_long_launch(ctx, dtype, granule, a, lr.list, s);
+    if (st != AS_OK) cudaMemsetAsync(ctx->d_long, 0, 2 * sizeof(unsigned), s);
+    return st;
 }
 
 }  // namespace as

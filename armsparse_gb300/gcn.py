@@ -166,34 +166,78 @@ class GCNConv(torch.nn.Module):
 class Net(torch.nn.Module):
     """2-layer GCN of gcn_custom.py:72-90: conv -> relu -> dropout -> conv -> log_softmax."""
 
-    def __init__(self, n_features, n_hidden, n_classes):
+    def __init__(self, n_features, n_hidden, n_classes, dropout: float = 0.5):
         super().__init__()
         self.conv1 = GCNConv(n_features, n_hidden)
         self.conv2 = GCNConv(n_hidden, n_classes)
+        self.dropout = dropout
 
     def forward(self, x, g: Graph):
         colptr, rowind, vcsc = g.csc
         args = (g.rowptr, g.colind, colptr, rowind, g.values, vcsc)
         x = F.relu(self.conv1(x, *args, variants=g.plan(self.conv1.out_channels, x.dtype)))
-        x = F.dropout(x, training=self.training)
+        x = F.dropout(x, p=self.dropout, training=self.training)
         x = self.conv2(x, *args, variants=g.plan(self.conv2.out_channels, x.dtype))
         return F.log_softmax(x, dim=1)
 
 
-def make_optimizer(model: Net):
-    """Adam, lr 0.01, weight decay 5e-4 on the first layer only (gcn_custom.py:116-119)."""
+def make_optimizer(model: Net, capturable: bool = False):
+    """Adam, lr 0.01, weight decay 5e-4 on the first layer only (gcn_custom.py:116-119).
+    capturable keeps Adam's step count on the device so that the step can be recorded in a
+    CUDA graph (``CapturedEpoch``)."""
     return torch.optim.Adam([dict(params=model.conv1.parameters(), weight_decay=5e-4),
-                             dict(params=model.conv2.parameters(), weight_decay=0)], lr=0.01)
+                             dict(params=model.conv2.parameters(), weight_decay=0)], lr=0.01,
+                            capturable=capturable)
 
 
-def train_epoch(model, opt, x, g, y, train_mask) -> torch.Tensor:
-    """One full-batch step (gcn_custom.py:122-126); returns the loss (on the device)."""
+def train_epoch(model, opt, x, g, y, train) -> torch.Tensor:
+    """One full-batch step (gcn_custom.py:122-126); returns the loss (on the device). ``train``
+    is the boolean training mask or the ascending indices of the training nodes (the same
+    loss; indices need no host synchronisation, which a boolean mask does)."""
     model.train()
-    opt.zero_grad()
-    loss = F.nll_loss(model(x, g)[train_mask], y[train_mask])
+    opt.zero_grad(set_to_none=True)
+    out = model(x, g)
+    if train.dtype == torch.bool:
+        loss = F.nll_loss(out[train], y[train])
+    else:
+        loss = F.nll_loss(out.index_select(0, train), y.index_select(0, train))
     loss.backward()
     opt.step()
     return loss.detach()
+
+
+class CapturedEpoch:
+    """A training epoch recorded once as a CUDA graph and replayed per call: on a graph of
+    PubMed's size an eager epoch is bound by host-side launch overhead (some 80 kernel
+    launches through autograd), a replay by the kernels themselves.
+
+    Before recording, ``warmup`` eager epochs run on a side stream (they are real training
+    epochs: the weights move), which also settles everything the recording must not do: the
+    CSC transpose and the selector's plans are cached on the graph, the library scratch has
+    reached its size, Adam's state exists. ``opt`` must be built with ``capturable=True``.
+    New node features are fed by copying into ``x`` in place; every replay draws fresh dropout
+    masks."""
+
+    def __init__(self, model, opt, x, g: Graph, y, train, warmup: int = 3):
+        if train.dtype == torch.bool:
+            train = train.nonzero().squeeze(1)
+        if not all(group.get("capturable", False) for group in opt.param_groups):
+            raise ValueError("CapturedEpoch needs an optimizer built with capturable=True")
+        dev = x.device
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            for _ in range(max(1, warmup)):
+                train_epoch(model, opt, x, g, y, train)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.loss = train_epoch(model, opt, x, g, y, train)
+
+    def __call__(self) -> torch.Tensor:
+        """One epoch; returns the loss tensor (overwritten by the next call)."""
+        self.graph.replay()
+        return self.loss
 
 
 def synthetic_task(n_nodes=19717, n_edges=88648, n_features=500, n_classes=3, seed=0,

@@ -43,6 +43,17 @@ def _from_sorted_keys(keys: np.ndarray, n_rows: int, n_cols: int) -> tuple[np.nd
     return rowptr.astype(np.int32), cols
 
 
+def _sorted_unique(keys: np.ndarray) -> np.ndarray:
+    """Sorted distinct values (sort + neighbour compare; faster than np.unique here)."""
+    keys = np.sort(keys)
+    if keys.size < 2:
+        return keys
+    keep = np.empty(keys.size, bool)
+    keep[0] = True
+    np.not_equal(keys[1:], keys[:-1], out=keep[1:])
+    return keys[keep]
+
+
 def uniform_csr(n_rows: int, n_cols: int, nnz: int, seed: int = 0, values: str = "u11") -> CSR:
     """``nnz`` distinct positions drawn uniformly without replacement."""
     rng = np.random.default_rng(seed)
@@ -52,10 +63,10 @@ def uniform_csr(n_rows: int, n_cols: int, nnz: int, seed: int = 0, values: str =
     if nnz > total // 4:
         keys = np.sort(rng.permutation(total)[:nnz])
     else:
-        keys = np.unique(rng.integers(0, total, size=int(nnz * 1.1) + 16, dtype=np.int64))
+        keys = _sorted_unique(rng.integers(0, total, size=int(nnz * 1.1) + 16, dtype=np.int64))
         while keys.size < nnz:
             more = rng.integers(0, total, size=nnz - keys.size + 64, dtype=np.int64)
-            keys = np.unique(np.concatenate([keys, more]))
+            keys = _sorted_unique(np.concatenate([keys, more]))
         keys = np.sort(rng.permutation(keys)[:nnz])
     rowptr, colind = _from_sorted_keys(keys, n_rows, n_cols)
     return CSR(rowptr, colind, make_values(rng, nnz, values), n_rows, n_cols)
@@ -80,9 +91,17 @@ def _rows_with_lengths(rng, lengths: np.ndarray, n_cols: int) -> tuple[np.ndarra
     rowptr = np.zeros(lengths.size + 1, np.int64)
     np.cumsum(lengths, out=rowptr[1:])
     nnz = int(rowptr[-1])
-    row_of = np.repeat(np.arange(lengths.size, dtype=np.int64), lengths)
-    cols = rng.integers(0, n_cols, size=nnz, dtype=np.int64)
-    keys = np.unique(row_of * n_cols + cols)
+    # rows holding more than an eighth of the columns draw without replacement (rejection
+    # would need many refill rounds for them); the rest draw with rejection below
+    big = np.flatnonzero(lengths > max(n_cols // 8, 64))
+    small = lengths.copy()
+    small[big] = 0
+    row_of = np.repeat(np.arange(lengths.size, dtype=np.int64), small)
+    cols = rng.integers(0, n_cols, size=row_of.size, dtype=np.int64)
+    parts = [row_of * n_cols + cols]
+    for r in big:
+        parts.append(r * n_cols + rng.choice(n_cols, int(lengths[r]), replace=False).astype(np.int64))
+    keys = _sorted_unique(np.concatenate(parts) if big.size else parts[0])
     # refill duplicates until every row has its length (a few rounds at most)
     for _ in range(64):
         got = np.bincount(keys // n_cols, minlength=lengths.size)
@@ -91,7 +110,7 @@ def _rows_with_lengths(rng, lengths: np.ndarray, n_cols: int) -> tuple[np.ndarra
             break
         need = np.repeat(np.arange(lengths.size, dtype=np.int64), short)
         extra = need * n_cols + rng.integers(0, n_cols, size=need.size, dtype=np.int64)
-        keys = np.unique(np.concatenate([keys, extra]))
+        keys = _sorted_unique(np.concatenate([keys, extra]))
     return _from_sorted_keys(keys, lengths.size, n_cols)
 
 
@@ -151,7 +170,7 @@ def powerlaw_graph(n_nodes: int, n_edges: int, exponent: float = 2.1, seed: int 
         u, v = u[ok], v[ok]
         if undirected:
             u, v = np.minimum(u, v), np.maximum(u, v)
-        fresh = np.setdiff1d(np.unique(u * n_nodes + v), keys, assume_unique=True)
+        fresh = np.setdiff1d(_sorted_unique(u * n_nodes + v), keys, assume_unique=True)
         fresh = rng.permutation(fresh)[:need]
         keys = np.union1d(keys, fresh)
     keys = keys[:target] if keys.size > target else keys
@@ -161,7 +180,7 @@ def powerlaw_graph(n_nodes: int, n_edges: int, exponent: float = 2.1, seed: int 
     if self_loops:
         ids = np.arange(n_nodes, dtype=np.int64)
         u, v = np.concatenate([u, ids]), np.concatenate([v, ids])
-    allk = np.unique(u * n_nodes + v)
+    allk = _sorted_unique(u * n_nodes + v)
     rowptr, colind = _from_sorted_keys(allk, n_nodes, n_nodes)
     return CSR(rowptr, colind, np.ones(colind.size, np.float32), n_nodes, n_nodes)
 

@@ -123,3 +123,32 @@ def test_gcn_training_is_reproducible():
     l1, l2 = run(), run()
     assert torch.equal(l1, l2)
     assert torch.isfinite(l1).all() and l1[-1] < l1[0]
+
+
+def test_captured_epoch_matches_eager():
+    """The CUDA-graph epoch replays the same training step as the eager one: with dropout off
+    and the same initial weights, losses agree epoch by epoch; with dropout on, training
+    still converges and fresh masks are drawn per replay."""
+    from armsparse_gb300 import selector
+    x, g, y, train, _ = gcn.synthetic_task(seed=0)
+    g.selector = selector.Selector.load()
+    idx = train.nonzero().squeeze(1)
+
+    def make(dropout):
+        torch.manual_seed(0)
+        model = gcn.Net(x.shape[1], 64, 3, dropout=dropout).to(dev())
+        return model, gcn.make_optimizer(model, capturable=True)
+
+    m1, o1 = make(0.0)
+    eager = [float(gcn.train_epoch(m1, o1, x, g, y, idx)) for _ in range(13)]
+    m2, o2 = make(0.0)
+    step = gcn.CapturedEpoch(m2, o2, x, g, y, train, warmup=3)
+    replay = [float(step()) for _ in range(10)]
+    assert np.allclose(replay, eager[3:], rtol=0, atol=1e-5), (replay, eager[3:])
+
+    m3, o3 = make(0.5)
+    step = gcn.CapturedEpoch(m3, o3, x, g, y, train, warmup=3)
+    losses = [float(step()) for _ in range(30)]
+    assert np.isfinite(losses).all() and losses[-1] < losses[0]
+    with pytest.raises(ValueError):
+        gcn.CapturedEpoch(m3, gcn.make_optimizer(m3), x, g, y, train)

@@ -241,3 +241,61 @@ def test_reduce_aggregations(oracle, op):
             ref = oracle.spmm_reduce_f32(a.rowptr, a.colind, B, val=val, op=op)
             assert np.array_equal(bits(got), bits(ref)), (op, N_, val is None)
     A.sync_status()
+
+
+def _skewed(seed, n_rows=3000, n_cols=40000, long_lens=(50000, 4097, 2048, 257, 256, 300)):
+    """Short rows plus rows at and past the long-row threshold (256 entries): one long enough
+    to cross many (colind, val) chunks of 2048 entries."""
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(0, 40, n_rows)
+    for i, l in enumerate(long_lens):
+        lens[7 + 211 * i] = min(l, n_cols)
+    lens[:5] = 0
+    rp = np.zeros(n_rows + 1, np.int32)
+    np.cumsum(lens, out=rp[1:])
+    ci = np.concatenate([np.sort(rng.choice(n_cols, l, replace=False)) for l in lens]).astype(np.int32)
+    return S.CSR(rp, ci, rng.uniform(-1, 1, ci.size).astype(np.float32), n_rows, n_cols)
+
+
+@pytest.mark.parametrize("N_", [47, 64, 256, 300])
+def test_long_rows_row_split_bit_exact(oracle, N_):
+    """Rows longer than 256 entries go to the long-row kernel; every row-split variant stays
+    bit-identical to the reference's chain, for 16-byte and 4-byte copy layouts (N = 47 and 300
+    give 4-byte copies), with beta = 1 accumulation, and call after call."""
+    a = _skewed(7 + N_)
+    B = S.dense_uniform((a.n_cols, N_), 8)
+    ref = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, B)
+    ref2 = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, B, C=ref)
+    rp, ci, v = csr_dev(a)
+    Bd = to_dev(B)
+    names = A.spmm_variants()
+    for var in [0] + _variant_ids("rowsplit"):
+        try:
+            C = A.spmm(rp, ci, v, Bd, variant=var)
+        except N.NativeError as e:
+            assert e.status == 3
+            continue
+        assert np.array_equal(bits(C), bits(ref)), names[var - 1] if var else "default"
+        A.spmm(rp, ci, v, Bd, C=C, beta=1.0, variant=var)
+        assert np.array_equal(bits(C), bits(ref2)), names[var - 1] if var else "default"
+    A.sync_status()
+
+
+def test_long_rows_strided_and_bf16(oracle):
+    a = _skewed(99)
+    rp, ci, v = csr_dev(a)
+    # B and C inside wider buffers (ldb = 72, ldc = 80)
+    Bw = S.dense_uniform((a.n_cols, 72), 3)
+    ref = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, np.ascontiguousarray(Bw[:, :64]))
+    Cw = torch.zeros((a.n_rows, 80), device=dev())
+    A.spmm(rp, ci, v, to_dev(Bw)[:, :64], C=Cw[:, 8:72])
+    assert np.array_equal(bits(Cw[:, 8:72].contiguous()), bits(ref))
+    assert torch.count_nonzero(Cw[:, :8]) == 0 and torch.count_nonzero(Cw[:, 72:]) == 0
+    # bf16 storage: the same chain over the bf16-rounded inputs
+    for N_ in (64, 256, 46):
+        B = S.dense_uniform((a.n_cols, N_), N_)
+        vb, Bb = oracle.bf16_round(a.val), oracle.bf16_round(B)
+        refb = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, vb, Bb)
+        C = A.spmm(rp, ci, v.to(torch.bfloat16), to_dev(B).to(torch.bfloat16))
+        assert np.array_equal(bits(C), bits(refb)), N_
+    A.sync_status()
