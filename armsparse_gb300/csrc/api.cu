@@ -24,23 +24,19 @@ as_status scratch(as_ctx *ctx, size_t bytes, void **out) {
     bytes = (bytes + 255) & ~size_t(255);
     if (bytes == 0) bytes = 256;
     if (bytes > ctx->scratch_bytes) {
-        if (ctx->scratch) {
-            cudaError_t e = cudaDeviceSynchronize();
-            if (e != cudaSuccess) return check_cuda(e, "scratch sync");
-            cudaFree(ctx->scratch);
-            ctx->scratch = nullptr;
-            ctx->scratch_bytes = 0;
-        }
         size_t grow = bytes + bytes / 4;
-        if (cudaMalloc(&ctx->scratch, grow) != cudaSuccess) {
+        void *p = nullptr;
+        if (cudaMalloc(&p, grow) != cudaSuccess) {
             cudaGetLastError();
-            if (cudaMalloc(&ctx->scratch, bytes) != cudaSuccess) {
+            if (cudaMalloc(&p, bytes) != cudaSuccess) {
                 cudaGetLastError();
                 return fail(AS_ERR_ALLOC, "scratch allocation of " + std::to_string(bytes) +
                                               " bytes failed");
             }
             grow = bytes;
         }
+        if (ctx->scratch) ctx->retired.push_back(ctx->scratch);
+        ctx->scratch = p;
         ctx->scratch_bytes = grow;
     }
     *out = ctx->scratch;
@@ -135,6 +131,7 @@ as_status as_ctx_destroy(as_ctx *c) {
     DeviceGuard g(c->device);
     cudaDeviceSynchronize();
     if (c->scratch) cudaFree(c->scratch);
+    for (void *p : c->retired) cudaFree(p);
     if (c->d_status) cudaFree(c->d_status);
     delete c;
     return AS_OK;

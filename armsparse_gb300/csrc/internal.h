@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "armsparse_gpu.h"
 
@@ -17,6 +18,8 @@ struct as_ctx {
     int sms = 1;                   // multiprocessors of the device
     void *scratch = nullptr;       // scratch arena
     size_t scratch_bytes = 0;
+    std::vector<void *> retired;   // outgrown arenas: kept until the context is destroyed, since
+                                   // kernels in flight or recorded in a CUDA graph may use them
     uint64_t launches = 0;         // kernels this library launched through the context
 };
 
@@ -26,7 +29,9 @@ namespace as {
 as_status fail(as_status s, const std::string &msg);
 // Maps a CUDA error (from the last launch or a runtime call) to AS_ERR_CUDA with its text.
 as_status check_cuda(cudaError_t e, const char *what);
-// Scratch arena of at least `bytes` (256-byte aligned); grows by reallocation.
+// Scratch arena of at least `bytes` (256-byte aligned). Growing allocates a larger arena and
+// retires the old one (freed by as_ctx_destroy), so no call synchronises or invalidates a
+// pointer that earlier work still holds.
 as_status scratch(as_ctx *ctx, size_t bytes, void **out);
 
 // ---- launchers (return AS_OK or an error; count launches in ctx) ----
@@ -43,7 +48,7 @@ struct SpmmArgs {
 as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cudaStream_t s);
 as_status spmm_reduce_launch(as_ctx *ctx, int op, const SpmmArgs &a, cudaStream_t s);
 as_status spmm_nnz_launch(as_ctx *ctx, int dtype, int vb, int group, int cpl, int chunk,
-                          const SpmmArgs &a, cudaStream_t s);
+                          int unroll, const SpmmArgs &a, cudaStream_t s);
 as_status spmm_bulk_launch(as_ctx *ctx, int dtype, int lane_bytes, int stages, const SpmmArgs &a,
                            cudaStream_t s);
 // Long rows of the row-split kernels: the cp.async size (16 or 4 bytes) the layout allows,

@@ -527,54 +527,81 @@ sddmm_tc_persistent(const __grid_constant__ CUtensorMap tmXhi, const __grid_cons
     }
 }
 
-// occ[tm * tiles_n + tn] = 1 for every output tile holding a pattern entry (one warp per row;
-// concurrent stores of the same value).
+// One warp per row: flags rows whose columns do not ascend (or leave [0, N)), and sets
+// occ[tm * tiles_n + tn] = 1 for every output tile holding a pattern entry -- one store per
+// (row, tile) since the columns ascend (the first entry of the row in each tile stores).
 __global__ void __launch_bounds__(256)
-mark_tiles(int M, int N, int nnz, const int *__restrict__ rowptr, const int *__restrict__ colind,
-           int BN, int tiles_n, unsigned char *__restrict__ occ) {
+check_and_mark(int M, int N, int nnz, const int *__restrict__ rowptr,
+               const int *__restrict__ colind, int BN, int tiles_n, unsigned char *__restrict__ occ,
+               unsigned *status) {
     const long w = (static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= M) return;
-    int lo = __ldg(rowptr + w), hi = __ldg(rowptr + w + 1);
-    if (lo < 0 || hi < lo || hi > nnz) return;
+    int lo, hi;
+    row_range(rowptr, static_cast<int>(w), nnz, status, lo, hi);
     unsigned char *rowocc = occ + (w / kBM) * static_cast<long>(tiles_n);
+    bool bad = false;
     for (int e = lo + lane; e < hi; e += 32) {
         const int c = __ldg(colind + e);
-        if (c >= 0 && c < N) rowocc[c / BN] = 1;
+        const int prev = e > lo ? __ldg(colind + e - 1) : -1;
+        if (c < 0 || c >= N || prev >= c)
+            bad = true;
+        else if (prev < 0 || prev / BN != c / BN)
+            rowocc[c / BN] = 1;
+    }
+    if (__any_sync(0xffffffffu, bad) && lane == 0) flag(status, kFlagBadColind);
+}
+
+// X's rows then Y's rows -> bf16 hi/lo planes: hi = bf16(x), lo = bf16(x - hi), columns
+// [K, Kp) zero. A block takes (row, 4096-column segment) items; each thread issues its four
+// 16-byte loads before converting, so a block keeps 16 KB of loads in flight.
+__global__ void __launch_bounds__(256)
+split_xy(long M, long N, int K, int Kp, const float *__restrict__ X, long ldx, bool vx,
+         const float *__restrict__ Y, long ldy, bool vy, uint16_t *__restrict__ xhi,
+         uint16_t *__restrict__ xlo, uint16_t *__restrict__ yhi, uint16_t *__restrict__ ylo) {
+    constexpr int kSeg = 4096;
+    const long segs = (Kp + kSeg - 1) / kSeg;
+    const long items = (M + N) * segs;
+    for (long item = blockIdx.x; item < items; item += gridDim.x) {
+        const long row = item / segs;
+        const int base = static_cast<int>(item - row * segs) * kSeg;
+        const bool isx = row < M;
+        const long r = isx ? row : row - M;
+        const float *x = isx ? X + r * ldx : Y + r * ldy;
+        const bool vec = isx ? vx : vy;
+        uint16_t *hi = (isx ? xhi : yhi) + r * Kp, *lo = (isx ? xlo : ylo) + r * Kp;
+        float v[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int k = base + (u * 256 + static_cast<int>(threadIdx.x)) * 4;
+            if (vec && k + 4 <= K) {
+                const float4 t = __ldcs(reinterpret_cast<const float4 *>(x + k));
+                v[u][0] = t.x; v[u][1] = t.y; v[u][2] = t.z; v[u][3] = t.w;
+            } else {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) v[u][i] = k + i < K ? __ldcs(x + k + i) : 0.0f;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int k = base + (u * 256 + static_cast<int>(threadIdx.x)) * 4;
+            if (k >= Kp) continue;
+            uint16_t h[4], l[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                h[i] = f32_to_bf16(v[u][i]);
+                l[i] = f32_to_bf16(v[u][i] - bf16_to_f32(h[i]));
+            }
+            *reinterpret_cast<uint2 *>(hi + k) =
+                make_uint2(h[0] | (unsigned(h[1]) << 16), h[2] | (unsigned(h[3]) << 16));
+            *reinterpret_cast<uint2 *>(lo + k) =
+                make_uint2(l[0] | (unsigned(l[1]) << 16), l[2] | (unsigned(l[3]) << 16));
+        }
     }
 }
 
 // hi = bf16(x), lo = bf16(x - hi); columns [K, Kp) are zero. Blocks stride over rows,
 // threads over groups of four columns.
-template <bool VEC>
-__global__ void __launch_bounds__(256)
-split_bf16(long rows, int K, int Kp, const float *__restrict__ src, long ld,
-           uint16_t *__restrict__ hi, uint16_t *__restrict__ lo) {
-    for (long r = blockIdx.x; r < rows; r += gridDim.x) {
-        const float *x = src + r * ld;
-        for (int k = threadIdx.x * 4; k < Kp; k += blockDim.x * 4) {
-            float v[4];
-            if (VEC && k + 4 <= K) {
-                const float4 t = __ldg(reinterpret_cast<const float4 *>(x + k));
-                v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
-            } else {
-#pragma unroll
-                for (int i = 0; i < 4; ++i) v[i] = k + i < K ? __ldg(x + k + i) : 0.0f;
-            }
-            uint16_t h[4], l[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                h[i] = f32_to_bf16(v[i]);
-                l[i] = f32_to_bf16(v[i] - bf16_to_f32(h[i]));
-            }
-            const long o = r * Kp + k;
-            *reinterpret_cast<uint2 *>(hi + o) =
-                make_uint2(h[0] | (unsigned(h[1]) << 16), h[2] | (unsigned(h[3]) << 16));
-            *reinterpret_cast<uint2 *>(lo + o) =
-                make_uint2(l[0] | (unsigned(l[1]) << 16), l[2] | (unsigned(l[3]) << 16));
-        }
-    }
-}
 
 // Columns must ascend within rows for the tile walk; flag rows that break it (one warp per
 // row, coalesced).
@@ -666,12 +693,8 @@ as_status launch_persistent(as_ctx *ctx, int M, int N, int Kp, int nnz, const in
         !make_map(&myh, yhi, N, Kp, BN, BK) || !make_map(&myl, ylo, N, Kp, BN, BK))
         return fail(AS_ERR_CUDA, "sddmm_bf16x3: cuTensorMapEncodeTiled failed");
     const int tiles_m = static_cast<int>(ceil_div(M, kBM)), tiles_n = static_cast<int>(ceil_div(N, BN));
-    cudaError_t e = cudaMemsetAsync(occ, 0, static_cast<size_t>(tiles_m) * tiles_n, s);
-    if (e != cudaSuccess) return check_cuda(e, "sddmm_bf16x3: occupancy clear");
-    mark_tiles<<<static_cast<unsigned>(ceil_div(static_cast<long>(M) * 32, 256)), 256, 0, s>>>(
-        M, N, nnz, rowptr, colind, BN, tiles_n, occ);
     const int smem = PSmem<BN, BK>::kBytes;
-    e = cudaFuncSetAttribute(sddmm_tc_persistent<BN, BK>,
+    cudaError_t e = cudaFuncSetAttribute(sddmm_tc_persistent<BN, BK>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return check_cuda(e, "sddmm_bf16x3: shared memory attribute");
     const long ntiles = static_cast<long>(tiles_m) * tiles_n;
@@ -679,7 +702,7 @@ as_status launch_persistent(as_ctx *ctx, int M, int N, int Kp, int nnz, const in
     sddmm_tc_persistent<BN, BK><<<grid, kThreads, smem, s>>>(
         mxh, mxl, myh, myl, M, N, Kp / BK, nnz, rowptr, colind, aval, out, occ, tiles_m, tiles_n,
         ctx->d_status);
-    ctx->launches += 2;
+    ctx->launches++;
     return check_cuda(cudaGetLastError(), "sddmm_bf16x3 persistent launch");
 }
 
@@ -694,38 +717,44 @@ as_status sddmm_bf16x3_launch(as_ctx *ctx, int M, int N, int K, int nnz, const i
                               const float *Y, long ldy, float *out, int variant, cudaStream_t s) {
     if (variant == 0) variant = 3;  // persistent, 4-stage pipeline: fastest on GB300
     if (M == 0) return fail(AS_ERR_INVALID_CSR, "sddmm: nnz > 0 with zero rows");
-    check_sorted_rows<<<static_cast<unsigned>(ceil_div(static_cast<long>(M) * 32, 256)), 256, 0, s>>>(
-        M, N, nnz, rowptr, colind, ctx->d_status);
+    const int BN = 256;
+    const int Kp = static_cast<int>(ceil_div(K, kBK) * kBK);
+    const size_t xs = static_cast<size_t>(M) * Kp * 2, ys = static_cast<size_t>(N) * Kp * 2;
+    auto al = [](size_t b) { return (b + 1023) & ~size_t(1023); };
+    const int tiles_m = static_cast<int>(ceil_div(M, kBM)), tiles_n = static_cast<int>(ceil_div(N, BN));
+    const size_t occ_bytes = static_cast<size_t>(tiles_m) * tiles_n;
+    void *w = nullptr;
+    as_status st = scratch(ctx, 2 * al(xs) + 2 * al(ys) + al(occ_bytes), &w);
+    if (st != AS_OK) return st;
+    uint8_t *p = static_cast<uint8_t *>(w);
+    unsigned char *occ = p + 2 * al(xs) + 2 * al(ys);
+    const unsigned rows_grid = static_cast<unsigned>(ceil_div(static_cast<long>(M) * 32, 256));
+    if (variant == 1 || K == 0) {
+        check_sorted_rows<<<rows_grid, 256, 0, s>>>(M, N, nnz, rowptr, colind, ctx->d_status);
+    } else {
+        cudaError_t e = cudaMemsetAsync(occ, 0, occ_bytes, s);
+        if (e != cudaSuccess) return check_cuda(e, "sddmm_bf16x3: occupancy clear");
+        check_and_mark<<<rows_grid, 256, 0, s>>>(M, N, nnz, rowptr, colind, BN, tiles_n, occ,
+                                                 ctx->d_status);
+    }
     ctx->launches++;
     if (K == 0) {
         fill_zero<<<static_cast<unsigned>(ceil_div(nnz, 256) < 4096 ? ceil_div(nnz, 256) : 4096), 256, 0, s>>>(out, nnz);
         ctx->launches++;
         return check_cuda(cudaGetLastError(), "sddmm_bf16x3 fill");
     }
-    const int Kp = static_cast<int>(ceil_div(K, kBK) * kBK);
-    const size_t xs = static_cast<size_t>(M) * Kp * 2, ys = static_cast<size_t>(N) * Kp * 2;
-    auto al = [](size_t b) { return (b + 1023) & ~size_t(1023); };
-    const size_t occ_bytes = static_cast<size_t>(ceil_div(M, kBM)) * ceil_div(N, 256);
-    void *w = nullptr;
-    as_status st = scratch(ctx, 2 * al(xs) + 2 * al(ys) + al(occ_bytes), &w);
-    if (st != AS_OK) return st;
-    uint8_t *p = static_cast<uint8_t *>(w);
     uint16_t *xhi = reinterpret_cast<uint16_t *>(p);
     uint16_t *xlo = reinterpret_cast<uint16_t *>(p + al(xs));
     uint16_t *yhi = reinterpret_cast<uint16_t *>(p + 2 * al(xs));
     uint16_t *ylo = reinterpret_cast<uint16_t *>(p + 2 * al(xs) + al(ys));
-    const unsigned sbx = static_cast<unsigned>(M < 152 * 16 ? M : 152 * 16);
-    const unsigned sby = static_cast<unsigned>(N < 152 * 16 ? N : 152 * 16);
     const bool vx = ldx % 4 == 0 && reinterpret_cast<uintptr_t>(X) % 16 == 0;
     const bool vy = ldy % 4 == 0 && reinterpret_cast<uintptr_t>(Y) % 16 == 0;
-    if (vx) split_bf16<true><<<sbx, 256, 0, s>>>(M, K, Kp, X, ldx, xhi, xlo);
-    else split_bf16<false><<<sbx, 256, 0, s>>>(M, K, Kp, X, ldx, xhi, xlo);
-    if (vy) split_bf16<true><<<sby, 256, 0, s>>>(N, K, Kp, Y, ldy, yhi, ylo);
-    else split_bf16<false><<<sby, 256, 0, s>>>(N, K, Kp, Y, ldy, yhi, ylo);
-    ctx->launches += 2;
+    const long items = (static_cast<long>(M) + N) * ceil_div(Kp, 4096);
+    const unsigned sg = static_cast<unsigned>(items < 152L * 8 ? items : 152L * 8);
+    split_xy<<<sg, 256, 0, s>>>(M, N, K, Kp, X, ldx, vx, Y, ldy, vy, xhi, xlo, yhi, ylo);
+    ctx->launches++;
     st = check_cuda(cudaGetLastError(), "sddmm_bf16x3 split");
     if (st != AS_OK) return st;
-    unsigned char *occ = p + 2 * al(xs) + 2 * al(ys);
     if (variant == 2)
         return launch_persistent<256, 64>(ctx, M, N, Kp, nnz, rowptr, colind, aval, out, xhi, xlo,
                                           yhi, ylo, occ, s);

@@ -17,100 +17,10 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "spmm_vec.cuh"
 
 namespace as {
 namespace {
-
-// Vector loads of B: Raw is the register form a load lands in (bf16 stays packed until the
-// FMA that consumes it, so a deep unroll keeps more bytes in flight per register).
-template <typename T, int VB>
-struct Vec;
-template <>
-struct Vec<float, 16> {
-    static constexpr int E = 4;
-    using Raw = float4;
-    __device__ static Raw raw(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
-    __device__ static float at(const Raw &r, int i) {
-        return i == 0 ? r.x : i == 1 ? r.y : i == 2 ? r.z : r.w;
-    }
-    __device__ static void load(const float *p, float *o) {
-        const Raw r = raw(p);
-        o[0] = r.x; o[1] = r.y; o[2] = r.z; o[3] = r.w;
-    }
-};
-template <>
-struct Vec<float, 8> {
-    static constexpr int E = 2;
-    using Raw = float2;
-    __device__ static Raw raw(const float *p) { return __ldg(reinterpret_cast<const float2 *>(p)); }
-    __device__ static float at(const Raw &r, int i) { return i == 0 ? r.x : r.y; }
-    __device__ static void load(const float *p, float *o) {
-        const Raw r = raw(p);
-        o[0] = r.x; o[1] = r.y;
-    }
-};
-template <>
-struct Vec<float, 4> {
-    static constexpr int E = 1;
-    using Raw = float;
-    __device__ static Raw raw(const float *p) { return __ldg(p); }
-    __device__ static float at(const Raw &r, int) { return r; }
-    __device__ static void load(const float *p, float *o) { o[0] = __ldg(p); }
-};
-__device__ __forceinline__ float bf16_lo(unsigned w) { return __uint_as_float(w << 16); }
-__device__ __forceinline__ float bf16_hi(unsigned w) { return __uint_as_float(w & 0xffff0000u); }
-template <>
-struct Vec<uint16_t, 16> {
-    static constexpr int E = 8;
-    using Raw = uint4;
-    __device__ static Raw raw(const uint16_t *p) { return __ldg(reinterpret_cast<const uint4 *>(p)); }
-    __device__ static float at(const Raw &r, int i) {
-        const unsigned w = (i >> 1) == 0 ? r.x : (i >> 1) == 1 ? r.y : (i >> 1) == 2 ? r.z : r.w;
-        return (i & 1) ? bf16_hi(w) : bf16_lo(w);
-    }
-    __device__ static void load(const uint16_t *p, float *o) {
-        const Raw r = raw(p);
-#pragma unroll
-        for (int i = 0; i < 8; ++i) o[i] = at(r, i);
-    }
-};
-template <>
-struct Vec<uint16_t, 8> {
-    static constexpr int E = 4;
-    using Raw = uint2;
-    __device__ static Raw raw(const uint16_t *p) { return __ldg(reinterpret_cast<const uint2 *>(p)); }
-    __device__ static float at(const Raw &r, int i) {
-        const unsigned w = (i >> 1) == 0 ? r.x : r.y;
-        return (i & 1) ? bf16_hi(w) : bf16_lo(w);
-    }
-    __device__ static void load(const uint16_t *p, float *o) {
-        const Raw r = raw(p);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) o[i] = at(r, i);
-    }
-};
-template <>
-struct Vec<uint16_t, 4> {
-    static constexpr int E = 2;
-    using Raw = unsigned;
-    __device__ static Raw raw(const uint16_t *p) { return __ldg(reinterpret_cast<const unsigned *>(p)); }
-    __device__ static float at(const Raw &r, int i) { return (i & 1) ? bf16_hi(r) : bf16_lo(r); }
-    __device__ static void load(const uint16_t *p, float *o) {
-        const Raw r = raw(p);
-        o[0] = bf16_lo(r); o[1] = bf16_hi(r);
-    }
-};
-template <>
-struct Vec<uint16_t, 2> {
-    static constexpr int E = 1;
-    using Raw = unsigned short;
-    __device__ static Raw raw(const uint16_t *p) { return __ldg(reinterpret_cast<const unsigned short *>(p)); }
-    __device__ static float at(const Raw &r, int) { return __uint_as_float(static_cast<unsigned>(r) << 16); }
-    __device__ static void load(const uint16_t *p, float *o) { o[0] = at(raw(p), 0); }
-};
-
-__device__ __forceinline__ float to_f32(float v) { return v; }
-__device__ __forceinline__ float to_f32(uint16_t v) { return bf16_to_f32(v); }
 
 template <int E>
 __device__ __forceinline__ void store_c(float *p, const float *v) {
@@ -252,12 +162,12 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 }
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
-                    const float vu = kk[u] < 0 ? 0.0f : vv[u];
+                    // v came from bf16, so its fp32 bits are the bf16 bits followed by zeros
+                    const unsigned short vu = kk[u] < 0
+                        ? static_cast<unsigned short>(0)
+                        : static_cast<unsigned short>(__float_as_uint(vv[u]) >> 16);
 #pragma unroll
-                    for (int j = 0; j < CPL; ++j)
-#pragma unroll
-                        for (int i = 0; i < E; ++i)
-                            acc[j][i] = fmaf(V::at(b[u][j], i), vu, acc[j][i]);
+                    for (int j = 0; j < CPL; ++j) V::fma(b[u][j], vu, acc[j]);
                 }
             }
         }
@@ -291,13 +201,18 @@ struct Variant {
     int vb, group, cpl, unroll;
     const char *name;
     int kind;  // 0 = row-split (registers), 1 = bulk-copy staged (spmm_bulk.cu: vb = bytes per
-               // lane, unroll = ring stages), 2 = nnz-split (spmm_nnz.cu: unroll = chunk size)
+               // lane, unroll = ring stages), 2 = nnz-split (spmm_nnz.cu: unroll = chunk size,
+               // steps = entries per load batch)
+    int steps = 4;
 };
 
 #define AS_V(vb, g, c, u) {vb, g, c, u, "rowsplit_v" #vb "_g" #g "_c" #c "_u" #u, 0}
 #define AS_BULK(lb, st) {lb, 32, 1, st, "bulk_lb" #lb "_s" #st, 1}
 #define AS_BULKS AS_BULK(16, 8), AS_BULK(32, 8), AS_BULK(16, 16), AS_BULK(32, 4)
 #define AS_NNZ(vb, g, c, ch) {vb, g, c, ch, "nnzsplit_v" #vb "_g" #g "_c" #c "_ch" #ch, 2}
+#define AS_NNZ8(vb, g, c, ch) {vb, g, c, ch, "nnzsplit_v" #vb "_g" #g "_c" #c "_ch" #ch "_u8", 2, 8}
+#define AS_NNZS8(ch) AS_NNZ8(16, 16, 1, ch), AS_NNZ8(16, 32, 1, ch), AS_NNZ8(16, 32, 2, ch), \
+    AS_NNZ8(4, 32, 1, ch), AS_NNZ8(4, 32, 2, ch)
 #define AS_NNZS(ch) AS_NNZ(16, 8, 1, ch), AS_NNZ(16, 16, 1, ch), AS_NNZ(16, 32, 1, ch), \
     AS_NNZ(16, 32, 2, ch), AS_NNZ(4, 32, 1, ch), AS_NNZ(4, 32, 2, ch)
 #define AS_NNZS_BF16_SCALAR(ch) AS_NNZ(2, 32, 1, ch), AS_NNZ(2, 32, 2, ch)
@@ -306,10 +221,11 @@ struct Variant {
 #define AS_VROW(vb) AS_VG(vb, 1), AS_VG(vb, 2), AS_VG(vb, 4), AS_VG(vb, 8), AS_VG(vb, 16), AS_VG(vb, 32)
 
 const Variant kF32[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_BULKS, AS_NNZS(128),
-                        AS_NNZS(1024)};
+                        AS_NNZS(1024), AS_NNZS8(256), AS_NNZS8(1024)};
 const Variant kBF16[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_VROW(2), AS_BULKS,
                          AS_NNZS(128), AS_NNZS(1024), AS_NNZS_BF16_SCALAR(128),
-                         AS_NNZS_BF16_SCALAR(1024)};
+                         AS_NNZS_BF16_SCALAR(1024), AS_NNZS8(256), AS_NNZS8(1024),
+                         AS_NNZ8(2, 32, 2, 256), AS_NNZ8(2, 32, 2, 1024)};
 constexpr int kNF32 = sizeof(kF32) / sizeof(kF32[0]);
 constexpr int kNBF16 = sizeof(kBF16) / sizeof(kBF16[0]);
 
@@ -453,7 +369,8 @@ bool spmm_variant_supported(int dtype, int variant, int N, long ldb, long ldc, c
 as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cudaStream_t s) {
     const Variant &v = dtype == 0 ? kF32[variant - 1] : kBF16[variant - 1];
     if (v.kind == 1) return spmm_bulk_launch(ctx, dtype, v.vb, v.unroll, a, s);
-    if (v.kind == 2) return spmm_nnz_launch(ctx, dtype, v.vb, v.group, v.cpl, v.unroll, a, s);
+    if (v.kind == 2)
+        return spmm_nnz_launch(ctx, dtype, v.vb, v.group, v.cpl, v.unroll, v.steps, a, s);
     if (!vb_ok(dtype, v.vb, a.N, a.ldb, a.ldc, a.B, a.C))
         return fail(AS_ERR_UNSUPPORTED, std::string("spmm: variant ") + v.name +
                                             " needs N, ldb, ldc and pointer alignment to match its vector width");

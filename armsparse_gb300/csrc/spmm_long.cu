@@ -66,7 +66,7 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
     const int slice0 = blockIdx.y * W;
     const int w = min(W, N - slice0);         // columns of this slice
     const int seg = w * static_cast<int>(sizeof(T));  // bytes of B per entry in this slice
-    const int pieces = seg / GB;              // cp.async pieces per entry
+    const int pieces = seg / GB;              // cp.async pieces per entry (<= 64)
     const int n_long = static_cast<int>(
         min(*reinterpret_cast<volatile unsigned *>(counters), static_cast<unsigned>(M)));
 
@@ -89,6 +89,7 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 if (static_cast<unsigned>(k) >= static_cast<unsigned>(K)) {
                     flag(status, kFlagBadColind);
                     k = -1;
+                    v = 0.0f;
                 }
             }
             kbuf[i] = k;
@@ -96,21 +97,30 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         }
         __syncthreads();
 
-        // B segments of stage st into ring slot st % kStages (entries past the row: none)
+        // B segments of stage st into ring slot st % kStages: warp w copies entries w, w + 8,
+        // ..., its lanes the segment's pieces (at most 64). Entries past the row are not
+        // copied (never read); a flagged entry gets zeros (its value is 0 as well).
+        const int warp = tid >> 5, lane = tid & 31;
         auto issue = [&](int st) {
             if (st < n_stages) {
                 const int base = st * kStage;  // first entry of the stage, relative to lo
                 const int *kb = kbuf + ((base / kChunk) & 1) * kChunk + base % kChunk;
                 unsigned char *dst = ring + (st % kStages) * kStage * kSliceBytes;
-                const int total = kStage * pieces;
-                for (int p = tid; p < total; p += kThreads) {
-                    const int j = p / pieces, q = p - j * pieces;
-                    if (base + j >= L) continue;
+                for (int j = warp; j < kStage && base + j < L; j += kThreads / 32) {
                     const int k = kb[j];
-                    if (k < 0) continue;
                     const unsigned char *src = reinterpret_cast<const unsigned char *>(
-                        B + static_cast<long>(k) * ldb + slice0) + q * GB;
-                    cp_async<GB>(dst + j * kSliceBytes + q * GB, src);
+                        B + static_cast<long>(k < 0 ? 0 : k) * ldb + slice0);
+#pragma unroll
+                    for (int t = 0; t < 2; ++t) {
+                        const int q = lane + 32 * t;
+                        if (q >= pieces) break;
+                        if (k >= 0)
+                            cp_async<GB>(dst + j * kSliceBytes + q * GB, src + q * GB);
+                        else if constexpr (GB == 16)
+                            *reinterpret_cast<uint4 *>(dst + j * kSliceBytes + q * GB) = make_uint4(0, 0, 0, 0);
+                        else
+                            *reinterpret_cast<unsigned *>(dst + j * kSliceBytes + q * GB) = 0u;
+                    }
                 }
             }
             cp_async_commit();  // one group per stage, empty or not, to keep the counting uniform
@@ -145,12 +155,14 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
 #pragma unroll
                 for (int i = 0; i < kChunkPerThread; ++i) {
                     int k = kreg[i];
+                    float v = vreg[i];
                     if (k != -1 && static_cast<unsigned>(k) >= static_cast<unsigned>(K)) {
                         flag(status, kFlagBadColind);
                         k = -1;
+                        v = 0.0f;
                     }
                     kd[i * kThreads + tid] = k;
-                    vd[i * kThreads + tid] = vreg[i];
+                    vd[i * kThreads + tid] = v;
                 }
             }
             __syncthreads();  // slot (st - 1) % kStages is free; staged (colind, val) visible
@@ -160,12 +172,25 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
             if (tid < w) {
                 const int base = st * kStage;
                 const int n = min(kStage, L - base);
-                const int off = ((base / kChunk) & 1) * kChunk + base % kChunk;
-                const T *bs = reinterpret_cast<const T *>(ring + (st % kStages) * kStage * kSliceBytes);
-                for (int j = 0; j < n; ++j) {
-                    if (kbuf[off + j] < 0) continue;
-                    acc = fmaf(to_f32(bs[j * W + tid]), vbuf[off + j], acc);
+                const float *vs = vbuf + ((base / kChunk) & 1) * kChunk + base % kChunk;
+                const T *bs = reinterpret_cast<const T *>(ring + (st % kStages) * kStage * kSliceBytes) + tid;
+                int j = 0;
+                for (; j + 8 <= n; j += 8) {  // loads first, then the chain in entry order
+                    const float4 v0 = *reinterpret_cast<const float4 *>(vs + j);
+                    const float4 v1 = *reinterpret_cast<const float4 *>(vs + j + 4);
+                    float b[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) b[i] = to_f32(bs[(j + i) * W]);
+                    acc = fmaf(b[0], v0.x, acc);
+                    acc = fmaf(b[1], v0.y, acc);
+                    acc = fmaf(b[2], v0.z, acc);
+                    acc = fmaf(b[3], v0.w, acc);
+                    acc = fmaf(b[4], v1.x, acc);
+                    acc = fmaf(b[5], v1.y, acc);
+                    acc = fmaf(b[6], v1.z, acc);
+                    acc = fmaf(b[7], v1.w, acc);
                 }
+                for (; j < n; ++j) acc = fmaf(to_f32(bs[j * W]), vs[j], acc);
             }
         }
         cp_async_wait<0>();

@@ -14,59 +14,12 @@
 // Pass 3 (spmm_empty_rows): rows without entries get beta * C (zeros when beta == 0).
 #include "common.cuh"
 #include "internal.h"
+#include "spmm_vec.cuh"
 
 namespace as {
 namespace {
 
 constexpr int kThreads = 256;
-
-template <typename T, int VB>
-struct V;
-template <>
-struct V<float, 16> {
-    static constexpr int E = 4;
-    __device__ static void load(const float *p, float *o) {
-        const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
-        o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
-    }
-};
-template <>
-struct V<float, 4> {
-    static constexpr int E = 1;
-    __device__ static void load(const float *p, float *o) { o[0] = __ldg(p); }
-};
-template <>
-struct V<uint16_t, 16> {
-    static constexpr int E = 8;
-    __device__ static void load(const uint16_t *p, float *o) {
-        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
-        const unsigned w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            o[2 * i] = __uint_as_float(w[i] << 16);
-            o[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
-        }
-    }
-};
-template <>
-struct V<uint16_t, 2> {
-    static constexpr int E = 1;
-    __device__ static void load(const uint16_t *p, float *o) {
-        o[0] = bf16_to_f32(__ldg(reinterpret_cast<const unsigned short *>(p)));
-    }
-};
-template <>
-struct V<uint16_t, 4> {
-    static constexpr int E = 2;
-    __device__ static void load(const uint16_t *p, float *o) {
-        const unsigned v = __ldg(reinterpret_cast<const unsigned *>(p));
-        o[0] = __uint_as_float(v << 16);
-        o[1] = __uint_as_float(v & 0xffff0000u);
-    }
-};
-
-__device__ __forceinline__ float to_f32(float v) { return v; }
-__device__ __forceinline__ float to_f32(uint16_t v) { return bf16_to_f32(v); }
 
 __device__ __forceinline__ int find_row(const int *__restrict__ rowptr, int M, int e) {
     int lo = 0, hi = M;  // largest r with rowptr[r] <= e
@@ -80,13 +33,14 @@ __device__ __forceinline__ int find_row(const int *__restrict__ rowptr, int M, i
     return lo;
 }
 
-template <typename T, int VB, int GROUP, int CPL>
+template <typename T, int VB, int GROUP, int CPL, int U>
 __global__ void __launch_bounds__(kThreads)
 spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowptr,
               const int *__restrict__ colind, const T *__restrict__ val,
               const T *__restrict__ B, long ldb, float *__restrict__ C, long ldc, float beta,
               float *__restrict__ carry, unsigned *status) {
-    constexpr int E = V<T, VB>::E;
+    using V = Vec<T, VB>;
+    constexpr int E = V::E;
     constexpr int TILE = GROUP * E * CPL;
     const int lane = threadIdx.x & 31;
     const int g = threadIdx.x % GROUP;
@@ -134,33 +88,59 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
             }
             const int cnt = min(GROUP, se - base);
             int t = 0;
-            for (; t + 4 <= cnt; t += 4) {
-                int kk[4];
-                float vv[4];
+            // U entries per step, loads before FMAs (as in the row-split kernels: fp32 with
+            // per-load predicates, bf16 packed until the mixed-precision FMA)
+            for (; t + U <= cnt; t += U) {
+                int kk[U];
+                float vv[U];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
+                for (int u = 0; u < U; ++u) {
                     kk[u] = __shfl_sync(gmask, k, t + u, GROUP);
                     vv[u] = __shfl_sync(gmask, v, t + u, GROUP);
                 }
-                float b[4][CPL][E];
+                if constexpr (sizeof(T) == 4) {
+                    float b[U][CPL][E];
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
+                    for (int u = 0; u < U; ++u) {
+                        const T *brow = B + static_cast<long>(kk[u] < 0 ? 0 : kk[u]) * ldb;
 #pragma unroll
-                    for (int j = 0; j < CPL; ++j) {
-                        const int cc = tile0 + (j * GROUP + g) * E;
-                        if (cc < N && kk[u] >= 0)
-                            V<T, VB>::load(B + static_cast<long>(kk[u]) * ldb + cc, b[u][j]);
-                        else
+                        for (int j = 0; j < CPL; ++j) {
+                            const int cc = tile0 + (j * GROUP + g) * E;
+                            if (cc < N && kk[u] >= 0) {
+                                V::load(brow + cc, b[u][j]);
+                            } else {
 #pragma unroll
-                            for (int i = 0; i < E; ++i) b[u][j][i] = 0.0f;
+                                for (int i = 0; i < E; ++i) b[u][j][i] = 0.0f;
+                            }
+                        }
                     }
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
-                    if (kk[u] >= 0)
+                    for (int u = 0; u < U; ++u)
+                        if (kk[u] >= 0)
 #pragma unroll
-                        for (int j = 0; j < CPL; ++j)
+                            for (int j = 0; j < CPL; ++j)
 #pragma unroll
-                            for (int i = 0; i < E; ++i) acc[j][i] = fmaf(b[u][j][i], vv[u], acc[j][i]);
+                                for (int i = 0; i < E; ++i)
+                                    acc[j][i] = fmaf(b[u][j][i], vv[u], acc[j][i]);
+                } else {
+                    typename V::Raw b[U][CPL];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        const T *brow = B + static_cast<long>(kk[u] < 0 ? 0 : kk[u]) * ldb;
+#pragma unroll
+                        for (int j = 0; j < CPL; ++j) {
+                            const int cc = tile0 + (j * GROUP + g) * E;
+                            b[u][j] = V::raw(brow + (cc < N ? cc : 0));
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        if (kk[u] < 0) continue;
+                        const unsigned short vu = static_cast<unsigned short>(__float_as_uint(vv[u]) >> 16);
+#pragma unroll
+                        for (int j = 0; j < CPL; ++j) V::fma(b[u][j], vu, acc[j]);
+                    }
+                }
             }
             for (; t < cnt; ++t) {
                 const int kk = __shfl_sync(gmask, k, t, GROUP);
@@ -171,7 +151,7 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
                     const int cc = tile0 + (j * GROUP + g) * E;
                     if (cc < N) {
                         float b[E];
-                        V<T, VB>::load(B + static_cast<long>(kk) * ldb + cc, b);
+                        V::load(B + static_cast<long>(kk) * ldb + cc, b);
 #pragma unroll
                         for (int i = 0; i < E; ++i) acc[j][i] = fmaf(b[i], vv, acc[j][i]);
                     }
@@ -225,9 +205,9 @@ spmm_empty_rows(int M, int N, const int *__restrict__ rowptr, float *__restrict_
         C[r * ldc + col] = beta == 0.0f ? 0.0f : beta * C[r * ldc + col];
 }
 
-template <typename T, int VB, int G, int CPL>
+template <typename T, int VB, int G, int CPL, int U>
 as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, cudaStream_t s) {
-    constexpr int E = V<T, VB>::E;
+    constexpr int E = Vec<T, VB>::E;
     constexpr int TILE = G * E * CPL;
     const int esz = sizeof(T);
     if ((a.N % E) || (a.ldb % E) || (reinterpret_cast<uintptr_t>(a.B) % (E * esz)))
@@ -241,7 +221,7 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, cudaStream_t s) {
     if (nchunks > 0) {
         dim3 g1(static_cast<unsigned>(ceil_div(nchunks, kThreads / G)),
                 static_cast<unsigned>(ceil_div(a.N, TILE)));
-        spmm_nnzsplit<T, VB, G, CPL><<<g1, kThreads, 0, s>>>(
+        spmm_nnzsplit<T, VB, G, CPL, U><<<g1, kThreads, 0, s>>>(
             a.M, a.K, a.N, a.nnz, CH, a.rowptr, a.colind, static_cast<const T *>(a.val),
             static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, carry, a.status);
         dim3 g2(static_cast<unsigned>(nchunks),
@@ -259,9 +239,11 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, cudaStream_t s) {
 }  // namespace
 
 as_status spmm_nnz_launch(as_ctx *ctx, int dtype, int vb, int group, int cpl, int chunk,
-                          const SpmmArgs &a, cudaStream_t s) {
-#define AS_NNZ_CASE(T, VBV, G, C)                                      \
-    if (vb == VBV && group == G && cpl == C) return launch<T, VBV, G, C>(ctx, a, chunk, s);
+                          int unroll, const SpmmArgs &a, cudaStream_t s) {
+#define AS_NNZ_CASE(T, VBV, G, C)                                                   \
+    if (vb == VBV && group == G && cpl == C)                                        \
+        return unroll == 8 ? launch<T, VBV, G, C, 8>(ctx, a, chunk, s)              \
+                           : launch<T, VBV, G, C, 4>(ctx, a, chunk, s);
     if (dtype == 0) {
         AS_NNZ_CASE(float, 16, 8, 1) AS_NNZ_CASE(float, 16, 16, 1) AS_NNZ_CASE(float, 16, 32, 1)
         AS_NNZ_CASE(float, 16, 32, 2) AS_NNZ_CASE(float, 4, 32, 1) AS_NNZ_CASE(float, 4, 32, 2)

@@ -230,6 +230,8 @@ class CapturedEpoch:
             for _ in range(max(1, warmup)):
                 train_epoch(model, opt, x, g, y, train)
         torch.cuda.current_stream(dev).wait_stream(side)
+        # the recorded kernels read these tensors' memory at every replay: keep them alive
+        self.static = (model, opt, x, g, y, train)
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
             self.loss = train_epoch(model, opt, x, g, y, train)

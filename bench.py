@@ -598,7 +598,7 @@ class GcnLarge(Workload):
         raise NotImplementedError("no CPU arm at this size (hours on the host cores)")
 
     def cpu_value(self, threads, budget_s):
-        return float("nan"), "not run: the reference's CPU path at 62M edges takes hours"
+        return None, "not run: the reference's CPU path at 62M edges takes hours"
 
     def extra(self):
         import torch
@@ -866,7 +866,8 @@ def cpu_baseline(wl, budget_s=10.0):
     threads = os.cpu_count() or 1
     v, sample = wl.cpu_value(threads, budget_s)
     cores = getattr(wl, "cpu_threads_used", threads)
-    return {"value": round(v, 3), "unit": wl.unit, "cores": cores, "kind": "port",
+    return {"value": None if v is None else round(v, 3), "unit": wl.unit, "cores": cores,
+            "kind": "port",
             "sample": sample + " (oracle restatement of the reference kernel, OpenMP over all "
                                "host cores)"}
 

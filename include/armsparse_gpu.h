@@ -35,7 +35,8 @@ typedef struct as_ctx as_ctx;
 
 /* ---- context ---------------------------------------------------------------------------
  * One context per host thread and device. It owns the device status word and the scratch
- * arena (grown on demand; growth synchronises the device). */
+ * arena. The arena grows on demand: a larger one is allocated and the outgrown one is kept
+ * until as_ctx_destroy, so device work already issued keeps valid pointers. */
 as_status as_ctx_create(as_ctx **ctx, int device);
 as_status as_ctx_destroy(as_ctx *ctx);
 /* Waits for `stream`, returns and clears the device status word (AS_OK if no kernel since

@@ -292,10 +292,43 @@ def test_long_rows_strided_and_bf16(oracle):
     assert np.array_equal(bits(Cw[:, 8:72].contiguous()), bits(ref))
     assert torch.count_nonzero(Cw[:, :8]) == 0 and torch.count_nonzero(Cw[:, 72:]) == 0
     # bf16 storage: the same chain over the bf16-rounded inputs
-    for N_ in (64, 256, 46):
+    names = A.spmm_variants(torch.bfloat16)
+    for N_ in (64, 256, 46, 47):
         B = S.dense_uniform((a.n_cols, N_), N_)
         vb, Bb = oracle.bf16_round(a.val), oracle.bf16_round(B)
         refb = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, vb, Bb)
-        C = A.spmm(rp, ci, v.to(torch.bfloat16), to_dev(B).to(torch.bfloat16))
-        assert np.array_equal(bits(C), bits(refb)), N_
+        vd, Bd = v.to(torch.bfloat16), to_dev(B).to(torch.bfloat16)
+        for var in [0] + (_variant_ids("rowsplit", torch.bfloat16) if N_ == 64 else []):
+            try:
+                C = A.spmm(rp, ci, vd, Bd, variant=var)
+            except N.NativeError as e:
+                assert e.status == 3
+                continue
+            assert np.array_equal(bits(C), bits(refb)), (N_, names[var - 1] if var else "default")
+    A.sync_status()
+
+
+def test_nnzsplit_bf16_variants(oracle):
+    """bf16 storage through the entry-balanced kernels (4- and 8-entry load batches): fp32
+    accumulation error only, against FP64 of the bf16-rounded inputs; deterministic."""
+    a = _skewed(5, n_rows=2000, n_cols=30000, long_lens=(30000, 3000, 700))
+    rp, ci, v = csr_dev(a)
+    vb = oracle.bf16_round(a.val)
+    names = A.spmm_variants(torch.bfloat16)
+    for N_ in (64, 46):
+        B = S.dense_uniform((a.n_cols, N_), 6 + N_)
+        Bb = oracle.bf16_round(B)
+        R, Ab = oracle.spmm_f64(a.rowptr, a.colind, vb, Bb)
+        vd, Bd = v.to(torch.bfloat16), to_dev(B).to(torch.bfloat16)
+        ran = 0
+        for var in _variant_ids("nnzsplit", torch.bfloat16):
+            try:
+                C = A.spmm(rp, ci, vd, Bd, variant=var)
+            except N.NativeError as e:
+                assert e.status == 3
+                continue
+            ran += 1
+            assert oracle.scaled_err(C.cpu().numpy(), R, Ab).max() < 1e-5, names[var - 1]
+            assert torch.equal(C, A.spmm(rp, ci, vd, Bd, variant=var)), names[var - 1]
+        assert ran >= 4
     A.sync_status()
