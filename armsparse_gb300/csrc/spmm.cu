@@ -69,6 +69,9 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
     const int g = threadIdx.x % GROUP;
     const unsigned gmask =
         GROUP == 32 ? 0xffffffffu : (((1u << GROUP) - 1u) << (lane & ~(GROUP - 1)));
+    // let a programmatic dependent (the long-row kernel) be scheduled early; it waits for
+    // this grid to complete before it reads anything
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
     const long row = static_cast<long>(blockIdx.x) * (kThreads / GROUP) + threadIdx.x / GROUP;
     if (row >= M) return;  // the whole group leaves together
     int lo, hi;

@@ -8,7 +8,7 @@
 //
 // Each output element is still one fused-FMA chain over the row's entries in CSR order (the
 // order cannot be split without changing the bits), so the speed comes from feeding the
-// chains: a CTA owns one (long row, 256-byte column slice); all 256 threads copy B segments
+// chains: a CTA owns one (long row, 64-byte column slice); all 256 threads copy B segments
 // of upcoming entries into a shared-memory ring with cp.async (kStages stages of kStage
 // entries in flight), and the slice's columns -- one per consumer thread -- run their chains
 // out of shared memory. Column indices and values are staged a chunk of kChunk entries ahead
@@ -25,12 +25,16 @@ namespace as {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kSliceBytes = 256;  // B bytes per entry per stage (64 fp32 / 128 bf16 columns)
+constexpr int kSliceBytes = 64;   // B bytes per entry per stage (16 fp32 / 32 bf16 columns)
 constexpr int kStage = 64;        // entries per pipeline stage
-constexpr int kStages = 4;        // stages in the B ring
+constexpr int kStages = 12;       // stages in the B ring: 704 entries in flight cover the
+                                  // gather latency at the chain's ~4 cycles per entry
 constexpr int kChunk = 2048;      // entries per (colind, val) chunk; a multiple of kStage
 constexpr int kChunkPerThread = kChunk / kThreads;
 constexpr int kSmemBytes = kStages * kStage * kSliceBytes + 2 * kChunk * 8;
+// the next chunk's (colind, val) reach shared memory half a chunk in, before the B lookahead
+// of kStages - 1 stages first needs them
+static_assert(kStages - 1 < kChunk / kStage / 2, "B lookahead must not outrun the chunk staging");
 
 __device__ __forceinline__ float to_f32(float v) { return v; }
 __device__ __forceinline__ float to_f32(uint16_t v) { return bf16_to_f32(v); }
@@ -62,6 +66,9 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
     int *kbuf = reinterpret_cast<int *>(smem + kStages * kStage * kSliceBytes);  // [2][kChunk]
     float *vbuf = reinterpret_cast<float *>(kbuf + 2 * kChunk);                  // [2][kChunk]
 
+    // launched as a programmatic dependent of the row-split kernel: wait for it to finish
+    // (and its list writes to be visible) before reading the list
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
     const int tid = threadIdx.x;
     const int slice0 = blockIdx.y * W;
     const int w = min(W, N - slice0);         // columns of this slice
@@ -228,12 +235,25 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, const int *list, cudaStream_t s
     const int gy = static_cast<int>(ceil_div(a.N, W));
     const int gx = std::max(1, std::min(a.M, static_cast<int>(ceil_div(2 * ctx->sms, gy))));
     dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(gy));
-    k<<<grid, kThreads, kSmemBytes, s>>>(a.M, a.K, a.N, a.nnz, a.rowptr, a.colind,
-                                         static_cast<const T *>(a.val),
-                                         static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta,
-                                         a.status, list, ctx->d_long);
+    // programmatic dependent launch (outside stream capture): the CTAs are scheduled while
+    // the row-split kernel drains, hiding this launch when there are no long rows
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cap);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = kSmemBytes;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = cap == cudaStreamCaptureStatusNone ? 1 : 0;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k, a.M, a.K, a.N, a.nnz, a.rowptr, a.colind,
+                                       static_cast<const T *>(a.val), static_cast<const T *>(a.B),
+                                       a.ldb, a.C, a.ldc, a.beta, a.status, list, ctx->d_long);
     ctx->launches++;
-    return check_cuda(cudaGetLastError(), "spmm long rows launch");
+    return check_cuda(e != cudaSuccess ? e : cudaGetLastError(), "spmm long rows launch");
 }
 
 }  // namespace
