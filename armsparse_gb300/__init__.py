@@ -2,14 +2,16 @@
 
 CSR SpMM (fp32 bit-identical to the reference's rowBaseSpmm3; bf16 storage with fp32
 accumulation), CSR SpMV (plain and the reference's 1x4-blocked layout), SDDMM (FP32 CUDA
-cores and tcgen05 split-bf16) and a deterministic CSR->CSC transpose, behind the C ABI in
-include/armsparse_gpu.h. The ops need the CUDA library built in-tree and a GPU; there is no
-CPU fallback.
+cores and tcgen05 split-bf16), a deterministic CSR->CSC transpose, the sum/max aggregations
+and the sparse x sparse -> dense product, behind the C ABI in include/armsparse_gpu.h. The
+ops need the CUDA library built in-tree and a GPU; there is no CPU fallback.
 """
-from .sparse import (spmm_reduce, csr2csc, csr_to_vcsr4, dense_to_csr, sddmm, sddmm_coo, spmm, spmm_default_variant, spmm_variant_supported, spmm_variants, spmv,
-                     spmv_vcsr4, sync_status, to_bf16, validate_csr)
+from .sparse import (csr2csc, csr_to_vcsr4, dense_to_csr, sddmm, sddmm_coo, spgemm_dense, spmm,
+                     spmm_default_variant, spmm_reduce, spmm_variant_supported, spmm_variants,
+                     spmv, spmv_vcsr4, sync_status, to_bf16, validate_csr)
 from ._native import NativeError, Context, context
 
-__all__ = ["spmm_reduce", "csr_to_vcsr4", "dense_to_csr", "spmm", "spmv", "spmv_vcsr4", "sddmm", "sddmm_coo", "csr2csc", "validate_csr", "sync_status",
-           "to_bf16", "spmm_variants", "spmm_default_variant", "spmm_variant_supported", "NativeError", "Context",
-           "context"]
+__all__ = ["spmm", "spmm_reduce", "spgemm_dense", "spmv", "spmv_vcsr4", "sddmm", "sddmm_coo",
+           "csr2csc", "csr_to_vcsr4", "dense_to_csr", "validate_csr", "sync_status", "to_bf16",
+           "spmm_variants", "spmm_default_variant", "spmm_variant_supported", "NativeError",
+           "Context", "context"]

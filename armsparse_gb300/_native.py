@@ -32,6 +32,8 @@ SIGNATURES = {
     "as_spmm_csr_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _F, _I, _P]),
     "as_spmm_csr_bf16": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _F, _I, _P]),
     "as_spmm_csr_reduce_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _I, _P]),
+    "as_spgemm_csr_dense_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _I, _P, _P, _P, _P, _L, _F,
+                                     _P]),
     "as_spmm_variant_count": (_I, [_I]),
     "as_spmm_variant_name": (ctypes.c_char_p, [_I, _I]),
     "as_spmm_variant_supported": (_I, [_I, _I, _I, _L, _L, _P, _P]),

@@ -236,6 +236,26 @@ as_status as_spmm_csr_reduce_f32(as_ctx *c, int M, int K, int N, int nnz, const 
     return spmm_reduce_launch(c, op, a, static_cast<cudaStream_t>(stream));
 }
 
+as_status as_spgemm_csr_dense_f32(as_ctx *c, int M, int K, int N, int nnz_a,
+                                  const int *a_rowptr, const int *a_colind, const float *a_val,
+                                  int nnz_b, const int *b_rowptr, const int *b_colind,
+                                  const float *b_val, float *C, long ldc, float beta,
+                                  void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_spgemm_csr_dense_f32: ctx is NULL");
+    as_status st = check_csr_args("as_spgemm_csr_dense_f32 (A)", M, K, nnz_a, a_rowptr, a_colind,
+                                  a_val, true);
+    if (st != AS_OK) return st;
+    st = check_csr_args("as_spgemm_csr_dense_f32 (B)", K, N, nnz_b, b_rowptr, b_colind, b_val,
+                        true);
+    if (st != AS_OK) return st;
+    if (N < 0) return fail(AS_ERR_INVALID_VALUE, "as_spgemm_csr_dense_f32: negative N");
+    if (M == 0 || N == 0) return AS_OK;
+    if (!C || ldc < N) return fail(AS_ERR_INVALID_VALUE, "as_spgemm_csr_dense_f32: bad C");
+    DeviceGuard g(c->device);
+    return spgemm_dense_launch(c, M, K, N, nnz_a, a_rowptr, a_colind, a_val, nnz_b, b_rowptr,
+                               b_colind, b_val, C, ldc, beta, static_cast<cudaStream_t>(stream));
+}
+
 int as_spmm_variant_count(int dtype) { return spmm_variant_count(dtype); }
 int as_spmm_variant_supported(int dtype, int variant, int N, long ldb, long ldc, const void *B,
                               const void *C) {

@@ -109,7 +109,50 @@ as_status spmm_host(const int *rowPtr, const int *colInd, const float *val, cons
     return finish(s, C, dC, sizeof(float) * size_t(M) * N);
 }
 
+as_status spgemm_host(const int *rp1, const int *ci1, const float *v1, const int *rp2,
+                      const int *ci2, const float *v2, float *C, int M, int K, int N) {
+    State &s = state();
+    if (M < 0 || K < 0 || N < 0 || !rp1 || !rp2) return AS_ERR_INVALID_VALUE;
+    const int nnz_a = rp1[M], nnz_b = rp2[K];
+    if (nnz_a < 0 || nnz_b < 0) return AS_ERR_INVALID_CSR;
+    const size_t bytes = al(sizeof(int) * (M + 1)) + 2 * al(sizeof(int) * nnz_a) +
+                         al(sizeof(int) * (K + 1)) + 2 * al(sizeof(int) * nnz_b) +
+                         al(sizeof(float) * size_t(M) * N);
+    char *base = nullptr;
+    as_status st = prepare(s, bytes, &base);
+    if (st != AS_OK) return st;
+    Arena a{base};
+    int *drp1 = a.take<int>(M + 1);
+    int *dci1 = a.take<int>(nnz_a);
+    float *dv1 = a.take<float>(nnz_a);
+    int *drp2 = a.take<int>(K + 1);
+    int *dci2 = a.take<int>(nnz_b);
+    float *dv2 = a.take<float>(nnz_b);
+    float *dC = a.take<float>(size_t(M) * N);
+    if ((st = h2d(s, drp1, rp1, sizeof(int) * (M + 1))) != AS_OK) return st;
+    if ((st = h2d(s, dci1, ci1, sizeof(int) * nnz_a)) != AS_OK) return st;
+    if ((st = h2d(s, dv1, v1, sizeof(float) * nnz_a)) != AS_OK) return st;
+    if ((st = h2d(s, drp2, rp2, sizeof(int) * (K + 1))) != AS_OK) return st;
+    if ((st = h2d(s, dci2, ci2, sizeof(int) * nnz_b)) != AS_OK) return st;
+    if ((st = h2d(s, dv2, v2, sizeof(float) * nnz_b)) != AS_OK) return st;
+    if ((st = h2d(s, dC, C, sizeof(float) * size_t(M) * N)) != AS_OK) return st;
+    st = as_spgemm_csr_dense_f32(s.ctx, M, K, N, nnz_a, drp1, dci1, dv1, nnz_b, drp2, dci2, dv2,
+                                 dC, N, 1.0f, s.stream);
+    if (st != AS_OK) return st;
+    return finish(s, C, dC, sizeof(float) * size_t(M) * N);
+}
+
 }  // namespace
+
+void sparse_matrix_mul3(int rowPtr1[], int colInd1[], float val1[], int rowPtr2[],
+                        int colInd2[], float val2[], float *matrixC, int M, int K, int N,
+                        int threads) {
+    (void)threads;
+    State &s = state();
+    std::lock_guard<std::mutex> g(s.mu);
+    report(s, spgemm_host(rowPtr1, colInd1, val1, rowPtr2, colInd2, val2, matrixC, M, K, N),
+           "sparse_matrix_mul3");
+}
 
 void rowBaseSpmm3(int rowPtr[], int colInd[], float val[], float B[], float C[], int M, int K,
                   int N, int threads) {
@@ -251,6 +294,11 @@ void as_drv_rowBaseSpmm3(int *rowPtr, int *colInd, float *val, float *B, float *
 void as_drv_origin(int *rowPtr, int *colInd, float *val, float *B, float *C, int M, int K, int N,
                    int threads) {
     origin(rowPtr, colInd, val, B, C, M, K, N, threads);
+}
+void as_drv_sparse_matrix_mul3(int *rowPtr1, int *colInd1, float *val1, int *rowPtr2,
+                               int *colInd2, float *val2, float *C, int M, int K, int N,
+                               int threads) {
+    sparse_matrix_mul3(rowPtr1, colInd1, val1, rowPtr2, colInd2, val2, C, M, K, N, threads);
 }
 void as_drv_sparse_dense_vector(float *B, float *C, int *rowPtr, int *colInd, float *val, int M,
                                 int threads) {

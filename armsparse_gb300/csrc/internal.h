@@ -56,6 +56,10 @@ as_status spmm_bulk_launch(as_ctx *ctx, int dtype, int lane_bytes, int stages, c
 int spmm_long_granule(int dtype, int N, long ldb, const void *B);
 as_status spmm_long_launch(as_ctx *ctx, int dtype, int granule, const SpmmArgs &a,
                            const int *list, cudaStream_t s);
+as_status spgemm_dense_launch(as_ctx *ctx, int M, int K, int N, int nnz_a, const int *rp1,
+                              const int *ci1, const float *v1, int nnz_b, const int *rp2,
+                              const int *ci2, const float *v2, float *C, long ldc, float beta,
+                              cudaStream_t s);
 int spmm_variant_count(int dtype);
 bool spmm_variant_supported(int dtype, int variant, int N, long ldb, long ldc, const void *B,
                             const void *C);

@@ -233,8 +233,11 @@ class CapturedEpoch:
         # the recorded kernels read these tensors' memory at every replay: keep them alive
         self.static = (model, opt, x, g, y, train)
         self.graph = torch.cuda.CUDAGraph()
+        from . import _native
+        before = _native.total_launches()
         with torch.cuda.graph(self.graph):
             self.loss = train_epoch(model, opt, x, g, y, train)
+        self.launches = _native.total_launches() - before  # this library's kernels per replay
 
     def __call__(self) -> torch.Tensor:
         """One epoch; returns the loss tensor (overwritten by the next call)."""

@@ -117,6 +117,32 @@ def _spmm_f64(rowptr, colind, val, B, C, beta):
     return C
 
 
+def spgemm_dense(a_rowptr, a_colind, a_val, b_rowptr, b_colind, b_val, n_cols: int, C=None,
+                 beta: float = 0.0):
+    """C = A*B + beta*C with A and B in CSR (fp32 values) and C a dense fp32 (M, n_cols)
+    matrix: the reference's sparse_matrix_mul3 (SpMM.cpp:309-327), bit for bit."""
+    dev = _dev(a_rowptr, a_colind, a_val, b_rowptr, b_colind, b_val, C)
+    M, nnz_a = _csr(a_rowptr, a_colind)
+    K, nnz_b = _csr(b_rowptr, b_colind)
+    _need(a_val, torch.float32, "a_val", 1)
+    _need(b_val, torch.float32, "b_val", 1)
+    if a_val.numel() != nnz_a or b_val.numel() != nnz_b:
+        raise ValueError("value and column-index lengths differ")
+    if C is None:
+        if beta != 0.0:
+            raise ValueError("beta != 0 needs C")
+        C = torch.empty((M, n_cols), dtype=torch.float32, device=dev)
+    elif C.dtype != torch.float32 or C.shape != (M, n_cols) or C.stride(1) != 1:
+        raise ValueError("C must be float32 (M, n_cols) row-major")
+    ctx = N.context(dev.index)
+    N.check(N.load().as_spgemm_csr_dense_f32(ctx.handle, M, K, n_cols, nnz_a, _ptr(a_rowptr),
+                                             _ptr(a_colind), _ptr(a_val), nnz_b, _ptr(b_rowptr),
+                                             _ptr(b_colind), _ptr(b_val), _ptr(C),
+                                             C.stride(0) if M > 1 else n_cols, float(beta),
+                                             _stream(dev)), "as_spgemm_csr_dense_f32")
+    return C
+
+
 def spmm_reduce(rowptr, colind, B, val=None, op: str = "sum", C=None):
     """C[i,:] = reduce over row i of w_e * B[col(e),:], reduce in {"sum", "max"}, w_e = val or 1
     (the unweighted copy-sum / copy-max aggregations); rows without entries give 0."""

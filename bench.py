@@ -212,12 +212,109 @@ class SpmmBf16(_Generic, SpmmF32):
         return 4 * (m + 1) + 6 * nnz + 2 * self.K * self.N + 4 * m * self.N
 
 
+class SpmmPowerlaw(_Generic, SpmmF32):
+    """SpMM on a skewed matrix: power-law row lengths (exponent 2.0, mean 20 entries per
+    row; the longest row holds all 300,000 columns), 300,000 x 300,000, 5.83M entries, N = 128,
+    fp32. `value` is the library-default, bit-exact path (row-split kernels, rows past 256
+    entries in the long-row kernel); `extra` times the learned selector's pick."""
+    name = "spmm_powerlaw"
+    metric = "SpMM GB/s (algorithmic bytes), power-law rows, library default (bit-exact)"
+    profile = "spmm_long_powerlaw_300k_n128"
+    kernel = "spmm_rowsplit + spmm_long (the call)"
+    e2e_api = "armsparse_gb300.spmm with pinned host inputs copied in and C copied back"
+
+    def __init__(self, seed=5):
+        from armsparse_gb300 import synthetic as S
+        self.a = S.powerlaw_csr(300_000, 2.0, 20.0, seed=seed)
+        self.M = self.K = 300_000
+        self.N = 128
+        self.B = S.dense_uniform((self.K, self.N), seed + 1)
+        nnz = self.a.nnz
+        self.bytes = 4 * (self.M + 1) + 8 * nnz + 4 * self.K * self.N + 4 * self.M * self.N
+        self.flops = 2 * nnz * self.N
+        lens = np.diff(self.a.rowptr)
+        self.config = {"workload": "spmm_csr_f32 C=A*B, A 300,000 x 300,000 with power-law row "
+                                   "lengths (exponent 2.0, mean 20, column ids uniform), "
+                                   "B 300,000 x 128 U(-1,1)",
+                       "M": self.M, "K": self.K, "N": self.N, "nnz": nnz,
+                       "longest_row": int(lens.max()), "rows_over_256": int((lens > 256).sum()),
+                       "alg_bytes_per_step": self.bytes, "alg_flops_per_step": self.flops,
+                       "l2": "flushed between steps (256 MiB write, outside the timed events)"}
+
+    def inputs(self):
+        return {"rp": self.rp, "ci": self.ci, "v": self.v, "B": self.Bd}
+
+    def output(self):
+        return self.C
+
+    def extra(self):
+        from armsparse_gb300 import selector, tuner
+        import armsparse_gb300 as A
+        sel = selector.Selector.load()
+        v = sel.choose(self.rp, self.K, self.N)
+        ms = tuner.time_cuda(lambda: A.spmm(self.rp, self.ci, self.v, self.Bd, C=self.C,
+                                             variant=v), reps=10)
+        return {"selector_pick": A.spmm_variants()[v - 1], "selector_ms": round(ms, 4),
+                "selector_gbs": round(self.bytes / (ms * 1e-3) / 1e9, 1)}
+
+
+class SpgemmDense(_Generic):
+    """Sparse x sparse -> dense as the SpMM driver times it (SpMM.cpp:105-160): A and B
+    4096 x 4096 at density 0.01, C += A * B (sparse_matrix_mul3, SpMM.cpp:309-327)."""
+    name = "spgemm"
+    metric = "SpGEMM (sparse x sparse -> dense) GB/s (algorithmic bytes)"
+    unit = "GB/s"
+    dtype = "f32"
+    kernel = "spgemm_dense"
+    profile = "spgemm_dense_4096_d001"
+
+    def __init__(self, seed=0):
+        from armsparse_gb300 import synthetic as S
+        self.M = self.K = self.N = 4096
+        self.a = S.spmm_4096_d001(seed)
+        self.b = S.spmm_4096_d001(seed + 1)
+        self.C0 = np.zeros((self.M, self.N), np.float32)
+        na, nb = self.a.nnz, self.b.nnz
+        self.bytes = 4 * (self.M + 1) + 8 * na + 4 * (self.K + 1) + 8 * nb + 8 * self.M * self.N
+        self.config = {"workload": "spgemm_csr_dense_f32 C += A*B, A and B 4096x4096 uniform "
+                                   "density 0.01 (167,772 entries each) U(-1,1), C dense fp32",
+                       "M": 4096, "K": 4096, "N": 4096, "nnz_a": na, "nnz_b": nb,
+                       "alg_bytes_per_step": self.bytes,
+                       "l2": "flushed between steps (256 MiB write, outside the timed events)"}
+
+    def to_device(self, dev):
+        import torch
+        t = lambda x: torch.from_numpy(x).to(dev)
+        self.A = (t(self.a.rowptr), t(self.a.colind), t(self.a.val))
+        self.B = (t(self.b.rowptr), t(self.b.colind), t(self.b.val))
+        self.C = t(self.C0)
+
+    def inputs(self):
+        return {"arp": self.A[0], "aci": self.A[1], "av": self.A[2], "brp": self.B[0],
+                "bci": self.B[1], "bv": self.B[2]}
+
+    def output(self):
+        return self.C
+
+    def step(self):
+        import armsparse_gb300 as A
+        A.spgemm_dense(*self.A, *self.B, self.N, C=self.C, beta=1.0)
+
+    def cpu_step(self, threads, rows=None):
+        from oracle import oracle as O
+        a, b = self.a, self.b
+        O.spgemm_dense_f32(a.rowptr, a.colind, a.val, b.rowptr, b.colind, b.val, self.N,
+                           threads=threads)
+        return self.bytes
+
+
 class SddmmTc(_Generic):
     name = "sddmm_tc"
     metric = "SDDMM GB/s (algorithmic bytes), tensor-core split-bf16 path"
     unit = "GB/s"
     dtype = "bf16x3 (fp32 in/out, fp32 accumulate)"
-    kernel = "sddmm_tc_kernel"
+    kernel = ("the whole as_sddmm_csr_bf16x3 call: fp32 -> bf16 hi/lo split of X and Y, "
+              "tile pre-pass, sddmm_tc_persistent")
     profile = "sddmm_tc_persistent_4096x4096x4096_d01"
     bound = "tensor"
     tensor_cores = True
@@ -381,6 +478,9 @@ class GcnEpoch(Workload):
 
     def step(self):
         self.loss = self.captured()
+
+    def launches_per_replay(self):
+        return self.captured.launches
 
     def eager_step(self):
         from armsparse_gb300 import gcn
@@ -737,7 +837,7 @@ class Csr2Csc(_Generic):
         return v, sample + " (single-threaded counting transpose)"
 
 
-WORKLOADS = {c.name: c for c in [SpmmF32, SpmmBf16, SddmmTc, SddmmF32, GcnEpoch, GcnLarge, SpmvF32,
+WORKLOADS = {c.name: c for c in [SpmmF32, SpmmBf16, SpmmPowerlaw, SpgemmDense, SddmmTc, SddmmF32, GcnEpoch, GcnLarge, SpmvF32,
                                  Csr2Csc]}
 
 
@@ -915,6 +1015,8 @@ def run_ours(args, wl_cls):
         wall = time.perf_counter() - t0
     barrier()
     launches = N.total_launches() - l0
+    if hasattr(wl, "launches_per_replay"):  # steps replayed from a CUDA graph
+        launches += args.steps * wl.launches_per_replay()
     times = [s.elapsed_time(e) for s, e in evs]  # ms
     kernel_ms = sum(times) / len(times)
     if ws > 1:

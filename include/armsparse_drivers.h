@@ -30,6 +30,10 @@ void rowBaseSpmm2(int rowPtr[], int colInd[], float val[], float B[], float C[],
 /* SDMM.cpp:422 -- C = A * B (overwrite). */
 void origin(int rowPtr[], int colInd[], float val[], float B[], float C[], int M, int K, int N,
             int threads);
+/* SpMM.cpp:309 -- matrixC[M x N] += A * B with A (M x K) and B (K x N) both CSR. */
+void sparse_matrix_mul3(int rowPtr1[], int colInd1[], float val1[], int rowPtr2[],
+                        int colInd2[], float val2[], float *matrixC, int M, int K, int N,
+                        int threads);
 /* SpMV.cpp:155 -- y[M] += A * x over the 1x4-blocked layout (rowPtr[M] slots). The length of
  * x is not an argument in the reference; the shim takes max(colInd) + 4. */
 void sparse_dense_vector(float *B, float *C, int rowPtr[], int colInd[], float val[], int M,
@@ -53,6 +57,9 @@ void as_drv_origin(int *rowPtr, int *colInd, float *val, float *B, float *C, int
                    int threads);
 void as_drv_sparse_dense_vector(float *B, float *C, int *rowPtr, int *colInd, float *val, int M,
                                 int threads);
+void as_drv_sparse_matrix_mul3(int *rowPtr1, int *colInd1, float *val1, int *rowPtr2,
+                               int *colInd2, float *val2, float *C, int M, int K, int N,
+                               int threads);
 void as_drv_csr_spmm_kernel(int A_nrows, int B_ncols, int *rowptr, int *colind, float *val,
                             float *B, float *C);
 void as_drv_fast_transpose(int *sm, int *res);

@@ -88,6 +88,17 @@ as_status as_spmm_csr_reduce_f32(as_ctx *ctx, int M, int K, int N, int nnz, cons
                                  const int *colind, const float *val, const float *B, long ldb,
                                  float *C, long ldc, int op, void *stream);
 
+/* Sparse x sparse -> dense: C = beta*C + A*B with A (M x K, nnz_a entries) and B (K x N,
+ * nnz_b entries) in CSR and C dense row-major (ldc >= N). Replaces sparse_matrix_mul3
+ * (SpMM.cpp:309-327; beta = 1 is its accumulate): every output element is the reference's
+ * fused-FMA chain over A's row in CSR order, bit for bit. B's rows must hold distinct column
+ * indices (as CSR does). */
+as_status as_spgemm_csr_dense_f32(as_ctx *ctx, int M, int K, int N, int nnz_a,
+                                  const int *a_rowptr, const int *a_colind, const float *a_val,
+                                  int nnz_b, const int *b_rowptr, const int *b_colind,
+                                  const float *b_val, float *C, long ldc, float beta,
+                                  void *stream);
+
 /* Variant table for tuning: ids are 1..count. dtype 0 = f32, 1 = bf16. */
 int as_spmm_variant_count(int dtype);
 const char *as_spmm_variant_name(int dtype, int variant);

@@ -48,6 +48,25 @@ void or_spmm_fma_chain_f32(int M, int N, const int *rowptr, const int *colind,
     }
 }
 
+/* Sparse x sparse -> dense: C += A*B with A (M x K) and B (K x N) both CSR and C dense
+ * row-major. For each row of A, its entries in CSR order, each contributing its B row's
+ * entries in order, as the reference's sparse_matrix_mul3 does (SpMM.cpp:309-327, built with
+ * FMA contraction): per output element a fused-FMA chain over A's row. */
+void or_spgemm_dense_f32(int M, int N, const int *rp1, const int *ci1, const float *v1,
+                         const int *rp2, const int *ci2, const float *v2, float *C, long ldc,
+                         int threads) {
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int m = 0; m < M; ++m) {
+        float *c = C + (long)m * ldc;
+        for (int idx = rp1[m]; idx < rp1[m + 1]; ++idx) {
+            const int k = ci1[idx];
+            const float a = v1[idx];
+            for (int t = rp2[k]; t < rp2[k + 1]; ++t) c[ci2[t]] = fmaf(a, v2[t], c[ci2[t]]);
+        }
+    }
+    (void)N;
+}
+
 /* SpMM in double precision with the per-output absolute sum sum_k |a_mk * b_kj|, used as
  * the FP64 oracle and as the scale of the relative-error metric. Inputs are double so that
  * callers can pass bf16-rounded values exactly. */

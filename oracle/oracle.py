@@ -76,6 +76,8 @@ def lib():
                                                  _f32p, _c_long, _f32p, _c_long, _f32p, _c_int]
             L.or_csr2csc.argtypes = [_c_int, _c_int, _i32p, _i32p, _f32p, _i32p, _i32p, _f32p]
             L.or_max_threads.restype = _c_int
+            L.or_spgemm_dense_f32.argtypes = [_c_int, _c_int, _i32p, _i32p, _f32p, _i32p, _i32p,
+                                              _f32p, _f32p, _c_long, _c_int]
             L.or_spmm_reduce_f32.argtypes = [_c_int, _c_int, _i32p, _i32p, ctypes.c_void_p, _f32p,
                                              _c_long, _f32p, _c_int]
             _LIB = L
@@ -115,6 +117,31 @@ def spmm_fma_chain_f32(rowptr, colind, val, B, C=None, threads=None):
     lib().or_spmm_fma_chain_f32(M, N, rowptr, colind, np.ascontiguousarray(val, np.float32), B,
                                 N, out, N, int(acc), threads or max_threads())
     return out
+
+
+def spgemm_dense_f32(a_rowptr, a_colind, a_val, b_rowptr, b_colind, b_val, n_cols, C=None,
+                     threads=None):
+    """C (+)= A*B with A and B in CSR, C dense, as the reference's sparse_matrix_mul3
+    (SpMM.cpp:309-327) computes it. ``C`` None means a zero-initialised output."""
+    rp1, ci1 = _csr(a_rowptr, a_colind)
+    rp2, ci2 = _csr(b_rowptr, b_colind)
+    M = rp1.size - 1
+    out = (np.zeros((M, n_cols), np.float32) if C is None
+           else np.ascontiguousarray(C, dtype=np.float32).copy())
+    lib().or_spgemm_dense_f32(M, n_cols, rp1, ci1, np.ascontiguousarray(a_val, np.float32), rp2,
+                              ci2, np.ascontiguousarray(b_val, np.float32), out, n_cols,
+                              threads or max_threads())
+    return out
+
+
+def spgemm_dense_f64(a_rowptr, a_colind, a_val, b_rowptr, b_colind, b_val, n_cols):
+    """(A*B, |A|*|B|) in double precision for the sparse x sparse product (small cases)."""
+    import scipy.sparse as sp
+    M = len(a_rowptr) - 1
+    K = len(b_rowptr) - 1
+    A = sp.csr_matrix((np.asarray(a_val, np.float64), a_colind, a_rowptr), shape=(M, K))
+    B = sp.csr_matrix((np.asarray(b_val, np.float64), b_colind, b_rowptr), shape=(K, n_cols))
+    return (A @ B).toarray(), (abs(A) @ abs(B)).toarray()
 
 
 def spmm_reduce_f32(rowptr, colind, B, val=None, op="sum"):

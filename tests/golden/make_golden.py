@@ -2,7 +2,7 @@
 
 Run in a checkout that has the reference sources (REF, default /root/reference):
 
-    python tests/golden/make_golden.py [REF]
+    python tests/golden/make_golden.py [REF] [--only NAME]
 
 It compiles the reference's SDMM.cpp, SpMV.cpp and sparseTranspose.cpp unmodified through
 oracle/Makefile (target ``ref``; on x86_64 a scalar NEON shim stands in for <arm_neon.h>),
@@ -14,6 +14,8 @@ runs them on small seeded inputs and saves inputs and outputs as .npz files:
   matrix;
 * spmv_vcsr4.npz -- toVectorAwareCSR (SpMV.cpp:15-38) and sparse_dense_vector
   (SpMV.cpp:155-179);
+* spgemm_dense.npz -- sparse_matrix_mul3 (SpMM.cpp:309-327): A and B in CSR (row-major
+  scan, ascending columns, as toCSR writes them), C dense, accumulated over two calls;
 * transpose_triplets.npz -- convert (sparseTranspose.cpp:71-92) and fast_transpose
   (sparseTranspose.cpp:95-142) run on one thread (stable order);
 * gcn_op.npz -- the reference's own gcn/pytorch-custom/op.py imported as is: its
@@ -113,6 +115,40 @@ def spmv_cases(ref):
     np.savez_compressed(os.path.join(HERE, "spmv_vcsr4.npz"), **out)
 
 
+def _csr_of(dense):
+    rows, cols = np.nonzero(dense)
+    rp = np.zeros(dense.shape[0] + 1, np.int32)
+    np.cumsum(np.bincount(rows, minlength=dense.shape[0]), out=rp[1:])
+    return rp, cols.astype(np.int32), dense[rows, cols].astype(np.float32)
+
+
+def spgemm_cases(ref):
+    cases = [(64, 48, 40, 0.1, 0.1, 31), (30, 50, 7, 0.2, 0.3, 32), (16, 16, 16, 0.3, 0.3, 33),
+             (100, 80, 130, 0.05, 0.08, 34)]
+    out = {}
+    for i, (M, K, N, da, db, seed) in enumerate(cases):
+        rng = np.random.default_rng(4000 + seed)
+        A = dense_sparse(rng, M, K, da, kind="u11")
+        B = dense_sparse(rng, K, N, db, kind="u11")
+        if i == 0:
+            A[3, :] = 0  # an empty row of A
+            B[7, :] = 0  # an empty row of B
+        rp1, ci1, v1 = _csr_of(A)
+        rp2, ci2, v2 = _csr_of(B)
+        C1 = np.zeros((M, N), np.float32)
+        ref.ref_sparse_matrix_mul3(_p(rp1), _p(ci1), _p(v1), _p(rp2), _p(ci2), _p(v2), _p(C1),
+                                   M, K, N, 4)
+        C2 = C1.copy()
+        ref.ref_sparse_matrix_mul3(_p(rp1), _p(ci1), _p(v1), _p(rp2), _p(ci2), _p(v2), _p(C2),
+                                   M, K, N, 4)
+        out.update({f"c{i}_shape": np.array([M, K, N], np.int32), f"c{i}_a_rowptr": rp1,
+                    f"c{i}_a_colind": ci1, f"c{i}_a_val": v1, f"c{i}_b_rowptr": rp2,
+                    f"c{i}_b_colind": ci2, f"c{i}_b_val": v2, f"c{i}_C": C1,
+                    f"c{i}_C_twice": C2})
+    out["n_cases"] = np.array(len(cases), np.int32)
+    np.savez_compressed(os.path.join(HERE, "spgemm_dense.npz"), **out)
+
+
 def transpose_cases(ref):
     cases = [(30, 20, 0.1, 21), (7, 40, 0.3, 22), (64, 64, 0.05, 23)]
     out = {}
@@ -202,13 +238,21 @@ def gcn_cases(ref_dir):
 
 
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    if only:
+        args = [a for a in args if a != only]
+    ref_dir = args[0] if args else "/root/reference"
     if not O.build_ref(ref_dir):
         raise SystemExit("could not build the reference kernels from " + ref_dir)
-    spmm_cases(O.ref_lib("sdmm"))
-    spmv_cases(O.ref_lib("spmv"))
-    transpose_cases(O.ref_lib("transpose"))
-    if O.build_ref(ref_dir, gcn=True):
+    makers = {"spmm": lambda: spmm_cases(O.ref_lib("sdmm")),
+              "spmv": lambda: spmv_cases(O.ref_lib("spmv")),
+              "transpose": lambda: transpose_cases(O.ref_lib("transpose")),
+              "spgemm": lambda: spgemm_cases(O.ref_lib("spgemm"))}
+    for name, make in makers.items():
+        if only in (None, name):
+            make()
+    if only in (None, "gcn") and O.build_ref(ref_dir, gcn=True):
         gcn_cases(ref_dir)
     print("golden vectors written to", HERE)
 

@@ -140,3 +140,33 @@ def test_bf16_round(oracle):
     # 1 + 2^-8 is a tie -> even (1.0); 1 + 1.5*2^-8 rounds up to 1 + 2^-7
     assert r[0] == 1.0 and r[1] == 1.0 and r[2] == np.float32(1.0078125)
     assert (r.view(np.uint32) & 0xFFFF).max() == 0
+
+
+def test_spgemm_dense_matches_sparse_matrix_mul3_golden(oracle, golden):
+    """The sparse x sparse -> dense restatement against the reference's sparse_matrix_mul3
+    (SpMM.cpp:309-327) run here: bit-identical, also for the driver's accumulate pattern."""
+    g = golden["spgemm_dense"]
+    for i in range(int(g["n_cases"])):
+        M, K, N = g[f"c{i}_shape"]
+        args = [g[f"c{i}_{x}"] for x in ("a_rowptr", "a_colind", "a_val", "b_rowptr",
+                                         "b_colind", "b_val")]
+        C = oracle.spgemm_dense_f32(*args, int(N), threads=2)
+        assert np.array_equal(C.view(np.uint32), g[f"c{i}_C"].view(np.uint32)), i
+        C2 = oracle.spgemm_dense_f32(*args, int(N), C=C, threads=2)
+        assert np.array_equal(C2.view(np.uint32), g[f"c{i}_C_twice"].view(np.uint32)), i
+        R, Ab = oracle.spgemm_dense_f64(*args, int(N))
+        assert oracle.scaled_err(C, R, Ab).max() < 1e-5
+
+
+def test_spgemm_dense_against_compiled_reference(oracle):
+    ref = oracle.ref_lib("spgemm")
+    if ref is None:
+        pytest.skip("reference sources not compiled here")
+    a = S.uniform_csr(120, 90, 1500, 3)
+    b = S.uniform_csr(90, 70, 1200, 4)
+    mine = oracle.spgemm_dense_f32(a.rowptr, a.colind, a.val, b.rowptr, b.colind, b.val, 70,
+                                   threads=2)
+    C = np.zeros((120, 70), np.float32)
+    arrs = [x.copy() for x in (a.rowptr, a.colind, a.val, b.rowptr, b.colind, b.val)]
+    ref.ref_sparse_matrix_mul3(*[_p(x) for x in arrs], _p(C), 120, 90, 70, 2)
+    assert np.array_equal(mine.view(np.uint32), C.view(np.uint32))
