@@ -8,7 +8,8 @@
 //
 // Each output element is still one fused-FMA chain over the row's entries in CSR order (the
 // order cannot be split without changing the bits), so the speed comes from feeding the
-// chains: a CTA owns one (long row, 64-byte column slice); all 256 threads copy B segments
+// chains: a CTA takes one (long row, 64-byte column slice) at a time; all 256 threads copy B
+// segments
 // of upcoming entries into a shared-memory ring with cp.async (kStages stages of kStage
 // entries in flight), and the slice's columns -- one per consumer thread -- run their chains
 // out of shared memory. Column indices and values are staged a chunk of kChunk entries ahead
@@ -70,14 +71,18 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
     // (and its list writes to be visible) before reading the list
     asm volatile("griddepcontrol.wait;\n" ::: "memory");
     const int tid = threadIdx.x;
-    const int slice0 = blockIdx.y * W;
-    const int w = min(W, N - slice0);         // columns of this slice
-    const int seg = w * static_cast<int>(sizeof(T));  // bytes of B per entry in this slice
-    const int pieces = seg / GB;              // cp.async pieces per entry (<= 64)
     const int n_long = static_cast<int>(
         min(*reinterpret_cast<volatile unsigned *>(counters), static_cast<unsigned>(M)));
+    const int n_slices = static_cast<int>(ceil_div(N, W));
+    const long units = static_cast<long>(n_long) * n_slices;
 
-    for (int item = blockIdx.x; item < n_long; item += gridDim.x) {
+    // work units (long row, column slice), the slices of one row on consecutive CTAs
+    for (long u = blockIdx.x; u < units; u += gridDim.x) {
+        const int item = static_cast<int>(u / n_slices);
+        const int slice0 = static_cast<int>(u - static_cast<long>(item) * n_slices) * W;
+        const int w = min(W, N - slice0);                  // columns of this slice
+        const int seg = w * static_cast<int>(sizeof(T));   // bytes of B per entry in this slice
+        const int pieces = seg / GB;                       // cp.async pieces per entry
         const int r = list[item];
         if (r < 0 || r >= M) continue;
         int lo, hi;
@@ -104,29 +109,34 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         }
         __syncthreads();
 
-        // B segments of stage st into ring slot st % kStages: warp w copies entries w, w + 8,
-        // ..., its lanes the segment's pieces (at most 64). Entries past the row are not
-        // copied (never read); a flagged entry gets zeros (its value is 0 as well).
+        // B segments of stage st into ring slot st % kStages. Warp w copies entries 8w..8w+7 of
+        // the stage; lane l takes piece l % P of entry l / P (P pieces per full slice), so a
+        // full warp instruction moves 512 bytes (a copy instruction costs the same issue slot
+        // however few lanes it carries). Entries past the row are not copied (never read); a
+        // flagged entry gets zeros (its value is 0 as well).
         const int warp = tid >> 5, lane = tid & 31;
         auto issue = [&](int st) {
             if (st < n_stages) {
                 const int base = st * kStage;  // first entry of the stage, relative to lo
                 const int *kb = kbuf + ((base / kChunk) & 1) * kChunk + base % kChunk;
                 unsigned char *dst = ring + (st % kStages) * kStage * kSliceBytes;
-                for (int j = warp; j < kStage && base + j < L; j += kThreads / 32) {
-                    const int k = kb[j];
-                    const unsigned char *src = reinterpret_cast<const unsigned char *>(
-                        B + static_cast<long>(k < 0 ? 0 : k) * ldb + slice0);
+                constexpr int P = kSliceBytes / GB;           // pieces of a full slice (4 or 16)
+                constexpr int kPerWarp = kStage / (kThreads / 32);
 #pragma unroll
-                    for (int t = 0; t < 2; ++t) {
-                        const int q = lane + 32 * t;
-                        if (q >= pieces) break;
-                        if (k >= 0)
-                            cp_async<GB>(dst + j * kSliceBytes + q * GB, src + q * GB);
-                        else if constexpr (GB == 16)
-                            *reinterpret_cast<uint4 *>(dst + j * kSliceBytes + q * GB) = make_uint4(0, 0, 0, 0);
-                        else
-                            *reinterpret_cast<unsigned *>(dst + j * kSliceBytes + q * GB) = 0u;
+                for (int t = 0; t < kPerWarp * P / 32; ++t) {
+                    const int p = lane + 32 * t;
+                    const int j = warp * kPerWarp + p / P, q = p % P;
+                    if (q >= pieces || base + j >= L) continue;
+                    const int k = kb[j];
+                    unsigned char *d = dst + j * kSliceBytes + q * GB;
+                    if (k >= 0) {
+                        const unsigned char *src = reinterpret_cast<const unsigned char *>(
+                            B + static_cast<long>(k) * ldb + slice0);
+                        cp_async<GB>(d, src + q * GB);
+                    } else if constexpr (GB == 16) {
+                        *reinterpret_cast<uint4 *>(d) = make_uint4(0, 0, 0, 0);
+                    } else {
+                        *reinterpret_cast<unsigned *>(d) = 0u;
                     }
                 }
             }
@@ -182,20 +192,36 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 const float *vs = vbuf + ((base / kChunk) & 1) * kChunk + base % kChunk;
                 const T *bs = reinterpret_cast<const T *>(ring + (st % kStages) * kStage * kSliceBytes) + tid;
                 int j = 0;
-                for (; j + 8 <= n; j += 8) {  // loads first, then the chain in entry order
-                    const float4 v0 = *reinterpret_cast<const float4 *>(vs + j);
-                    const float4 v1 = *reinterpret_cast<const float4 *>(vs + j + 4);
-                    float b[8];
+                if (n >= 8) {  // the next 8 entries' loads are in flight during this 8's chain
+                    float b[8], bn[8];
+                    float4 v0 = *reinterpret_cast<const float4 *>(vs);
+                    float4 v1 = *reinterpret_cast<const float4 *>(vs + 4);
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) b[i] = to_f32(bs[(j + i) * W]);
-                    acc = fmaf(b[0], v0.x, acc);
-                    acc = fmaf(b[1], v0.y, acc);
-                    acc = fmaf(b[2], v0.z, acc);
-                    acc = fmaf(b[3], v0.w, acc);
-                    acc = fmaf(b[4], v1.x, acc);
-                    acc = fmaf(b[5], v1.y, acc);
-                    acc = fmaf(b[6], v1.z, acc);
-                    acc = fmaf(b[7], v1.w, acc);
+                    for (int i = 0; i < 8; ++i) b[i] = to_f32(bs[i * W]);
+                    for (; j + 8 <= n; j += 8) {
+                        const bool more = j + 16 <= n;
+                        float4 n0 = v0, n1 = v1;
+                        if (more) {
+                            n0 = *reinterpret_cast<const float4 *>(vs + j + 8);
+                            n1 = *reinterpret_cast<const float4 *>(vs + j + 12);
+#pragma unroll
+                            for (int i = 0; i < 8; ++i) bn[i] = to_f32(bs[(j + 8 + i) * W]);
+                        }
+                        acc = fmaf(b[0], v0.x, acc);
+                        acc = fmaf(b[1], v0.y, acc);
+                        acc = fmaf(b[2], v0.z, acc);
+                        acc = fmaf(b[3], v0.w, acc);
+                        acc = fmaf(b[4], v1.x, acc);
+                        acc = fmaf(b[5], v1.y, acc);
+                        acc = fmaf(b[6], v1.z, acc);
+                        acc = fmaf(b[7], v1.w, acc);
+                        if (more) {
+                            v0 = n0;
+                            v1 = n1;
+#pragma unroll
+                            for (int i = 0; i < 8; ++i) b[i] = bn[i];
+                        }
+                    }
                 }
                 for (; j < n; ++j) acc = fmaf(to_f32(bs[j * W]), vs[j], acc);
             }
@@ -209,7 +235,7 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
     __syncthreads();
     if (tid == 0) {
         __threadfence();
-        const unsigned total = gridDim.x * gridDim.y;
+        const unsigned total = gridDim.x;
         if (atomicAdd(counters + 1, 1u) == total - 1) {
             counters[0] = 0;
             counters[1] = 0;
@@ -230,11 +256,9 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, const int *list, cudaStream_t s
         if (e != cudaSuccess) return check_cuda(e, "spmm long rows: shared memory attribute");
         attr_set[dev] = true;
     }
-    const int W = kSliceBytes / static_cast<int>(sizeof(T));
-    // about two CTAs per multiprocessor in all: slices x rows in flight
-    const int gy = static_cast<int>(ceil_div(a.N, W));
-    const int gx = std::max(1, std::min(a.M, static_cast<int>(ceil_div(2 * ctx->sms, gy))));
-    dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(gy));
+    // two CTAs per multiprocessor (one wave), striding over the (row, slice) units
+    const long max_units = static_cast<long>(a.M) * ceil_div(a.N, kSliceBytes / static_cast<int>(sizeof(T)));
+    dim3 grid(static_cast<unsigned>(std::max(1L, std::min(max_units, 2L * ctx->sms))));
     // programmatic dependent launch (outside stream capture): the CTAs are scheduled while
     // the row-split kernel drains, hiding this launch when there are no long rows
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
