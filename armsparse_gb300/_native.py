@@ -41,6 +41,7 @@ SIGNATURES = {
     "as_spmv_csr_f32": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _F, _P]),
     "as_spmv_vcsr4_f32": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _F, _P]),
     "as_sddmm_csr_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P, _P]),
+    "as_sddmm_csr_bf16": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P, _P]),
     "as_sddmm_csr_bf16x3": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P, _P]),
     "as_csr2csc_static": (_I, [_I, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
     "as_sddmm_csr_bf16x3_v": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P, _I, _P]),

@@ -329,6 +329,26 @@ as_status as_sddmm_csr_f32(as_ctx *c, int M, int N, int K, int nnz, const int *r
                         ldx, Y, ldy, out, stream);
 }
 
+as_status as_sddmm_csr_bf16(as_ctx *c, int M, int N, int K, int nnz, const int *rowptr,
+                            const int *colind, const float *aval, const uint16_t *X, long ldx,
+                            const uint16_t *Y, long ldy, float *out, void *stream) {
+    const char *fn = "as_sddmm_csr_bf16";
+    if (!c) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": ctx is NULL");
+    as_status st = check_csr_args(fn, M, N, nnz, rowptr, colind, nullptr, false);
+    if (st != AS_OK) return st;
+    if (K < 0) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": negative K");
+    if (nnz == 0) return AS_OK;
+    if (!out) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": out is NULL");
+    if (K > 0 && (!X || !Y)) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": X or Y is NULL");
+    if (ldx < K || ldy < K)
+        return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": leading dimension below K");
+    if (!aligned_to(X, 2) || !aligned_to(Y, 2))
+        return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": X and Y must be 2-byte aligned");
+    DeviceGuard g(c->device);
+    return sddmm_bf16_launch(c, M, N, K, nnz, rowptr, colind, aval, X, ldx, Y, ldy, out,
+                             static_cast<cudaStream_t>(stream));
+}
+
 as_status as_sddmm_csr_bf16x3(as_ctx *c, int M, int N, int K, int nnz, const int *rowptr,
                               const int *colind, const float *aval, const float *X, long ldx,
                               const float *Y, long ldy, float *out, void *stream) {

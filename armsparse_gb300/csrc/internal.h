@@ -77,6 +77,9 @@ as_status spmv_vcsr4_launch(as_ctx *ctx, int M, int K, int nslots, const int *ro
 as_status sddmm_f32_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
                            const int *colind, const float *aval, const float *X, long ldx,
                            const float *Y, long ldy, float *out, cudaStream_t s);
+as_status sddmm_bf16_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
+                            const int *colind, const float *aval, const uint16_t *X, long ldx,
+                            const uint16_t *Y, long ldy, float *out, cudaStream_t s);
 as_status sddmm_coo_f32_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowind,
                                const int *colind, const float *aval, const float *X, long ldx,
                                const float *Y, long ldy, float *out, cudaStream_t s);

@@ -529,7 +529,9 @@ sddmm_tc_persistent(const __grid_constant__ CUtensorMap tmXhi, const __grid_cons
 
 // One warp per row: flags rows whose columns do not ascend (or leave [0, N)), and sets
 // occ[tm * tiles_n + tn] = 1 for every output tile holding a pattern entry -- one store per
-// (row, tile) since the columns ascend (the first entry of the row in each tile stores).
+// (row, tile) since the columns ascend (the first entry of the row in each tile stores). Each
+// lane issues four column loads before using them; a lane's predecessor column comes from
+// the lane below (lane 0: the last column of the previous batch).
 __global__ void __launch_bounds__(256)
 check_and_mark(int M, int N, int nnz, const int *__restrict__ rowptr,
                const int *__restrict__ colind, int BN, int tiles_n, unsigned char *__restrict__ occ,
@@ -541,13 +543,28 @@ check_and_mark(int M, int N, int nnz, const int *__restrict__ rowptr,
     row_range(rowptr, static_cast<int>(w), nnz, status, lo, hi);
     unsigned char *rowocc = occ + (w / kBM) * static_cast<long>(tiles_n);
     bool bad = false;
-    for (int e = lo + lane; e < hi; e += 32) {
-        const int c = __ldg(colind + e);
-        const int prev = e > lo ? __ldg(colind + e - 1) : -1;
-        if (c < 0 || c >= N || prev >= c)
-            bad = true;
-        else if (prev < 0 || prev / BN != c / BN)
-            rowocc[c / BN] = 1;
+    int carry = -1;  // column of the entry before this batch (-1 before the row's first)
+    for (int base = lo; base < hi; base += 128) {
+        int c[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = base + 32 * q + lane;
+            c[q] = e < hi ? __ldg(colind + e) : 0;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = base + 32 * q + lane;
+            const int up = __shfl_up_sync(0xffffffffu, c[q], 1);
+            const int last = __shfl_sync(0xffffffffu, c[q], 31);
+            const int prev = lane == 0 ? carry : up;
+            if (e < hi) {
+                if (c[q] < 0 || c[q] >= N || prev >= c[q])
+                    bad = true;
+                else if (prev < 0 || prev / BN != c[q] / BN)
+                    rowocc[c[q] / BN] = 1;
+            }
+            carry = last;
+        }
     }
     if (__any_sync(0xffffffffu, bad) && lane == 0) flag(status, kFlagBadColind);
 }

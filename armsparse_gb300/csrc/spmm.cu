@@ -149,9 +149,7 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
 #pragma unroll
                 for (int u = 0; u < U; ++u)
 #pragma unroll
-                    for (int j = 0; j < CPL; ++j)
-#pragma unroll
-                        for (int i = 0; i < E; ++i) acc[j][i] = fmaf(b[u][j][i], vv[u], acc[j][i]);
+                    for (int j = 0; j < CPL; ++j) fma_vec_f32<E>(b[u][j], vv[u], acc[j]);
             } else {
                 typename V::Raw b[U][CPL];
 #pragma unroll

@@ -118,10 +118,7 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
                     for (int u = 0; u < U; ++u)
                         if (kk[u] >= 0)
 #pragma unroll
-                            for (int j = 0; j < CPL; ++j)
-#pragma unroll
-                                for (int i = 0; i < E; ++i)
-                                    acc[j][i] = fmaf(b[u][j][i], vv[u], acc[j][i]);
+                            for (int j = 0; j < CPL; ++j) fma_vec_f32<E>(b[u][j], vv[u], acc[j]);
                 } else {
                     typename V::Raw b[U][CPL];
 #pragma unroll

@@ -55,6 +55,23 @@ __device__ __forceinline__ void fma_bf16x2(unsigned w, unsigned short v, float &
         " fma.rn.f32.bf16 %1, h, %3, %1;\n}\n"
         : "+f"(acc_lo), "+f"(acc_hi) : "r"(w), "h"(v));
 }
+// acc[i] = fmaf(b[i], v, acc[i]) for the E elements of one vector, two at a time with the
+// packed fp32x2 FMA of sm_100+ (two independent round-to-nearest FMAs: the same bits as two
+// fmaf calls, half the issued instructions).
+template <int E>
+__device__ __forceinline__ void fma_vec_f32(const float *b, float v, float *acc) {
+#pragma unroll
+    for (int i = 0; i + 1 < E; i += 2) {
+        unsigned long long a2, b2, v2;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(a2) : "f"(acc[i]), "f"(acc[i + 1]));
+        asm("mov.b64 %0, {%1, %2};" : "=l"(b2) : "f"(b[i]), "f"(b[i + 1]));
+        asm("mov.b64 %0, {%1, %1};" : "=l"(v2) : "f"(v));
+        asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(a2) : "l"(b2), "l"(v2));
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(acc[i]), "=f"(acc[i + 1]) : "l"(a2));
+    }
+    if constexpr (E % 2) acc[E - 1] = fmaf(b[E - 1], v, acc[E - 1]);
+}
+
 __device__ __forceinline__ void fma_bf16x1(unsigned short b, unsigned short v, float &acc) {
     asm("fma.rn.f32.bf16 %0, %1, %2, %0;\n" : "+f"(acc) : "h"(b), "h"(v));
 }

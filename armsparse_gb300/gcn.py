@@ -64,9 +64,13 @@ class SPMMFunction(torch.autograd.Function):
                                    "values_csr, values_csc))")
             grad_feat = _spmm(colptr, rowind, w_csc, g, ctx.bwd_variant)
         if ctx.needs_input_grad[5]:
-            gf = g if g.dtype in (torch.float32, torch.float64) else g.float()
-            ff = feat if feat.dtype == gf.dtype else feat.to(gf.dtype)
-            grad_w = S.sddmm(rowptr, colind, gf, ff.contiguous()).to(w_csr.dtype)
+            if g.dtype == torch.bfloat16 and feat.dtype == torch.bfloat16:
+                # bf16 layer: bf16 operands, fp32 products and sums
+                grad_w = S.sddmm(rowptr, colind, g, feat.contiguous()).to(w_csr.dtype)
+            else:
+                gf = g if g.dtype in (torch.float32, torch.float64) else g.float()
+                ff = feat if feat.dtype == gf.dtype else feat.to(gf.dtype)
+                grad_w = S.sddmm(rowptr, colind, gf, ff.contiguous()).to(w_csr.dtype)
         return None, None, None, None, grad_feat, grad_w, None, None
 
 

@@ -228,15 +228,16 @@ def spmv_vcsr4(vrowptr, vcolind, vval, x, y=None, beta: float = 0.0):
 def sddmm(rowptr, colind, X, Y, aval=None, out=None, tensor_cores: bool = False,
           variant: int = 0):
     """out[e] = aval[e] * <X[row(e)], Y[col(e)]> (aval None -> unscaled, the reference's
-    sddmm_cuda_csr). X: M x K, Y: N x K, fp32. tensor_cores selects the tcgen05 split-bf16
-    path."""
+    sddmm_cuda_csr). X: M x K, Y: N x K, fp32 -- or both bf16 (fp32 products and sums, fp32
+    out). tensor_cores selects the tcgen05 split-bf16 path (fp32 inputs)."""
     dev = _dev(rowptr, colind, X, Y, aval, out)
     M, nnz = _csr(rowptr, colind)
     if X.dtype == torch.float64:
         return _sddmm_f64(rowptr, colind, X, Y, aval, out)
+    bf16 = X.dtype == torch.bfloat16 and Y.dtype == torch.bfloat16 and not tensor_cores
     for t, n in ((X, "X"), (Y, "Y")):
-        if t.dtype != torch.float32 or t.dim() != 2 or t.stride(1) != 1:
-            raise ValueError(f"{n} must be float32, 2-D, row-major")
+        if (t.dtype != torch.float32 and not bf16) or t.dim() != 2 or t.stride(1) != 1:
+            raise ValueError(f"{n} must be float32 (or both X and Y bfloat16), 2-D, row-major")
     if X.shape[0] != M:
         raise ValueError("X must have one row per pattern row")
     if X.shape[1] != Y.shape[1]:
@@ -250,7 +251,11 @@ def sddmm(rowptr, colind, X, Y, aval=None, out=None, tensor_cores: bool = False,
     ldx = X.stride(0) if M > 1 else K
     ldy = Y.stride(0) if Y.shape[0] > 1 else K
     ctx = N.context(dev.index)
-    if tensor_cores:
+    if bf16:
+        N.check(N.load().as_sddmm_csr_bf16(ctx.handle, M, Y.shape[0], K, nnz, _ptr(rowptr),
+                                           _ptr(colind), _ptr(aval), _ptr(X), ldx, _ptr(Y), ldy,
+                                           _ptr(out), _stream(dev)), "as_sddmm_csr_bf16")
+    elif tensor_cores:
         N.check(N.load().as_sddmm_csr_bf16x3_v(ctx.handle, M, Y.shape[0], K, nnz, _ptr(rowptr),
                                                _ptr(colind), _ptr(aval), _ptr(X), ldx, _ptr(Y),
                                                ldy, _ptr(out), int(variant), _stream(dev)),

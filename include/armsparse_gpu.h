@@ -138,6 +138,13 @@ as_status as_sddmm_csr_f32(as_ctx *ctx, int M, int N, int K, int nnz, const int 
 as_status as_sddmm_csr_bf16x3(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
                               const int *colind, const float *aval, const float *X, long ldx,
                               const float *Y, long ldy, float *out, void *stream);
+/* X and Y stored as bf16 (uint16_t bit patterns), FP32 products and sums, FP32 out: the
+ * dot products of as_sddmm_csr_f32 run on the bf16 values (bit for bit what
+ * as_sddmm_csr_f32 gives for those values widened to FP32), with half the bytes gathered.
+ * Used for the edge-value gradient of bf16 GCN layers. */
+as_status as_sddmm_csr_bf16(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
+                            const int *colind, const float *aval, const uint16_t *X, long ldx,
+                            const uint16_t *Y, long ldy, float *out, void *stream);
 
 /* as_sddmm_csr_bf16x3 with an explicit kernel variant (tuning): 0 = library choice,
  * 1 = one 128 x 256 output tile per CTA, 2 = persistent CTAs with two tensor-memory

@@ -134,3 +134,20 @@ def test_coo_any_order(oracle):
     lanes = oracle.sddmm_f32_lanes(a.rowptr, a.colind, X, Y, aval=a.val)
     assert np.array_equal(bits(out), bits(lanes[perm]))
     A.sync_status()
+
+
+@pytest.mark.parametrize("K", [64, 47, 256])
+def test_bf16_inputs_bit_exact(oracle, K):
+    """bf16 X and Y, fp32 products and sums: bit for bit the eight-lane fp32 restatement run
+    on the bf16 values widened to fp32 (vector path for K % 8 == 0, scalar otherwise)."""
+    a = S.uniform_csr(500, 400, 20000, seed=K, values="u0515")
+    X = S.dense_normal((500, K), K + 1)
+    Y = S.dense_normal((400, K), K + 2)
+    Xb, Yb = oracle.bf16_round(X), oracle.bf16_round(Y)
+    rp, ci, v = to_dev(a.rowptr), to_dev(a.colind), to_dev(a.val)
+    Xd, Yd = to_dev(X).to(torch.bfloat16), to_dev(Y).to(torch.bfloat16)
+    for aval, av in ((None, None), (v, a.val)):
+        out = A.sddmm(rp, ci, Xd, Yd, aval=aval)
+        ref = oracle.sddmm_f32_lanes(a.rowptr, a.colind, Xb, Yb, aval=av)
+        assert np.array_equal(bits(out), bits(ref)), (K, aval is None)
+    A.sync_status()
