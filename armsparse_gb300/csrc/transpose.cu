@@ -14,7 +14,9 @@
 //   3. stable scatter   -- each CTA re-reads its tile in rounds of 256 entries and ranks
 //                          every entry among equal digits that precede it (warp
 //                          __match_any_sync + per-warp counts + a running per-digit count),
-//                          then writes key, row and value to their slots.
+//                          parks the tile in shared memory sorted by digit, then writes
+//                          key, row and value out in that order, so each digit's entries
+//                          leave as one coalesced run.
 // No position depends on timing, so the output is identical run to run. colptr comes
 // from the sorted keys (first slot of every column). All indices stay inside their
 // buffers for any input; malformed input sets the status word instead of faulting.
@@ -25,7 +27,7 @@ namespace as {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kRounds = 16;
+constexpr int kRounds = 8;
 constexpr int kTile = kThreads * kRounds;  // entries per tile
 constexpr int kBins = 256;
 constexpr int kWarps = kThreads / 32;
@@ -165,21 +167,38 @@ radix_scatter(const int *__restrict__ keys, const int *__restrict__ rows,
               const float *__restrict__ vals, int nnz, int shift, int tiles,
               const int *__restrict__ offsets, int *__restrict__ okeys, int *__restrict__ orows,
               float *__restrict__ ovals) {
-    __shared__ int run[kBins];            // running count per digit inside this tile
+    static_assert(kBins == kThreads, "one digit per thread");
+    __shared__ int run[kBins];            // running local slot per digit inside this tile
+    __shared__ int start[kBins];          // first local slot of each digit in this tile
+    __shared__ int goff[kBins];           // first global slot of each digit for this tile
     __shared__ int wcnt[kWarps][kBins];   // per-warp counts of the current round
+    __shared__ int sw[kWarps];
+    __shared__ int sk[kTile];             // the tile, sorted by digit (stable)
+    __shared__ int sr[kTile];
+    __shared__ float sv[kTile];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    run[threadIdx.x] = offsets[static_cast<long>(threadIdx.x) * tiles + blockIdx.x];
     const long base = static_cast<long>(blockIdx.x) * kTile;
+    const int n_tile = static_cast<int>(nnz - base < kTile ? nnz - base : kTile);
+    {   // this tile's digit counts from the scanned (digit, tile) offsets; local starts
+        const long idx = static_cast<long>(threadIdx.x) * tiles + blockIdx.x;
+        const int off = offsets[idx];
+        const int nxt = idx + 1 < static_cast<long>(kBins) * tiles ? offsets[idx + 1] : nnz;
+        int total;
+        const int st = block_exclusive_scan(nxt - off, sw, total);
+        goff[threadIdx.x] = off;
+        start[threadIdx.x] = st;
+        run[threadIdx.x] = st;
+    }
     const unsigned lt_mask = (1u << lane) - 1u;
     for (int i = 0; i < kRounds; ++i) {
-        const long idx = base + static_cast<long>(i) * kThreads + threadIdx.x;
-        const bool valid = idx < nnz;
+        const int li = i * kThreads + threadIdx.x;
+        const bool valid = li < n_tile;
         int k = 0, r = 0;
         float v = 0.0f;
         if (valid) {
-            k = keys[idx];
-            r = rows[idx];
-            if (vals) v = vals[idx];
+            k = keys[base + li];
+            r = rows[base + li];
+            if (vals) v = vals[base + li];
         }
         const int d = valid ? static_cast<int>((static_cast<unsigned>(k) >> shift) & (kBins - 1))
                             : kBins;  // invalid lanes get a digit of their own
@@ -204,11 +223,21 @@ radix_scatter(const int *__restrict__ keys, const int *__restrict__ rows,
         __syncthreads();
         if (valid) {
             const int pos = wcnt[warp][d] + rank;
-            okeys[pos] = k;
-            orows[pos] = r;
-            if (vals) ovals[pos] = v;
+            sk[pos] = k;
+            sr[pos] = r;
+            sv[pos] = v;
         }
-        __syncthreads();
+        __syncthreads();  // wcnt is cleared by the next round
+    }
+    // write out in local (digit-sorted) order: a digit's entries go to consecutive global
+    // slots, so neighbouring threads write neighbouring addresses
+    for (int p = threadIdx.x; p < n_tile; p += kThreads) {
+        const int k = sk[p];
+        const int d = static_cast<int>((static_cast<unsigned>(k) >> shift) & (kBins - 1));
+        const int g = goff[d] + (p - start[d]);
+        okeys[g] = k;
+        orows[g] = sr[p];
+        if (vals) ovals[g] = sv[p];
     }
 }
 
