@@ -116,16 +116,39 @@ scan_downsweep(const int *__restrict__ in, long n, const int *__restrict__ block
 }
 
 // ---- transpose kernels -----------------------------------------------------------------
-// rowidx[e] = row of entry e (one warp per row); malformed rows flag and write nothing.
+// rowidx[e] = row of entry e. Each thread takes kExpand consecutive entries: one binary
+// search over rowptr for its first entry, then it steps the row forward -- so one row with
+// millions of entries is spread over many threads. Rows with malformed pointers flag and
+// write nothing.
+constexpr int kExpand = 8;
 __global__ void __launch_bounds__(kThreads)
 expand_rows(int M, int nnz, const int *__restrict__ rowptr, int *__restrict__ rowidx,
             unsigned *status) {
-    const long warp = (static_cast<long>(blockIdx.x) * kThreads + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (warp >= M) return;
-    int lo, hi;
-    row_range(rowptr, static_cast<int>(warp), nnz, status, lo, hi);
-    for (int e = lo + lane; e < hi; e += 32) rowidx[e] = static_cast<int>(warp);
+    const long e0 = (static_cast<long>(blockIdx.x) * kThreads + threadIdx.x) * kExpand;
+    if (e0 >= nnz) return;
+    int lo = 0, hi = M;  // largest r with rowptr[r] <= e0 (rowptr monotone for valid input)
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(rowptr + mid) <= e0)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    int r = lo;
+    int rs = __ldg(rowptr + r), re = __ldg(rowptr + r + 1);
+    const long e1 = e0 + kExpand < nnz ? e0 + kExpand : nnz;
+    for (long e = e0; e < e1; ++e) {
+        while (e >= re && r + 1 < M) {  // advance to the row that holds e
+            ++r;
+            rs = re;
+            re = __ldg(rowptr + r + 1);
+        }
+        if (rs < 0 || re < rs || re > nnz || e < rs || e >= re) {
+            flag(status, kFlagBadRowptr);
+            continue;  // malformed pointers: the slot keeps its value (check_rowptr_ends)
+        }
+        rowidx[e] = r;
+    }
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -149,10 +172,17 @@ radix_histogram(const int *__restrict__ keys, int nnz, int shift, int tiles, int
     h[threadIdx.x] = 0;
     __syncthreads();
     const long base = static_cast<long>(blockIdx.x) * kTile;
+    int kv[kRounds];  // all of this thread's keys are loaded before any is counted
+#pragma unroll
+    for (int i = 0; i < kRounds; ++i) {
+        const long idx = base + static_cast<long>(i) * kThreads + threadIdx.x;
+        kv[i] = idx < nnz ? keys[idx] : 0;
+    }
+#pragma unroll
     for (int i = 0; i < kRounds; ++i) {
         const long idx = base + static_cast<long>(i) * kThreads + threadIdx.x;
         if (idx < nnz) {
-            const int k = keys[idx];
+            const int k = kv[i];
             if (check_range && static_cast<unsigned>(k) >= static_cast<unsigned>(N))
                 flag(status, kFlagBadColind);
             atomicAdd(&h[(static_cast<unsigned>(k) >> shift) & (kBins - 1)], 1);
@@ -190,16 +220,26 @@ radix_scatter(const int *__restrict__ keys, const int *__restrict__ rows,
         run[threadIdx.x] = st;
     }
     const unsigned lt_mask = (1u << lane) - 1u;
+    int kr[kRounds], rr[kRounds];  // the thread's entries, loaded before the ranking rounds
+    float vr[kRounds];
+#pragma unroll
+    for (int i = 0; i < kRounds; ++i) {
+        const int li = i * kThreads + threadIdx.x;
+        kr[i] = 0;
+        rr[i] = 0;
+        vr[i] = 0.0f;
+        if (li < n_tile) {
+            kr[i] = keys[base + li];
+            rr[i] = rows[base + li];
+            if (vals) vr[i] = vals[base + li];
+        }
+    }
+#pragma unroll
     for (int i = 0; i < kRounds; ++i) {
         const int li = i * kThreads + threadIdx.x;
         const bool valid = li < n_tile;
-        int k = 0, r = 0;
-        float v = 0.0f;
-        if (valid) {
-            k = keys[base + li];
-            r = rows[base + li];
-            if (vals) v = vals[base + li];
-        }
+        const int k = kr[i], r = rr[i];
+        const float v = vr[i];
         const int d = valid ? static_cast<int>((static_cast<unsigned>(k) >> shift) & (kBins - 1))
                             : kBins;  // invalid lanes get a digit of their own
 #pragma unroll
@@ -349,7 +389,7 @@ as_status csr2csc_launch(as_ctx *ctx, int M, int N, int nnz, const int *rowptr,
     int *hist = reinterpret_cast<int *>(take(sizeof(int) * static_cast<size_t>(hist_n)));
     int *sums = reinterpret_cast<int *>(take(sizeof(int) * static_cast<size_t>(ceil_div(hist_n, kScanChunk) + 1)));
 
-    const unsigned gw = static_cast<unsigned>(ceil_div(static_cast<long>(M) * 32, kThreads));
+    const unsigned gw = static_cast<unsigned>(ceil_div(ceil_div(nnz, kExpand), kThreads));
     expand_rows<<<gw, kThreads, 0, s>>>(M, nnz, rowptr, rowidx, ctx->d_status);
     check_rowptr_ends<<<static_cast<unsigned>(ceil_div(nnz, kThreads) < 4096 ? ceil_div(nnz, kThreads) : 4096),
                         kThreads, 0, s>>>(M, nnz, rowptr, rowidx, ctx->d_status);
@@ -479,7 +519,7 @@ cudaError_t csr2csc_static_run(int M, int N, int nnz, const int *rowptr, const i
     int *hist = reinterpret_cast<int *>(work + 5 * cap);
     int *sums = reinterpret_cast<int *>(work + 5 * cap + align256c(sizeof(int) * kStaticHist));
 
-    const unsigned gw = static_cast<unsigned>(ceil_div(static_cast<long>(M) * 32, kThreads));
+    const unsigned gw = static_cast<unsigned>(ceil_div(ceil_div(nnz, kExpand), kThreads));
     expand_rows<<<gw, kThreads, 0, s>>>(M, nnz, rowptr, rowidx, status);
     const long cb = ceil_div(nnz, kThreads);
     check_rowptr_ends<<<static_cast<unsigned>(cb < 4096 ? cb : 4096), kThreads, 0, s>>>(
