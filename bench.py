@@ -468,13 +468,17 @@ class GcnEpoch(Workload):
         self.model_plain = gcn.Net(500, 64, 3).to(dev)
         self.opt_plain = gcn.make_optimizer(self.model_plain)
         self.plan = self.g.plan(64, torch.float32), self.g.plan(3, torch.float32)
+        # the features are 10 % non-zero: the tuned path keeps them as CSR, so the first
+        # layer's X @ W is an SpMM (and its weight gradient an SpMM with X^T)
+        self.feats = gcn.SparseFeatures(self.xd, self.g.selector)
         torch.manual_seed(0)
         self.model_graph = gcn.Net(500, 64, 3).to(dev)
         self.captured = gcn.CapturedEpoch(self.model_graph,
                                           gcn.make_optimizer(self.model_graph, capturable=True),
-                                          self.xd, self.g, self.yd, self.td)
-        self.config["execution"] = ("selector-tuned kernels, the epoch recorded once as a CUDA "
-                                    "graph and replayed (eager epochs reported in extra)")
+                                          self.feats, self.g, self.yd, self.td)
+        self.config["execution"] = ("selector-tuned kernels, features as CSR (X @ W as SpMM), "
+                                    "the epoch recorded once as a CUDA graph and replayed "
+                                    "(eager epochs reported in extra)")
 
     def step(self):
         self.loss = self.captured()
@@ -484,7 +488,7 @@ class GcnEpoch(Workload):
 
     def eager_step(self):
         from armsparse_gb300 import gcn
-        return gcn.train_epoch(self.model, self.opt, self.xd, self.g, self.yd, self.td)
+        return gcn.train_epoch(self.model, self.opt, self.feats, self.g, self.yd, self.td)
 
     def plain_step(self):
         from armsparse_gb300 import gcn
@@ -504,13 +508,17 @@ class GcnEpoch(Workload):
                                               C=C, variant=v), reps=20)
 
     def e2e_setup(self):
-        import torch
-        self.hx = torch.from_numpy(self.x).pin_memory()
-        self.h2d = self.hx.numel() * 4
+        # the features arrive as CSR from pinned host memory (same pattern every epoch)
+        self.hcsr = [t.cpu().pin_memory() for t in (self.feats.rowptr, self.feats.colind,
+                                                     self.feats.values)]
+        self.h2d = sum(t.numel() * t.element_size() for t in self.hcsr)
         self.d2h = 4
 
     def e2e_step(self):
-        self.xd.copy_(self.hx, non_blocking=True)
+        f = self.feats
+        f.rowptr.copy_(self.hcsr[0], non_blocking=True)
+        f.colind.copy_(self.hcsr[1], non_blocking=True)
+        f.load_values(self.hcsr[2])
         self.step()
         float(self.loss)
 
@@ -588,7 +596,7 @@ class GcnEpoch(Workload):
             torch.manual_seed(_)
             l1.append(float(gcn.train_epoch(m1, o1, self.xd, self.g_plain, self.yd, self.td)))
             torch.manual_seed(_)
-            l2.append(float(gcn.train_epoch(m2, o2, self.xd, self.g, self.yd, self.td)))
+            l2.append(float(gcn.train_epoch(m2, o2, self.feats, self.g, self.yd, self.td)))
         return {"plain_ms_per_epoch": round(plain_ms, 4),
                 "plain": "eager epochs, library-default kernels",
                 "tuned_eager_ms_per_epoch": round(tuned_ms, 4),

@@ -152,3 +152,32 @@ def test_captured_epoch_matches_eager():
     assert np.isfinite(losses).all() and losses[-1] < losses[0]
     with pytest.raises(ValueError):
         gcn.CapturedEpoch(m3, gcn.make_optimizer(m3), x, g, y, train)
+
+
+def test_sparse_features_product(oracle):
+    """X @ W with X held as CSR (SpMM forward, SpMM with X^T for dW) against the dense
+    product in FP64, and a captured epoch that reads the sparse features."""
+    x, g, y, train, _ = gcn.synthetic_task(seed=1)
+    feats = gcn.SparseFeatures(x)
+    torch.manual_seed(3)
+    W = (torch.randn(500, 64, device=dev()) * 0.1).requires_grad_(True)
+    G = torch.randn(x.shape[0], 64, device=dev())
+    out = feats.matmul(W)
+    (out * G).sum().backward()
+    xd, Wd, Gd = x.double(), W.detach().double(), G.double()
+    ref = xd @ Wd
+    scale = xd.abs() @ Wd.abs()
+    assert ((out.double() - ref).abs() / scale.clamp_min(1e-30)).max() < 1e-5
+    dref = xd.t() @ Gd
+    dscale = xd.abs().t() @ Gd.abs()
+    assert ((W.grad.double() - dref).abs() / dscale.clamp_min(1e-30)).max() < 1e-5
+    # a training epoch on sparse features tracks the dense one
+    torch.manual_seed(0)
+    m1 = gcn.Net(500, 64, 3, dropout=0.0).to(dev())
+    torch.manual_seed(0)
+    m2 = gcn.Net(500, 64, 3, dropout=0.0).to(dev())
+    o1, o2 = gcn.make_optimizer(m1), gcn.make_optimizer(m2, capturable=True)
+    dense = [float(gcn.train_epoch(m1, o1, x, g, y, train)) for _ in range(8)]
+    step = gcn.CapturedEpoch(m2, o2, feats, g, y, train, warmup=3)
+    sparse = [float(step()) for _ in range(5)]
+    assert np.allclose(sparse, dense[3:], rtol=0, atol=1e-4), (sparse, dense[3:])
