@@ -169,6 +169,10 @@ class SparseFeatures:
     def device(self) -> torch.device:
         return self.values.device
 
+    @property
+    def dtype(self) -> torch.dtype:
+        return self.values.dtype
+
     def matmul(self, W: torch.Tensor) -> torch.Tensor:
         return _FeatureProduct.apply(self, W)
 
