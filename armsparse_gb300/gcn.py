@@ -156,13 +156,22 @@ class SparseFeatures:
                                            self.shape[1])[2])
 
     def plan(self, width: int, forward: bool) -> int:
+        """Kernel variant for X @ W (forward) or X^T @ dY, chosen once per width by timing the
+        selector's candidate kernels on these matrices (X^T has few, very long rows -- outside
+        the shapes the learned selector was trained on)."""
         if self.selector is None:
             return 0
         key = (width, forward)
         if key not in self._plans:
-            rp = self.rowptr if forward else self.transposed[0]
-            n_cols = self.shape[1] if forward else self.shape[0]
-            self._plans[key] = self.selector.choose(rp, n_cols, width, torch.float32)
+            from . import selector as SEL
+            from . import tuner
+            rp, ci, v = (self.rowptr, self.colind, self.values) if forward else self.transposed
+            n_in = self.shape[1] if forward else self.shape[0]
+            B = torch.zeros(n_in, width, device=self.device)
+            ids = SEL.variant_ids(SEL.CANDIDATES, torch.float32)
+            best = tuner.best(tuner.autotune_spmm(rp, ci, v, B, variants=ids, reps=3,
+                                                   max_ratio=3.0))
+            self._plans[key] = best.variant
         return self._plans[key]
 
     @property
