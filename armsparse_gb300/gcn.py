@@ -74,6 +74,44 @@ class SPMMFunction(torch.autograd.Function):
         return None, None, None, None, grad_feat, grad_w, None, None
 
 
+def _time_pick(rowptr, colind, values, n_in: int, width: int, dtype) -> int:
+    """The fastest of the selector's candidate SpMM kernels on these arrays (timed once)."""
+    from . import selector as SEL
+    from . import tuner
+    B = torch.zeros(n_in, width, device=rowptr.device, dtype=dtype)
+    ids = SEL.variant_ids(SEL.CANDIDATES, dtype)
+    return tuner.best(tuner.autotune_spmm(rowptr, colind, values.to(dtype), B, variants=ids,
+                                          reps=3, max_ratio=3.0)).variant
+
+
+class _DenseProduct(torch.autograd.Function):
+    """x @ W for a tall dense x and a narrow W. The weight gradient x^T dY reduces over all
+    rows into a few outputs (64 x 3 for the GCN's second layer); as one GEMM that runs on a
+    single tile for the whole reduction, so it is split into row blocks of kRows, reduced by
+    a batched GEMM and a sum."""
+
+    kRows = 1024
+
+    @staticmethod
+    def forward(ctx, x, W):
+        ctx.save_for_backward(x, W)
+        return x @ W
+
+    @staticmethod
+    def backward(ctx, g):
+        x, W = ctx.saved_tensors
+        dx = g @ W.t() if ctx.needs_input_grad[0] else None
+        dW = None
+        if ctx.needs_input_grad[1]:
+            n, r = x.shape[0], _DenseProduct.kRows
+            pad = (-n) % r
+            xp = torch.nn.functional.pad(x, (0, 0, 0, pad)) if pad else x
+            gp = torch.nn.functional.pad(g, (0, 0, 0, pad)) if pad else g
+            b = xp.shape[0] // r
+            dW = torch.bmm(xp.reshape(b, r, -1).transpose(1, 2), gp.reshape(b, r, -1)).sum(0)
+        return dx, dW
+
+
 class Graph:
     """A sparse adjacency on the GPU with its transpose computed once (GPU, deterministic)."""
 
@@ -93,14 +131,21 @@ class Graph:
         return self._csc
 
     def plan(self, N: int, dtype=torch.float32):
-        """(forward, backward) kernel variants for dense width N, from the selector."""
+        """(forward, backward) kernel variants for dense width N: the learned selector's pick,
+        or -- for widths below the 16..256 it was trained on -- the fastest of its candidate
+        kernels timed once on this graph."""
         if self.selector is None or dtype == torch.float64:
             return (0, 0)
         key = (N, dtype)
         if key not in self._plans:
-            colptr, _, _ = self.csc
-            self._plans[key] = (self.selector.choose(self.rowptr, self.n_cols, N, dtype),
-                                self.selector.choose(colptr, self.n_rows, N, dtype))
+            colptr, rowind, vcsc = self.csc
+            if N < 16:
+                self._plans[key] = (_time_pick(self.rowptr, self.colind, self.values,
+                                               self.n_cols, N, dtype),
+                                    _time_pick(colptr, rowind, vcsc, self.n_rows, N, dtype))
+            else:
+                self._plans[key] = (self.selector.choose(self.rowptr, self.n_cols, N, dtype),
+                                    self.selector.choose(colptr, self.n_rows, N, dtype))
         return self._plans[key]
 
     @classmethod
@@ -220,7 +265,12 @@ class GCNConv(torch.nn.Module):
 
     def forward(self, x, rowptr, colind, colptr, rowind, edge_weight_csr, edge_weight_csc,
                 variants=None):
-        x = x.matmul(self.weight) if isinstance(x, SparseFeatures) else torch.matmul(x, self.weight)
+        if isinstance(x, SparseFeatures):
+            x = x.matmul(self.weight)
+        elif x.dim() == 2 and x.shape[0] >= 8 * _DenseProduct.kRows:
+            x = _DenseProduct.apply(x, self.weight)
+        else:
+            x = torch.matmul(x, self.weight)
         if not self.cached or self.cached_result is None:
             if self.normalize:
                 in_norm, out_norm = self.deg_inv_sqrt(rowptr), self.deg_inv_sqrt(colptr)
