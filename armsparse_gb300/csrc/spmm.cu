@@ -221,12 +221,17 @@ struct Variant {
     AS_V(vb, g, 2, 8)
 #define AS_VROW(vb) AS_VG(vb, 1), AS_VG(vb, 2), AS_VG(vb, 4), AS_VG(vb, 8), AS_VG(vb, 16), AS_VG(vb, 32)
 
+// 32-entry chunks: many short chains for small graphs (N <= kSmallChunkMaxN: their carry
+// scratch, 2 x nnz/32 x N floats, stays modest)
+#define AS_NNZS32 AS_NNZ(4, 32, 1, 32), AS_NNZ(4, 32, 2, 32), AS_NNZ(16, 32, 1, 32)
+constexpr int kSmallChunk = 32;
+constexpr int kSmallChunkMaxN = 64;
 const Variant kF32[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_BULKS, AS_NNZS(128),
-                        AS_NNZS(1024), AS_NNZS8(256), AS_NNZS8(1024)};
+                        AS_NNZS(1024), AS_NNZS8(256), AS_NNZS8(1024), AS_NNZS32};
 const Variant kBF16[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_VROW(2), AS_BULKS,
                          AS_NNZS(128), AS_NNZS(1024), AS_NNZS_BF16_SCALAR(128),
                          AS_NNZS_BF16_SCALAR(1024), AS_NNZS8(256), AS_NNZS8(1024),
-                         AS_NNZ8(2, 32, 2, 256), AS_NNZ8(2, 32, 2, 1024)};
+                         AS_NNZ8(2, 32, 2, 256), AS_NNZ8(2, 32, 2, 1024), AS_NNZS32};
 constexpr int kNF32 = sizeof(kF32) / sizeof(kF32[0]);
 constexpr int kNBF16 = sizeof(kBF16) / sizeof(kBF16[0]);
 
@@ -363,6 +368,7 @@ bool spmm_variant_supported(int dtype, int variant, int N, long ldb, long ldc, c
                ceil_div(N, tile) <= 65535;
     }
     const int E = v.vb / esz;  // nnz-split
+    if (v.unroll == kSmallChunk && N > kSmallChunkMaxN) return false;
     return N % E == 0 && ldb % E == 0 && pb % (E * esz) == 0 &&
            ceil_div(N, E * v.group * v.cpl) <= 65535;
 }
@@ -370,8 +376,12 @@ bool spmm_variant_supported(int dtype, int variant, int N, long ldb, long ldc, c
 as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cudaStream_t s) {
     const Variant &v = dtype == 0 ? kF32[variant - 1] : kBF16[variant - 1];
     if (v.kind == 1) return spmm_bulk_launch(ctx, dtype, v.vb, v.unroll, a, s);
-    if (v.kind == 2)
+    if (v.kind == 2) {
+        if (v.unroll == kSmallChunk && a.N > kSmallChunkMaxN)
+            return fail(AS_ERR_UNSUPPORTED, std::string("spmm: variant ") + v.name +
+                                                " serves N <= 64 only");
         return spmm_nnz_launch(ctx, dtype, v.vb, v.group, v.cpl, v.unroll, v.steps, a, s);
+    }
     if (!vb_ok(dtype, v.vb, a.N, a.ldb, a.ldc, a.B, a.C))
         return fail(AS_ERR_UNSUPPORTED, std::string("spmm: variant ") + v.name +
                                             " needs N, ldb, ldc and pointer alignment to match its vector width");

@@ -47,6 +47,7 @@ CANDIDATES = [
     "nnzsplit_v16_g32_c2_ch1024", "nnzsplit_v4_g32_c1_ch1024",
     "rowsplit_v16_g32_c2_u8", "nnzsplit_v16_g32_c1_ch256_u8", "nnzsplit_v4_g32_c2_ch256_u8",
     "nnzsplit_v16_g32_c1_ch1024_u8", "nnzsplit_v4_g32_c2_ch1024_u8",
+    "nnzsplit_v4_g32_c1_ch32", "nnzsplit_v4_g32_c2_ch32", "nnzsplit_v16_g32_c1_ch32",
 ]
 
 
