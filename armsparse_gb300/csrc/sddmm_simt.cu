@@ -1,14 +1,19 @@
-// FP32 SDDMM on CUDA cores: out[e] = s_e * <X[row(e), :], Y[col(e), :]> (sm_103a).
+// SDDMM on CUDA cores: out[e] = s_e * <X[row(e), :], Y[col(e), :]> (sm_103a), fp32 or bf16
+// operands, fp32 products and sums.
 //
-// One lane per edge, edges in CSR order across the grid. A lane finds its row with one
-// binary search over rowptr (the reference searches per edge as well, findRow in
-// gcn/pytorch-custom/computeUtil.h:11-28), or reads it from the COO row array (the
-// reference's sddmm_cuda_coo, sddmm.cu:427-457), and then streams both operand rows with 32-byte
-// steps (two float4 loads per row per step when K and the leading dimensions are multiples
-// of 8 floats, else scalar). Lanes of a warp mostly share the row, so the X loads
-// broadcast; each lane's Y reads are full 32-byte sectors. Eight interleaved partial sums
-// (k mod 8) are combined as ((p0+p4)+(p1+p5)) + ((p2+p6)+(p3+p7)), the same order the
-// CPU baseline uses.
+// A group of G lanes takes one edge at a time (G = one lane per 4-element block of K, a power
+// of two up to a warp), so each Y row is read by neighbouring lanes in 16-byte (fp32) or
+// 8-byte (bf16) pieces -- coalesced -- and the X row, shared by the consecutive edges of one
+// row, comes from L1. A group walks a chunk of consecutive edges in CSR order: one binary
+// search over rowptr for its first edge (the reference searches per edge, findRow in
+// gcn/pytorch-custom/computeUtil.h:11-28), then the row pointer steps forward; the COO form
+// reads each edge's row from the row array (the reference's sddmm_cuda_coo, sddmm.cu:427-457).
+//
+// Summation order (the oracle's or_sddmm_csr_f32_group): lane l runs one fused-FMA chain over
+// the blocks l, l + G, l + 2G, ... of K in order; the lanes are summed by a butterfly
+// (acc += shfl_xor(acc, off), off = G/2 .. 1); lane 0 writes s_e * sum. bf16 operands use the
+// mixed-precision FMA of sm_100+ (a bf16 x bf16 product is exact in fp32), so the bf16 kernel
+// gives bit for bit the fp32 kernel's result on the widened values.
 #include "common.cuh"
 #include "internal.h"
 
@@ -17,7 +22,7 @@ namespace {
 
 constexpr int kThreads = 256;
 
-__device__ __forceinline__ int find_row(const int *__restrict__ rowptr, int M, int e) {
+__device__ __forceinline__ int find_row(const int *__restrict__ rowptr, int M, long e) {
     // largest r in [0, M) with rowptr[r] <= e
     int lo = 0, hi = M;  // invariant: rowptr[lo] <= e < rowptr[hi] for valid CSR
     while (hi - lo > 1) {
@@ -30,155 +35,193 @@ __device__ __forceinline__ int find_row(const int *__restrict__ rowptr, int M, i
     return lo;
 }
 
-// COO: rows come per entry from `rows` (any order); CSR: `rows` is the row pointer.
-template <bool VEC, bool COO>
-__global__ void __launch_bounds__(kThreads)
-sddmm_f32_lane(int M, int N, int K, int nnz, const int *__restrict__ rows,
-               const int *__restrict__ colind, const float *__restrict__ aval,
-               const float *__restrict__ X, long ldx, const float *__restrict__ Y, long ldy,
-               float *__restrict__ out, unsigned *status) {
-    const long e = static_cast<long>(blockIdx.x) * kThreads + threadIdx.x;
-    if (e >= nnz) return;
-    const int c = ld_stream(colind + e);
-    int r;
-    if (COO) {
-        r = ld_stream(rows + e);
-        if (static_cast<unsigned>(r) >= static_cast<unsigned>(M)) {
-            flag(status, kFlagBadRowptr);
-            out[e] = 0.0f;
-            return;
+// acc = fma(x0, y0, acc); acc = fma(x1, y1, acc) for the bf16 halves of x and y, in order.
+__device__ __forceinline__ void fma_bf16_seq2(unsigned x, unsigned y, float &acc) {
+    asm("{\n .reg .b16 xl, xh, yl, yh;\n mov.b32 {xl, xh}, %1;\n mov.b32 {yl, yh}, %2;\n"
+        " fma.rn.f32.bf16 %0, xl, yl, %0;\n fma.rn.f32.bf16 %0, xh, yh, %0;\n}\n"
+        : "+f"(acc) : "r"(x), "r"(y));
+}
+
+// One 4-element block of the dot product, elements in order.
+template <typename T>
+struct Block;
+template <>
+struct Block<float> {
+    using Raw = float4;
+    __device__ static Raw load(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
+    __device__ static void chain(const Raw &x, const Raw &y, float &acc) {
+        acc = fmaf(x.x, y.x, acc);
+        acc = fmaf(x.y, y.y, acc);
+        acc = fmaf(x.z, y.z, acc);
+        acc = fmaf(x.w, y.w, acc);
+    }
+    __device__ static void tail(const float *x, const float *y, int n, float &acc) {
+        for (int i = 0; i < n; ++i) acc = fmaf(__ldg(x + i), __ldg(y + i), acc);
+    }
+};
+template <>
+struct Block<uint16_t> {
+    using Raw = uint2;
+    __device__ static Raw load(const uint16_t *p) { return __ldg(reinterpret_cast<const uint2 *>(p)); }
+    __device__ static void chain(const Raw &x, const Raw &y, float &acc) {
+        fma_bf16_seq2(x.x, y.x, acc);
+        fma_bf16_seq2(x.y, y.y, acc);
+    }
+    __device__ static void tail(const uint16_t *x, const uint16_t *y, int n, float &acc) {
+        for (int i = 0; i < n; ++i) acc = fmaf(bf16_to_f32(x[i]), bf16_to_f32(y[i]), acc);
+    }
+};
+
+// Lane's chain over the blocks g, g + G, ... of one edge. VEC: K % 4 == 0 and 4-element
+// aligned rows, four blocks' loads in flight before their FMAs; else element loads.
+template <typename T, bool VEC, int G>
+__device__ __forceinline__ float lane_chain(const T *xr, const T *yr, int K, int g) {
+    using B = Block<T>;
+    const int nq = (K + 3) >> 2;
+    float acc = 0.0f;
+    int q = g;
+    if (VEC) {
+        for (; q + 3 * G < nq; q += 4 * G) {
+            typename B::Raw x[4], y[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                x[u] = B::load(xr + 4 * (q + u * G));
+                y[u] = B::load(yr + 4 * (q + u * G));
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) B::chain(x[u], y[u], acc);
         }
+        for (; q < nq; q += G) B::chain(B::load(xr + 4 * q), B::load(yr + 4 * q), acc);
     } else {
-        r = find_row(rows, M, static_cast<int>(e));
-        if (__ldg(rows + r) > e || __ldg(rows + r + 1) <= e) {
-            flag(status, kFlagBadRowptr);
-            out[e] = 0.0f;
-            return;
+        for (; q < nq; q += G) {
+            const int k = 4 * q;
+            B::tail(xr + k, yr + k, K - k < 4 ? K - k : 4, acc);
         }
     }
-    if (static_cast<unsigned>(c) >= static_cast<unsigned>(N)) {
-        flag(status, kFlagBadColind);
-        out[e] = 0.0f;
-        return;
-    }
-    const float *xr = X + static_cast<long>(r) * ldx;
-    const float *yr = Y + static_cast<long>(c) * ldy;
-    float p[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    int k = 0;
-    if (VEC) {
-        for (; k + 8 <= K; k += 8) {
-            const float4 x0 = __ldg(reinterpret_cast<const float4 *>(xr + k));
-            const float4 x1 = __ldg(reinterpret_cast<const float4 *>(xr + k + 4));
-            const float4 y0 = __ldg(reinterpret_cast<const float4 *>(yr + k));
-            const float4 y1 = __ldg(reinterpret_cast<const float4 *>(yr + k + 4));
-            p[0] = fmaf(x0.x, y0.x, p[0]); p[1] = fmaf(x0.y, y0.y, p[1]);
-            p[2] = fmaf(x0.z, y0.z, p[2]); p[3] = fmaf(x0.w, y0.w, p[3]);
-            p[4] = fmaf(x1.x, y1.x, p[4]); p[5] = fmaf(x1.y, y1.y, p[5]);
-            p[6] = fmaf(x1.z, y1.z, p[6]); p[7] = fmaf(x1.w, y1.w, p[7]);
-        }
-    }
-    for (; k < K; ++k) p[k & 7] = fmaf(__ldg(xr + k), __ldg(yr + k), p[k & 7]);
-    const float t = ((p[0] + p[4]) + (p[1] + p[5])) + ((p[2] + p[6]) + (p[3] + p[7]));
-    out[e] = aval ? __ldg(aval + e) * t : t;
+    return acc;
 }
 
-// bf16 X and Y (fp32 products and partial sums, fp32 out): the same eight interleaved
-// partials as sddmm_f32_lane, each step the mixed-precision FMA of sm_100+ on two bf16
-// operands (their product is exact in fp32, so the bits equal the fp32 kernel run on the
-// bf16 values widened to fp32). Half the gathered bytes of the fp32 kernel.
-__device__ __forceinline__ void fma_bf16_pair(unsigned x, unsigned y, float &p0, float &p1) {
-    asm("{\n .reg .b16 xl, xh, yl, yh;\n mov.b32 {xl, xh}, %2;\n mov.b32 {yl, yh}, %3;\n"
-        " fma.rn.f32.bf16 %0, xl, yl, %0;\n fma.rn.f32.bf16 %1, xh, yh, %1;\n}\n"
-        : "+f"(p0), "+f"(p1) : "r"(x), "r"(y));
-}
-
-template <bool VEC>
+// COO: rows come per edge from `rows` (any order); CSR: `rows` is the row pointer.
+template <typename T, bool VEC, int G, bool COO>
 __global__ void __launch_bounds__(kThreads)
-sddmm_bf16_lane(int M, int N, int K, int nnz, const int *__restrict__ rowptr,
-                const int *__restrict__ colind, const float *__restrict__ aval,
-                const uint16_t *__restrict__ X, long ldx, const uint16_t *__restrict__ Y,
-                long ldy, float *__restrict__ out, unsigned *status) {
-    const long e = static_cast<long>(blockIdx.x) * kThreads + threadIdx.x;
-    if (e >= nnz) return;
-    const int c = ld_stream(colind + e);
-    const int r = find_row(rowptr, M, static_cast<int>(e));
-    if (__ldg(rowptr + r) > e || __ldg(rowptr + r + 1) <= e) {
-        flag(status, kFlagBadRowptr);
-        out[e] = 0.0f;
-        return;
+sddmm_group(int M, int N, int K, int nnz, int CH, const int *__restrict__ rows,
+            const int *__restrict__ colind, const float *__restrict__ aval,
+            const T *__restrict__ X, long ldx, const T *__restrict__ Y, long ldy,
+            float *__restrict__ out, unsigned *status) {
+    const long grp = (static_cast<long>(blockIdx.x) * kThreads + threadIdx.x) / G;
+    const int g = threadIdx.x % G;
+    const unsigned gmask =
+        G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+    const long e0 = grp * CH;
+    if (e0 >= nnz) return;  // the whole group leaves together
+    const long e1 = e0 + CH < nnz ? e0 + CH : nnz;
+    int r = 0, rs = 0, re = 0;
+    if (!COO) {
+        r = find_row(rows, M, e0);
+        rs = __ldg(rows + r);
+        re = __ldg(rows + r + 1);
     }
-    if (static_cast<unsigned>(c) >= static_cast<unsigned>(N)) {
-        flag(status, kFlagBadColind);
-        out[e] = 0.0f;
-        return;
-    }
-    const uint16_t *xr = X + static_cast<long>(r) * ldx;
-    const uint16_t *yr = Y + static_cast<long>(c) * ldy;
-    float p[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    int k = 0;
-    if (VEC) {
-        for (; k + 8 <= K; k += 8) {
-            const uint4 x = __ldg(reinterpret_cast<const uint4 *>(xr + k));
-            const uint4 y = __ldg(reinterpret_cast<const uint4 *>(yr + k));
-            fma_bf16_pair(x.x, y.x, p[0], p[1]);
-            fma_bf16_pair(x.y, y.y, p[2], p[3]);
-            fma_bf16_pair(x.z, y.z, p[4], p[5]);
-            fma_bf16_pair(x.w, y.w, p[6], p[7]);
+    for (long e = e0; e < e1; ++e) {  // every branch below is the same for the whole group
+        int row;
+        if (COO) {
+            row = ld_stream(rows + e);
+            if (static_cast<unsigned>(row) >= static_cast<unsigned>(M)) {
+                if (g == 0) {
+                    flag(status, kFlagBadRowptr);
+                    out[e] = 0.0f;
+                }
+                continue;
+            }
+        } else {
+            while (e >= re && r + 1 < M) {
+                ++r;
+                rs = re;
+                re = __ldg(rows + r + 1);
+            }
+            if (rs > e || re <= e) {
+                if (g == 0) {
+                    flag(status, kFlagBadRowptr);
+                    out[e] = 0.0f;
+                }
+                continue;
+            }
+            row = r;
         }
+        const int c = ld_stream(colind + e);
+        if (static_cast<unsigned>(c) >= static_cast<unsigned>(N)) {
+            if (g == 0) {
+                flag(status, kFlagBadColind);
+                out[e] = 0.0f;
+            }
+            continue;
+        }
+        float acc = lane_chain<T, VEC, G>(X + static_cast<long>(row) * ldx,
+                                          Y + static_cast<long>(c) * ldy, K, g);
+#pragma unroll
+        for (int off = G / 2; off > 0; off >>= 1) acc += __shfl_xor_sync(gmask, acc, off, G);
+        if (g == 0) out[e] = aval ? __ldg(aval + e) * acc : acc;
     }
-    for (; k < K; ++k)
-        p[k & 7] = fmaf(bf16_to_f32(xr[k]), bf16_to_f32(yr[k]), p[k & 7]);
-    const float t = ((p[0] + p[4]) + (p[1] + p[5])) + ((p[2] + p[6]) + (p[3] + p[7]));
-    out[e] = aval ? __ldg(aval + e) * t : t;
+}
+
+int group_size(int K) {  // the oracle's or_sddmm_group_size
+    const int q = (K + 3) / 4;
+    int g = 1;
+    while (g < q && g < 32) g <<= 1;
+    return g;
+}
+
+template <typename T, bool COO>
+as_status launch_group(as_ctx *ctx, int M, int N, int K, int nnz, const int *rows,
+                       const int *colind, const float *aval, const T *X, long ldx, const T *Y,
+                       long ldy, float *out, cudaStream_t s, const char *what) {
+    if (M == 0) return fail(AS_ERR_INVALID_CSR, "sddmm: nnz > 0 with zero rows");
+    const int esz = static_cast<int>(sizeof(T));
+    const bool vec = K % 4 == 0 && ldx % 4 == 0 && ldy % 4 == 0 &&
+                     reinterpret_cast<uintptr_t>(X) % (4 * esz) == 0 &&
+                     reinterpret_cast<uintptr_t>(Y) % (4 * esz) == 0;
+    const int G = group_size(K);
+    const int CH = G >= 32 ? 4 : 128 / G;  // edges per group: more for short dot products
+    const long groups = ceil_div(nnz, CH);
+    const unsigned grid = static_cast<unsigned>(ceil_div(groups * G, kThreads));
+#define AS_SDDMM_G(GV)                                                                      \
+    case GV:                                                                                \
+        if (vec)                                                                            \
+            sddmm_group<T, true, GV, COO><<<grid, kThreads, 0, s>>>(                        \
+                M, N, K, nnz, CH, rows, colind, aval, X, ldx, Y, ldy, out, ctx->d_status);  \
+        else                                                                                \
+            sddmm_group<T, false, GV, COO><<<grid, kThreads, 0, s>>>(                       \
+                M, N, K, nnz, CH, rows, colind, aval, X, ldx, Y, ldy, out, ctx->d_status);  \
+        break;
+    switch (G) {
+        AS_SDDMM_G(1) AS_SDDMM_G(2) AS_SDDMM_G(4) AS_SDDMM_G(8) AS_SDDMM_G(16) AS_SDDMM_G(32)
+        default: return fail(AS_ERR_UNSUPPORTED, "sddmm: group size");
+    }
+#undef AS_SDDMM_G
+    ctx->launches++;
+    return check_cuda(cudaGetLastError(), what);
 }
 
 }  // namespace
 
-static as_status sddmm_lane_launch(as_ctx *ctx, bool coo, int M, int N, int K, int nnz,
-                                   const int *rows, const int *colind, const float *aval,
-                                   const float *X, long ldx, const float *Y, long ldy,
-                                   float *out, cudaStream_t s) {
-    if (M == 0) {
-        // a pattern with entries but no rows is malformed
-        return fail(AS_ERR_INVALID_CSR, "sddmm: nnz > 0 with zero rows");
-    }
-    const bool vec = (K % 8 == 0) && (ldx % 4 == 0) && (ldy % 4 == 0) &&
-                     reinterpret_cast<uintptr_t>(X) % 16 == 0 &&
-                     reinterpret_cast<uintptr_t>(Y) % 16 == 0;
-    const unsigned grid = static_cast<unsigned>(ceil_div(nnz, kThreads));
-    auto k = vec ? (coo ? sddmm_f32_lane<true, true> : sddmm_f32_lane<true, false>)
-                 : (coo ? sddmm_f32_lane<false, true> : sddmm_f32_lane<false, false>);
-    k<<<grid, kThreads, 0, s>>>(M, N, K, nnz, rows, colind, aval, X, ldx, Y, ldy, out,
-                                ctx->d_status);
-    ctx->launches++;
-    return check_cuda(cudaGetLastError(), "sddmm_f32 launch");
-}
-
 as_status sddmm_f32_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
                            const int *colind, const float *aval, const float *X, long ldx,
                            const float *Y, long ldy, float *out, cudaStream_t s) {
-    return sddmm_lane_launch(ctx, false, M, N, K, nnz, rowptr, colind, aval, X, ldx, Y, ldy, out, s);
+    return launch_group<float, false>(ctx, M, N, K, nnz, rowptr, colind, aval, X, ldx, Y, ldy,
+                                      out, s, "sddmm_f32 launch");
 }
 
 as_status sddmm_bf16_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowptr,
                             const int *colind, const float *aval, const uint16_t *X, long ldx,
                             const uint16_t *Y, long ldy, float *out, cudaStream_t s) {
-    if (M == 0) return fail(AS_ERR_INVALID_CSR, "sddmm: nnz > 0 with zero rows");
-    const bool vec = (K % 8 == 0) && (ldx % 8 == 0) && (ldy % 8 == 0) &&
-                     reinterpret_cast<uintptr_t>(X) % 16 == 0 &&
-                     reinterpret_cast<uintptr_t>(Y) % 16 == 0;
-    const unsigned grid = static_cast<unsigned>(ceil_div(nnz, kThreads));
-    auto k = vec ? sddmm_bf16_lane<true> : sddmm_bf16_lane<false>;
-    k<<<grid, kThreads, 0, s>>>(M, N, K, nnz, rowptr, colind, aval, X, ldx, Y, ldy, out,
-                                ctx->d_status);
-    ctx->launches++;
-    return check_cuda(cudaGetLastError(), "sddmm_bf16 launch");
+    return launch_group<uint16_t, false>(ctx, M, N, K, nnz, rowptr, colind, aval, X, ldx, Y,
+                                         ldy, out, s, "sddmm_bf16 launch");
 }
 
 as_status sddmm_coo_f32_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int *rowind,
                                const int *colind, const float *aval, const float *X, long ldx,
                                const float *Y, long ldy, float *out, cudaStream_t s) {
-    return sddmm_lane_launch(ctx, true, M, N, K, nnz, rowind, colind, aval, X, ldx, Y, ldy, out, s);
+    return launch_group<float, true>(ctx, M, N, K, nnz, rowind, colind, aval, X, ldx, Y, ldy,
+                                     out, s, "sddmm_coo_f32 launch");
 }
 
 }  // namespace as

@@ -206,6 +206,49 @@ void or_sddmm_csr_f32_lanes(int M, int K, const int *rowptr, const int *colind,
     }
 }
 
+/* Lanes per edge of the group-cooperative GPU SDDMM: one lane per 4-element block of K, up to a
+ * warp (a power of two). */
+static int or_sddmm_group_size(int K) {
+    const int q = (K + 3) / 4;
+    int g = 1;
+    while (g < q && g < 32) g <<= 1;
+    return g;
+}
+
+/* SDDMM in the summation order of the GPU's group-cooperative kernel: G lanes per edge
+ * (or_sddmm_group_size(K)); lane l takes the 4-element blocks l, l + G, l + 2G, ... of K in
+ * order with one fused-FMA chain; the lanes are then summed by a butterfly (at each step,
+ * every lane adds its partner l ^ off, off = G/2 .. 1) and lane 0's value is the result.
+ * Inputs are fp32 (bf16 inputs enter widened to fp32, which the GPU's bf16 kernel matches). */
+void or_sddmm_csr_f32_group(int M, int K, const int *rowptr, const int *colind,
+                            const float *aval, const float *X, long ldx, const float *Y,
+                            long ldy, float *out, int threads) {
+    const int G = or_sddmm_group_size(K);
+    const int nq = (K + 3) / 4;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 16)
+    for (int m = 0; m < M; ++m) {
+        const float *x = X + (long)m * ldx;
+        for (int e = rowptr[m]; e < rowptr[m + 1]; ++e) {
+            const float *y = Y + (long)colind[e] * ldy;
+            float a[32], b[32];
+            for (int l = 0; l < G; ++l) {
+                float acc = 0.0f;
+                for (int q = l; q < nq; q += G)
+                    for (int i = 0; i < 4; ++i) {
+                        const int k = 4 * q + i;
+                        if (k < K) acc = fmaf(x[k], y[k], acc);
+                    }
+                a[l] = acc;
+            }
+            for (int off = G / 2; off >= 1; off /= 2) {
+                for (int l = 0; l < G; ++l) b[l] = a[l] + a[l ^ off];
+                for (int l = 0; l < G; ++l) a[l] = b[l];
+            }
+            out[e] = aval ? aval[e] * a[0] : a[0];
+        }
+    }
+}
+
 /* ----------------------------------------------------------------------------------------
  * CSR -> CSC, stable: within each column the entries keep ascending row order. This is
  * the ordering scipy's tocsc() gives on the GCN path (gcn/pytorch-custom/gcn_custom.py:52)

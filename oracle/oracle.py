@@ -72,6 +72,8 @@ def lib():
             L.or_spmv_f64.argtypes = [_c_int, _i32p, _i32p, _f64p, _f64p, _f64p, _f64p]
             L.or_sddmm_csr_f64.argtypes = [_c_int, _c_int, _i32p, _i32p, ctypes.c_void_p, _f64p,
                                            _c_long, _f64p, _c_long, _f64p, _f64p, _c_int]
+            L.or_sddmm_csr_f32_group.argtypes = [_c_int, _c_int, _i32p, _i32p, ctypes.c_void_p,
+                                                 _f32p, _c_long, _f32p, _c_long, _f32p, _c_int]
             L.or_sddmm_csr_f32_lanes.argtypes = [_c_int, _c_int, _i32p, _i32p, ctypes.c_void_p,
                                                  _f32p, _c_long, _f32p, _c_long, _f32p, _c_int]
             L.or_csr2csc.argtypes = [_c_int, _c_int, _i32p, _i32p, _f32p, _i32p, _i32p, _f32p]
@@ -229,6 +231,22 @@ def sddmm_f32_lanes(rowptr, colind, X, Y, aval=None, threads=None):
     out = np.empty(int(rowptr[-1]), np.float32)
     av = None if aval is None else np.ascontiguousarray(aval, np.float32)
     lib().or_sddmm_csr_f32_lanes(M, X.shape[1], rowptr, colind,
+                                 None if av is None else av.ctypes.data, X, X.shape[1], Y,
+                                 Y.shape[1], out, threads or max_threads())
+    return out
+
+
+def sddmm_f32_group(rowptr, colind, X, Y, aval=None, threads=None):
+    """FP32 SDDMM in the GPU kernel's order: per edge, G lanes (a power of two, one per
+    4-element block of K up to 32) each run one fused-FMA chain over their blocks, then a
+    butterfly sum across the lanes. The parity oracle of the GPU SIMT SDDMM."""
+    rowptr, colind = _csr(rowptr, colind)
+    M = rowptr.size - 1
+    X = np.ascontiguousarray(X, np.float32)
+    Y = np.ascontiguousarray(Y, np.float32)
+    out = np.empty(int(rowptr[-1]), np.float32)
+    av = None if aval is None else np.ascontiguousarray(aval, np.float32)
+    lib().or_sddmm_csr_f32_group(M, X.shape[1], rowptr, colind,
                                  None if av is None else av.ctypes.data, X, X.shape[1], Y,
                                  Y.shape[1], out, threads or max_threads())
     return out

@@ -25,7 +25,7 @@ def test_extension_ops(oracle):
     assert ob.dtype == torch.float32
     X, Y = S.dense_normal((700, 32), 5), S.dense_normal((500, 32), 6)
     s = spmm.csr_sddmm(rp, ci, to_dev(X), to_dev(Y))
-    assert np.array_equal(bits(s), bits(oracle.sddmm_f32_lanes(a.rowptr, a.colind, X, Y)))
+    assert np.array_equal(bits(s), bits(oracle.sddmm_f32_group(a.rowptr, a.colind, X, Y)))
     rows = np.repeat(np.arange(700, dtype=np.int32), np.diff(a.rowptr))
     s2 = spmm.coo_sddmm(to_dev(rows), ci, to_dev(X), to_dev(Y))
     assert torch.equal(s, s2)
@@ -107,7 +107,7 @@ def test_edge_value_gradient_is_sddmm(oracle):
     out = gcn.SPMMFunction.apply(G.rowptr, G.colind, colptr, rowind, f, w, vcsc)
     gy = torch.randn_like(out)
     out.backward(gy)
-    ref = oracle.sddmm_f32_lanes(a.rowptr, a.colind, gy.cpu().numpy(), f.cpu().numpy())
+    ref = oracle.sddmm_f32_group(a.rowptr, a.colind, gy.cpu().numpy(), f.cpu().numpy())
     assert np.array_equal(bits(w.grad), bits(ref))
 
 

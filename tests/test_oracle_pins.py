@@ -111,6 +111,11 @@ def test_sddmm_oracles_agree(oracle):
     o64, ab = oracle.sddmm_f64(a.rowptr, a.colind, X, Y, aval=a.val)
     o32 = oracle.sddmm_f32_lanes(a.rowptr, a.colind, X, Y, aval=a.val)
     assert oracle.scaled_err(o32, o64, ab).max() < 1e-5
+    for K in (40, 3, 130):  # the GPU kernel's order: group sizes 16, 1 and 32 lanes
+        Xk, Yk = S.dense_normal((64, K), 10 + K), S.dense_normal((48, K), 20 + K)
+        r64, rab = oracle.sddmm_f64(a.rowptr, a.colind, Xk, Yk, aval=a.val)
+        og = oracle.sddmm_f32_group(a.rowptr, a.colind, Xk, Yk, aval=a.val)
+        assert oracle.scaled_err(og, r64, rab).max() < 1e-5
     # against a dense formula
     rows = np.repeat(np.arange(64), np.diff(a.rowptr))
     dense = (X.astype(np.float64) @ Y.astype(np.float64).T)[rows, a.colind] * a.val

@@ -22,7 +22,7 @@ def test_f32_against_oracle(oracle, M, Ncol, K, nnz):
     rp, ci, av = csr_dev(a)
     for aval in (None, a.val):
         out = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=None if aval is None else av)
-        lanes = oracle.sddmm_f32_lanes(a.rowptr, a.colind, X, Y, aval=aval)
+        lanes = oracle.sddmm_f32_group(a.rowptr, a.colind, X, Y, aval=aval)
         assert np.array_equal(bits(out), bits(lanes))
         r64, ab = oracle.sddmm_f64(a.rowptr, a.colind, X, Y, aval=aval)
         assert oracle.scaled_err(out.cpu().numpy(), r64, ab).max() < 1e-5
@@ -35,7 +35,7 @@ def test_powerlaw_and_empty_rows(oracle):
     Y = S.dense_normal((5000, 32), 4)
     rp, ci, av = csr_dev(a)
     out = A.sddmm(rp, ci, to_dev(X), to_dev(Y), aval=av)
-    lanes = oracle.sddmm_f32_lanes(a.rowptr, a.colind, X, Y, aval=a.val)
+    lanes = oracle.sddmm_f32_group(a.rowptr, a.colind, X, Y, aval=a.val)
     assert np.array_equal(bits(out), bits(lanes))
     empty = A.sddmm(to_dev(np.zeros(5, np.int32)), to_dev(np.zeros(0, np.int32)),
                     torch.randn(4, 8, device=dev()), torch.randn(3, 8, device=dev()))
@@ -131,7 +131,7 @@ def test_coo_any_order(oracle):
     perm = np.random.default_rng(24).permutation(a.nnz)
     out = A.sddmm_coo(to_dev(rows[perm]), to_dev(a.colind[perm]), to_dev(X), to_dev(Y),
                       aval=to_dev(a.val[perm]))
-    lanes = oracle.sddmm_f32_lanes(a.rowptr, a.colind, X, Y, aval=a.val)
+    lanes = oracle.sddmm_f32_group(a.rowptr, a.colind, X, Y, aval=a.val)
     assert np.array_equal(bits(out), bits(lanes[perm]))
     A.sync_status()
 
@@ -148,6 +148,6 @@ def test_bf16_inputs_bit_exact(oracle, K):
     Xd, Yd = to_dev(X).to(torch.bfloat16), to_dev(Y).to(torch.bfloat16)
     for aval, av in ((None, None), (v, a.val)):
         out = A.sddmm(rp, ci, Xd, Yd, aval=aval)
-        ref = oracle.sddmm_f32_lanes(a.rowptr, a.colind, Xb, Yb, aval=av)
+        ref = oracle.sddmm_f32_group(a.rowptr, a.colind, Xb, Yb, aval=av)
         assert np.array_equal(bits(out), bits(ref)), (K, aval is None)
     A.sync_status()
