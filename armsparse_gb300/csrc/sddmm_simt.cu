@@ -1,8 +1,8 @@
 // SDDMM on CUDA cores: out[e] = s_e * <X[row(e), :], Y[col(e), :]> (sm_103a), fp32 or bf16
 // operands, fp32 products and sums.
 //
-// A group of G lanes takes one edge at a time (G = one lane per 4-element block of K, a power
-// of two up to a warp), so each Y row is read by neighbouring lanes in 16-byte (fp32) or
+// A group of G lanes takes one edge at a time (G = about one lane per four 4-element blocks of
+// K, a power of two up to a warp), so each Y row is read by neighbouring lanes in 16-byte (fp32) or
 // 8-byte (bf16) pieces -- coalesced -- and the X row, shared by the consecutive edges of one
 // row, comes from L1. A group walks a chunk of consecutive edges in CSR order: one binary
 // search over rowptr for its first edge (the reference searches per edge, findRow in
@@ -42,6 +42,9 @@ __device__ __forceinline__ void fma_bf16_seq2(unsigned x, unsigned y, float &acc
         : "+f"(acc) : "r"(x), "r"(y));
 }
 
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(uint16_t v) { return bf16_to_f32(v); }
+
 // One 4-element block of the dot product, elements in order.
 template <typename T>
 struct Block;
@@ -55,9 +58,6 @@ struct Block<float> {
         acc = fmaf(x.z, y.z, acc);
         acc = fmaf(x.w, y.w, acc);
     }
-    __device__ static void tail(const float *x, const float *y, int n, float &acc) {
-        for (int i = 0; i < n; ++i) acc = fmaf(__ldg(x + i), __ldg(y + i), acc);
-    }
 };
 template <>
 struct Block<uint16_t> {
@@ -67,35 +67,45 @@ struct Block<uint16_t> {
         fma_bf16_seq2(x.x, y.x, acc);
         fma_bf16_seq2(x.y, y.y, acc);
     }
-    __device__ static void tail(const uint16_t *x, const uint16_t *y, int n, float &acc) {
-        for (int i = 0; i < n; ++i) acc = fmaf(bf16_to_f32(x[i]), bf16_to_f32(y[i]), acc);
-    }
 };
 
-// Lane's chain over the blocks g, g + G, ... of one edge. VEC: K % 4 == 0 and 4-element
-// aligned rows, four blocks' loads in flight before their FMAs; else element loads.
+// Lane's chain over the blocks g, g + G, ... of one edge, four blocks at a time with all
+// their loads issued before the FMAs. VEC: K % 4 == 0 and 4-element aligned rows, one vector
+// load per block; else element loads (elements past K contribute nothing).
 template <typename T, bool VEC, int G>
 __device__ __forceinline__ float lane_chain(const T *xr, const T *yr, int K, int g) {
     using B = Block<T>;
     const int nq = (K + 3) >> 2;
     float acc = 0.0f;
-    int q = g;
-    if (VEC) {
-        for (; q + 3 * G < nq; q += 4 * G) {
+    for (int q = g; q < nq; q += 4 * G) {
+        if (VEC) {
             typename B::Raw x[4], y[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                x[u] = B::load(xr + 4 * (q + u * G));
-                y[u] = B::load(yr + 4 * (q + u * G));
+                const int qq = q + u * G;
+                if (qq < nq) {
+                    x[u] = B::load(xr + 4 * qq);
+                    y[u] = B::load(yr + 4 * qq);
+                }
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) B::chain(x[u], y[u], acc);
-        }
-        for (; q < nq; q += G) B::chain(B::load(xr + 4 * q), B::load(yr + 4 * q), acc);
-    } else {
-        for (; q < nq; q += G) {
-            const int k = 4 * q;
-            B::tail(xr + k, yr + k, K - k < 4 ? K - k : 4, acc);
+            for (int u = 0; u < 4; ++u)
+                if (q + u * G < nq) B::chain(x[u], y[u], acc);
+        } else {
+            float x[4][4], y[4][4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int k = 4 * (q + u * G) + i;
+                    x[u][i] = k < K ? to_f32(xr[k]) : 0.0f;
+                    y[u][i] = k < K ? to_f32(yr[k]) : 0.0f;
+                }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    if (4 * (q + u * G) + i < K) acc = fmaf(x[u][i], y[u][i], acc);
         }
     }
     return acc;
@@ -163,8 +173,8 @@ sddmm_group(int M, int N, int K, int nnz, int CH, const int *__restrict__ rows,
     }
 }
 
-int group_size(int K) {  // the oracle's or_sddmm_group_size
-    const int q = (K + 3) / 4;
+int group_size(int K) {  // the oracle's or_sddmm_group_size: about four blocks per lane
+    const int q = (K + 15) / 16;
     int g = 1;
     while (g < q && g < 32) g <<= 1;
     return g;

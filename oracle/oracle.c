@@ -206,10 +206,10 @@ void or_sddmm_csr_f32_lanes(int M, int K, const int *rowptr, const int *colind,
     }
 }
 
-/* Lanes per edge of the group-cooperative GPU SDDMM: one lane per 4-element block of K, up to a
- * warp (a power of two). */
+/* Lanes per edge of the group-cooperative GPU SDDMM: about one lane per four 4-element blocks
+ * of K (16 elements), a power of two up to a warp. */
 static int or_sddmm_group_size(int K) {
-    const int q = (K + 3) / 4;
+    const int q = (K + 15) / 16;
     int g = 1;
     while (g < q && g < 32) g <<= 1;
     return g;

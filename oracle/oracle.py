@@ -237,9 +237,10 @@ def sddmm_f32_lanes(rowptr, colind, X, Y, aval=None, threads=None):
 
 
 def sddmm_f32_group(rowptr, colind, X, Y, aval=None, threads=None):
-    """FP32 SDDMM in the GPU kernel's order: per edge, G lanes (a power of two, one per
-    4-element block of K up to 32) each run one fused-FMA chain over their blocks, then a
-    butterfly sum across the lanes. The parity oracle of the GPU SIMT SDDMM."""
+    """FP32 SDDMM in the GPU kernel's order: per edge, G lanes (a power of two, about one per
+    16 elements of K, up to 32) each run one fused-FMA chain over their 4-element blocks
+    (blocks l, l + G, ...), then a butterfly sum across the lanes. The parity oracle of the
+    GPU SIMT SDDMM."""
     rowptr, colind = _csr(rowptr, colind)
     M = rowptr.size - 1
     X = np.ascontiguousarray(X, np.float32)

@@ -111,7 +111,7 @@ def test_sddmm_oracles_agree(oracle):
     o64, ab = oracle.sddmm_f64(a.rowptr, a.colind, X, Y, aval=a.val)
     o32 = oracle.sddmm_f32_lanes(a.rowptr, a.colind, X, Y, aval=a.val)
     assert oracle.scaled_err(o32, o64, ab).max() < 1e-5
-    for K in (40, 3, 130):  # the GPU kernel's order: group sizes 16, 1 and 32 lanes
+    for K in (40, 3, 130, 600):  # the GPU kernel's order: group sizes 4, 1, 16 and 32 lanes
         Xk, Yk = S.dense_normal((64, K), 10 + K), S.dense_normal((48, K), 20 + K)
         r64, rab = oracle.sddmm_f64(a.rowptr, a.colind, Xk, Yk, aval=a.val)
         og = oracle.sddmm_f32_group(a.rowptr, a.colind, Xk, Yk, aval=a.val)
