@@ -370,7 +370,7 @@ bool spmm_variant_supported(int dtype, int variant, int N, long ldb, long ldc, c
     const int E = v.vb / esz;  // nnz-split
     if (v.unroll == kSmallChunk && N > kSmallChunkMaxN) return false;
     return N % E == 0 && ldb % E == 0 && pb % (E * esz) == 0 &&
-           ceil_div(N, E * v.group * v.cpl) <= 65535;
+           ceil_div(N, E * v.group * v.cpl) <= 65535 && ceil_div(N, 32) <= 65535;
 }
 
 as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cudaStream_t s) {

@@ -8,9 +8,9 @@
 //   SDMM.cpp:90-114). A row that crosses a chunk boundary leaves its segment's partial sum in
 //   a carry slot: slot 0 when the segment starts the chunk, slot 1 otherwise.
 // Pass 2 (spmm_nnz_fixup): for every row that ends inside chunk c after starting in an earlier
-//   chunk, the group of chunk c adds that row's partial sums in chunk order (then beta * C):
-//   a fixed order, so the result is deterministic run to run (not bit-identical to a single
-//   chain for those rows).
+//   chunk, a CTA of chunk c adds that row's partial sums (8 runs of chunks, then the runs in
+//   order; then beta * C): a fixed order, so the result is deterministic run to run (not
+//   bit-identical to a single chain for those rows).
 // Pass 3 (spmm_empty_rows): rows without entries get beta * C (zeros when beta == 0).
 #include "common.cuh"
 #include "internal.h"
@@ -169,10 +169,16 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
     }
 }
 
-// Rows that end in chunk c after starting in an earlier chunk: sum the partials in order.
+// Rows that end in chunk c after starting in an earlier chunk: sum their partials. A CTA
+// takes one such chunk and 32 columns (lane = column); its 8 warps split the row's chunks
+// into 8 consecutive runs, each summed in chunk order with 8 loads in flight, and warp 0
+// adds the 8 run sums in warp order -- a fixed order, so the result is deterministic. (One
+// row of a power-law graph can span thousands of chunks; a single chain over them was the
+// fix-up's bottleneck.)
 __global__ void __launch_bounds__(kThreads)
 spmm_nnz_fixup(int M, int N, int nnz, int CH, const int *__restrict__ rowptr,
                const float *__restrict__ carry, float *__restrict__ C, long ldc, float beta) {
+    __shared__ float part[kThreads / 32][32];
     const long chunk = blockIdx.x;
     const long e0l = chunk * CH;
     if (e0l >= nnz) return;
@@ -180,15 +186,35 @@ spmm_nnz_fixup(int M, int N, int nnz, int CH, const int *__restrict__ rowptr,
     const int e1 = static_cast<int>(e0l + CH < nnz ? e0l + CH : nnz);
     const int r = find_row(rowptr, M, e0);
     const int rs = __ldg(rowptr + r), re = __ldg(rowptr + r + 1);
-    if (!(rs < e0 && re <= e1 && re > e0)) return;
+    if (!(rs < e0 && re <= e1 && re > e0)) return;  // the same for the whole CTA
     const long c_first = rs / CH;
-    for (int col = blockIdx.y * kThreads + threadIdx.x; col < N; col += gridDim.y * kThreads) {
-        float acc = 0.0f;
-        for (long cc = c_first; cc <= chunk; ++cc) {
-            const int slot = (cc == c_first && static_cast<long>(rs) != cc * CH) ? 1 : 0;
-            acc += carry[(2 * cc + slot) * static_cast<long>(N) + col];
+    const long n = chunk - c_first + 1;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int col = blockIdx.y * 32 + lane;
+    const long b0 = c_first + n * warp / (kThreads / 32), b1 = c_first + n * (warp + 1) / (kThreads / 32);
+    float acc = 0.0f;
+    if (col < N) {
+        auto slot_of = [&](long cc) {
+            return (cc == c_first && static_cast<long>(rs) != cc * CH) ? 1 : 0;
+        };
+        long cc = b0;
+        for (; cc + 8 <= b1; cc += 8) {
+            float v[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                v[i] = carry[(2 * (cc + i) + slot_of(cc + i)) * static_cast<long>(N) + col];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) acc += v[i];
         }
-        C[r * ldc + col] = beta == 0.0f ? acc : fmaf(beta, C[r * ldc + col], acc);
+        for (; cc < b1; ++cc) acc += carry[(2 * cc + slot_of(cc)) * static_cast<long>(N) + col];
+    }
+    part[warp][lane] = acc;
+    __syncthreads();
+    if (warp == 0 && col < N) {
+        float t = part[0][lane];
+#pragma unroll
+        for (int w = 1; w < kThreads / 32; ++w) t += part[w][lane];
+        C[r * ldc + col] = beta == 0.0f ? t : fmaf(beta, C[r * ldc + col], t);
     }
 }
 
@@ -209,7 +235,8 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, cudaStream_t s) {
     const int esz = sizeof(T);
     if ((a.N % E) || (a.ldb % E) || (reinterpret_cast<uintptr_t>(a.B) % (E * esz)))
         return fail(AS_ERR_UNSUPPORTED, "spmm nnz-split: layout does not fit the vector width");
-    if (ceil_div(a.N, TILE) > 65535) return fail(AS_ERR_UNSUPPORTED, "spmm nnz-split: N too large");
+    if (ceil_div(a.N, TILE) > 65535 || ceil_div(a.N, 32) > 65535)
+        return fail(AS_ERR_UNSUPPORTED, "spmm nnz-split: N too large");
     const long nchunks = ceil_div(a.nnz, CH);
     void *w = nullptr;
     as_status st = scratch(ctx, sizeof(float) * static_cast<size_t>(2 * nchunks) * a.N, &w);
@@ -221,8 +248,7 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, cudaStream_t s) {
         spmm_nnzsplit<T, VB, G, CPL, U><<<g1, kThreads, 0, s>>>(
             a.M, a.K, a.N, a.nnz, CH, a.rowptr, a.colind, static_cast<const T *>(a.val),
             static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, carry, a.status);
-        dim3 g2(static_cast<unsigned>(nchunks),
-                static_cast<unsigned>(ceil_div(a.N, kThreads) < 64 ? ceil_div(a.N, kThreads) : 64));
+        dim3 g2(static_cast<unsigned>(nchunks), static_cast<unsigned>(ceil_div(a.N, 32)));
         spmm_nnz_fixup<<<g2, kThreads, 0, s>>>(a.M, a.N, a.nnz, CH, a.rowptr, carry, a.C, a.ldc,
                                                a.beta);
         ctx->launches += 2;
