@@ -170,7 +170,7 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
 }
 
 // Rows that end in chunk c after starting in an earlier chunk: sum their partials. A CTA
-// takes one such chunk and 32 columns (lane = column); its 8 warps split the row's chunks
+// takes one such chunk, 32 columns at a time (lane = column); its 8 warps split the row's chunks
 // into 8 consecutive runs, each summed in chunk order with 8 loads in flight, and warp 0
 // adds the 8 run sums in warp order -- a fixed order, so the result is deterministic. (One
 // row of a power-law graph can span thousands of chunks; a single chain over them was the
@@ -190,8 +190,9 @@ spmm_nnz_fixup(int M, int N, int nnz, int CH, const int *__restrict__ rowptr,
     const long c_first = rs / CH;
     const long n = chunk - c_first + 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int col = blockIdx.y * 32 + lane;
     const long b0 = c_first + n * warp / (kThreads / 32), b1 = c_first + n * (warp + 1) / (kThreads / 32);
+    for (int col0 = 0; col0 < N; col0 += 32) {  // 32-column tiles
+    const int col = col0 + lane;
     float acc = 0.0f;
     if (col < N) {
         auto slot_of = [&](long cc) {
@@ -215,6 +216,8 @@ spmm_nnz_fixup(int M, int N, int nnz, int CH, const int *__restrict__ rowptr,
 #pragma unroll
         for (int w = 1; w < kThreads / 32; ++w) t += part[w][lane];
         C[r * ldc + col] = beta == 0.0f ? t : fmaf(beta, C[r * ldc + col], t);
+    }
+    __syncthreads();  // part[] is reused by the next tile
     }
 }
 
@@ -248,7 +251,7 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, cudaStream_t s) {
         spmm_nnzsplit<T, VB, G, CPL, U><<<g1, kThreads, 0, s>>>(
             a.M, a.K, a.N, a.nnz, CH, a.rowptr, a.colind, static_cast<const T *>(a.val),
             static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, carry, a.status);
-        dim3 g2(static_cast<unsigned>(nchunks), static_cast<unsigned>(ceil_div(a.N, 32)));
+        dim3 g2(static_cast<unsigned>(nchunks));
         spmm_nnz_fixup<<<g2, kThreads, 0, s>>>(a.M, a.N, a.nnz, CH, a.rowptr, carry, a.C, a.ldc,
                                                a.beta);
         ctx->launches += 2;
