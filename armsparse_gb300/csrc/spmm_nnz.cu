@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(kThreads)
 spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowptr,
               const int *__restrict__ colind, const T *__restrict__ val,
               const T *__restrict__ B, long ldb, float *__restrict__ C, long ldc, float beta,
-              float *__restrict__ carry, unsigned *status) {
+              float *__restrict__ carry, int *__restrict__ fix, unsigned *status) {
     using V = Vec<T, VB>;
     constexpr int E = V::E;
     constexpr int TILE = GROUP * E * CPL;
@@ -54,6 +54,7 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
     const int tile0 = blockIdx.y * TILE;
     int r = find_row(rowptr, M, e0);
     int e = e0;
+    int fix_row = -1;  // the row that started in an earlier chunk and ends in this one
     while (e < e1 && r < M) {
         const int rs = __ldg(rowptr + r), re = __ldg(rowptr + r + 1);
         if (re <= e || rs > e) {  // empty row before e, or malformed pointers
@@ -66,6 +67,7 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
         }
         const int se = re < e1 ? re : e1;
         const bool split = rs < e0 || re > e1;
+        if (rs < e0 && re <= e1) fix_row = r;
         float acc[CPL][E];
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {
@@ -167,6 +169,7 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
         e = se;
         ++r;
     }
+    if (blockIdx.y == 0 && g == 0) fix[chunk] = fix_row;
 }
 
 // Rows that end in chunk c after starting in an earlier chunk: sum their partials. A CTA
@@ -177,16 +180,13 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
 // fix-up's bottleneck.)
 __global__ void __launch_bounds__(kThreads)
 spmm_nnz_fixup(int M, int N, int nnz, int CH, const int *__restrict__ rowptr,
-               const float *__restrict__ carry, float *__restrict__ C, long ldc, float beta) {
+               const float *__restrict__ carry, const int *__restrict__ fix,
+               float *__restrict__ C, long ldc, float beta) {
     __shared__ float part[kThreads / 32][32];
     const long chunk = blockIdx.x;
-    const long e0l = chunk * CH;
-    if (e0l >= nnz) return;
-    const int e0 = static_cast<int>(e0l);
-    const int e1 = static_cast<int>(e0l + CH < nnz ? e0l + CH : nnz);
-    const int r = find_row(rowptr, M, e0);
-    const int rs = __ldg(rowptr + r), re = __ldg(rowptr + r + 1);
-    if (!(rs < e0 && re <= e1 && re > e0)) return;  // the same for the whole CTA
+    const int r = fix[chunk];  // recorded by the first pass; -1: nothing ends here
+    if (r < 0 || r >= M) return;  // the same for the whole CTA
+    const int rs = __ldg(rowptr + r);
     const long c_first = rs / CH;
     const long n = chunk - c_first + 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -242,18 +242,20 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, cudaStream_t s) {
         return fail(AS_ERR_UNSUPPORTED, "spmm nnz-split: N too large");
     const long nchunks = ceil_div(a.nnz, CH);
     void *w = nullptr;
-    as_status st = scratch(ctx, sizeof(float) * static_cast<size_t>(2 * nchunks) * a.N, &w);
+    const size_t carry_bytes = (sizeof(float) * static_cast<size_t>(2 * nchunks) * a.N + 255) & ~size_t(255);
+    as_status st = scratch(ctx, carry_bytes + sizeof(int) * static_cast<size_t>(nchunks), &w);
     if (st != AS_OK) return st;
     float *carry = static_cast<float *>(w);
+    int *fix = reinterpret_cast<int *>(static_cast<char *>(w) + carry_bytes);
     if (nchunks > 0) {
         dim3 g1(static_cast<unsigned>(ceil_div(nchunks, kThreads / G)),
                 static_cast<unsigned>(ceil_div(a.N, TILE)));
         spmm_nnzsplit<T, VB, G, CPL, U><<<g1, kThreads, 0, s>>>(
             a.M, a.K, a.N, a.nnz, CH, a.rowptr, a.colind, static_cast<const T *>(a.val),
-            static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, carry, a.status);
+            static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, carry, fix, a.status);
         dim3 g2(static_cast<unsigned>(nchunks));
-        spmm_nnz_fixup<<<g2, kThreads, 0, s>>>(a.M, a.N, a.nnz, CH, a.rowptr, carry, a.C, a.ldc,
-                                               a.beta);
+        spmm_nnz_fixup<<<g2, kThreads, 0, s>>>(a.M, a.N, a.nnz, CH, a.rowptr, carry, fix, a.C,
+                                               a.ldc, a.beta);
         ctx->launches += 2;
     }
     spmm_empty_rows<<<static_cast<unsigned>(ceil_div(a.M, kThreads / 32)), kThreads, 0, s>>>(
