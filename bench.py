@@ -377,8 +377,8 @@ class SddmmF32(SddmmTc):
     name = "sddmm_f32"
     metric = "SDDMM GB/s (algorithmic bytes), FP32 CUDA-core path"
     dtype = "f32"
-    kernel = "sddmm_f32_lane"
-    profile = "sddmm_f32_lane_4096x4096x4096_d01"
+    kernel = "sddmm_group (a lane group per edge)"
+    profile = "sddmm_group_f32_4096x4096x4096_d01"
     bound = "hbm"
     tensor_cores = False
 
