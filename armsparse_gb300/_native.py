@@ -31,6 +31,10 @@ SIGNATURES = {
     "as_csr_validate": (_I, [_P, _I, _I, _I, _P, _P, _I, _P]),
     "as_spmm_csr_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _F, _I, _P]),
     "as_spmm_csr_bf16": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _F, _I, _P]),
+    "as_spmm_sddmm_csr_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _F, _P, _L,
+                                  _P, _P, _I, _P]),
+    "as_spmm_sddmm_csr_bf16": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _F, _P, _L,
+                                   _P, _P, _I, _P]),
     "as_spmm_csr_reduce_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _I, _P]),
     "as_spgemm_csr_dense_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _I, _P, _P, _P, _P, _L, _F,
                                      _P]),
@@ -48,6 +52,7 @@ SIGNATURES = {
     "as_sddmm_bf16x3_variant_count": (_I, []),
     "as_sddmm_coo_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P, _P]),
     "as_csr2csc": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
+    "as_csr2csc_perm": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _P]),
     "as_spmm_csr_f64": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, ctypes.c_double, _P]),
     "as_sddmm_csr_f64": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P, _P]),
     "as_f32_to_bf16": (_I, [_P, _L, _P, _P, _P]),

@@ -152,6 +152,8 @@ as_status as_ctx_sync_status(as_ctx *c, void *stream) {
     if (h & kFlagLongList)
         return fail(AS_ERR_CUDA, "SpMM long-row list found non-empty at the start of a call "
                                  "(an earlier call on this context failed part-way)");
+    if (h & kFlagBadPerm)
+        return fail(AS_ERR_INVALID_VALUE, "permutation entry out of range seen on the device");
     if (h & (kFlagBadRowptr | kFlagBadColind))
         return fail(AS_ERR_INVALID_CSR,
                     (h & kFlagBadRowptr) ? "malformed rowptr seen on the device"
@@ -217,6 +219,56 @@ as_status as_spmm_csr_bf16(as_ctx *c, int M, int K, int N, int nnz, const int *r
                            void *stream) {
     return spmm_common("as_spmm_csr_bf16", 1, c, M, K, N, nnz, rowptr, colind, val, B, ldb, C,
                        ldc, beta, variant, stream);
+}
+
+static as_status spmm_sddmm_common(const char *fn, int dtype, as_ctx *c, int M, int K, int N,
+                                   int nnz, const int *rowptr, const int *colind,
+                                   const void *val, const void *B, long ldb, float *C, long ldc,
+                                   float beta, const void *F, long ldf, const int *perm,
+                                   float *dA, int variant, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": ctx is NULL");
+    as_status st = check_csr_args(fn, M, K, nnz, rowptr, colind, val, true);
+    if (st != AS_OK) return st;
+    if (N < 0) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": negative N");
+    if (M == 0) return AS_OK;
+    if (N == 0) {  // empty dot products
+        if (nnz > 0 && !dA) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": dA is NULL");
+        if (nnz == 0) return AS_OK;
+        if (perm)
+            return fail(AS_ERR_UNSUPPORTED, std::string(fn) + ": N = 0 with a permutation");
+        DeviceGuard g(c->device);
+        return check_cuda(cudaMemsetAsync(dA, 0, sizeof(float) * static_cast<size_t>(nnz),
+                                          static_cast<cudaStream_t>(stream)),
+                          fn);
+    }
+    if (!C) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": C is NULL");
+    if (nnz > 0 && (!B || !F || !dA))
+        return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": B, F or dA is NULL");
+    if (ldb < N || ldc < N || ldf < N)
+        return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": leading dimension below N");
+    if (variant < 0 || variant > spmm_variant_count(dtype))
+        return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": unknown variant");
+    DeviceGuard g(c->device);
+    SpmmArgs a{M, K, N, nnz, rowptr, colind, val, B, ldb, C, ldc, beta, c->d_status};
+    SddmmFuse f{F, ldf, perm, dA};
+    return spmm_sddmm_launch(c, dtype, variant, a, f, static_cast<cudaStream_t>(stream));
+}
+
+as_status as_spmm_sddmm_csr_f32(as_ctx *c, int M, int K, int N, int nnz, const int *rowptr,
+                                const int *colind, const float *val, const float *B, long ldb,
+                                float *C, long ldc, float beta, const float *F, long ldf,
+                                const int *perm, float *dA, int variant, void *stream) {
+    return spmm_sddmm_common("as_spmm_sddmm_csr_f32", 0, c, M, K, N, nnz, rowptr, colind, val,
+                             B, ldb, C, ldc, beta, F, ldf, perm, dA, variant, stream);
+}
+
+as_status as_spmm_sddmm_csr_bf16(as_ctx *c, int M, int K, int N, int nnz, const int *rowptr,
+                                 const int *colind, const uint16_t *val, const uint16_t *B,
+                                 long ldb, float *C, long ldc, float beta, const uint16_t *F,
+                                 long ldf, const int *perm, float *dA, int variant,
+                                 void *stream) {
+    return spmm_sddmm_common("as_spmm_sddmm_csr_bf16", 1, c, M, K, N, nnz, rowptr, colind, val,
+                             B, ldb, C, ldc, beta, F, ldf, perm, dA, variant, stream);
 }
 
 as_status as_spmm_csr_reduce_f32(as_ctx *c, int M, int K, int N, int nnz, const int *rowptr,
@@ -397,6 +449,22 @@ as_status as_csr2csc(as_ctx *c, int M, int N, int nnz, const int *rowptr, const 
     if (st != AS_OK) return st;
     return csr2csc_launch(c, M, N, nnz, rowptr, colind, val, colptr, rowind, cscval, w,
                           static_cast<cudaStream_t>(stream));
+}
+
+as_status as_csr2csc_perm(as_ctx *c, int M, int N, int nnz, const int *rowptr,
+                          const int *colind, int *colptr, int *rowind, int *perm, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_csr2csc_perm: ctx is NULL");
+    as_status st = check_csr_args("as_csr2csc_perm", M, N, nnz, rowptr, colind, nullptr, false);
+    if (st != AS_OK) return st;
+    if (!colptr) return fail(AS_ERR_INVALID_VALUE, "as_csr2csc_perm: colptr is NULL");
+    if (nnz > 0 && (!rowind || !perm))
+        return fail(AS_ERR_INVALID_VALUE, "as_csr2csc_perm: rowind or perm is NULL");
+    DeviceGuard g(c->device);
+    void *w = nullptr;
+    st = scratch(c, csr2csc_scratch_bytes(nnz, N, true), &w);
+    if (st != AS_OK) return st;
+    return csr2csc_launch(c, M, N, nnz, rowptr, colind, nullptr, colptr, rowind, nullptr, w,
+                          static_cast<cudaStream_t>(stream), perm);
 }
 
 as_status as_spmm_csr_f64(as_ctx *c, int M, int K, int N, int nnz, const int *rowptr,

@@ -15,6 +15,7 @@ enum : unsigned {
     kFlagBadColind = 2u,
     kFlagTimeout = 4u,
     kFlagLongList = 8u,  // the long-row list was not empty at the start of a call (internal)
+    kFlagBadPerm = 16u,  // a permutation entry out of [0, nnz) (the write was skipped)
 };
 
 __device__ __forceinline__ void flag(unsigned *status, unsigned bit) {

@@ -45,10 +45,23 @@ struct SpmmArgs {
     float beta;
     unsigned *status;
 };
+// The SDDMM fused into an nnz-split SpMM pass: dA[perm ? perm[e] : e] = <B[k, :], F[r, :]> for
+// each entry e (row r, column k) of A; F is M x N (leading dimension ldf, A's value type).
+struct SddmmFuse {
+    const void *F;
+    long ldf;
+    const int *perm;
+    float *dA;
+};
 as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cudaStream_t s);
+// C = A*B + beta*C with the fused SDDMM; variant 0 picks an nnz-split variant whose column tile
+// covers N. AS_ERR_UNSUPPORTED when the variant is not nnz-split or its tile is narrower than N.
+as_status spmm_sddmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a,
+                            const SddmmFuse &f, cudaStream_t s);
 as_status spmm_reduce_launch(as_ctx *ctx, int op, const SpmmArgs &a, cudaStream_t s);
 as_status spmm_nnz_launch(as_ctx *ctx, int dtype, int vb, int group, int cpl, int chunk,
-                          int unroll, const SpmmArgs &a, cudaStream_t s);
+                          int unroll, const SpmmArgs &a, cudaStream_t s,
+                          const SddmmFuse *fuse = nullptr);
 as_status spmm_bulk_launch(as_ctx *ctx, int dtype, int lane_bytes, int stages, const SpmmArgs &a,
                            cudaStream_t s);
 // Long rows of the row-split kernels: the cp.async size (16 or 4 bytes) the layout allows,
@@ -95,11 +108,13 @@ as_status sddmm_f64_launch(as_ctx *ctx, int M, int N, int K, int nnz, const int 
                            const int *colind, const double *aval, const double *X, long ldx,
                            const double *Y, long ldy, double *out, cudaStream_t s);
 
-// Transpose; `work` is caller-provided scratch of csr2csc_scratch_bytes(nnz, N) bytes.
+// Transpose; `work` is caller-provided scratch of csr2csc_scratch_bytes(nnz, N) bytes (with_val
+// also when perm is given). perm (optional): the CSR position of each CSC entry, written in
+// place of the values (val and cscval are then ignored).
 size_t csr2csc_scratch_bytes(int nnz, int N, bool with_val);
 as_status csr2csc_launch(as_ctx *ctx, int M, int N, int nnz, const int *rowptr,
                          const int *colind, const float *val, int *colptr, int *rowind,
-                         float *cscval, void *work, cudaStream_t s);
+                         float *cscval, void *work, cudaStream_t s, int *perm = nullptr);
 
 as_status csr_validate_launch(as_ctx *ctx, int n_rows, int n_cols, int nnz, const int *rowptr,
                               const int *colind, int require_sorted, unsigned *result,

@@ -422,4 +422,40 @@ as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cu
     return st;
 }
 
+// The SpMM with the SDDMM fused in (spmm_nnz.cu): nnz-split variants only, one column tile.
+// Library choice: the narrowest full-warp tile that covers N (chunks of 1024 entries, four
+// entries per load batch -- the variants the autotuner picks for the power-law GCN layers).
+as_status spmm_sddmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a,
+                            const SddmmFuse &f, cudaStream_t s) {
+    const int esz = dtype == 0 ? 4 : 2;
+    const Variant *t = dtype == 0 ? kF32 : kBF16;
+    const int n = spmm_variant_count(dtype);
+    auto tile = [&](const Variant &v) { return (v.vb / esz) * v.group * v.cpl; };
+    if (variant == 0) {
+        const int picks[][3] = {{4, 32, 1}, {16, 32, 1}, {16, 32, 2}};  // vb, group, cpl
+        for (const auto &pk : picks) {
+            for (int i = 0; i < n && variant == 0; ++i)
+                if (t[i].kind == 2 && t[i].vb == pk[0] && t[i].group == pk[1] &&
+                    t[i].cpl == pk[2] && t[i].unroll == 1024 && t[i].steps == 4 &&
+                    tile(t[i]) >= a.N &&
+                    spmm_variant_supported(dtype, i + 1, a.N, a.ldb, a.ldc, a.B, a.C))
+                    variant = i + 1;
+            if (variant) break;
+        }
+        if (variant == 0)
+            return fail(AS_ERR_UNSUPPORTED, "spmm+sddmm: no variant covers this N and layout");
+    }
+    const Variant &v = t[variant - 1];
+    if (v.kind != 2)
+        return fail(AS_ERR_UNSUPPORTED, std::string("spmm+sddmm: variant ") + v.name +
+                                            " is not an nnz-split variant");
+    if (tile(v) < a.N)
+        return fail(AS_ERR_UNSUPPORTED, std::string("spmm+sddmm: variant ") + v.name +
+                                            " covers fewer than N columns");
+    if (v.unroll == kSmallChunk && a.N > kSmallChunkMaxN)
+        return fail(AS_ERR_UNSUPPORTED, std::string("spmm+sddmm: variant ") + v.name +
+                                            " serves N <= 64 only");
+    return spmm_nnz_launch(ctx, dtype, v.vb, v.group, v.cpl, v.unroll, v.steps, a, s, &f);
+}
+
 }  // namespace as

@@ -12,6 +12,16 @@
 //   order; then beta * C): a fixed order, so the result is deterministic run to run (not
 //   bit-identical to a single chain for those rows).
 // Pass 3 (spmm_empty_rows): rows without entries get beta * C (zeros when beta == 0).
+//
+// Fused form (FUSE): pass 1 also computes, for every entry e (row r, column k), the dot product
+// dA[perm[e]] = <B[k, :], F[r, :]> from the B row it has just loaded for the SpMM and F's row r
+// (loaded once per row segment): the SDDMM that the backward of out = A^T-free SpMM with
+// trainable values needs, without a second gather of B. Each lane chains over its own
+// columns of the row (its E-element slices j = 0..CPL-1, in order), then the GROUP lanes are
+// summed by a butterfly (lane l adds lane l ^ off, off = GROUP/2 .. 1) -- for a step of U
+// entries the butterflies of all U run interleaved (each lane hands half of its values to its
+// partner at the first log2(U) steps), which pairs the same lanes in the same order, so each
+// dot product is the single-entry butterfly's bit for bit. One column tile only (TILE >= N).
 #include "common.cuh"
 #include "internal.h"
 #include "spmm_vec.cuh"
@@ -33,12 +43,63 @@ __device__ __forceinline__ int find_row(const int *__restrict__ rowptr, int M, i
     return lo;
 }
 
-template <typename T, int VB, int GROUP, int CPL, int U>
+// Sum of each of the U values d[0..U) over the GROUP lanes of a group (U <= GROUP, both powers
+// of two). While a lane holds more than one value, it keeps one half and sends the other to its
+// partner lane ^ off; then plain butterfly steps. Lane g ends with the total of value
+// g / (GROUP / U); the pairing tree is the single-value butterfly's.
+template <int U, int GROUP>
+__device__ __forceinline__ float reduce_entries(float (&d)[U], unsigned gmask, int g) {
+    static_assert(U <= GROUP && (U & (U - 1)) == 0 && (GROUP & (GROUP - 1)) == 0, "shape");
+#pragma unroll
+    for (int h = U / 2, off = GROUP / 2; h >= 1; h >>= 1, off >>= 1) {
+        const bool up = (g & off) != 0;
+#pragma unroll
+        for (int i = 0; i < h; ++i) {
+            const float send = up ? d[i] : d[i + h];
+            const float keep = up ? d[i + h] : d[i];
+            d[i] = keep + __shfl_xor_sync(gmask, send, off, GROUP);
+        }
+    }
+#pragma unroll
+    for (int off = GROUP / (2 * U); off >= 1; off >>= 1)
+        d[0] += __shfl_xor_sync(gmask, d[0], off, GROUP);
+    return d[0];
+}
+
+// dA[perm[e]] (dA[e] without perm) = v, skipping and flagging a position outside [0, nnz).
+__device__ __forceinline__ void store_dot(int e, float v, int nnz, const int *__restrict__ perm,
+                                          float *__restrict__ dA, unsigned *status) {
+    const int p = perm ? __ldg(perm + e) : e;
+    if (static_cast<unsigned>(p) < static_cast<unsigned>(nnz))
+        dA[p] = v;
+    else
+        flag(status, kFlagBadPerm);
+}
+
+// The U dot products of a step (entries e0 .. e0 + U - 1) reduced over the group and stored
+// at their CSR positions; an entry with an out-of-range column (kk < 0, already flagged) is
+// left unwritten.
+template <int U, int GROUP>
+__device__ __forceinline__ void write_dots(float (&d)[U], const int (&kk)[U], unsigned gmask,
+                                           int g, int e0, int nnz, const int *__restrict__ perm,
+                                           float *__restrict__ dA, unsigned *status) {
+    unsigned ok = 0;
+#pragma unroll
+    for (int u = 0; u < U; ++u) ok |= (kk[u] >= 0 ? 1u : 0u) << u;
+    const float sum = reduce_entries<U, GROUP>(d, gmask, g);
+    constexpr int SUB = GROUP / U;
+    const int u = g / SUB;
+    if (g % SUB == 0 && ((ok >> u) & 1u)) store_dot(e0 + u, sum, nnz, perm, dA, status);
+}
+
+template <typename T, int VB, int GROUP, int CPL, int U, bool FUSE>
 __global__ void __launch_bounds__(kThreads)
 spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowptr,
               const int *__restrict__ colind, const T *__restrict__ val,
               const T *__restrict__ B, long ldb, float *__restrict__ C, long ldc, float beta,
-              float *__restrict__ carry, int *__restrict__ fix, unsigned *status) {
+              float *__restrict__ carry, int *__restrict__ fix, unsigned *status,
+              const T *__restrict__ F, long ldf, const int *__restrict__ perm,
+              float *__restrict__ dA) {
     using V = Vec<T, VB>;
     constexpr int E = V::E;
     constexpr int TILE = GROUP * E * CPL;
@@ -68,6 +129,14 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
         const int se = re < e1 ? re : e1;
         const bool split = rs < e0 || re > e1;
         if (rs < e0 && re <= e1) fix_row = r;
+        typename V::Raw fr[CPL];  // FUSE: this row's slices of F
+        if constexpr (FUSE) {
+#pragma unroll
+            for (int j = 0; j < CPL; ++j) {
+                const int cc = tile0 + (j * GROUP + g) * E;
+                fr[j] = V::raw(F + static_cast<long>(r) * ldf + (cc < N ? cc : 0));
+            }
+        }
         float acc[CPL][E];
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {
@@ -121,6 +190,20 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
                         if (kk[u] >= 0)
 #pragma unroll
                             for (int j = 0; j < CPL; ++j) fma_vec_f32<E>(b[u][j], vv[u], acc[j]);
+                    if constexpr (FUSE) {
+                        float d[U];
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            d[u] = 0.0f;
+#pragma unroll
+                            for (int j = 0; j < CPL; ++j)
+                                if (tile0 + (j * GROUP + g) * E < N)
+#pragma unroll
+                                    for (int i = 0; i < E; ++i)
+                                        d[u] = fmaf(b[u][j][i], V::at(fr[j], i), d[u]);
+                        }
+                        write_dots<U, GROUP>(d, kk, gmask, g, base + t, nnz, perm, dA, status);
+                    }
                 } else {
                     typename V::Raw b[U][CPL];
 #pragma unroll
@@ -139,12 +222,27 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
 #pragma unroll
                         for (int j = 0; j < CPL; ++j) V::fma(b[u][j], vu, acc[j]);
                     }
+                    if constexpr (FUSE) {
+                        float d[U];
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            d[u] = 0.0f;
+#pragma unroll
+                            for (int j = 0; j < CPL; ++j)
+                                if (tile0 + (j * GROUP + g) * E < N)
+#pragma unroll
+                                    for (int i = 0; i < E; ++i)
+                                        d[u] = fmaf(V::at(b[u][j], i), V::at(fr[j], i), d[u]);
+                        }
+                        write_dots<U, GROUP>(d, kk, gmask, g, base + t, nnz, perm, dA, status);
+                    }
                 }
             }
             for (; t < cnt; ++t) {
                 const int kk = __shfl_sync(gmask, k, t, GROUP);
                 const float vv = __shfl_sync(gmask, v, t, GROUP);
                 if (kk < 0) continue;
+                float d = 0.0f;
 #pragma unroll
                 for (int j = 0; j < CPL; ++j) {
                     const int cc = tile0 + (j * GROUP + g) * E;
@@ -153,7 +251,17 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
                         V::load(B + static_cast<long>(kk) * ldb + cc, b);
 #pragma unroll
                         for (int i = 0; i < E; ++i) acc[j][i] = fmaf(b[i], vv, acc[j][i]);
+                        if constexpr (FUSE) {
+#pragma unroll
+                            for (int i = 0; i < E; ++i) d = fmaf(b[i], V::at(fr[j], i), d);
+                        }
                     }
+                }
+                if constexpr (FUSE) {
+#pragma unroll
+                    for (int off = GROUP / 2; off >= 1; off >>= 1)
+                        d += __shfl_xor_sync(gmask, d, off, GROUP);
+                    if (g == 0) store_dot(base + t, d, nnz, perm, dA, status);
                 }
             }
         }
@@ -231,8 +339,8 @@ spmm_empty_rows(int M, int N, const int *__restrict__ rowptr, float *__restrict_
         C[r * ldc + col] = beta == 0.0f ? 0.0f : beta * C[r * ldc + col];
 }
 
-template <typename T, int VB, int G, int CPL, int U>
-as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, cudaStream_t s) {
+template <typename T, int VB, int G, int CPL, int U, bool FUSE>
+as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, const SddmmFuse *fu, cudaStream_t s) {
     constexpr int E = Vec<T, VB>::E;
     constexpr int TILE = G * E * CPL;
     const int esz = sizeof(T);
@@ -240,6 +348,9 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, cudaStream_t s) {
         return fail(AS_ERR_UNSUPPORTED, "spmm nnz-split: layout does not fit the vector width");
     if (ceil_div(a.N, TILE) > 65535 || ceil_div(a.N, 32) > 65535)
         return fail(AS_ERR_UNSUPPORTED, "spmm nnz-split: N too large");
+    if (FUSE && (a.N > TILE || (fu->ldf % E) || (reinterpret_cast<uintptr_t>(fu->F) % (E * esz))))
+        return fail(AS_ERR_UNSUPPORTED,
+                    "spmm+sddmm: the variant's column tile must cover N, F aligned to its vectors");
     const long nchunks = ceil_div(a.nnz, CH);
     void *w = nullptr;
     const size_t carry_bytes = (sizeof(float) * static_cast<size_t>(2 * nchunks) * a.N + 255) & ~size_t(255);
@@ -250,9 +361,11 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, cudaStream_t s) {
     if (nchunks > 0) {
         dim3 g1(static_cast<unsigned>(ceil_div(nchunks, kThreads / G)),
                 static_cast<unsigned>(ceil_div(a.N, TILE)));
-        spmm_nnzsplit<T, VB, G, CPL, U><<<g1, kThreads, 0, s>>>(
+        spmm_nnzsplit<T, VB, G, CPL, U, FUSE><<<g1, kThreads, 0, s>>>(
             a.M, a.K, a.N, a.nnz, CH, a.rowptr, a.colind, static_cast<const T *>(a.val),
-            static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, carry, fix, a.status);
+            static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, carry, fix, a.status,
+            FUSE ? static_cast<const T *>(fu->F) : nullptr, FUSE ? fu->ldf : 0,
+            FUSE ? fu->perm : nullptr, FUSE ? fu->dA : nullptr);
         dim3 g2(static_cast<unsigned>(nchunks));
         spmm_nnz_fixup<<<g2, kThreads, 0, s>>>(a.M, a.N, a.nnz, CH, a.rowptr, carry, fix, a.C,
                                                a.ldc, a.beta);
@@ -264,14 +377,23 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, cudaStream_t s) {
     return check_cuda(cudaGetLastError(), "spmm nnz-split launch");
 }
 
+template <typename T, int VB, int G, int CPL>
+as_status launch_u(as_ctx *ctx, const SpmmArgs &a, int CH, int unroll, const SddmmFuse *fu,
+                   cudaStream_t s) {
+    if (fu)
+        return unroll == 8 ? launch<T, VB, G, CPL, 8, true>(ctx, a, CH, fu, s)
+                           : launch<T, VB, G, CPL, 4, true>(ctx, a, CH, fu, s);
+    return unroll == 8 ? launch<T, VB, G, CPL, 8, false>(ctx, a, CH, fu, s)
+                       : launch<T, VB, G, CPL, 4, false>(ctx, a, CH, fu, s);
+}
+
 }  // namespace
 
 as_status spmm_nnz_launch(as_ctx *ctx, int dtype, int vb, int group, int cpl, int chunk,
-                          int unroll, const SpmmArgs &a, cudaStream_t s) {
-#define AS_NNZ_CASE(T, VBV, G, C)                                                   \
-    if (vb == VBV && group == G && cpl == C)                                        \
-        return unroll == 8 ? launch<T, VBV, G, C, 8>(ctx, a, chunk, s)              \
-                           : launch<T, VBV, G, C, 4>(ctx, a, chunk, s);
+                          int unroll, const SpmmArgs &a, cudaStream_t s, const SddmmFuse *fuse) {
+#define AS_NNZ_CASE(T, VBV, G, C)            \
+    if (vb == VBV && group == G && cpl == C) \
+        return launch_u<T, VBV, G, C>(ctx, a, chunk, unroll, fuse, s);
     if (dtype == 0) {
         AS_NNZ_CASE(float, 16, 8, 1) AS_NNZ_CASE(float, 16, 16, 1) AS_NNZ_CASE(float, 16, 32, 1)
         AS_NNZ_CASE(float, 16, 32, 2) AS_NNZ_CASE(float, 4, 32, 1) AS_NNZ_CASE(float, 4, 32, 2)

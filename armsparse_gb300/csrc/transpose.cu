@@ -194,9 +194,9 @@ radix_histogram(const int *__restrict__ keys, int nnz, int shift, int tiles, int
 
 __global__ void __launch_bounds__(kThreads)
 radix_scatter(const int *__restrict__ keys, const int *__restrict__ rows,
-              const float *__restrict__ vals, int nnz, int shift, int tiles,
+              const unsigned *__restrict__ vals, bool iota, int nnz, int shift, int tiles,
               const int *__restrict__ offsets, int *__restrict__ okeys, int *__restrict__ orows,
-              float *__restrict__ ovals) {
+              unsigned *__restrict__ ovals) {
     static_assert(kBins == kThreads, "one digit per thread");
     __shared__ int run[kBins];            // running local slot per digit inside this tile
     __shared__ int start[kBins];          // first local slot of each digit in this tile
@@ -205,7 +205,7 @@ radix_scatter(const int *__restrict__ keys, const int *__restrict__ rows,
     __shared__ int sw[kWarps];
     __shared__ int sk[kTile];             // the tile, sorted by digit (stable)
     __shared__ int sr[kTile];
-    __shared__ float sv[kTile];
+    __shared__ unsigned sv[kTile];  // the payload: value bits or entry index
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long base = static_cast<long>(blockIdx.x) * kTile;
     const int n_tile = static_cast<int>(nnz - base < kTile ? nnz - base : kTile);
@@ -221,17 +221,20 @@ radix_scatter(const int *__restrict__ keys, const int *__restrict__ rows,
     }
     const unsigned lt_mask = (1u << lane) - 1u;
     int kr[kRounds], rr[kRounds];  // the thread's entries, loaded before the ranking rounds
-    float vr[kRounds];
+    unsigned vr[kRounds];
 #pragma unroll
     for (int i = 0; i < kRounds; ++i) {
         const int li = i * kThreads + threadIdx.x;
         kr[i] = 0;
         rr[i] = 0;
-        vr[i] = 0.0f;
+        vr[i] = 0u;
         if (li < n_tile) {
             kr[i] = keys[base + li];
             rr[i] = rows[base + li];
-            if (vals) vr[i] = vals[base + li];
+            if (vals)
+                vr[i] = vals[base + li];
+            else if (iota)
+                vr[i] = static_cast<unsigned>(base + li);  // the entry's CSR position
         }
     }
 #pragma unroll
@@ -239,7 +242,7 @@ radix_scatter(const int *__restrict__ keys, const int *__restrict__ rows,
         const int li = i * kThreads + threadIdx.x;
         const bool valid = li < n_tile;
         const int k = kr[i], r = rr[i];
-        const float v = vr[i];
+        const unsigned v = vr[i];
         const int d = valid ? static_cast<int>((static_cast<unsigned>(k) >> shift) & (kBins - 1))
                             : kBins;  // invalid lanes get a digit of their own
 #pragma unroll
@@ -277,7 +280,7 @@ radix_scatter(const int *__restrict__ keys, const int *__restrict__ rows,
         const int g = goff[d] + (p - start[d]);
         okeys[g] = k;
         orows[g] = sr[p];
-        if (vals) ovals[g] = sv[p];
+        if (ovals) ovals[g] = sv[p];
     }
 }
 
@@ -368,7 +371,7 @@ size_t csr2csc_scratch_bytes(int nnz, int N, bool with_val) {
 
 as_status csr2csc_launch(as_ctx *ctx, int M, int N, int nnz, const int *rowptr,
                          const int *colind, const float *val, int *colptr, int *rowind,
-                         float *cscval, void *work, cudaStream_t s) {
+                         float *cscval, void *work, cudaStream_t s, int *perm) {
     if (nnz == 0) {
         if (cudaMemsetAsync(colptr, 0, sizeof(int) * (static_cast<size_t>(N) + 1), s) != cudaSuccess)
             return check_cuda(cudaGetLastError(), "csr2csc memset");
@@ -376,7 +379,10 @@ as_status csr2csc_launch(as_ctx *ctx, int M, int N, int nnz, const int *rowptr,
     }
     if (M == 0) return fail(AS_ERR_INVALID_CSR, "csr2csc: nnz > 0 with zero rows");
     if (N == 0) return fail(AS_ERR_INVALID_CSR, "csr2csc: nnz > 0 with zero columns");
-    const bool wv = val != nullptr;
+    // the payload: the values' bits, or (perm given) each entry's CSR position
+    const bool wv = val != nullptr || perm != nullptr;
+    unsigned *final_v = perm ? reinterpret_cast<unsigned *>(perm)
+                             : reinterpret_cast<unsigned *>(cscval);
     const int tiles = static_cast<int>(ceil_div(nnz, kTile));
     const long hist_n = static_cast<long>(tiles) * kBins;
     char *p = static_cast<char *>(work);
@@ -385,7 +391,7 @@ as_status csr2csc_launch(as_ctx *ctx, int M, int N, int nnz, const int *rowptr,
     int *keysA = reinterpret_cast<int *>(take(sizeof(int) * static_cast<size_t>(nnz)));
     int *keysB = reinterpret_cast<int *>(take(sizeof(int) * static_cast<size_t>(nnz)));
     int *rowsT = reinterpret_cast<int *>(take(sizeof(int) * static_cast<size_t>(nnz)));
-    float *valsT = wv ? reinterpret_cast<float *>(take(sizeof(float) * static_cast<size_t>(nnz))) : nullptr;
+    unsigned *valsT = wv ? reinterpret_cast<unsigned *>(take(sizeof(unsigned) * static_cast<size_t>(nnz))) : nullptr;
     int *hist = reinterpret_cast<int *>(take(sizeof(int) * static_cast<size_t>(hist_n)));
     int *sums = reinterpret_cast<int *>(take(sizeof(int) * static_cast<size_t>(ceil_div(hist_n, kScanChunk) + 1)));
 
@@ -402,21 +408,21 @@ as_status csr2csc_launch(as_ctx *ctx, int M, int N, int nnz, const int *rowptr,
     const int passes = radix_passes(N);
     const int *src_k = colind;
     const int *src_r = rowidx;
-    const float *src_v = val;
+    const unsigned *src_v = perm ? nullptr : reinterpret_cast<const unsigned *>(val);
     for (int pass = 0; pass < passes; ++pass) {
         const bool last = pass == passes - 1;
         const bool to_scratch = ((passes - 1 - pass) & 1) != 0;
         int *dk = (pass & 1) ? keysB : keysA;
         int *dr = (last || !to_scratch) ? rowind : rowsT;
-        float *dv = wv ? ((last || !to_scratch) ? cscval : valsT) : nullptr;
+        unsigned *dv = wv ? ((last || !to_scratch) ? final_v : valsT) : nullptr;
         const int shift = 8 * pass;
         radix_histogram<<<tiles, kThreads, 0, s>>>(src_k, nnz, shift, tiles, N, hist,
                                                    ctx->d_status, pass == 0);
         ctx->launches++;
         as_status st = exclusive_scan(ctx, hist, hist, hist_n, sums, s);
         if (st != AS_OK) return st;
-        radix_scatter<<<tiles, kThreads, 0, s>>>(src_k, src_r, src_v, nnz, shift, tiles, hist,
-                                                 dk, dr, dv);
+        radix_scatter<<<tiles, kThreads, 0, s>>>(src_k, src_r, src_v, perm && pass == 0, nnz,
+                                                 shift, tiles, hist, dk, dr, dv);
         ctx->launches++;
         src_k = dk;
         src_r = dr;
@@ -527,22 +533,23 @@ cudaError_t csr2csc_static_run(int M, int N, int nnz, const int *rowptr, const i
     const int passes = radix_passes(N);
     const int *src_k = colind;
     const int *src_r = rowidx;
-    const float *src_v = val;
+    const unsigned *src_v = reinterpret_cast<const unsigned *>(val);  // value bits, moved as is
     const long nb = ceil_div(hist_n, kScanChunk);
     for (int pass = 0; pass < passes; ++pass) {
         const bool last = pass == passes - 1;
         const bool to_scratch = ((passes - 1 - pass) & 1) != 0;
         int *dk = (pass & 1) ? keysB : keysA;
         int *dr = (last || !to_scratch) ? rowind : rowsT;
-        float *dv = wv ? ((last || !to_scratch) ? cscval : valsT) : nullptr;
+        unsigned *dv = wv ? reinterpret_cast<unsigned *>((last || !to_scratch) ? cscval : valsT)
+                          : nullptr;
         const int shift = 8 * pass;
         radix_histogram<<<tiles, kThreads, 0, s>>>(src_k, nnz, shift, tiles, N, hist, status,
                                                    pass == 0);
         scan_reduce<<<static_cast<unsigned>(nb), kThreads, 0, s>>>(hist, hist_n, sums);
         scan_block_sums<<<1, kThreads, 0, s>>>(sums, static_cast<int>(nb));
         scan_downsweep<<<static_cast<unsigned>(nb), kThreads, 0, s>>>(hist, hist_n, sums, hist);
-        radix_scatter<<<tiles, kThreads, 0, s>>>(src_k, src_r, src_v, nnz, shift, tiles, hist,
-                                                 dk, dr, dv);
+        radix_scatter<<<tiles, kThreads, 0, s>>>(src_k, src_r, src_v, false, nnz, shift, tiles,
+                                                 hist, dk, dr, dv);
         src_k = dk;
         src_r = dr;
         src_v = dv;

@@ -38,25 +38,36 @@ class SPMMFunction(torch.autograd.Function):
     """out = A * feat, A given as CSR (rowptr, colind, edge_weight_csr) and as CSC (colptr, rowind,
     edge_weight_csc). Same ``apply`` signature as the reference (op.py:9), plus an optional
     ``variants`` pair (kernel variant ids for the forward CSR product and the backward CSC
-    product; 0 = library choice)."""
+    product; 0 = library choice) and an optional ``perm`` (the CSR position of each CSC entry,
+    ``Graph.perm``): given it, a backward that needs both gradients runs them in one pass over
+    the CSC (``sparse.spmm_sddmm``: dOut's rows gathered once for dB and dA)."""
 
     @staticmethod
     def forward(ctx, rowptr, colind, colptr, rowind, feat, edge_weight_csr=None,
-                edge_weight_csc=None, variants=None):
+                edge_weight_csc=None, variants=None, perm=None):
         if edge_weight_csr is None:
             raise ValueError("SPMMFunction needs edge values (pass ones for an unweighted graph)")
         fwd_v, bwd_v = variants if variants is not None else (0, 0)
         out = _spmm(rowptr, colind, edge_weight_csr, feat, fwd_v)
         ctx.save_for_backward(rowptr, colind, colptr, rowind, feat, edge_weight_csr,
-                              edge_weight_csc)
+                              edge_weight_csc, perm)
         ctx.bwd_variant = bwd_v
         return out
 
     @staticmethod
     def backward(ctx, grad_out):
-        rowptr, colind, colptr, rowind, feat, w_csr, w_csc = ctx.saved_tensors
+        rowptr, colind, colptr, rowind, feat, w_csr, w_csc, perm = ctx.saved_tensors
         grad_feat = grad_w = None
         g = grad_out.contiguous()
+        if (perm is not None and ctx.needs_input_grad[4] and ctx.needs_input_grad[5] and
+                w_csc is not None and w_csc.numel() == w_csr.numel() and g.dtype == feat.dtype
+                and g.dtype in (torch.float32, torch.bfloat16)):
+            fused = _spmm_sddmm_t(colptr, rowind, w_csc, g, feat.contiguous(), perm,
+                                  ctx.bwd_variant)
+            if fused is not None:
+                grad_feat, grad_w = fused
+                return (None, None, None, None, grad_feat, grad_w.to(w_csr.dtype), None, None,
+                        None)
         if ctx.needs_input_grad[4]:
             if w_csc is None or w_csc.numel() != w_csr.numel():
                 raise RuntimeError("backward of SPMMFunction needs the edge values in CSC order "
@@ -71,7 +82,21 @@ class SPMMFunction(torch.autograd.Function):
                 gf = g if g.dtype in (torch.float32, torch.float64) else g.float()
                 ff = feat if feat.dtype == gf.dtype else feat.to(gf.dtype)
                 grad_w = S.sddmm(rowptr, colind, gf, ff.contiguous()).to(w_csr.dtype)
-        return None, None, None, None, grad_feat, grad_w, None, None
+        return None, None, None, None, grad_feat, grad_w, None, None, None
+
+
+def _spmm_sddmm_t(colptr, rowind, w_csc, g, feat, perm, variant):
+    """(A^T g, dA) in one pass over the CSC, or None when the backward variant cannot carry
+    the SDDMM (not an nnz-split kernel, or its column tile is narrower than the width)."""
+    from ._native import NativeError
+    try:
+        C, dA = S.spmm_sddmm(colptr, rowind, w_csc.to(g.dtype), g, feat, perm=perm,
+                             variant=variant)
+    except NativeError as e:
+        if e.status != 3:  # AS_ERR_UNSUPPORTED: run the two products separately
+            raise
+        return None
+    return C.to(g.dtype), dA
 
 
 def _time_pick(rowptr, colind, values, n_in: int, width: int, dtype) -> int:
@@ -121,14 +146,25 @@ class Graph:
         self.n_rows = rowptr.numel() - 1
         self.n_cols = self.n_rows if n_cols is None else n_cols
         self._csc = None
+        self._perm = None
         self.selector = None  # a selector.Selector: per-width kernel choice (None = library choice)
         self._plans = {}
 
     @property
     def csc(self):
+        """(colptr, rowind, values in CSC order), from the transpose that also gives ``perm``."""
         if self._csc is None:
-            self._csc = S.csr2csc(self.rowptr, self.colind, self.values, self.n_cols)
+            colptr, rowind, perm = S.csr2csc_perm(self.rowptr, self.colind, self.n_cols)
+            self._perm = perm
+            self._csc = (colptr, rowind, torch.index_select(self.values, 0, perm))
         return self._csc
+
+    @property
+    def perm(self) -> torch.Tensor:
+        """The CSR position of each CSC entry (int32): ``values[perm]`` is the values in CSC
+        order for any values, and the fused backward writes the edge gradient through it."""
+        self.csc
+        return self._perm
 
     def plan(self, N: int, dtype=torch.float32):
         """(forward, backward) kernel variants for dense width N: the learned selector's pick,
@@ -156,7 +192,7 @@ class Graph:
     def aggregate(self, feat: torch.Tensor) -> torch.Tensor:
         colptr, rowind, vcsc = self.csc
         return SPMMFunction.apply(self.rowptr, self.colind, colptr, rowind, feat, self.values,
-                                  vcsc, self.plan(feat.shape[1], feat.dtype))
+                                  vcsc, self.plan(feat.shape[1], feat.dtype), self.perm)
 
 
 class _FeatureProduct(torch.autograd.Function):
@@ -305,6 +341,14 @@ class Net(torch.nn.Module):
         x = F.dropout(x, p=self.dropout, training=self.training)
         x = self.conv2(x, *args, variants=g.plan(self.conv2.out_channels, x.dtype))
         return F.log_softmax(x, dim=1)
+
+
+def nll_mean(logp: torch.Tensor, y: torch.Tensor) -> torch.Tensor:
+    """F.nll_loss(logp, y) (mean over the rows) as a gather and a mean: the same value up to
+    fp32 summation order, but both directions run as elementwise and tree-reduction kernels,
+    where torch's nll_loss reduces over all rows in one thread block (milliseconds on a
+    million-row batch)."""
+    return -logp.gather(1, y.unsqueeze(1)).mean()
 
 
 def make_optimizer(model: Net, capturable: bool = False):

@@ -330,6 +330,70 @@ def csr2csc(rowptr, colind, val, n_cols: int):
     return colptr, rowind, cscval
 
 
+def csr2csc_perm(rowptr, colind, n_cols: int):
+    """(colptr, rowind, perm): the transpose's pattern and, for each CSC entry j, its CSR
+    position perm[j] (so values in CSC order are ``val[perm]`` for any values)."""
+    dev = _dev(rowptr, colind)
+    M, nnz = _csr(rowptr, colind)
+    colptr = torch.empty(n_cols + 1, dtype=torch.int32, device=dev)
+    rowind = torch.empty(nnz, dtype=torch.int32, device=dev)
+    perm = torch.empty(nnz, dtype=torch.int32, device=dev)
+    ctx = N.context(dev.index)
+    N.check(N.load().as_csr2csc_perm(ctx.handle, M, n_cols, nnz, _ptr(rowptr), _ptr(colind),
+                                     _ptr(colptr), _ptr(rowind), _ptr(perm), _stream(dev)),
+            "as_csr2csc_perm")
+    return colptr, rowind, perm
+
+
+def spmm_sddmm(rowptr, colind, val, B, F, perm=None, C=None, beta: float = 0.0,
+               variant: int = 0, dA=None):
+    """(C, dA): C = A*B + beta*C as ``spmm`` and, in the same pass over A, the SDDMM
+    dA[perm[e]] = <B[col(e), :], F[row(e), :]> (dA[e] when perm is None) in fp32. With A the
+    CSC of a forward matrix, B = dOut, F = the forward's input and perm from
+    ``csr2csc_perm``, this is the backward of out = A_fwd * F with trainable values.
+    variant: 0 = library choice, else an nnz-split variant whose column tile covers N."""
+    dev = _dev(rowptr, colind, val, B, F, perm, C, dA)
+    M, nnz = _csr(rowptr, colind)
+    if B.dim() != 2 or F.dim() != 2 or B.stride(1) != 1 or F.stride(1) != 1:
+        raise ValueError("B and F must be 2-D row-major with unit column stride")
+    K, Ncols = B.shape
+    if F.shape != (M, Ncols):
+        raise ValueError("F must be (M, N)")
+    if val.dtype == torch.float32 and B.dtype == torch.float32 and F.dtype == torch.float32:
+        fn, dname = N.load().as_spmm_sddmm_csr_f32, "as_spmm_sddmm_csr_f32"
+    elif val.dtype == torch.bfloat16 and B.dtype == torch.bfloat16 and F.dtype == torch.bfloat16:
+        fn, dname = N.load().as_spmm_sddmm_csr_bf16, "as_spmm_sddmm_csr_bf16"
+    else:
+        raise TypeError("val, B and F must all be float32 or all bfloat16")
+    _need(val, val.dtype, "val", 1)
+    if val.numel() != nnz:
+        raise ValueError("val and colind lengths differ")
+    if perm is not None:
+        _need(perm, torch.int32, "perm", 1)
+        if perm.numel() != nnz:
+            raise ValueError("perm and colind lengths differ")
+    if C is None:
+        if beta != 0.0:
+            raise ValueError("beta != 0 needs C")
+        C = torch.empty((M, Ncols), dtype=torch.float32, device=dev)
+    elif C.dtype != torch.float32 or C.dim() != 2 or C.shape != (M, Ncols) or C.stride(1) != 1:
+        raise ValueError("C must be float32 (M, N) row-major")
+    if dA is None:
+        dA = torch.empty(nnz, dtype=torch.float32, device=dev)
+    else:
+        _need(dA, torch.float32, "dA", 1)
+        if dA.numel() != nnz:
+            raise ValueError("dA and colind lengths differ")
+    ldb = B.stride(0) if K > 1 else Ncols
+    ldc = C.stride(0) if M > 1 else Ncols
+    ldf = F.stride(0) if M > 1 else Ncols
+    ctx = N.context(dev.index)
+    N.check(fn(ctx.handle, M, K, Ncols, nnz, _ptr(rowptr), _ptr(colind), _ptr(val), _ptr(B), ldb,
+               _ptr(C), ldc, float(beta), _ptr(F), ldf, _ptr(perm), _ptr(dA), int(variant),
+               _stream(dev)), dname)
+    return C, dA
+
+
 def to_bf16(x: torch.Tensor) -> torch.Tensor:
     """fp32 -> bf16 (round to nearest even) with this library's kernel."""
     dev = _dev(x)

@@ -146,6 +146,29 @@ as_status as_sddmm_csr_bf16(as_ctx *ctx, int M, int N, int K, int nnz, const int
                             const int *colind, const float *aval, const uint16_t *X, long ldx,
                             const uint16_t *Y, long ldy, float *out, void *stream);
 
+/* ---- SpMM and SDDMM in one pass over A ---------------------------------------------------------
+ * C = A*B + beta*C (A: M x K CSR, B: K x N, C: M x N, as as_spmm_csr_*) and, for every entry e
+ * of A (row r, column k):  dA[perm ? perm[e] : e] = <B[k, :], F[r, :]>  (F: M x N, ldf >= N,
+ * same storage type as B; FP32 products and sums). No reference counterpart: it is the
+ * backward of out = A_fwd * X with trainable edge values (gcn/pytorch-custom/op.py:30 computes
+ * only the first half and returns no gradient for the values, op.py:31). Called with A = the
+ * CSC of A_fwd (colptr, rowind, values in CSC order), B = dOut, F = X and perm from
+ * as_csr2csc_perm, it gives dX = A_fwd^T * dOut and the values' gradient in CSR order, gathering
+ * dOut's rows once for both (separately, the SDDMM gathers a second time).
+ * C follows the nnz-split SpMM variants (see as_spmm_csr_f32); each dA value is one FMA chain
+ * per lane over the lane's columns, then a butterfly sum over the variant's lane group.
+ * variant: 0 = library choice, else an nnz-split variant whose column tile (vector elements x
+ * group x vectors per lane) covers N; others return AS_ERR_UNSUPPORTED. */
+as_status as_spmm_sddmm_csr_f32(as_ctx *ctx, int M, int K, int N, int nnz, const int *rowptr,
+                                const int *colind, const float *val, const float *B, long ldb,
+                                float *C, long ldc, float beta, const float *F, long ldf,
+                                const int *perm, float *dA, int variant, void *stream);
+as_status as_spmm_sddmm_csr_bf16(as_ctx *ctx, int M, int K, int N, int nnz, const int *rowptr,
+                                 const int *colind, const uint16_t *val, const uint16_t *B,
+                                 long ldb, float *C, long ldc, float beta, const uint16_t *F,
+                                 long ldf, const int *perm, float *dA, int variant,
+                                 void *stream);
+
 /* as_sddmm_csr_bf16x3 with an explicit kernel variant (tuning): 0 = library choice,
  * 1 = one 128 x 256 output tile per CTA, 2 = persistent CTAs with two tensor-memory
  * accumulators (epilogue of one tile under the MMAs of the next), 64-wide K stages,
@@ -170,6 +193,14 @@ as_status as_sddmm_coo_f32(as_ctx *ctx, int M, int N, int K, int nnz, const int 
  * fast_transpose (sparseTranspose.cpp:95-142). */
 as_status as_csr2csc(as_ctx *ctx, int M, int N, int nnz, const int *rowptr, const int *colind,
                      const float *val, int *colptr, int *rowind, float *cscval, void *stream);
+
+/* as_csr2csc giving, in place of the values, the permutation perm[nnz]: perm[j] is the CSR
+ * position of CSC entry j (so cscval[j] = val[perm[j]] for any values). No reference
+ * counterpart: it lets a caller whose edge values change every step (trainable edge weights)
+ * gather them into CSC order, and lets as_spmm_sddmm_* write results at CSR positions while
+ * walking the CSC. */
+as_status as_csr2csc_perm(as_ctx *ctx, int M, int N, int nnz, const int *rowptr,
+                          const int *colind, int *colptr, int *rowind, int *perm, void *stream);
 
 /* ---- CSR -> CSC without allocating ------------------------------------------------------------
  * No counterpart in the reference. Some callers of this library cannot allocate device

@@ -249,6 +249,41 @@ void or_sddmm_csr_f32_group(int M, int K, const int *rowptr, const int *colind,
     }
 }
 
+/* SDDMM in the summation order of the SpMM pass with the SDDMM fused in (the GPU's nnz-split
+ * kernel, spmm_nnz.cu): out[perm ? perm[e] : e] = <X[row(e)], Y[col(e)]> where G lanes hold
+ * E-element slices of K -- lane l the slices starting at (j*G + l)*E, j = 0 .. CPL-1, in that
+ * order (slices at or past K skipped) -- and run one fused-FMA chain each; the lanes are then
+ * summed by the butterfly of or_sddmm_csr_f32_group and lane 0's value is the result. There
+ * is no reference counterpart (the reference computes no gradient for the edge values,
+ * gcn/pytorch-custom/op.py:31); this states the GPU kernel's order so that its dot products
+ * can be checked bit for bit. */
+void or_sddmm_csr_f32_slices(int M, int K, const int *rowptr, const int *colind,
+                             const float *X, long ldx, const float *Y, long ldy,
+                             const int *perm, int G, int E, int CPL, float *out, int threads) {
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 16)
+    for (int m = 0; m < M; ++m) {
+        const float *x = X + (long)m * ldx;
+        for (int e = rowptr[m]; e < rowptr[m + 1]; ++e) {
+            const float *y = Y + (long)colind[e] * ldy;
+            float a[32], b[32];
+            for (int l = 0; l < G; ++l) {
+                float acc = 0.0f;
+                for (int j = 0; j < CPL; ++j) {
+                    const int c = (j * G + l) * E;
+                    if (c >= K) continue;
+                    for (int i = 0; i < E; ++i) acc = fmaf(y[c + i], x[c + i], acc);
+                }
+                a[l] = acc;
+            }
+            for (int off = G / 2; off >= 1; off /= 2) {
+                for (int l = 0; l < G; ++l) b[l] = a[l] + a[l ^ off];
+                for (int l = 0; l < G; ++l) a[l] = b[l];
+            }
+            out[perm ? perm[e] : e] = a[0];
+        }
+    }
+}
+
 /* ----------------------------------------------------------------------------------------
  * CSR -> CSC, stable: within each column the entries keep ascending row order. This is
  * the ordering scipy's tocsc() gives on the GCN path (gcn/pytorch-custom/gcn_custom.py:52)

@@ -76,6 +76,9 @@ def lib():
                                                  _f32p, _c_long, _f32p, _c_long, _f32p, _c_int]
             L.or_sddmm_csr_f32_lanes.argtypes = [_c_int, _c_int, _i32p, _i32p, ctypes.c_void_p,
                                                  _f32p, _c_long, _f32p, _c_long, _f32p, _c_int]
+            L.or_sddmm_csr_f32_slices.argtypes = [_c_int, _c_int, _i32p, _i32p, _f32p, _c_long,
+                                                  _f32p, _c_long, ctypes.c_void_p, _c_int,
+                                                  _c_int, _c_int, _f32p, _c_int]
             L.or_csr2csc.argtypes = [_c_int, _c_int, _i32p, _i32p, _f32p, _i32p, _i32p, _f32p]
             L.or_max_threads.restype = _c_int
             L.or_spgemm_dense_f32.argtypes = [_c_int, _c_int, _i32p, _i32p, _f32p, _i32p, _i32p,
@@ -250,6 +253,25 @@ def sddmm_f32_group(rowptr, colind, X, Y, aval=None, threads=None):
     lib().or_sddmm_csr_f32_group(M, X.shape[1], rowptr, colind,
                                  None if av is None else av.ctypes.data, X, X.shape[1], Y,
                                  Y.shape[1], out, threads or max_threads())
+    return out
+
+
+def sddmm_f32_slices(rowptr, colind, X, Y, group, elems, cpl, perm=None, threads=None):
+    """FP32 SDDMM in the order of the SpMM pass with the SDDMM fused in: per entry, `group`
+    lanes each chain over their `elems`-element slices (lane l: slices (j*group + l)*elems,
+    j < cpl), then a butterfly across the lanes; written at perm[e] (e when perm is None).
+    The parity oracle of as_spmm_sddmm_csr_*'s dot products."""
+    rowptr, colind = _csr(rowptr, colind)
+    M = rowptr.size - 1
+    X = np.ascontiguousarray(X, np.float32)
+    Y = np.ascontiguousarray(Y, np.float32)
+    if group > 32 or group & (group - 1):
+        raise ValueError("group must be a power of two <= 32")
+    out = np.zeros(int(rowptr[-1]), np.float32)
+    pp = None if perm is None else np.ascontiguousarray(perm, np.int32)
+    lib().or_sddmm_csr_f32_slices(M, X.shape[1], rowptr, colind, X, X.shape[1], Y, Y.shape[1],
+                                  None if pp is None else pp.ctypes.data, group, elems, cpl, out,
+                                  threads or max_threads())
     return out
 
 

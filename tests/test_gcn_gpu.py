@@ -111,6 +111,34 @@ def test_edge_value_gradient_is_sddmm(oracle):
     assert np.array_equal(bits(w.grad), bits(ref))
 
 
+def test_fused_backward_matches_separate(oracle):
+    """With Graph.perm, a backward needing both gradients runs one pass over the CSC: dB is the
+    unfused nnz-split SpMM's bits, dA the slices-order oracle's bits placed through perm."""
+    a = S.powerlaw_graph(3000, 20000, seed=5)
+    G = gcn.Graph.from_csr(a, dev())
+    colptr, rowind, vcsc = G.csc
+    cp, ri, _ = oracle.csr2csc(a.rowptr, a.colind, a.val, a.n_cols)
+    assert np.array_equal(colptr.cpu().numpy(), cp) and np.array_equal(rowind.cpu().numpy(), ri)
+    var = A.spmm_variants().index("nnzsplit_v4_g32_c1_ch1024") + 1
+    gen = torch.Generator(device=dev()).manual_seed(6)
+    f0 = torch.randn(3000, 24, generator=gen, device=dev())
+    gy = torch.randn(3000, 24, generator=gen, device=dev())
+    grads = []
+    for perm in (G.perm, None):
+        w = G.values.clone().requires_grad_(True)
+        f = f0.clone().requires_grad_(True)
+        out = gcn.SPMMFunction.apply(G.rowptr, G.colind, colptr, rowind, f, w, vcsc, (0, var),
+                                     perm)
+        out.backward(gy)
+        grads.append((f.grad, w.grad))
+    assert torch.equal(grads[0][0], grads[1][0])
+    ref = oracle.sddmm_f32_slices(cp, ri, f0.cpu().numpy(), gy.cpu().numpy(), 32, 1, 1,
+                                  perm=G.perm.cpu().numpy())
+    assert np.array_equal(bits(grads[0][1]), bits(ref))
+    r64, ab = oracle.sddmm_f64(a.rowptr, a.colind, gy.cpu().numpy(), f0.cpu().numpy())
+    assert oracle.scaled_err(grads[1][1].cpu().numpy(), r64, ab).max() < 1e-5
+
+
 def test_gcn_training_is_reproducible():
     x, g, y, train, _ = gcn.synthetic_task(seed=0)
 
