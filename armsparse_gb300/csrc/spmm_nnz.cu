@@ -8,15 +8,16 @@
 //   SDMM.cpp:90-114). A row that crosses a chunk boundary leaves its segment's partial sum in
 //   a carry slot: slot 0 when the segment starts the chunk, slot 1 otherwise.
 // Pass 2 (spmm_nnz_fixup): for every row that ends inside chunk c after starting in an earlier
-//   chunk, a CTA of chunk c adds that row's partial sums (8 runs of chunks, then the runs in
-//   order; then beta * C): a fixed order, so the result is deterministic run to run (not
-//   bit-identical to a single chain for those rows).
+//   chunk, a CTA of chunk c adds that row's partial sums (in chunk order when the row spans at
+//   most 8 chunks, else 8 runs of chunks and then the runs in order; then beta * C): a fixed
+//   order, so the result is deterministic run to run (not bit-identical to a single chain for
+//   those rows).
 // Pass 3 (spmm_empty_rows): rows without entries get beta * C (zeros when beta == 0).
 //
 // Fused form (FUSE): pass 1 also computes, for every entry e (row r, column k), the dot product
 // dA[perm[e]] = <B[k, :], F[r, :]> from the B row it has just loaded for the SpMM and F's row r
-// (loaded once per row segment): the SDDMM that the backward of out = A^T-free SpMM with
-// trainable values needs, without a second gather of B. Each lane chains over its own
+// (loaded once per row segment): the SDDMM that the backward of a product with trainable
+// values needs, without a second gather of B. Each lane chains over its own
 // columns of the row (its E-element slices j = 0..CPL-1, in order), then the GROUP lanes are
 // summed by a butterfly (lane l adds lane l ^ off, off = GROUP/2 .. 1) -- for a step of U
 // entries the butterflies of all U run interleaved (each lane hands half of its values to its
@@ -229,10 +230,7 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
                             d[u] = 0.0f;
 #pragma unroll
                             for (int j = 0; j < CPL; ++j)
-                                if (tile0 + (j * GROUP + g) * E < N)
-#pragma unroll
-                                    for (int i = 0; i < E; ++i)
-                                        d[u] = fmaf(V::at(b[u][j], i), V::at(fr[j], i), d[u]);
+                                if (tile0 + (j * GROUP + g) * E < N) V::dot(b[u][j], fr[j], d[u]);
                         }
                         write_dots<U, GROUP>(d, kk, gmask, g, base + t, nnz, perm, dA, status);
                     }
@@ -280,63 +278,121 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
     if (blockIdx.y == 0 && g == 0) fix[chunk] = fix_row;
 }
 
+constexpr int kShortSpan = 8;  // rows over at most this many chunks: the one-pass fix-up
+
+template <int VW>
+struct Lanes;  // VW consecutive fp32 columns of a carry row, one load
+template <>
+struct Lanes<4> {
+    __device__ static void load(const float *p, float *v) {
+        const float4 t = *reinterpret_cast<const float4 *>(p);
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    }
+};
+template <>
+struct Lanes<1> {
+    __device__ static void load(const float *p, float *v) { v[0] = *p; }
+};
+
 // Rows that end in chunk c after starting in an earlier chunk: sum their partials. A CTA
-// takes one such chunk, 32 columns at a time (lane = column); its 8 warps split the row's chunks
-// into 8 consecutive runs, each summed in chunk order with 8 loads in flight, and warp 0
-// adds the 8 run sums in warp order -- a fixed order, so the result is deterministic. (One
-// row of a power-law graph can span thousands of chunks; a single chain over them was the
-// fix-up's bottleneck.)
+// takes one such chunk.
+//  - A row over at most kShortSpan chunks (nearly all of them): one thread per column loads
+//    the chunks' partials together and adds them in chunk order.
+//  - A longer row: the threads split into R consecutive runs of the row's chunks times groups
+//    of VW columns (R = threads / column groups, so all threads load at once); each sums its
+//    run in chunk order with 8 loads in flight, and the runs are then added in run order.
+// Both orders are fixed by the row's span and N, so the result is deterministic. (One row of a
+// power-law graph can span thousands of chunks: this CTA is then the fix-up's critical path.)
+template <int VW>
 __global__ void __launch_bounds__(kThreads)
 spmm_nnz_fixup(int M, int N, int nnz, int CH, const int *__restrict__ rowptr,
                const float *__restrict__ carry, const int *__restrict__ fix,
                float *__restrict__ C, long ldc, float beta) {
-    __shared__ float part[kThreads / 32][32];
+    __shared__ float part[kThreads * VW];
     const long chunk = blockIdx.x;
     const int r = fix[chunk];  // recorded by the first pass; -1: nothing ends here
     if (r < 0 || r >= M) return;  // the same for the whole CTA
     const int rs = __ldg(rowptr + r);
     const long c_first = rs / CH;
     const long n = chunk - c_first + 1;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long b0 = c_first + n * warp / (kThreads / 32), b1 = c_first + n * (warp + 1) / (kThreads / 32);
-    for (int col0 = 0; col0 < N; col0 += 32) {  // 32-column tiles
-    const int col = col0 + lane;
-    float acc = 0.0f;
-    if (col < N) {
-        auto slot_of = [&](long cc) {
-            return (cc == c_first && static_cast<long>(rs) != cc * CH) ? 1 : 0;
-        };
-        long cc = b0;
-        for (; cc + 8 <= b1; cc += 8) {
-            float v[8];
+    // slot 1 holds the first chunk's partial when the row starts inside that chunk
+    auto row_of = [&](long cc) {
+        return (2 * cc + ((cc == c_first && static_cast<long>(rs) != cc * CH) ? 1 : 0)) *
+               static_cast<long>(N);
+    };
+    if (n <= kShortSpan) {
+        for (int col = threadIdx.x; col < N; col += kThreads) {
+            float v[kShortSpan];
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
-                v[i] = carry[(2 * (cc + i) + slot_of(cc + i)) * static_cast<long>(N) + col];
+            for (int i = 0; i < kShortSpan; ++i)
+                v[i] = i < n ? carry[row_of(c_first + i) + col] : 0.0f;
+            float acc = v[0];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) acc += v[i];
+            for (int i = 1; i < kShortSpan; ++i)
+                if (i < n) acc += v[i];
+            C[r * ldc + col] = beta == 0.0f ? acc : fmaf(beta, C[r * ldc + col], acc);
         }
-        for (; cc < b1; ++cc) acc += carry[(2 * cc + slot_of(cc)) * static_cast<long>(N) + col];
+        return;
     }
-    part[warp][lane] = acc;
-    __syncthreads();
-    if (warp == 0 && col < N) {
-        float t = part[0][lane];
+    const int ncg = N / VW;  // column groups (the launcher guarantees N % VW == 0)
+    for (int cg0 = 0; cg0 < ncg; cg0 += kThreads) {
+        const int cgs = min(kThreads, ncg - cg0);
+        const int R = kThreads / cgs;
+        const int run = threadIdx.x / cgs, gi = threadIdx.x % cgs;
+        const int col = (cg0 + gi) * VW;
+        float acc[VW];
 #pragma unroll
-        for (int w = 1; w < kThreads / 32; ++w) t += part[w][lane];
-        C[r * ldc + col] = beta == 0.0f ? t : fmaf(beta, C[r * ldc + col], t);
-    }
-    __syncthreads();  // part[] is reused by the next tile
+        for (int j = 0; j < VW; ++j) acc[j] = 0.0f;
+        if (run < R) {
+            const long b0 = c_first + n * run / R, b1 = c_first + n * (run + 1) / R;
+            for (long cc = b0; cc < b1; cc += 8) {
+                float v[8][VW];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    if (cc + i < b1) {
+                        Lanes<VW>::load(carry + row_of(cc + i) + col, v[i]);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < VW; ++j) v[i][j] = 0.0f;
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    if (cc + i < b1)
+#pragma unroll
+                        for (int j = 0; j < VW; ++j) acc[j] += v[i][j];
+            }
+#pragma unroll
+            for (int j = 0; j < VW; ++j) part[(run * cgs + gi) * VW + j] = acc[j];
+        }
+        __syncthreads();
+        if (run == 0) {
+#pragma unroll
+            for (int j = 0; j < VW; ++j) {
+                float t = part[gi * VW + j];
+                for (int q = 1; q < R; ++q) t += part[(q * cgs + gi) * VW + j];
+                C[r * ldc + col + j] = beta == 0.0f ? t : fmaf(beta, C[r * ldc + col + j], t);
+            }
+        }
+        __syncthreads();  // part[] is reused by the next column block
     }
 }
 
+// Rows without entries get beta * C. A warp checks 32 consecutive rows with one load each and
+// writes only the empty ones, 32 columns at a time.
 __global__ void __launch_bounds__(kThreads)
 spmm_empty_rows(int M, int N, const int *__restrict__ rowptr, float *__restrict__ C, long ldc,
                 float beta) {
-    const long r = static_cast<long>(blockIdx.x) * (kThreads / 32) + (threadIdx.x >> 5);
-    if (r >= M) return;
-    if (__ldg(rowptr + r) != __ldg(rowptr + r + 1)) return;
-    for (int col = threadIdx.x & 31; col < N; col += 32)
-        C[r * ldc + col] = beta == 0.0f ? 0.0f : beta * C[r * ldc + col];
+    const long base = (static_cast<long>(blockIdx.x) * (kThreads / 32) + (threadIdx.x >> 5)) * 32;
+    const int lane = threadIdx.x & 31;
+    if (base >= M) return;  // the same for the whole warp
+    const long r = base + lane;
+    const bool empty = r < M && __ldg(rowptr + r) == __ldg(rowptr + r + 1);
+    for (unsigned m = __ballot_sync(0xffffffffu, empty); m; m &= m - 1) {
+        const long rr = base + (__ffs(m) - 1);
+        for (int col = lane; col < N; col += 32)
+            C[rr * ldc + col] = beta == 0.0f ? 0.0f : beta * C[rr * ldc + col];
+    }
 }
 
 template <typename T, int VB, int G, int CPL, int U, bool FUSE>
@@ -367,11 +423,15 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, const SddmmFuse *fu, cu
             FUSE ? static_cast<const T *>(fu->F) : nullptr, FUSE ? fu->ldf : 0,
             FUSE ? fu->perm : nullptr, FUSE ? fu->dA : nullptr);
         dim3 g2(static_cast<unsigned>(nchunks));
-        spmm_nnz_fixup<<<g2, kThreads, 0, s>>>(a.M, a.N, a.nnz, CH, a.rowptr, carry, fix, a.C,
-                                               a.ldc, a.beta);
+        if (a.N % 4 == 0)  // carry rows are 16-byte aligned: whole-vector loads
+            spmm_nnz_fixup<4><<<g2, kThreads, 0, s>>>(a.M, a.N, a.nnz, CH, a.rowptr, carry, fix,
+                                                      a.C, a.ldc, a.beta);
+        else
+            spmm_nnz_fixup<1><<<g2, kThreads, 0, s>>>(a.M, a.N, a.nnz, CH, a.rowptr, carry, fix,
+                                                      a.C, a.ldc, a.beta);
         ctx->launches += 2;
     }
-    spmm_empty_rows<<<static_cast<unsigned>(ceil_div(a.M, kThreads / 32)), kThreads, 0, s>>>(
+    spmm_empty_rows<<<static_cast<unsigned>(ceil_div(a.M, kThreads)), kThreads, 0, s>>>(
         a.M, a.N, a.rowptr, a.C, a.ldc, a.beta);
     ctx->launches++;
     return check_cuda(cudaGetLastError(), "spmm nnz-split launch");

@@ -75,6 +75,13 @@ __device__ __forceinline__ void fma_vec_f32(const float *b, float v, float *acc)
 __device__ __forceinline__ void fma_bf16x1(unsigned short b, unsigned short v, float &acc) {
     asm("fma.rn.f32.bf16 %0, %1, %2, %0;\n" : "+f"(acc) : "h"(b), "h"(v));
 }
+// d = fma(lo(b), lo(f), d); d = fma(hi(b), hi(f), d): one step of a dot product over two bf16
+// pairs with the mixed-precision FMA (each step equals fmaf on the widened values).
+__device__ __forceinline__ void dot_bf16x2(unsigned b, unsigned f, float &d) {
+    asm("{\n .reg .b16 bl, bh, fl, fh;\n mov.b32 {bl, bh}, %1;\n mov.b32 {fl, fh}, %2;\n"
+        " fma.rn.f32.bf16 %0, bl, fl, %0;\n fma.rn.f32.bf16 %0, bh, fh, %0;\n}\n"
+        : "+f"(d) : "r"(b), "r"(f));
+}
 template <>
 struct Vec<uint16_t, 16> {
     static constexpr int E = 8;
@@ -95,6 +102,13 @@ struct Vec<uint16_t, 16> {
         fma_bf16x2(r.z, v, acc[4], acc[5]);
         fma_bf16x2(r.w, v, acc[6], acc[7]);
     }
+    // d = fma chain over the elements of b and f in order
+    __device__ static void dot(const Raw &b, const Raw &f, float &d) {
+        dot_bf16x2(b.x, f.x, d);
+        dot_bf16x2(b.y, f.y, d);
+        dot_bf16x2(b.z, f.z, d);
+        dot_bf16x2(b.w, f.w, d);
+    }
 };
 template <>
 struct Vec<uint16_t, 8> {
@@ -114,6 +128,10 @@ struct Vec<uint16_t, 8> {
         fma_bf16x2(r.x, v, acc[0], acc[1]);
         fma_bf16x2(r.y, v, acc[2], acc[3]);
     }
+    __device__ static void dot(const Raw &b, const Raw &f, float &d) {
+        dot_bf16x2(b.x, f.x, d);
+        dot_bf16x2(b.y, f.y, d);
+    }
 };
 template <>
 struct Vec<uint16_t, 4> {
@@ -128,6 +146,7 @@ struct Vec<uint16_t, 4> {
     __device__ static void fma(const Raw &r, unsigned short v, float *acc) {
         fma_bf16x2(r, v, acc[0], acc[1]);
     }
+    __device__ static void dot(const Raw &b, const Raw &f, float &d) { dot_bf16x2(b, f, d); }
 };
 template <>
 struct Vec<uint16_t, 2> {
@@ -137,6 +156,7 @@ struct Vec<uint16_t, 2> {
     __device__ static float at(const Raw &r, int) { return __uint_as_float(static_cast<unsigned>(r) << 16); }
     __device__ static void load(const uint16_t *p, float *o) { o[0] = at(raw(p), 0); }
     __device__ static void fma(const Raw &r, unsigned short v, float *acc) { fma_bf16x1(r, v, acc[0]); }
+    __device__ static void dot(const Raw &b, const Raw &f, float &d) { fma_bf16x1(b, f, d); }
 };
 
 __device__ __forceinline__ float to_f32(float v) { return v; }

@@ -109,6 +109,41 @@ def _time_pick(rowptr, colind, values, n_in: int, width: int, dtype) -> int:
                                           reps=3, max_ratio=3.0)).variant
 
 
+def _nnz_tile(name: str, esz: int) -> int:
+    """Column tile (vector elements x lanes x vectors per lane) of an nnz-split variant name."""
+    f = {p[0]: int(p[1:]) for p in name.split("_")[1:] if p[:1] in "vgc" and p[1:].isdigit()}
+    return (f["v"] // esz) * f["g"] * f["c"]
+
+
+def _time_pick_fused(colptr, rowind, values, perm, n_out: int, width: int, dtype) -> int:
+    """The fastest nnz-split kernel for the fused backward pass (A^T dOut with the edge-value
+    SDDMM, ``sparse.spmm_sddmm``) on these arrays, timed once; 0 when none can carry it."""
+    from . import tuner
+    from ._native import NativeError
+    esz = 4 if dtype == torch.float32 else 2
+    dev = colptr.device
+    g = torch.zeros(n_out, width, device=dev, dtype=dtype)
+    f = torch.zeros(colptr.numel() - 1, width, device=dev, dtype=dtype)
+    C = torch.empty(colptr.numel() - 1, width, device=dev)
+    dA = torch.empty(rowind.numel(), device=dev)
+    vals = values.to(dtype)
+    best, best_ms = 0, float("inf")
+    for i, name in enumerate(S.spmm_variants(dtype)):
+        v = i + 1
+        if (not name.startswith("nnzsplit") or _nnz_tile(name, esz) < width
+                or not S.spmm_variant_supported(v, width, dtype)):
+            continue
+        fn = lambda: S.spmm_sddmm(colptr, rowind, vals, g, f, perm=perm, C=C, variant=v, dA=dA)
+        try:
+            fn()
+        except NativeError:
+            continue
+        ms = tuner.time_cuda(fn, reps=3, warmup=1, flush=False)
+        if ms < best_ms:
+            best, best_ms = v, ms
+    return best
+
+
 class _DenseProduct(torch.autograd.Function):
     """x @ W for a tall dense x and a narrow W. The weight gradient x^T dY reduces over all
     rows into a few outputs (64 x 3 for the GCN's second layer); as one GEMM that runs on a
@@ -166,12 +201,21 @@ class Graph:
         self.csc
         return self._perm
 
-    def plan(self, N: int, dtype=torch.float32):
+    def plan(self, N: int, dtype=torch.float32, fused: bool = False):
         """(forward, backward) kernel variants for dense width N: the learned selector's pick,
         or -- for widths below the 16..256 it was trained on -- the fastest of its candidate
-        kernels timed once on this graph."""
+        kernels timed once on this graph. fused: the backward variant is for the fused pass
+        (``SPMMFunction`` given ``perm`` and trainable values) -- the fastest nnz-split kernel
+        that carries the SDDMM, timed once."""
         if self.selector is None or dtype == torch.float64:
             return (0, 0)
+        if fused:
+            key = (N, dtype, "fused")
+            if key not in self._plans:
+                colptr, rowind, vcsc = self.csc
+                bwd = _time_pick_fused(colptr, rowind, vcsc, self.perm, self.n_rows, N, dtype)
+                self._plans[key] = (self.plan(N, dtype)[0], bwd or self.plan(N, dtype)[1])
+            return self._plans[key]
         key = (N, dtype)
         if key not in self._plans:
             colptr, rowind, vcsc = self.csc
