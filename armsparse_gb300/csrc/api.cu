@@ -188,21 +188,23 @@ as_status as_csr_validate(as_ctx *c, int n_rows, int n_cols, int nnz, const int 
 static as_status spmm_common(const char *fn, int dtype, as_ctx *c, int M, int K, int N, int nnz,
                              const int *rowptr, const int *colind, const void *val,
                              const void *B, long ldb, float *C, long ldc, float beta,
-                             int variant, void *stream) {
+                             int variant, void *stream, uint16_t *C16 = nullptr) {
     if (!c) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": ctx is NULL");
     as_status st = check_csr_args(fn, M, K, nnz, rowptr, colind, val, true);
     if (st != AS_OK) return st;
     if (N < 0) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": negative N");
     if (M == 0 || N == 0) return AS_OK;
-    if (!C) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": C is NULL");
+    if (!C && !C16) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": C is NULL");
     if (K > 0 && nnz > 0 && !B) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": B is NULL");
     if (ldb < N || ldc < N)
         return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": leading dimension below N");
     if (variant < 0 || variant > spmm_variant_count(dtype))
         return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": unknown variant");
     DeviceGuard g(c->device);
-    SpmmArgs a{M, K, N, nnz, rowptr, colind, val, B, ldb, C, ldc, beta, c->d_status};
-    if (variant == 0) variant = spmm_default_variant(dtype, M, K, N, nnz, ldb, ldc, B, C);
+    SpmmArgs a{M, K, N, nnz, rowptr, colind, val, B, ldb, C, ldc, beta, c->d_status, C16};
+    if (variant == 0)
+        variant = spmm_default_variant(dtype, M, K, N, nnz, ldb, ldc, B,
+                                       C16 ? static_cast<const void *>(C16) : C);
     return spmm_launch(c, dtype, variant, a, static_cast<cudaStream_t>(stream));
 }
 
@@ -225,7 +227,8 @@ static as_status spmm_sddmm_common(const char *fn, int dtype, as_ctx *c, int M, 
                                    int nnz, const int *rowptr, const int *colind,
                                    const void *val, const void *B, long ldb, float *C, long ldc,
                                    float beta, const void *F, long ldf, const int *perm,
-                                   float *dA, int variant, void *stream) {
+                                   float *dA, int variant, void *stream,
+                                   uint16_t *C16 = nullptr) {
     if (!c) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": ctx is NULL");
     as_status st = check_csr_args(fn, M, K, nnz, rowptr, colind, val, true);
     if (st != AS_OK) return st;
@@ -241,7 +244,7 @@ static as_status spmm_sddmm_common(const char *fn, int dtype, as_ctx *c, int M, 
                                           static_cast<cudaStream_t>(stream)),
                           fn);
     }
-    if (!C) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": C is NULL");
+    if (!C && !C16) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": C is NULL");
     if (nnz > 0 && (!B || !F || !dA))
         return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": B, F or dA is NULL");
     if (ldb < N || ldc < N || ldf < N)
@@ -249,9 +252,26 @@ static as_status spmm_sddmm_common(const char *fn, int dtype, as_ctx *c, int M, 
     if (variant < 0 || variant > spmm_variant_count(dtype))
         return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": unknown variant");
     DeviceGuard g(c->device);
-    SpmmArgs a{M, K, N, nnz, rowptr, colind, val, B, ldb, C, ldc, beta, c->d_status};
+    SpmmArgs a{M, K, N, nnz, rowptr, colind, val, B, ldb, C, ldc, beta, c->d_status, C16};
     SddmmFuse f{F, ldf, perm, dA};
     return spmm_sddmm_launch(c, dtype, variant, a, f, static_cast<cudaStream_t>(stream));
+}
+
+as_status as_spmm_csr_bf16_out16(as_ctx *c, int M, int K, int N, int nnz, const int *rowptr,
+                                 const int *colind, const uint16_t *val, const uint16_t *B,
+                                 long ldb, uint16_t *C, long ldc, int variant, void *stream) {
+    return spmm_common("as_spmm_csr_bf16_out16", 1, c, M, K, N, nnz, rowptr, colind, val, B, ldb,
+                       nullptr, ldc, 0.0f, variant, stream, C);
+}
+
+as_status as_spmm_sddmm_csr_bf16_out16(as_ctx *c, int M, int K, int N, int nnz,
+                                       const int *rowptr, const int *colind,
+                                       const uint16_t *val, const uint16_t *B, long ldb,
+                                       uint16_t *C, long ldc, const uint16_t *F, long ldf,
+                                       const int *perm, float *dA, int variant, void *stream) {
+    return spmm_sddmm_common("as_spmm_sddmm_csr_bf16_out16", 1, c, M, K, N, nnz, rowptr, colind,
+                             val, B, ldb, nullptr, ldc, 0.0f, F, ldf, perm, dA, variant, stream,
+                             C);
 }
 
 as_status as_spmm_sddmm_csr_f32(as_ctx *c, int M, int K, int N, int nnz, const int *rowptr,

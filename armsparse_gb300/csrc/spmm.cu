@@ -61,7 +61,8 @@ __global__ void __launch_bounds__(kThreads)
 spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
               const int *__restrict__ colind, const T *__restrict__ val,
               const T *__restrict__ B, long ldb, float *__restrict__ C, long ldc, float beta,
-              unsigned *status, int long_thresh, int *long_list, unsigned *long_count) {
+              unsigned *status, int long_thresh, int *long_list, unsigned *long_count,
+              uint16_t *__restrict__ C16) {
     using V = Vec<T, VB>;
     constexpr int E = V::E;
     constexpr int TILE = GROUP * E * CPL;
@@ -193,7 +194,12 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
 #pragma unroll
     for (int j = 0; j < CPL; ++j) {
         const int c = tile0 + (j * GROUP + g) * E;
-        if (c < N) store_c<E>(crow + c, acc[j]);
+        if (c < N) {
+            if (C16)
+                store_bf16<E>(C16 + row * ldc + c, acc[j]);
+            else
+                store_c<E>(crow + c, acc[j]);
+        }
     }
 }
 
@@ -250,7 +256,7 @@ void launch_one(const SpmmArgs &a, const LongRows &lr, cudaStream_t s) {
     spmm_rowsplit<T, VB, G, CPL, U><<<grid, kThreads, 0, s>>>(
         a.M, a.K, a.N, a.nnz, a.rowptr, a.colind, static_cast<const T *>(a.val),
         static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, a.status, lr.thresh, lr.list,
-        lr.count);
+        lr.count, a.C16);
 }
 
 template <typename T, int VB, int G>
@@ -373,8 +379,23 @@ bool spmm_variant_supported(int dtype, int variant, int N, long ldb, long ldc, c
            ceil_div(N, E * v.group * v.cpl) <= 65535 && ceil_div(N, 32) <= 65535;
 }
 
+// A bf16 output (a.C16) in vectors of e elements: aligned to min(2e, 16) bytes, rows of e.
+static bool c16_ok(int e, long ldc, const void *C16) {
+    return ldc % e == 0 && aligned(C16, 2 * e > 16 ? 16 : 2 * e);
+}
+
 as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cudaStream_t s) {
     const Variant &v = dtype == 0 ? kF32[variant - 1] : kBF16[variant - 1];
+    if (a.C16) {
+        const int e = v.vb / (dtype == 0 ? 4 : 2);
+        if (v.kind == 1)
+            return fail(AS_ERR_UNSUPPORTED, std::string("spmm: variant ") + v.name +
+                                                " has no bf16 output");
+        if (a.beta != 0.0f) return fail(AS_ERR_INVALID_VALUE, "spmm: bf16 output needs beta = 0");
+        if (!c16_ok(e, a.ldc, a.C16))
+            return fail(AS_ERR_UNSUPPORTED, std::string("spmm: variant ") + v.name +
+                                                " needs the bf16 C aligned to its vectors");
+    }
     if (v.kind == 1) return spmm_bulk_launch(ctx, dtype, v.vb, v.unroll, a, s);
     if (v.kind == 2) {
         if (v.unroll == kSmallChunk && a.N > kSmallChunkMaxN)
@@ -382,7 +403,7 @@ as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cu
                                                 " serves N <= 64 only");
         return spmm_nnz_launch(ctx, dtype, v.vb, v.group, v.cpl, v.unroll, v.steps, a, s);
     }
-    if (!vb_ok(dtype, v.vb, a.N, a.ldb, a.ldc, a.B, a.C))
+    if (!vb_ok(dtype, v.vb, a.N, a.ldb, a.ldc, a.B, a.C16 ? nullptr : a.C))
         return fail(AS_ERR_UNSUPPORTED, std::string("spmm: variant ") + v.name +
                                             " needs N, ldb, ldc and pointer alignment to match its vector width");
     if (ceil_div(a.N, (v.vb / (dtype == 0 ? 4 : 2)) * v.group * v.cpl) > 65535)

@@ -100,7 +100,7 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
               const T *__restrict__ B, long ldb, float *__restrict__ C, long ldc, float beta,
               float *__restrict__ carry, int *__restrict__ fix, unsigned *status,
               const T *__restrict__ F, long ldf, const int *__restrict__ perm,
-              float *__restrict__ dA) {
+              float *__restrict__ dA, uint16_t *__restrict__ C16) {
     using V = Vec<T, VB>;
     constexpr int E = V::E;
     constexpr int TILE = GROUP * E * CPL;
@@ -268,9 +268,14 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {
             const int cc = tile0 + (j * GROUP + g) * E;
-            if (cc < N)
+            if (cc < N) {
+                if (!split && C16) {
+                    store_bf16<E>(C16 + r * ldc + cc, acc[j]);
+                } else {
 #pragma unroll
-                for (int i = 0; i < E; ++i) dst[cc + i] = acc[j][i];
+                    for (int i = 0; i < E; ++i) dst[cc + i] = acc[j][i];
+                }
+            }
         }
         e = se;
         ++r;
@@ -307,7 +312,7 @@ template <int VW>
 __global__ void __launch_bounds__(kThreads)
 spmm_nnz_fixup(int M, int N, int nnz, int CH, const int *__restrict__ rowptr,
                const float *__restrict__ carry, const int *__restrict__ fix,
-               float *__restrict__ C, long ldc, float beta) {
+               float *__restrict__ C, long ldc, float beta, uint16_t *__restrict__ C16) {
     __shared__ float part[kThreads * VW];
     const long chunk = blockIdx.x;
     const int r = fix[chunk];  // recorded by the first pass; -1: nothing ends here
@@ -330,7 +335,10 @@ spmm_nnz_fixup(int M, int N, int nnz, int CH, const int *__restrict__ rowptr,
 #pragma unroll
             for (int i = 1; i < kShortSpan; ++i)
                 if (i < n) acc += v[i];
-            C[r * ldc + col] = beta == 0.0f ? acc : fmaf(beta, C[r * ldc + col], acc);
+            if (C16)
+                C16[r * ldc + col] = f32_to_bf16(acc);
+            else
+                C[r * ldc + col] = beta == 0.0f ? acc : fmaf(beta, C[r * ldc + col], acc);
         }
         return;
     }
@@ -371,7 +379,10 @@ spmm_nnz_fixup(int M, int N, int nnz, int CH, const int *__restrict__ rowptr,
             for (int j = 0; j < VW; ++j) {
                 float t = part[gi * VW + j];
                 for (int q = 1; q < R; ++q) t += part[(q * cgs + gi) * VW + j];
-                C[r * ldc + col + j] = beta == 0.0f ? t : fmaf(beta, C[r * ldc + col + j], t);
+                if (C16)
+                    C16[r * ldc + col + j] = f32_to_bf16(t);
+                else
+                    C[r * ldc + col + j] = beta == 0.0f ? t : fmaf(beta, C[r * ldc + col + j], t);
             }
         }
         __syncthreads();  // part[] is reused by the next column block
@@ -382,7 +393,7 @@ spmm_nnz_fixup(int M, int N, int nnz, int CH, const int *__restrict__ rowptr,
 // writes only the empty ones, 32 columns at a time.
 __global__ void __launch_bounds__(kThreads)
 spmm_empty_rows(int M, int N, const int *__restrict__ rowptr, float *__restrict__ C, long ldc,
-                float beta) {
+                float beta, uint16_t *__restrict__ C16) {
     const long base = (static_cast<long>(blockIdx.x) * (kThreads / 32) + (threadIdx.x >> 5)) * 32;
     const int lane = threadIdx.x & 31;
     if (base >= M) return;  // the same for the whole warp
@@ -390,8 +401,12 @@ spmm_empty_rows(int M, int N, const int *__restrict__ rowptr, float *__restrict_
     const bool empty = r < M && __ldg(rowptr + r) == __ldg(rowptr + r + 1);
     for (unsigned m = __ballot_sync(0xffffffffu, empty); m; m &= m - 1) {
         const long rr = base + (__ffs(m) - 1);
-        for (int col = lane; col < N; col += 32)
-            C[rr * ldc + col] = beta == 0.0f ? 0.0f : beta * C[rr * ldc + col];
+        for (int col = lane; col < N; col += 32) {
+            if (C16)
+                C16[rr * ldc + col] = 0;
+            else
+                C[rr * ldc + col] = beta == 0.0f ? 0.0f : beta * C[rr * ldc + col];
+        }
     }
 }
 
@@ -404,6 +419,10 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, const SddmmFuse *fu, cu
         return fail(AS_ERR_UNSUPPORTED, "spmm nnz-split: layout does not fit the vector width");
     if (ceil_div(a.N, TILE) > 65535 || ceil_div(a.N, 32) > 65535)
         return fail(AS_ERR_UNSUPPORTED, "spmm nnz-split: N too large");
+    if (a.C16 && (a.beta != 0.0f || (a.ldc % E) ||
+                  (reinterpret_cast<uintptr_t>(a.C16) % (2 * E > 16 ? 16 : 2 * E))))
+        return fail(AS_ERR_UNSUPPORTED,
+                    "spmm nnz-split: bf16 output needs beta = 0 and C aligned to the vectors");
     if (FUSE && (a.N > TILE || (fu->ldf % E) || (reinterpret_cast<uintptr_t>(fu->F) % (E * esz))))
         return fail(AS_ERR_UNSUPPORTED,
                     "spmm+sddmm: the variant's column tile must cover N, F aligned to its vectors");
@@ -421,18 +440,18 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, const SddmmFuse *fu, cu
             a.M, a.K, a.N, a.nnz, CH, a.rowptr, a.colind, static_cast<const T *>(a.val),
             static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, carry, fix, a.status,
             FUSE ? static_cast<const T *>(fu->F) : nullptr, FUSE ? fu->ldf : 0,
-            FUSE ? fu->perm : nullptr, FUSE ? fu->dA : nullptr);
+            FUSE ? fu->perm : nullptr, FUSE ? fu->dA : nullptr, a.C16);
         dim3 g2(static_cast<unsigned>(nchunks));
         if (a.N % 4 == 0)  // carry rows are 16-byte aligned: whole-vector loads
             spmm_nnz_fixup<4><<<g2, kThreads, 0, s>>>(a.M, a.N, a.nnz, CH, a.rowptr, carry, fix,
-                                                      a.C, a.ldc, a.beta);
+                                                      a.C, a.ldc, a.beta, a.C16);
         else
             spmm_nnz_fixup<1><<<g2, kThreads, 0, s>>>(a.M, a.N, a.nnz, CH, a.rowptr, carry, fix,
-                                                      a.C, a.ldc, a.beta);
+                                                      a.C, a.ldc, a.beta, a.C16);
         ctx->launches += 2;
     }
     spmm_empty_rows<<<static_cast<unsigned>(ceil_div(a.M, kThreads)), kThreads, 0, s>>>(
-        a.M, a.N, a.rowptr, a.C, a.ldc, a.beta);
+        a.M, a.N, a.rowptr, a.C, a.ldc, a.beta, a.C16);
     ctx->launches++;
     return check_cuda(cudaGetLastError(), "spmm nnz-split launch");
 }

@@ -159,6 +159,29 @@ struct Vec<uint16_t, 2> {
     __device__ static void dot(const Raw &b, const Raw &f, float &d) { fma_bf16x1(b, f, d); }
 };
 
+// v[0..E) rounded to bf16 (nearest even) and stored at p, in whole vectors of up to 16 bytes
+// (p aligned to min(2E, 16) bytes): the bf16 form of an fp32 output row segment.
+__device__ __forceinline__ unsigned pack_bf16x2(float lo, float hi) {
+    return static_cast<unsigned>(f32_to_bf16(lo)) | (static_cast<unsigned>(f32_to_bf16(hi)) << 16);
+}
+template <int E>
+__device__ __forceinline__ void store_bf16(uint16_t *p, const float *v) {
+    if constexpr (E % 8 == 0) {
+#pragma unroll
+        for (int i = 0; i < E; i += 8)
+            *reinterpret_cast<uint4 *>(p + i) =
+                make_uint4(pack_bf16x2(v[i], v[i + 1]), pack_bf16x2(v[i + 2], v[i + 3]),
+                           pack_bf16x2(v[i + 4], v[i + 5]), pack_bf16x2(v[i + 6], v[i + 7]));
+    } else if constexpr (E == 4) {
+        *reinterpret_cast<uint2 *>(p) = make_uint2(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]));
+    } else if constexpr (E == 2) {
+        *reinterpret_cast<unsigned *>(p) = pack_bf16x2(v[0], v[1]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < E; ++i) p[i] = f32_to_bf16(v[i]);
+    }
+}
+
 __device__ __forceinline__ float to_f32(float v) { return v; }
 __device__ __forceinline__ float to_f32(uint16_t v) { return bf16_to_f32(v); }
 

@@ -23,14 +23,21 @@ import torch.nn.functional as F
 from torch.nn import Parameter
 
 from . import sparse as S
+from ._native import NativeError
 
 
 def _spmm(rowptr, colind, values, feat, variant=0):
     """A * feat for fp32 / fp64 / bf16 features (bf16 values and features are multiplied in fp32;
     the result is returned in the feature dtype)."""
     if feat.dtype == torch.bfloat16:
-        return S.spmm(rowptr, colind, values.to(torch.bfloat16), feat.contiguous(),
-                      variant=variant).to(torch.bfloat16)
+        vb = values.to(torch.bfloat16)
+        try:  # C written in bf16 by the kernel
+            return S.spmm(rowptr, colind, vb, feat.contiguous(), variant=variant,
+                          out_dtype=torch.bfloat16)
+        except NativeError as e:
+            if e.status != 3:  # AS_ERR_UNSUPPORTED (a bulk variant): fp32 C, then rounded
+                raise
+        return S.spmm(rowptr, colind, vb, feat.contiguous(), variant=variant).to(torch.bfloat16)
     return S.spmm(rowptr, colind, values.to(feat.dtype), feat.contiguous(), variant=variant)
 
 
@@ -88,15 +95,14 @@ class SPMMFunction(torch.autograd.Function):
 def _spmm_sddmm_t(colptr, rowind, w_csc, g, feat, perm, variant):
     """(A^T g, dA) in one pass over the CSC, or None when the backward variant cannot carry
     the SDDMM (not an nnz-split kernel, or its column tile is narrower than the width)."""
-    from ._native import NativeError
     try:
         C, dA = S.spmm_sddmm(colptr, rowind, w_csc.to(g.dtype), g, feat, perm=perm,
-                             variant=variant)
+                             variant=variant, out_dtype=g.dtype)
     except NativeError as e:
         if e.status != 3:  # AS_ERR_UNSUPPORTED: run the two products separately
             raise
         return None
-    return C.to(g.dtype), dA
+    return C, dA
 
 
 def _time_pick(rowptr, colind, values, n_in: int, width: int, dtype) -> int:
@@ -119,12 +125,11 @@ def _time_pick_fused(colptr, rowind, values, perm, n_out: int, width: int, dtype
     """The fastest nnz-split kernel for the fused backward pass (A^T dOut with the edge-value
     SDDMM, ``sparse.spmm_sddmm``) on these arrays, timed once; 0 when none can carry it."""
     from . import tuner
-    from ._native import NativeError
     esz = 4 if dtype == torch.float32 else 2
     dev = colptr.device
     g = torch.zeros(n_out, width, device=dev, dtype=dtype)
     f = torch.zeros(colptr.numel() - 1, width, device=dev, dtype=dtype)
-    C = torch.empty(colptr.numel() - 1, width, device=dev)
+    C = torch.empty(colptr.numel() - 1, width, device=dev, dtype=dtype)  # as the backward writes
     dA = torch.empty(rowind.numel(), device=dev)
     vals = values.to(dtype)
     best, best_ms = 0, float("inf")
@@ -133,7 +138,8 @@ def _time_pick_fused(colptr, rowind, values, perm, n_out: int, width: int, dtype
         if (not name.startswith("nnzsplit") or _nnz_tile(name, esz) < width
                 or not S.spmm_variant_supported(v, width, dtype)):
             continue
-        fn = lambda: S.spmm_sddmm(colptr, rowind, vals, g, f, perm=perm, C=C, variant=v, dA=dA)
+        fn = lambda: S.spmm_sddmm(colptr, rowind, vals, g, f, perm=perm, C=C, variant=v, dA=dA,
+                                  out_dtype=dtype)
         try:
             fn()
         except NativeError:

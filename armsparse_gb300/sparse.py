@@ -64,10 +64,12 @@ def sync_status(device=None) -> None:
     N.context(dev.index).sync_status(_stream(dev))
 
 
-def spmm(rowptr, colind, val, B, C=None, beta: float = 0.0, variant: int = 0):
+def spmm(rowptr, colind, val, B, C=None, beta: float = 0.0, variant: int = 0,
+         out_dtype: torch.dtype = torch.float32):
     """C = A*B + beta*C with A (M x K) in CSR. fp32 val/B -> fp32 path (bit-identical to the
     reference's rowBaseSpmm3 for row-split variants); bf16 val/B -> bf16 storage with fp32
-    accumulation. C is fp32 (allocated when None)."""
+    accumulation. C is fp32 (allocated when None); with bf16 val/B, out_dtype=torch.bfloat16
+    gives C in bf16 (the fp32 result rounded to nearest even, beta 0) without a second pass."""
     dev = _dev(rowptr, colind, val, B, C)
     M, nnz = _csr(rowptr, colind)
     if B.dim() != 2:
@@ -76,6 +78,11 @@ def spmm(rowptr, colind, val, B, C=None, beta: float = 0.0, variant: int = 0):
         raise ValueError("B must be row-major with unit column stride")
     K, Ncols = B.shape
     ldb = B.stride(0) if K > 1 else Ncols
+    if out_dtype == torch.bfloat16:
+        return _spmm_bf16_out16(rowptr, colind, val, B, C, beta, variant, dev, M, nnz, K, Ncols,
+                                ldb)
+    if out_dtype != torch.float32:
+        raise TypeError("out_dtype must be float32 or bfloat16")
     if val.dtype == torch.float32 and B.dtype == torch.float32:
         fn, dname = N.load().as_spmm_csr_f32, "as_spmm_csr_f32"
     elif val.dtype == torch.bfloat16 and B.dtype == torch.bfloat16:
@@ -98,6 +105,27 @@ def spmm(rowptr, colind, val, B, C=None, beta: float = 0.0, variant: int = 0):
     ctx = N.context(dev.index)
     N.check(fn(ctx.handle, M, K, Ncols, nnz, _ptr(rowptr), _ptr(colind), _ptr(val), _ptr(B),
                ldb, _ptr(C), ldc, float(beta), int(variant), _stream(dev)), dname)
+    return C
+
+
+def _spmm_bf16_out16(rowptr, colind, val, B, C, beta, variant, dev, M, nnz, K, Ncols, ldb):
+    if val.dtype != torch.bfloat16 or B.dtype != torch.bfloat16:
+        raise TypeError("a bf16 output needs bf16 val and B")
+    if beta != 0.0:
+        raise ValueError("a bf16 output is written with beta = 0")
+    _need(val, torch.bfloat16, "val", 1)
+    if val.numel() != nnz:
+        raise ValueError("val and colind lengths differ")
+    if C is None:
+        C = torch.empty((M, Ncols), dtype=torch.bfloat16, device=dev)
+    elif C.dtype != torch.bfloat16 or C.dim() != 2 or C.shape != (M, Ncols) or C.stride(1) != 1:
+        raise ValueError("C must be bfloat16 (M, N) row-major")
+    ldc = C.stride(0) if M > 1 else Ncols
+    ctx = N.context(dev.index)
+    N.check(N.load().as_spmm_csr_bf16_out16(ctx.handle, M, K, Ncols, nnz, _ptr(rowptr),
+                                            _ptr(colind), _ptr(val), _ptr(B), ldb, _ptr(C), ldc,
+                                            int(variant), _stream(dev)),
+            "as_spmm_csr_bf16_out16")
     return C
 
 
@@ -346,12 +374,13 @@ def csr2csc_perm(rowptr, colind, n_cols: int):
 
 
 def spmm_sddmm(rowptr, colind, val, B, F, perm=None, C=None, beta: float = 0.0,
-               variant: int = 0, dA=None):
+               variant: int = 0, dA=None, out_dtype: torch.dtype = torch.float32):
     """(C, dA): C = A*B + beta*C as ``spmm`` and, in the same pass over A, the SDDMM
     dA[perm[e]] = <B[col(e), :], F[row(e), :]> (dA[e] when perm is None) in fp32. With A the
     CSC of a forward matrix, B = dOut, F = the forward's input and perm from
     ``csr2csc_perm``, this is the backward of out = A_fwd * F with trainable values.
-    variant: 0 = library choice, else an nnz-split variant whose column tile covers N."""
+    variant: 0 = library choice, else an nnz-split variant whose column tile covers N.
+    out_dtype=torch.bfloat16 (bf16 inputs, beta 0): C in bf16, as ``spmm``."""
     dev = _dev(rowptr, colind, val, B, F, perm, C, dA)
     M, nnz = _csr(rowptr, colind)
     if B.dim() != 2 or F.dim() != 2 or B.stride(1) != 1 or F.stride(1) != 1:
@@ -372,12 +401,16 @@ def spmm_sddmm(rowptr, colind, val, B, F, perm=None, C=None, beta: float = 0.0,
         _need(perm, torch.int32, "perm", 1)
         if perm.numel() != nnz:
             raise ValueError("perm and colind lengths differ")
+    c16 = out_dtype == torch.bfloat16
+    if c16 and (val.dtype != torch.bfloat16 or beta != 0.0):
+        raise ValueError("a bf16 output needs bf16 inputs and beta = 0")
+    cdt = torch.bfloat16 if c16 else torch.float32
     if C is None:
         if beta != 0.0:
             raise ValueError("beta != 0 needs C")
-        C = torch.empty((M, Ncols), dtype=torch.float32, device=dev)
-    elif C.dtype != torch.float32 or C.dim() != 2 or C.shape != (M, Ncols) or C.stride(1) != 1:
-        raise ValueError("C must be float32 (M, N) row-major")
+        C = torch.empty((M, Ncols), dtype=cdt, device=dev)
+    elif C.dtype != cdt or C.dim() != 2 or C.shape != (M, Ncols) or C.stride(1) != 1:
+        raise ValueError(f"C must be {cdt} (M, N) row-major")
     if dA is None:
         dA = torch.empty(nnz, dtype=torch.float32, device=dev)
     else:
@@ -388,6 +421,12 @@ def spmm_sddmm(rowptr, colind, val, B, F, perm=None, C=None, beta: float = 0.0,
     ldc = C.stride(0) if M > 1 else Ncols
     ldf = F.stride(0) if M > 1 else Ncols
     ctx = N.context(dev.index)
+    if c16:
+        N.check(N.load().as_spmm_sddmm_csr_bf16_out16(
+            ctx.handle, M, K, Ncols, nnz, _ptr(rowptr), _ptr(colind), _ptr(val), _ptr(B), ldb,
+            _ptr(C), ldc, _ptr(F), ldf, _ptr(perm), _ptr(dA), int(variant), _stream(dev)),
+            "as_spmm_sddmm_csr_bf16_out16")
+        return C, dA
     N.check(fn(ctx.handle, M, K, Ncols, nnz, _ptr(rowptr), _ptr(colind), _ptr(val), _ptr(B), ldb,
                _ptr(C), ldc, float(beta), _ptr(F), ldf, _ptr(perm), _ptr(dA), int(variant),
                _stream(dev)), dname)

@@ -146,6 +146,15 @@ as_status as_sddmm_csr_bf16(as_ctx *ctx, int M, int N, int K, int nnz, const int
                             const int *colind, const float *aval, const uint16_t *X, long ldx,
                             const uint16_t *Y, long ldy, float *out, void *stream);
 
+/* bf16 output: C = bf16(A*B) (round to nearest even from the FP32 sums; beta is 0), so a bf16
+ * pipeline stores half the bytes and needs no conversion pass. The FP32 sums are those of
+ * as_spmm_csr_bf16 with the same variant, so C is that call's result rounded, bit for bit.
+ * C (ldc elements per row) is aligned to the variant's vectors (min(2 x elements, 16) bytes);
+ * the bulk-copy variants have no bf16 output (AS_ERR_UNSUPPORTED). */
+as_status as_spmm_csr_bf16_out16(as_ctx *ctx, int M, int K, int N, int nnz, const int *rowptr,
+                                 const int *colind, const uint16_t *val, const uint16_t *B,
+                                 long ldb, uint16_t *C, long ldc, int variant, void *stream);
+
 /* ---- SpMM and SDDMM in one pass over A ---------------------------------------------------------
  * C = A*B + beta*C (A: M x K CSR, B: K x N, C: M x N, as as_spmm_csr_*) and, for every entry e
  * of A (row r, column k):  dA[perm ? perm[e] : e] = <B[k, :], F[r, :]>  (F: M x N, ldf >= N,
@@ -168,6 +177,12 @@ as_status as_spmm_sddmm_csr_bf16(as_ctx *ctx, int M, int K, int N, int nnz, cons
                                  long ldb, float *C, long ldc, float beta, const uint16_t *F,
                                  long ldf, const int *perm, float *dA, int variant,
                                  void *stream);
+/* as_spmm_sddmm_csr_bf16 with C in bf16 (as as_spmm_csr_bf16_out16). */
+as_status as_spmm_sddmm_csr_bf16_out16(as_ctx *ctx, int M, int K, int N, int nnz,
+                                       const int *rowptr, const int *colind,
+                                       const uint16_t *val, const uint16_t *B, long ldb,
+                                       uint16_t *C, long ldc, const uint16_t *F, long ldf,
+                                       const int *perm, float *dA, int variant, void *stream);
 
 /* as_sddmm_csr_bf16x3 with an explicit kernel variant (tuning): 0 = library choice,
  * 1 = one 128 x 256 output tile per CTA, 2 = persistent CTAs with two tensor-memory

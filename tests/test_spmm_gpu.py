@@ -334,3 +334,37 @@ def test_nnzsplit_bf16_variants(oracle):
             assert torch.equal(C, A.spmm(rp, ci, vd, Bd, variant=var)), names[var - 1]
         assert ran >= 4
     A.sync_status()
+
+
+@pytest.mark.parametrize("N_", [46, 64, 256])
+def test_bf16_output_is_rounded_fp32_output(N_):
+    """C in bf16 (as_spmm_csr_bf16_out16) is the same variant's fp32 C rounded to nearest even,
+    bit for bit, through the row-split, long-row and entry-balanced kernels; the bulk-copy
+    variants have no bf16 output."""
+    a = _skewed(9, n_rows=2500, n_cols=20000, long_lens=(20000, 3000, 600, 257))
+    rp, ci, v = csr_dev(a)
+    vd = v.to(torch.bfloat16)
+    Bd = to_dev(S.dense_uniform((a.n_cols, N_), 10 + N_)).to(torch.bfloat16)
+    names = A.spmm_variants(torch.bfloat16)
+    ran = 0
+    for var in range(1, len(names) + 1):
+        try:
+            C32 = A.spmm(rp, ci, vd, Bd, variant=var)
+        except N.NativeError as e:
+            assert e.status == 3
+            continue
+        try:
+            C16 = A.spmm(rp, ci, vd, Bd, variant=var, out_dtype=torch.bfloat16)
+        except N.NativeError as e:
+            assert e.status == 3 and names[var - 1].startswith("bulk"), names[var - 1]
+            continue
+        ran += 1
+        assert C16.dtype == torch.bfloat16
+        assert torch.equal(C16.view(torch.int16), C32.to(torch.bfloat16).view(torch.int16)), \
+            names[var - 1]
+    assert ran >= 20
+    C0 = A.spmm(rp, ci, vd, Bd, out_dtype=torch.bfloat16)  # library choice
+    assert torch.equal(C0.view(torch.int16), A.spmm(rp, ci, vd, Bd).to(torch.bfloat16).view(torch.int16))
+    with pytest.raises(ValueError):
+        A.spmm(rp, ci, vd, Bd, C=torch.empty_like(C0), beta=1.0, out_dtype=torch.bfloat16)
+    A.sync_status()

@@ -139,3 +139,20 @@ def test_fused_bad_permutation_is_flagged_and_skipped():
         A.sync_status()
     assert e.value.status == 1  # AS_ERR_INVALID_VALUE
     assert dA.cpu().tolist() == [64.0, -1.0, 64.0]
+
+
+@pytest.mark.parametrize("N_", [48, 256])
+def test_fused_bf16_output(oracle, N_):
+    a = _skewed(20 + N_)
+    rp, ci, v = csr_dev(a)
+    vd = v.to(torch.bfloat16)
+    Bd = to_dev(S.dense_uniform((a.n_cols, N_), 21)).to(torch.bfloat16)
+    Fd = to_dev(S.dense_uniform((a.n_rows, N_), 22)).to(torch.bfloat16)
+    perm = to_dev(np.random.default_rng(N_).permutation(a.colind.size).astype(np.int32))
+    for var, name, *_ in _fusable(torch.bfloat16, N_):
+        C, dA = A.spmm_sddmm(rp, ci, vd, Bd, Fd, perm=perm, variant=var)
+        C16, dA16 = A.spmm_sddmm(rp, ci, vd, Bd, Fd, perm=perm, variant=var,
+                                 out_dtype=torch.bfloat16)
+        assert torch.equal(C16.view(torch.int16), C.to(torch.bfloat16).view(torch.int16)), name
+        assert torch.equal(dA16, dA), name
+    A.sync_status()
