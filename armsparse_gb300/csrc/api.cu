@@ -154,6 +154,8 @@ as_status as_ctx_sync_status(as_ctx *c, void *stream) {
                                  "(an earlier call on this context failed part-way)");
     if (h & kFlagBadPerm)
         return fail(AS_ERR_INVALID_VALUE, "permutation entry out of range seen on the device");
+    if (h & kFlagBadLabel)
+        return fail(AS_ERR_INVALID_VALUE, "class label out of range seen on the device");
     if (h & (kFlagBadRowptr | kFlagBadColind))
         return fail(AS_ERR_INVALID_CSR,
                     (h & kFlagBadRowptr) ? "malformed rowptr seen on the device"
@@ -289,6 +291,26 @@ as_status as_spmm_sddmm_csr_bf16(as_ctx *c, int M, int K, int N, int nnz, const 
                                  void *stream) {
     return spmm_sddmm_common("as_spmm_sddmm_csr_bf16", 1, c, M, K, N, nnz, rowptr, colind, val,
                              B, ldb, C, ldc, beta, F, ldf, perm, dA, variant, stream);
+}
+
+as_status as_softmax_xent_bf16(as_ctx *c, int n, int C, const uint16_t *S, long lds,
+                               const int64_t *labels, float *loss, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_softmax_xent_bf16: ctx is NULL");
+    if (n < 0 || lds < C || !loss || (n > 0 && (!S || !labels)))
+        return fail(AS_ERR_INVALID_VALUE, "as_softmax_xent_bf16: bad arguments");
+    DeviceGuard g(c->device);
+    return xent_fwd_launch(c, n, C, S, lds, labels, loss, static_cast<cudaStream_t>(stream));
+}
+
+as_status as_softmax_xent_bwd_bf16(as_ctx *c, int n, int C, const uint16_t *S, long lds,
+                                   const int64_t *labels, const float *gscale, uint16_t *G,
+                                   long ldg, int width, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_softmax_xent_bwd_bf16: ctx is NULL");
+    if (n < 0 || lds < C || ldg < width || !gscale || (n > 0 && (!S || !labels || !G)))
+        return fail(AS_ERR_INVALID_VALUE, "as_softmax_xent_bwd_bf16: bad arguments");
+    DeviceGuard g(c->device);
+    return xent_bwd_launch(c, n, C, S, lds, labels, gscale, G, ldg, width,
+                           static_cast<cudaStream_t>(stream));
 }
 
 as_status as_spmm_csr_reduce_f32(as_ctx *c, int M, int K, int N, int nnz, const int *rowptr,

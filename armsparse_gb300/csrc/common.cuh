@@ -16,6 +16,7 @@ enum : unsigned {
     kFlagTimeout = 4u,
     kFlagLongList = 8u,  // the long-row list was not empty at the start of a call (internal)
     kFlagBadPerm = 16u,  // a permutation entry out of [0, nnz) (the write was skipped)
+    kFlagBadLabel = 32u,  // a class label out of [0, C) (that row counts 0 in the loss)
 };
 
 __device__ __forceinline__ void flag(unsigned *status, unsigned bit) {

@@ -401,6 +401,24 @@ def nll_mean(logp: torch.Tensor, y: torch.Tensor) -> torch.Tensor:
     return -logp.gather(1, y.unsqueeze(1)).mean()
 
 
+class SoftmaxXent(torch.autograd.Function):
+    """Mean softmax cross-entropy of bf16 class scores (n x width, the first n_classes columns
+    are the classes): the model's log_softmax then F.nll_loss (gcn_custom.py:90, :122-126) as
+    one forward and one backward kernel of this library (``sparse.softmax_xent``). The
+    gradient is bf16, zero in the padding columns."""
+
+    @staticmethod
+    def forward(ctx, scores, labels, n_classes: int):
+        ctx.save_for_backward(scores, labels)
+        ctx.n_classes = n_classes
+        return S.softmax_xent(scores, labels, n_classes)
+
+    @staticmethod
+    def backward(ctx, g):
+        scores, labels = ctx.saved_tensors
+        return S.softmax_xent_grad(scores, labels, ctx.n_classes, g.float().contiguous()), None, None
+
+
 def make_optimizer(model: Net, capturable: bool = False):
     """Adam, lr 0.01, weight decay 5e-4 on the first layer only (gcn_custom.py:116-119).
     capturable keeps Adam's step count on the device so that the step can be recorded in a

@@ -433,6 +433,42 @@ def spmm_sddmm(rowptr, colind, val, B, F, perm=None, C=None, beta: float = 0.0,
     return C, dA
 
 
+def softmax_xent(scores, labels, n_classes: int):
+    """Mean softmax cross-entropy of bf16 class scores (the first n_classes columns of each row;
+    further columns are padding) against int64 labels: F.nll_loss(F.log_softmax(x), y) in one
+    pass, summed in a fixed order. Returns a 0-dim fp32 tensor on the device."""
+    dev = _dev(scores, labels)
+    if scores.dtype != torch.bfloat16 or scores.dim() != 2 or scores.stride(1) != 1:
+        raise ValueError("scores must be bfloat16 (n, width) row-major")
+    _need(labels, torch.int64, "labels", 1)
+    n = scores.shape[0]
+    if labels.numel() != n or not 1 <= n_classes <= scores.shape[1]:
+        raise ValueError("labels must have one entry per row; 1 <= n_classes <= width")
+    loss = torch.empty((), dtype=torch.float32, device=dev)
+    ctx = N.context(dev.index)
+    N.check(N.load().as_softmax_xent_bf16(ctx.handle, n, n_classes, _ptr(scores),
+                                          scores.stride(0) if n > 1 else scores.shape[1],
+                                          _ptr(labels), _ptr(loss), _stream(dev)),
+            "as_softmax_xent_bf16")
+    return loss
+
+
+def softmax_xent_grad(scores, labels, n_classes: int, gscale):
+    """d(softmax_xent)/d(scores) times the device scalar gscale, bf16, zero in the padding
+    columns."""
+    dev = _dev(scores, labels, gscale)
+    n, width = scores.shape
+    _need(gscale, torch.float32, "gscale")
+    G = torch.empty((n, width), dtype=torch.bfloat16, device=dev)
+    ctx = N.context(dev.index)
+    N.check(N.load().as_softmax_xent_bwd_bf16(ctx.handle, n, n_classes, _ptr(scores),
+                                              scores.stride(0) if n > 1 else width,
+                                              _ptr(labels), _ptr(gscale), _ptr(G), width, width,
+                                              _stream(dev)),
+            "as_softmax_xent_bwd_bf16")
+    return G
+
+
 def to_bf16(x: torch.Tensor) -> torch.Tensor:
     """fp32 -> bf16 (round to nearest even) with this library's kernel."""
     dev = _dev(x)

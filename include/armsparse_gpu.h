@@ -155,6 +155,22 @@ as_status as_spmm_csr_bf16_out16(as_ctx *ctx, int M, int K, int N, int nnz, cons
                                  const int *colind, const uint16_t *val, const uint16_t *B,
                                  long ldb, uint16_t *C, long ldc, int variant, void *stream);
 
+/* ---- Softmax cross-entropy of class scores (the GCN's loss) ----------------------------------
+ * n rows of C class scores in bf16 (row stride lds >= C elements), int64 labels in [0, C).
+ * as_softmax_xent_bf16: loss[0] = (1/n) sum_i (logsumexp(S_i) - S_i[label_i]) -- the mean
+ * negative log-likelihood of log_softmax (gcn/pytorch-custom/gcn_custom.py:90, :122-126), FP32,
+ * summed in a fixed order (deterministic). A label out of range counts 0 and is reported by
+ * as_ctx_sync_status (AS_ERR_INVALID_VALUE).
+ * as_softmax_xent_bwd_bf16: its gradient times the device scalar gscale[0] (the upstream
+ * gradient, read on the device): G[i, j] = bf16((softmax(S_i)_j - [j == label_i]) * gscale / n)
+ * for j < C and 0 for C <= j < width (padding columns); ldg >= width.
+ * 1 <= C <= width <= 64. */
+as_status as_softmax_xent_bf16(as_ctx *ctx, int n, int C, const uint16_t *S, long lds,
+                               const int64_t *labels, float *loss, void *stream);
+as_status as_softmax_xent_bwd_bf16(as_ctx *ctx, int n, int C, const uint16_t *S, long lds,
+                                   const int64_t *labels, const float *gscale, uint16_t *G,
+                                   long ldg, int width, void *stream);
+
 /* ---- SpMM and SDDMM in one pass over A ---------------------------------------------------------
  * C = A*B + beta*C (A: M x K CSR, B: K x N, C: M x N, as as_spmm_csr_*) and, for every entry e
  * of A (row r, column k):  dA[perm ? perm[e] : e] = <B[k, :], F[r, :]>  (F: M x N, ldf >= N,

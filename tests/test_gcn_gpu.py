@@ -209,3 +209,34 @@ def test_sparse_features_product(oracle):
     step = gcn.CapturedEpoch(m2, o2, feats, g, y, train, warmup=3)
     sparse = [float(step()) for _ in range(5)]
     assert np.allclose(sparse, dense[3:], rtol=0, atol=1e-4), (sparse, dense[3:])
+
+
+@pytest.mark.parametrize("n,width,C", [(5000, 48, 47), (3001, 47, 47), (1, 8, 3), (700, 64, 64)])
+def test_softmax_xent_matches_torch(n, width, C):
+    """The fused loss kernels against log_softmax + nll_loss in fp32 on the same bf16 scores:
+    the loss to fp32 rounding, the gradient to bf16 rounding, zero padding columns, the
+    upstream gradient applied on the device, deterministic."""
+    gen = torch.Generator(device=dev()).manual_seed(n + width)
+    s = (torch.randn(n, width, generator=gen, device=dev()) * 3).to(torch.bfloat16)
+    y = torch.randint(0, C, (n,), generator=gen, device=dev())
+    x = s.detach().clone().requires_grad_(True)
+    ref = torch.nn.functional.nll_loss(torch.nn.functional.log_softmax(x[:, :C].float(), 1), y)
+    (3.0 * ref).backward()
+    si = s.detach().clone().requires_grad_(True)
+    loss = gcn.SoftmaxXent.apply(si, y, C)
+    (3.0 * loss).backward()
+    assert abs(loss.item() - ref.item()) <= 2e-6 * max(1.0, abs(ref.item()))
+    g, gr = si.grad.float(), x.grad.float()
+    assert torch.allclose(g[:, :C], gr[:, :C], rtol=8e-3, atol=1e-9)
+    assert (g[:, C:] == 0).all()
+    assert torch.equal(gcn.SoftmaxXent.apply(s, y, C), gcn.SoftmaxXent.apply(s, y, C))
+    A.sync_status()
+
+
+def test_softmax_xent_bad_label_is_flagged():
+    s = torch.zeros(4, 8, dtype=torch.bfloat16, device=dev())
+    y = torch.tensor([0, 1, 9, 2], device=dev())
+    gcn.SoftmaxXent.apply(s, y, 8)
+    with pytest.raises(A.NativeError) as e:
+        A.sync_status()
+    assert e.value.status == 1
