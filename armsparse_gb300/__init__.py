@@ -7,13 +7,13 @@ a layer with trainable edge values), a deterministic CSR->CSC transpose (optiona
 CSR position of each entry), the sum/max aggregations and the sparse x sparse -> dense product, behind the C ABI in include/armsparse_gpu.h. The
 ops need the CUDA library built in-tree and a GPU; there is no CPU fallback.
 """
-from .sparse import (csr2csc, csr2csc_perm, csr_to_vcsr4, dense_to_csr, sddmm, sddmm_coo,
+from .sparse import (csr2csc, csr2csc_perm, csr_to_vcsr4, dense_to_csr, gather, sddmm, sddmm_coo,
                      spgemm_dense, spmm, spmm_default_variant, spmm_reduce, spmm_sddmm,
                      spmm_variant_supported, spmm_variants, spmv, spmv_vcsr4, sync_status,
                      to_bf16, validate_csr)
 from ._native import NativeError, Context, context
 
 __all__ = ["spmm", "spmm_reduce", "spmm_sddmm", "spgemm_dense", "spmv", "spmv_vcsr4", "sddmm",
-           "sddmm_coo", "csr2csc", "csr2csc_perm", "csr_to_vcsr4", "dense_to_csr", "validate_csr", "sync_status", "to_bf16",
+           "sddmm_coo", "csr2csc", "csr2csc_perm", "gather", "csr_to_vcsr4", "dense_to_csr", "validate_csr", "sync_status", "to_bf16",
            "spmm_variants", "spmm_default_variant", "spmm_variant_supported", "NativeError",
            "Context", "context"]

@@ -31,8 +31,8 @@ SIGNATURES = {
     "as_csr_validate": (_I, [_P, _I, _I, _I, _P, _P, _I, _P]),
     "as_spmm_csr_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _F, _I, _P]),
     "as_spmm_csr_bf16": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _F, _I, _P]),
-    "as_softmax_xent_bf16": (_I, [_P, _I, _I, _P, _L, _P, _P, _P]),
-    "as_softmax_xent_bwd_bf16": (_I, [_P, _I, _I, _P, _L, _P, _P, _P, _L, _I, _P]),
+    "as_softmax_xent_bf16": (_I, [_P, _I, _I, _P, _L, _P, _P, _P, _P]),
+    "as_softmax_xent_bwd_bf16": (_I, [_P, _I, _I, _P, _L, _P, _P, _P, _P, _L, _I, _P]),
     "as_spmm_csr_bf16_out16": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _I, _P]),
     "as_spmm_sddmm_csr_bf16_out16": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P,
                                          _L, _P, _P, _I, _P]),
@@ -57,6 +57,7 @@ SIGNATURES = {
     "as_sddmm_bf16x3_variant_count": (_I, []),
     "as_sddmm_coo_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P, _P]),
     "as_csr2csc": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
+    "as_gather_f32": (_I, [_P, _L, _L, _P, _P, _P, _P]),
     "as_csr2csc_perm": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _P]),
     "as_spmm_csr_f64": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, ctypes.c_double, _P]),
     "as_sddmm_csr_f64": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P, _P]),

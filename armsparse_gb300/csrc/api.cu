@@ -294,22 +294,22 @@ as_status as_spmm_sddmm_csr_bf16(as_ctx *c, int M, int K, int N, int nnz, const 
 }
 
 as_status as_softmax_xent_bf16(as_ctx *c, int n, int C, const uint16_t *S, long lds,
-                               const int64_t *labels, float *loss, void *stream) {
+                               const int64_t *labels, float *lse, float *loss, void *stream) {
     if (!c) return fail(AS_ERR_INVALID_VALUE, "as_softmax_xent_bf16: ctx is NULL");
-    if (n < 0 || lds < C || !loss || (n > 0 && (!S || !labels)))
+    if (n < 0 || lds < C || !loss || (n > 0 && (!S || !labels || !lse)))
         return fail(AS_ERR_INVALID_VALUE, "as_softmax_xent_bf16: bad arguments");
     DeviceGuard g(c->device);
-    return xent_fwd_launch(c, n, C, S, lds, labels, loss, static_cast<cudaStream_t>(stream));
+    return xent_fwd_launch(c, n, C, S, lds, labels, lse, loss, static_cast<cudaStream_t>(stream));
 }
 
 as_status as_softmax_xent_bwd_bf16(as_ctx *c, int n, int C, const uint16_t *S, long lds,
-                                   const int64_t *labels, const float *gscale, uint16_t *G,
-                                   long ldg, int width, void *stream) {
+                                   const int64_t *labels, const float *lse, const float *gscale,
+                                   uint16_t *G, long ldg, int width, void *stream) {
     if (!c) return fail(AS_ERR_INVALID_VALUE, "as_softmax_xent_bwd_bf16: ctx is NULL");
-    if (n < 0 || lds < C || ldg < width || !gscale || (n > 0 && (!S || !labels || !G)))
+    if (n < 0 || lds < C || ldg < width || !gscale || (n > 0 && (!S || !labels || !lse || !G)))
         return fail(AS_ERR_INVALID_VALUE, "as_softmax_xent_bwd_bf16: bad arguments");
     DeviceGuard g(c->device);
-    return xent_bwd_launch(c, n, C, S, lds, labels, gscale, G, ldg, width,
+    return xent_bwd_launch(c, n, C, S, lds, labels, lse, gscale, G, ldg, width,
                            static_cast<cudaStream_t>(stream));
 }
 
@@ -586,6 +586,15 @@ as_status as_csr_to_vcsr4_fill(as_ctx *c, int M, int nnz, const int *rowptr, con
     DeviceGuard g(c->device);
     return csr_to_vcsr4_fill_launch(c, M, nnz, rowptr, colind, val, vrowptr, vcolind, vval,
                                     static_cast<cudaStream_t>(stream));
+}
+
+as_status as_gather_f32(as_ctx *c, long n, long n_src, const float *src, const int *idx,
+                        float *dst, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_gather_f32: ctx is NULL");
+    if (n < 0 || n_src < 0 || (n > 0 && (!src || !idx || !dst)))
+        return fail(AS_ERR_INVALID_VALUE, "as_gather_f32: bad arguments");
+    DeviceGuard g(c->device);
+    return gather_f32_launch(c, n, n_src, src, idx, dst, static_cast<cudaStream_t>(stream));
 }
 
 as_status as_f32_to_bf16(as_ctx *c, long n, const float *src, uint16_t *dst, void *stream) {

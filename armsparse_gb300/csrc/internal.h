@@ -61,12 +61,15 @@ as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cu
 as_status spmm_sddmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a,
                             const SddmmFuse &f, cudaStream_t s);
 as_status spmm_reduce_launch(as_ctx *ctx, int op, const SpmmArgs &a, cudaStream_t s);
+// dst[i] = src[idx[i]] (transpose.cu); idx and dst 16-byte aligned.
+as_status gather_f32_launch(as_ctx *ctx, long n, long n_src, const float *src, const int *idx,
+                            float *dst, cudaStream_t s);
 // Softmax cross-entropy of bf16 class scores (xent.cu).
 as_status xent_fwd_launch(as_ctx *ctx, int n, int C, const uint16_t *S, long lds,
-                          const int64_t *labels, float *loss, cudaStream_t s);
+                          const int64_t *labels, float *lse, float *loss, cudaStream_t s);
 as_status xent_bwd_launch(as_ctx *ctx, int n, int C, const uint16_t *S, long lds,
-                          const int64_t *labels, const float *gscale, uint16_t *G, long ldg,
-                          int width, cudaStream_t s);
+                          const int64_t *labels, const float *lse, const float *gscale,
+                          uint16_t *G, long ldg, int width, cudaStream_t s);
 as_status spmm_nnz_launch(as_ctx *ctx, int dtype, int vb, int group, int cpl, int chunk,
                           int unroll, const SpmmArgs &a, cudaStream_t s,
                           const SddmmFuse *fuse = nullptr);

@@ -284,6 +284,7 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
 }
 
 constexpr int kShortSpan = 8;  // rows over at most this many chunks: the one-pass fix-up
+constexpr int kFixBatch = 16;  // partial loads in flight per thread on a long span
 
 template <int VW>
 struct Lanes;  // VW consecutive fp32 columns of a carry row, one load
@@ -305,7 +306,8 @@ struct Lanes<1> {
 //    the chunks' partials together and adds them in chunk order.
 //  - A longer row: the threads split into R consecutive runs of the row's chunks times groups
 //    of VW columns (R = threads / column groups, so all threads load at once); each sums its
-//    run in chunk order with 8 loads in flight, and the runs are then added in run order.
+//    run in chunk order with kFixBatch loads in flight, and the runs are then added in run
+//    order.
 // Both orders are fixed by the row's span and N, so the result is deterministic. (One row of a
 // power-law graph can span thousands of chunks: this CTA is then the fix-up's critical path.)
 template <int VW>
@@ -353,10 +355,10 @@ spmm_nnz_fixup(int M, int N, int nnz, int CH, const int *__restrict__ rowptr,
         for (int j = 0; j < VW; ++j) acc[j] = 0.0f;
         if (run < R) {
             const long b0 = c_first + n * run / R, b1 = c_first + n * (run + 1) / R;
-            for (long cc = b0; cc < b1; cc += 8) {
-                float v[8][VW];
+            for (long cc = b0; cc < b1; cc += kFixBatch) {
+                float v[kFixBatch][VW];
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
+                for (int i = 0; i < kFixBatch; ++i) {
                     if (cc + i < b1) {
                         Lanes<VW>::load(carry + row_of(cc + i) + col, v[i]);
                     } else {
@@ -365,7 +367,7 @@ spmm_nnz_fixup(int M, int N, int nnz, int CH, const int *__restrict__ rowptr,
                     }
                 }
 #pragma unroll
-                for (int i = 0; i < 8; ++i)
+                for (int i = 0; i < kFixBatch; ++i)
                     if (cc + i < b1)
 #pragma unroll
                         for (int j = 0; j < VW; ++j) acc[j] += v[i][j];

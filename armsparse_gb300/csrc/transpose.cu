@@ -444,6 +444,51 @@ as_status csr_validate_launch(as_ctx *ctx, int n_rows, int n_cols, int nnz, cons
     return check_cuda(cudaGetLastError(), "csr_validate launch");
 }
 
+// dst[i] = src[idx[i]] for i < n (idx in [0, n_src); others flag and give 0): values moved
+// between orderings of the same entries, e.g. from CSC to CSR order through the inverse of
+// as_csr2csc_perm's permutation. Four outputs per thread: one 16-byte index load, four
+// independent gathers, one 16-byte store.
+__global__ void __launch_bounds__(kThreads)
+gather_f32(long n, long n_src, const float *__restrict__ src, const int *__restrict__ idx,
+           float *__restrict__ dst, unsigned *status) {
+    const long stride = static_cast<long>(gridDim.x) * kThreads * 4;
+    for (long i = (static_cast<long>(blockIdx.x) * kThreads + threadIdx.x) * 4; i < n; i += stride) {
+        if (i + 4 <= n) {
+            const int4 k = __ldcs(reinterpret_cast<const int4 *>(idx + i));
+            const int kk[4] = {k.x, k.y, k.z, k.w};
+            float v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const bool ok = static_cast<unsigned long>(static_cast<unsigned>(kk[q])) <
+                                static_cast<unsigned long>(n_src);
+                if (!ok) flag(status, kFlagBadPerm);
+                v[q] = ok ? __ldg(src + kk[q]) : 0.0f;
+            }
+            __stcs(reinterpret_cast<float4 *>(dst + i), make_float4(v[0], v[1], v[2], v[3]));
+        } else {
+            for (long j = i; j < n; ++j) {
+                const int k = idx[j];
+                const bool ok = k >= 0 && static_cast<long>(k) < n_src;
+                if (!ok) flag(status, kFlagBadPerm);
+                dst[j] = ok ? src[k] : 0.0f;
+            }
+        }
+    }
+}
+
+as_status gather_f32_launch(as_ctx *ctx, long n, long n_src, const float *src, const int *idx,
+                            float *dst, cudaStream_t s) {
+    if (n == 0) return AS_OK;
+    if (reinterpret_cast<uintptr_t>(idx) % 16 || reinterpret_cast<uintptr_t>(dst) % 16)
+        return fail(AS_ERR_UNSUPPORTED, "gather_f32: idx and dst must be 16-byte aligned");
+    long blocks = ceil_div(ceil_div(n, 4), kThreads);
+    if (blocks > static_cast<long>(ctx->sms) * 16) blocks = static_cast<long>(ctx->sms) * 16;
+    gather_f32<<<static_cast<unsigned>(blocks), kThreads, 0, s>>>(n, n_src, src, idx, dst,
+                                                                  ctx->d_status);
+    ctx->launches++;
+    return check_cuda(cudaGetLastError(), "gather_f32 launch");
+}
+
 as_status f32_to_bf16_launch(as_ctx *ctx, long n, const float *src, uint16_t *dst,
                              cudaStream_t s) {
     long blocks = ceil_div(n, kThreads);

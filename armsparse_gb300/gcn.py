@@ -45,31 +45,32 @@ class SPMMFunction(torch.autograd.Function):
     """out = A * feat, A given as CSR (rowptr, colind, edge_weight_csr) and as CSC (colptr, rowind,
     edge_weight_csc). Same ``apply`` signature as the reference (op.py:9), plus an optional
     ``variants`` pair (kernel variant ids for the forward CSR product and the backward CSC
-    product; 0 = library choice) and an optional ``perm`` (the CSR position of each CSC entry,
-    ``Graph.perm``): given it, a backward that needs both gradients runs them in one pass over
-    the CSC (``sparse.spmm_sddmm``: dOut's rows gathered once for dB and dA)."""
+    product; 0 = library choice) and an optional ``csc_pos`` (the CSC position of each CSR
+    entry, ``Graph.csc_pos``): given it, a backward that needs both gradients runs them in one
+    pass over the CSC (``sparse.spmm_sddmm``: dOut's rows gathered once for dB and dA), the
+    edge gradient written in CSC order and then gathered into CSR order."""
 
     @staticmethod
     def forward(ctx, rowptr, colind, colptr, rowind, feat, edge_weight_csr=None,
-                edge_weight_csc=None, variants=None, perm=None):
+                edge_weight_csc=None, variants=None, csc_pos=None):
         if edge_weight_csr is None:
             raise ValueError("SPMMFunction needs edge values (pass ones for an unweighted graph)")
         fwd_v, bwd_v = variants if variants is not None else (0, 0)
         out = _spmm(rowptr, colind, edge_weight_csr, feat, fwd_v)
         ctx.save_for_backward(rowptr, colind, colptr, rowind, feat, edge_weight_csr,
-                              edge_weight_csc, perm)
+                              edge_weight_csc, csc_pos)
         ctx.bwd_variant = bwd_v
         return out
 
     @staticmethod
     def backward(ctx, grad_out):
-        rowptr, colind, colptr, rowind, feat, w_csr, w_csc, perm = ctx.saved_tensors
+        rowptr, colind, colptr, rowind, feat, w_csr, w_csc, csc_pos = ctx.saved_tensors
         grad_feat = grad_w = None
         g = grad_out.contiguous()
-        if (perm is not None and ctx.needs_input_grad[4] and ctx.needs_input_grad[5] and
+        if (csc_pos is not None and ctx.needs_input_grad[4] and ctx.needs_input_grad[5] and
                 w_csc is not None and w_csc.numel() == w_csr.numel() and g.dtype == feat.dtype
                 and g.dtype in (torch.float32, torch.bfloat16)):
-            fused = _spmm_sddmm_t(colptr, rowind, w_csc, g, feat.contiguous(), perm,
+            fused = _spmm_sddmm_t(colptr, rowind, w_csc, g, feat.contiguous(), csc_pos,
                                   ctx.bwd_variant)
             if fused is not None:
                 grad_feat, grad_w = fused
@@ -92,17 +93,19 @@ class SPMMFunction(torch.autograd.Function):
         return None, None, None, None, grad_feat, grad_w, None, None, None
 
 
-def _spmm_sddmm_t(colptr, rowind, w_csc, g, feat, perm, variant):
+def _spmm_sddmm_t(colptr, rowind, w_csc, g, feat, csc_pos, variant):
     """(A^T g, dA) in one pass over the CSC, or None when the backward variant cannot carry
-    the SDDMM (not an nnz-split kernel, or its column tile is narrower than the width)."""
+    the SDDMM (not an nnz-split kernel, or its column tile is narrower than the width). dA is
+    written in CSC order (coalesced) and gathered into CSR order: measured faster than
+    scattering it through the permutation inside the pass."""
     try:
-        C, dA = S.spmm_sddmm(colptr, rowind, w_csc.to(g.dtype), g, feat, perm=perm,
-                             variant=variant, out_dtype=g.dtype)
+        C, dA_csc = S.spmm_sddmm(colptr, rowind, w_csc.to(g.dtype), g, feat, variant=variant,
+                                 out_dtype=g.dtype)
     except NativeError as e:
         if e.status != 3:  # AS_ERR_UNSUPPORTED: run the two products separately
             raise
         return None
-    return C, dA
+    return C, S.gather(dA_csc, csc_pos)
 
 
 def _time_pick(rowptr, colind, values, n_in: int, width: int, dtype) -> int:
@@ -121,7 +124,7 @@ def _nnz_tile(name: str, esz: int) -> int:
     return (f["v"] // esz) * f["g"] * f["c"]
 
 
-def _time_pick_fused(colptr, rowind, values, perm, n_out: int, width: int, dtype) -> int:
+def _time_pick_fused(colptr, rowind, values, n_out: int, width: int, dtype) -> int:
     """The fastest nnz-split kernel for the fused backward pass (A^T dOut with the edge-value
     SDDMM, ``sparse.spmm_sddmm``) on these arrays, timed once; 0 when none can carry it."""
     from . import tuner
@@ -138,7 +141,7 @@ def _time_pick_fused(colptr, rowind, values, perm, n_out: int, width: int, dtype
         if (not name.startswith("nnzsplit") or _nnz_tile(name, esz) < width
                 or not S.spmm_variant_supported(v, width, dtype)):
             continue
-        fn = lambda: S.spmm_sddmm(colptr, rowind, vals, g, f, perm=perm, C=C, variant=v, dA=dA,
+        fn = lambda: S.spmm_sddmm(colptr, rowind, vals, g, f, C=C, variant=v, dA=dA,
                                   out_dtype=dtype)
         try:
             fn()
@@ -188,6 +191,7 @@ class Graph:
         self.n_cols = self.n_rows if n_cols is None else n_cols
         self._csc = None
         self._perm = None
+        self._csc_pos = None
         self.selector = None  # a selector.Selector: per-width kernel choice (None = library choice)
         self._plans = {}
 
@@ -203,9 +207,20 @@ class Graph:
     @property
     def perm(self) -> torch.Tensor:
         """The CSR position of each CSC entry (int32): ``values[perm]`` is the values in CSC
-        order for any values, and the fused backward writes the edge gradient through it."""
+        order for any values."""
         self.csc
         return self._perm
+
+    @property
+    def csc_pos(self) -> torch.Tensor:
+        """The CSC position of each CSR entry (int32, the inverse of ``perm``): the fused
+        backward gathers the edge gradient from CSC into CSR order through it."""
+        if self._csc_pos is None:
+            p = self.perm
+            pos = torch.empty_like(p)
+            pos[p.long()] = torch.arange(p.numel(), device=p.device, dtype=torch.int32)
+            self._csc_pos = pos
+        return self._csc_pos
 
     def plan(self, N: int, dtype=torch.float32, fused: bool = False):
         """(forward, backward) kernel variants for dense width N: the learned selector's pick,
@@ -219,7 +234,7 @@ class Graph:
             key = (N, dtype, "fused")
             if key not in self._plans:
                 colptr, rowind, vcsc = self.csc
-                bwd = _time_pick_fused(colptr, rowind, vcsc, self.perm, self.n_rows, N, dtype)
+                bwd = _time_pick_fused(colptr, rowind, vcsc, self.n_rows, N, dtype)
                 self._plans[key] = (self.plan(N, dtype)[0], bwd or self.plan(N, dtype)[1])
             return self._plans[key]
         key = (N, dtype)
@@ -242,7 +257,7 @@ class Graph:
     def aggregate(self, feat: torch.Tensor) -> torch.Tensor:
         colptr, rowind, vcsc = self.csc
         return SPMMFunction.apply(self.rowptr, self.colind, colptr, rowind, feat, self.values,
-                                  vcsc, self.plan(feat.shape[1], feat.dtype), self.perm)
+                                  vcsc, self.plan(feat.shape[1], feat.dtype), self.csc_pos)
 
 
 class _FeatureProduct(torch.autograd.Function):
@@ -409,14 +424,16 @@ class SoftmaxXent(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, scores, labels, n_classes: int):
-        ctx.save_for_backward(scores, labels)
+        loss, lse = S.softmax_xent(scores, labels, n_classes)
+        ctx.save_for_backward(scores, labels, lse)
         ctx.n_classes = n_classes
-        return S.softmax_xent(scores, labels, n_classes)
+        return loss
 
     @staticmethod
     def backward(ctx, g):
-        scores, labels = ctx.saved_tensors
-        return S.softmax_xent_grad(scores, labels, ctx.n_classes, g.float().contiguous()), None, None
+        scores, labels, lse = ctx.saved_tensors
+        G = S.softmax_xent_grad(scores, labels, ctx.n_classes, lse, g.float().contiguous())
+        return G, None, None
 
 
 def make_optimizer(model: Net, capturable: bool = False):

@@ -373,6 +373,23 @@ def csr2csc_perm(rowptr, colind, n_cols: int):
     return colptr, rowind, perm
 
 
+def gather(src, idx, out=None):
+    """out[i] = src[idx[i]] (fp32 values, int32 indices) with this library's kernel."""
+    dev = _dev(src, idx, out)
+    _need(src, torch.float32, "src", 1)
+    _need(idx, torch.int32, "idx", 1)
+    if out is None:
+        out = torch.empty(idx.numel(), dtype=torch.float32, device=dev)
+    else:
+        _need(out, torch.float32, "out", 1)
+        if out.numel() != idx.numel():
+            raise ValueError("out and idx lengths differ")
+    ctx = N.context(dev.index)
+    N.check(N.load().as_gather_f32(ctx.handle, idx.numel(), src.numel(), _ptr(src), _ptr(idx),
+                                   _ptr(out), _stream(dev)), "as_gather_f32")
+    return out
+
+
 def spmm_sddmm(rowptr, colind, val, B, F, perm=None, C=None, beta: float = 0.0,
                variant: int = 0, dA=None, out_dtype: torch.dtype = torch.float32):
     """(C, dA): C = A*B + beta*C as ``spmm`` and, in the same pass over A, the SDDMM
@@ -434,9 +451,10 @@ def spmm_sddmm(rowptr, colind, val, B, F, perm=None, C=None, beta: float = 0.0,
 
 
 def softmax_xent(scores, labels, n_classes: int):
-    """Mean softmax cross-entropy of bf16 class scores (the first n_classes columns of each row;
-    further columns are padding) against int64 labels: F.nll_loss(F.log_softmax(x), y) in one
-    pass, summed in a fixed order. Returns a 0-dim fp32 tensor on the device."""
+    """(loss, lse): the mean softmax cross-entropy of bf16 class scores (the first n_classes
+    columns of each row; further columns are padding) against int64 labels --
+    F.nll_loss(F.log_softmax(x), y) in one pass, summed in a fixed order -- as a 0-dim fp32
+    tensor, and each row's logsumexp (fp32, for ``softmax_xent_grad``)."""
     dev = _dev(scores, labels)
     if scores.dtype != torch.bfloat16 or scores.dim() != 2 or scores.stride(1) != 1:
         raise ValueError("scores must be bfloat16 (n, width) row-major")
@@ -445,26 +463,28 @@ def softmax_xent(scores, labels, n_classes: int):
     if labels.numel() != n or not 1 <= n_classes <= scores.shape[1]:
         raise ValueError("labels must have one entry per row; 1 <= n_classes <= width")
     loss = torch.empty((), dtype=torch.float32, device=dev)
+    lse = torch.empty(n, dtype=torch.float32, device=dev)
     ctx = N.context(dev.index)
     N.check(N.load().as_softmax_xent_bf16(ctx.handle, n, n_classes, _ptr(scores),
                                           scores.stride(0) if n > 1 else scores.shape[1],
-                                          _ptr(labels), _ptr(loss), _stream(dev)),
+                                          _ptr(labels), _ptr(lse), _ptr(loss), _stream(dev)),
             "as_softmax_xent_bf16")
-    return loss
+    return loss, lse
 
 
-def softmax_xent_grad(scores, labels, n_classes: int, gscale):
+def softmax_xent_grad(scores, labels, n_classes: int, lse, gscale):
     """d(softmax_xent)/d(scores) times the device scalar gscale, bf16, zero in the padding
-    columns."""
-    dev = _dev(scores, labels, gscale)
+    columns; lse from ``softmax_xent``."""
+    dev = _dev(scores, labels, lse, gscale)
     n, width = scores.shape
+    _need(lse, torch.float32, "lse", 1)
     _need(gscale, torch.float32, "gscale")
     G = torch.empty((n, width), dtype=torch.bfloat16, device=dev)
     ctx = N.context(dev.index)
     N.check(N.load().as_softmax_xent_bwd_bf16(ctx.handle, n, n_classes, _ptr(scores),
                                               scores.stride(0) if n > 1 else width,
-                                              _ptr(labels), _ptr(gscale), _ptr(G), width, width,
-                                              _stream(dev)),
+                                              _ptr(labels), _ptr(lse), _ptr(gscale), _ptr(G),
+                                              width, width, _stream(dev)),
             "as_softmax_xent_bwd_bf16")
     return G
 

@@ -674,7 +674,7 @@ class GcnLarge(Workload):
         colptr, rowind, vcsc = g.csc
         h = x @ W.to(dtype)  # bf16 layers: a bf16 tensor-core GEMM with fp32 accumulation
         return gcn.SPMMFunction.apply(g.rowptr, g.colind, colptr, rowind, h, self.w, vcsc, plan,
-                                      g.perm if fuse else None)
+                                      g.csc_pos if fuse else None)
 
     def _step(self, g, dtype, tuned):
         import torch

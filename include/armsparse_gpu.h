@@ -157,19 +157,20 @@ as_status as_spmm_csr_bf16_out16(as_ctx *ctx, int M, int K, int N, int nnz, cons
 
 /* ---- Softmax cross-entropy of class scores (the GCN's loss) ----------------------------------
  * n rows of C class scores in bf16 (row stride lds >= C elements), int64 labels in [0, C).
- * as_softmax_xent_bf16: loss[0] = (1/n) sum_i (logsumexp(S_i) - S_i[label_i]) -- the mean
- * negative log-likelihood of log_softmax (gcn/pytorch-custom/gcn_custom.py:90, :122-126), FP32,
- * summed in a fixed order (deterministic). A label out of range counts 0 and is reported by
+ * as_softmax_xent_bf16: loss[0] = (1/n) sum_i (lse_i - S_i[label_i]) with lse_i =
+ * logsumexp(S_i) (also written, n floats, for the backward) -- the mean negative
+ * log-likelihood of log_softmax (gcn/pytorch-custom/gcn_custom.py:90, :122-126), FP32, summed
+ * in a fixed order (deterministic). A label out of range counts 0 and is reported by
  * as_ctx_sync_status (AS_ERR_INVALID_VALUE).
  * as_softmax_xent_bwd_bf16: its gradient times the device scalar gscale[0] (the upstream
- * gradient, read on the device): G[i, j] = bf16((softmax(S_i)_j - [j == label_i]) * gscale / n)
- * for j < C and 0 for C <= j < width (padding columns); ldg >= width.
+ * gradient, read on the device): G[i, j] = bf16((exp(S_ij - lse_i) - [j == label_i]) * gscale
+ * / n) for j < C and 0 for C <= j < width (padding columns); ldg >= width.
  * 1 <= C <= width <= 64. */
 as_status as_softmax_xent_bf16(as_ctx *ctx, int n, int C, const uint16_t *S, long lds,
-                               const int64_t *labels, float *loss, void *stream);
+                               const int64_t *labels, float *lse, float *loss, void *stream);
 as_status as_softmax_xent_bwd_bf16(as_ctx *ctx, int n, int C, const uint16_t *S, long lds,
-                                   const int64_t *labels, const float *gscale, uint16_t *G,
-                                   long ldg, int width, void *stream);
+                                   const int64_t *labels, const float *lse, const float *gscale,
+                                   uint16_t *G, long ldg, int width, void *stream);
 
 /* ---- SpMM and SDDMM in one pass over A ---------------------------------------------------------
  * C = A*B + beta*C (A: M x K CSR, B: K x N, C: M x N, as as_spmm_csr_*) and, for every entry e
@@ -232,6 +233,13 @@ as_status as_csr2csc(as_ctx *ctx, int M, int N, int nnz, const int *rowptr, cons
  * walking the CSC. */
 as_status as_csr2csc_perm(as_ctx *ctx, int M, int N, int nnz, const int *rowptr,
                           const int *colind, int *colptr, int *rowind, int *perm, void *stream);
+
+/* dst[i] = src[idx[i]] for i < n: values moved between two orders of the same entries, e.g.
+ * an SDDMM result from CSC to CSR order with the inverse of as_csr2csc_perm's permutation. An
+ * index outside [0, n_src) gives 0 and is reported by as_ctx_sync_status. idx and dst are
+ * 16-byte aligned. */
+as_status as_gather_f32(as_ctx *ctx, long n, long n_src, const float *src, const int *idx,
+                        float *dst, void *stream);
 
 /* ---- CSR -> CSC without allocating ------------------------------------------------------------
  * No counterpart in the reference. Some callers of this library cannot allocate device

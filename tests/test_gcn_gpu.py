@@ -112,8 +112,8 @@ def test_edge_value_gradient_is_sddmm(oracle):
 
 
 def test_fused_backward_matches_separate(oracle):
-    """With Graph.perm, a backward needing both gradients runs one pass over the CSC: dB is the
-    unfused nnz-split SpMM's bits, dA the slices-order oracle's bits placed through perm."""
+    """With Graph.csc_pos, a backward needing both gradients runs one pass over the CSC: dB is
+    the unfused nnz-split SpMM's bits, dA the slices-order oracle's bits in CSR order."""
     a = S.powerlaw_graph(3000, 20000, seed=5)
     G = gcn.Graph.from_csr(a, dev())
     colptr, rowind, vcsc = G.csc
@@ -124,17 +124,19 @@ def test_fused_backward_matches_separate(oracle):
     f0 = torch.randn(3000, 24, generator=gen, device=dev())
     gy = torch.randn(3000, 24, generator=gen, device=dev())
     grads = []
-    for perm in (G.perm, None):
+    for pos in (G.csc_pos, None):
         w = G.values.clone().requires_grad_(True)
         f = f0.clone().requires_grad_(True)
         out = gcn.SPMMFunction.apply(G.rowptr, G.colind, colptr, rowind, f, w, vcsc, (0, var),
-                                     perm)
+                                     pos)
         out.backward(gy)
         grads.append((f.grad, w.grad))
     assert torch.equal(grads[0][0], grads[1][0])
     ref = oracle.sddmm_f32_slices(cp, ri, f0.cpu().numpy(), gy.cpu().numpy(), 32, 1, 1,
                                   perm=G.perm.cpu().numpy())
     assert np.array_equal(bits(grads[0][1]), bits(ref))
+    pos = G.csc_pos.cpu().numpy()
+    assert np.array_equal(G.perm.cpu().numpy()[pos], np.arange(pos.size))
     r64, ab = oracle.sddmm_f64(a.rowptr, a.colind, gy.cpu().numpy(), f0.cpu().numpy())
     assert oracle.scaled_err(grads[1][1].cpu().numpy(), r64, ab).max() < 1e-5
 

@@ -156,3 +156,20 @@ def test_fused_bf16_output(oracle, N_):
         assert torch.equal(C16.view(torch.int16), C.to(torch.bfloat16).view(torch.int16)), name
         assert torch.equal(dA16, dA), name
     A.sync_status()
+
+
+@pytest.mark.parametrize("n", [0, 3, 4, 1001, 100000])
+def test_gather(n):
+    gen = torch.Generator(device=dev()).manual_seed(n)
+    src = torch.randn(max(n, 1) * 2, generator=gen, device=dev())
+    idx = torch.randint(0, src.numel(), (n,), generator=gen, device=dev(), dtype=torch.int32)
+    assert torch.equal(A.gather(src, idx), src[idx.long()])
+    A.sync_status()
+    if n >= 4:
+        bad = idx.clone()
+        bad[n // 2] = src.numel()  # out of range: that output is 0 and the call is flagged
+        out = A.gather(src, bad)
+        assert out[n // 2].item() == 0.0
+        with pytest.raises(N.NativeError) as e:
+            A.sync_status()
+        assert e.value.status == 1
