@@ -8,10 +8,10 @@
 //   SDMM.cpp:90-114). A row that crosses a chunk boundary leaves its segment's partial sum in
 //   a carry slot: slot 0 when the segment starts the chunk, slot 1 otherwise.
 // Pass 2 (spmm_nnz_fixup): for every row that ends inside chunk c after starting in an earlier
-//   chunk, a CTA of chunk c adds that row's partial sums (in chunk order when the row spans at
-//   most 8 chunks, else 8 runs of chunks and then the runs in order; then beta * C): a fixed
-//   order, so the result is deterministic run to run (not bit-identical to a single chain for
-//   those rows).
+//   chunk, chunk c's warp (a whole CTA for a long span) adds that row's partial sums (in chunk
+//   order when the row spans at most 8 chunks, else runs of chunks and then the runs in order;
+//   then beta * C): a fixed order, so the result is deterministic run to run (not
+//   bit-identical to a single chain for those rows).
 // Pass 3 (spmm_empty_rows): rows without entries get beta * C (zeros when beta == 0).
 //
 // Fused form (FUSE): pass 1 also computes, for every entry e (row r, column k), the dot product
@@ -284,7 +284,7 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
 }
 
 constexpr int kShortSpan = 8;  // rows over at most this many chunks: the one-pass fix-up
-constexpr int kFixBatch = 16;  // partial loads in flight per thread on a long span
+constexpr int kFixBatch = 8;  // partial loads in flight per thread on a long span (16 measured slower)
 
 template <int VW>
 struct Lanes;  // VW consecutive fp32 columns of a carry row, one load
@@ -300,94 +300,127 @@ struct Lanes<1> {
     __device__ static void load(const float *p, float *v) { v[0] = *p; }
 };
 
-// Rows that end in chunk c after starting in an earlier chunk: sum their partials. A CTA
-// takes one such chunk.
-//  - A row over at most kShortSpan chunks (nearly all of them): one thread per column loads
-//    the chunks' partials together and adds them in chunk order.
-//  - A longer row: the threads split into R consecutive runs of the row's chunks times groups
-//    of VW columns (R = threads / column groups, so all threads load at once); each sums its
-//    run in chunk order with kFixBatch loads in flight, and the runs are then added in run
-//    order.
+// Rows that end in chunk c after starting in an earlier chunk: sum their partials. A CTA takes
+// kFixChunks consecutive chunks, one per warp.
+//  - A row over at most kShortSpan chunks (nearly all of them): the chunk's warp alone, each
+//    lane VW columns at a time, the chunks' partials loaded together and added in chunk order.
+//  - A longer row, afterwards with the whole CTA: the threads split into R consecutive runs of
+//    the row's chunks times groups of VW columns (R = threads / column groups, so all threads
+//    load at once); each sums its run in chunk order, kFixBatch loads in flight, and the runs
+//    are then added in run order.
 // Both orders are fixed by the row's span and N, so the result is deterministic. (One row of a
-// power-law graph can span thousands of chunks: this CTA is then the fix-up's critical path.)
+// power-law graph can span thousands of chunks: that CTA is the fix-up's critical path. One
+// CTA per chunk made the many short fix-ups cost more in CTA launches than in loads.)
+constexpr int kFixChunks = kThreads / 32;
+
+template <int VW>
+__device__ __forceinline__ void store_out(float *C, uint16_t *C16, long off, float beta, float v) {
+    if (C16)
+        C16[off] = f32_to_bf16(v);
+    else
+        C[off] = beta == 0.0f ? v : fmaf(beta, C[off], v);
+}
+
 template <int VW>
 __global__ void __launch_bounds__(kThreads)
-spmm_nnz_fixup(int M, int N, int nnz, int CH, const int *__restrict__ rowptr,
+spmm_nnz_fixup(int M, int N, long nchunks, int CH, const int *__restrict__ rowptr,
                const float *__restrict__ carry, const int *__restrict__ fix,
                float *__restrict__ C, long ldc, float beta, uint16_t *__restrict__ C16) {
     __shared__ float part[kThreads * VW];
-    const long chunk = blockIdx.x;
-    const int r = fix[chunk];  // recorded by the first pass; -1: nothing ends here
-    if (r < 0 || r >= M) return;  // the same for the whole CTA
-    const int rs = __ldg(rowptr + r);
-    const long c_first = rs / CH;
-    const long n = chunk - c_first + 1;
+    __shared__ int long_rows[kFixChunks];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // the chunk's row to fix (-1: none) and its span
+    auto span = [&](long chunk, int &r, int &rs, long &c_first, long &n) {
+        r = chunk < nchunks ? fix[chunk] : -1;  // recorded by the first pass
+        if (r < 0 || r >= M) {
+            r = -1;
+            return;
+        }
+        rs = __ldg(rowptr + r);
+        c_first = rs / CH;
+        n = chunk - c_first + 1;
+    };
     // slot 1 holds the first chunk's partial when the row starts inside that chunk
-    auto row_of = [&](long cc) {
+    auto row_of = [&](long cc, long c_first, int rs) {
         return (2 * cc + ((cc == c_first && static_cast<long>(rs) != cc * CH) ? 1 : 0)) *
                static_cast<long>(N);
     };
-    if (n <= kShortSpan) {
-        for (int col = threadIdx.x; col < N; col += kThreads) {
-            float v[kShortSpan];
+    {
+        int r, rs = 0;
+        long c_first = 0, n = 0;
+        span(static_cast<long>(blockIdx.x) * kFixChunks + warp, r, rs, c_first, n);
+        if (lane == 0) long_rows[warp] = r >= 0 && n > kShortSpan;
+        if (r >= 0 && n <= kShortSpan) {
+            for (int col = lane * VW; col < N; col += 32 * VW) {
+                float v[kShortSpan][VW];
 #pragma unroll
-            for (int i = 0; i < kShortSpan; ++i)
-                v[i] = i < n ? carry[row_of(c_first + i) + col] : 0.0f;
-            float acc = v[0];
-#pragma unroll
-            for (int i = 1; i < kShortSpan; ++i)
-                if (i < n) acc += v[i];
-            if (C16)
-                C16[r * ldc + col] = f32_to_bf16(acc);
-            else
-                C[r * ldc + col] = beta == 0.0f ? acc : fmaf(beta, C[r * ldc + col], acc);
-        }
-        return;
-    }
-    const int ncg = N / VW;  // column groups (the launcher guarantees N % VW == 0)
-    for (int cg0 = 0; cg0 < ncg; cg0 += kThreads) {
-        const int cgs = min(kThreads, ncg - cg0);
-        const int R = kThreads / cgs;
-        const int run = threadIdx.x / cgs, gi = threadIdx.x % cgs;
-        const int col = (cg0 + gi) * VW;
-        float acc[VW];
-#pragma unroll
-        for (int j = 0; j < VW; ++j) acc[j] = 0.0f;
-        if (run < R) {
-            const long b0 = c_first + n * run / R, b1 = c_first + n * (run + 1) / R;
-            for (long cc = b0; cc < b1; cc += kFixBatch) {
-                float v[kFixBatch][VW];
-#pragma unroll
-                for (int i = 0; i < kFixBatch; ++i) {
-                    if (cc + i < b1) {
-                        Lanes<VW>::load(carry + row_of(cc + i) + col, v[i]);
+                for (int i = 0; i < kShortSpan; ++i) {
+                    if (i < n) {
+                        Lanes<VW>::load(carry + row_of(c_first + i, c_first, rs) + col, v[i]);
                     } else {
 #pragma unroll
                         for (int j = 0; j < VW; ++j) v[i][j] = 0.0f;
                     }
                 }
 #pragma unroll
-                for (int i = 0; i < kFixBatch; ++i)
-                    if (cc + i < b1)
+                for (int j = 0; j < VW; ++j) {
+                    float acc = v[0][j];
 #pragma unroll
-                        for (int j = 0; j < VW; ++j) acc[j] += v[i][j];
-            }
-#pragma unroll
-            for (int j = 0; j < VW; ++j) part[(run * cgs + gi) * VW + j] = acc[j];
-        }
-        __syncthreads();
-        if (run == 0) {
-#pragma unroll
-            for (int j = 0; j < VW; ++j) {
-                float t = part[gi * VW + j];
-                for (int q = 1; q < R; ++q) t += part[(q * cgs + gi) * VW + j];
-                if (C16)
-                    C16[r * ldc + col + j] = f32_to_bf16(t);
-                else
-                    C[r * ldc + col + j] = beta == 0.0f ? t : fmaf(beta, C[r * ldc + col + j], t);
+                    for (int i = 1; i < kShortSpan; ++i)
+                        if (i < n) acc += v[i][j];
+                    store_out<VW>(C, C16, r * ldc + col + j, beta, acc);
+                }
             }
         }
-        __syncthreads();  // part[] is reused by the next column block
+    }
+    __syncthreads();
+    for (int w = 0; w < kFixChunks; ++w) {
+        if (!long_rows[w]) continue;  // shared: the same for the whole CTA
+        int r, rs = 0;
+        long c_first = 0, n = 0;
+        span(static_cast<long>(blockIdx.x) * kFixChunks + w, r, rs, c_first, n);
+        const int ncg = N / VW;  // column groups (the launcher guarantees N % VW == 0)
+        for (int cg0 = 0; cg0 < ncg; cg0 += kThreads) {
+            const int cgs = min(kThreads, ncg - cg0);
+            const int R = kThreads / cgs;
+            const int run = threadIdx.x / cgs, gi = threadIdx.x % cgs;
+            const int col = (cg0 + gi) * VW;
+            float acc[VW];
+#pragma unroll
+            for (int j = 0; j < VW; ++j) acc[j] = 0.0f;
+            if (run < R) {
+                const long b0 = c_first + n * run / R, b1 = c_first + n * (run + 1) / R;
+                for (long cc = b0; cc < b1; cc += kFixBatch) {
+                    float v[kFixBatch][VW];
+#pragma unroll
+                    for (int i = 0; i < kFixBatch; ++i) {
+                        if (cc + i < b1) {
+                            Lanes<VW>::load(carry + row_of(cc + i, c_first, rs) + col, v[i]);
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < VW; ++j) v[i][j] = 0.0f;
+                        }
+                    }
+#pragma unroll
+                    for (int i = 0; i < kFixBatch; ++i)
+                        if (cc + i < b1)
+#pragma unroll
+                            for (int j = 0; j < VW; ++j) acc[j] += v[i][j];
+                }
+#pragma unroll
+                for (int j = 0; j < VW; ++j) part[(run * cgs + gi) * VW + j] = acc[j];
+            }
+            __syncthreads();
+            if (run == 0) {
+#pragma unroll
+                for (int j = 0; j < VW; ++j) {
+                    float t = part[gi * VW + j];
+                    for (int q = 1; q < R; ++q) t += part[(q * cgs + gi) * VW + j];
+                    store_out<VW>(C, C16, r * ldc + col + j, beta, t);
+                }
+            }
+            __syncthreads();  // part[] is reused by the next column block or row
+        }
     }
 }
 
@@ -443,12 +476,12 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, const SddmmFuse *fu, cu
             static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, carry, fix, a.status,
             FUSE ? static_cast<const T *>(fu->F) : nullptr, FUSE ? fu->ldf : 0,
             FUSE ? fu->perm : nullptr, FUSE ? fu->dA : nullptr, a.C16);
-        dim3 g2(static_cast<unsigned>(nchunks));
+        dim3 g2(static_cast<unsigned>(ceil_div(nchunks, kFixChunks)));
         if (a.N % 4 == 0)  // carry rows are 16-byte aligned: whole-vector loads
-            spmm_nnz_fixup<4><<<g2, kThreads, 0, s>>>(a.M, a.N, a.nnz, CH, a.rowptr, carry, fix,
+            spmm_nnz_fixup<4><<<g2, kThreads, 0, s>>>(a.M, a.N, nchunks, CH, a.rowptr, carry, fix,
                                                       a.C, a.ldc, a.beta, a.C16);
         else
-            spmm_nnz_fixup<1><<<g2, kThreads, 0, s>>>(a.M, a.N, a.nnz, CH, a.rowptr, carry, fix,
+            spmm_nnz_fixup<1><<<g2, kThreads, 0, s>>>(a.M, a.N, nchunks, CH, a.rowptr, carry, fix,
                                                       a.C, a.ldc, a.beta, a.C16);
         ctx->launches += 2;
     }
