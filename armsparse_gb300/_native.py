@@ -33,7 +33,7 @@ SIGNATURES = {
     "as_spmm_csr_bf16": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _F, _I, _P]),
     "as_softmax_xent_bf16": (_I, [_P, _I, _I, _P, _L, _P, _P, _P, _P]),
     "as_softmax_xent_bwd_bf16": (_I, [_P, _I, _I, _P, _L, _P, _P, _P, _P, _L, _I, _P]),
-    "as_spmm_csr_bf16_out16": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _I, _P]),
+    "as_spmm_csr_bf16_out16": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _I, _I, _P]),
     "as_spmm_sddmm_csr_bf16_out16": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _P,
                                          _L, _P, _P, _I, _P]),
     "as_spmm_sddmm_csr_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _F, _P, _L,

@@ -190,7 +190,8 @@ as_status as_csr_validate(as_ctx *c, int n_rows, int n_cols, int nnz, const int 
 static as_status spmm_common(const char *fn, int dtype, as_ctx *c, int M, int K, int N, int nnz,
                              const int *rowptr, const int *colind, const void *val,
                              const void *B, long ldb, float *C, long ldc, float beta,
-                             int variant, void *stream, uint16_t *C16 = nullptr) {
+                             int variant, void *stream, uint16_t *C16 = nullptr,
+                             bool relu = false) {
     if (!c) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": ctx is NULL");
     as_status st = check_csr_args(fn, M, K, nnz, rowptr, colind, val, true);
     if (st != AS_OK) return st;
@@ -203,7 +204,7 @@ static as_status spmm_common(const char *fn, int dtype, as_ctx *c, int M, int K,
     if (variant < 0 || variant > spmm_variant_count(dtype))
         return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": unknown variant");
     DeviceGuard g(c->device);
-    SpmmArgs a{M, K, N, nnz, rowptr, colind, val, B, ldb, C, ldc, beta, c->d_status, C16};
+    SpmmArgs a{M, K, N, nnz, rowptr, colind, val, B, ldb, C, ldc, beta, c->d_status, C16, relu};
     if (variant == 0)
         variant = spmm_default_variant(dtype, M, K, N, nnz, ldb, ldc, B,
                                        C16 ? static_cast<const void *>(C16) : C);
@@ -261,9 +262,10 @@ static as_status spmm_sddmm_common(const char *fn, int dtype, as_ctx *c, int M, 
 
 as_status as_spmm_csr_bf16_out16(as_ctx *c, int M, int K, int N, int nnz, const int *rowptr,
                                  const int *colind, const uint16_t *val, const uint16_t *B,
-                                 long ldb, uint16_t *C, long ldc, int variant, void *stream) {
+                                 long ldb, uint16_t *C, long ldc, int relu, int variant,
+                                 void *stream) {
     return spmm_common("as_spmm_csr_bf16_out16", 1, c, M, K, N, nnz, rowptr, colind, val, B, ldb,
-                       nullptr, ldc, 0.0f, variant, stream, C);
+                       nullptr, ldc, 0.0f, variant, stream, C, relu != 0);
 }
 
 as_status as_spmm_sddmm_csr_bf16_out16(as_ctx *c, int M, int K, int N, int nnz,

@@ -42,6 +42,9 @@ __device__ __forceinline__ uint16_t f32_to_bf16(float f) {
     return static_cast<uint16_t>(u >> 16);
 }
 
+// A ReLU applied at an output store when `relu` is set (negative -> 0; -0 and NaN pass).
+__device__ __forceinline__ float relu_if(float v, bool relu) { return relu && v < 0.0f ? 0.0f : v; }
+
 // Valid row range [lo, hi) of row r; rows with malformed pointers become empty and flag.
 __device__ __forceinline__ void row_range(const int *rowptr, int r, int nnz, unsigned *status,
                                           int &lo, int &hi) {

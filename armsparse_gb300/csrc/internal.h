@@ -46,6 +46,7 @@ struct SpmmArgs {
     unsigned *status;
     uint16_t *C16 = nullptr;  // given: the output goes here in bf16 (ldc elements per row) and C
                               // is unused; beta must be 0
+    bool relu = false;        // with C16: negative outputs are stored as 0
 };
 // The SDDMM fused into an nnz-split SpMM pass: dA[perm ? perm[e] : e] = <B[k, :], F[r, :]> for
 // each entry e (row r, column k) of A; F is M x N (leading dimension ldf, A's value type).

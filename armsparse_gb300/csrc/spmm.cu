@@ -62,7 +62,7 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
               const int *__restrict__ colind, const T *__restrict__ val,
               const T *__restrict__ B, long ldb, float *__restrict__ C, long ldc, float beta,
               unsigned *status, int long_thresh, int *long_list, unsigned *long_count,
-              uint16_t *__restrict__ C16) {
+              uint16_t *__restrict__ C16, bool relu) {
     using V = Vec<T, VB>;
     constexpr int E = V::E;
     constexpr int TILE = GROUP * E * CPL;
@@ -196,7 +196,7 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         const int c = tile0 + (j * GROUP + g) * E;
         if (c < N) {
             if (C16)
-                store_bf16<E>(C16 + row * ldc + c, acc[j]);
+                store_bf16<E>(C16 + row * ldc + c, acc[j], relu);
             else
                 store_c<E>(crow + c, acc[j]);
         }
@@ -256,7 +256,7 @@ void launch_one(const SpmmArgs &a, const LongRows &lr, cudaStream_t s) {
     spmm_rowsplit<T, VB, G, CPL, U><<<grid, kThreads, 0, s>>>(
         a.M, a.K, a.N, a.nnz, a.rowptr, a.colind, static_cast<const T *>(a.val),
         static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, a.status, lr.thresh, lr.list,
-        lr.count, a.C16);
+        lr.count, a.C16, a.relu);
 }
 
 template <typename T, int VB, int G>

@@ -60,7 +60,8 @@ __global__ void __launch_bounds__(kThreads)
 spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
           const int *__restrict__ colind, const T *__restrict__ val, const T *__restrict__ B,
           long ldb, float *__restrict__ C, long ldc, float beta, unsigned *status,
-          const int *__restrict__ list, unsigned *counters, uint16_t *__restrict__ C16) {
+          const int *__restrict__ list, unsigned *counters, uint16_t *__restrict__ C16,
+          bool relu) {
     constexpr int W = kSliceBytes / static_cast<int>(sizeof(T));  // columns per slice
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned char *ring = smem;  // [kStages][kStage][kSliceBytes]
@@ -229,7 +230,7 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         cp_async_wait<0>();
         if (tid < w) {
             if (C16)
-                C16[static_cast<long>(r) * ldc + slice0 + tid] = f32_to_bf16(acc);
+                C16[static_cast<long>(r) * ldc + slice0 + tid] = f32_to_bf16(relu_if(acc, relu));
             else
                 crow[tid] = acc;
         }
@@ -281,7 +282,7 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, const int *list, cudaStream_t s
     cudaError_t e = cudaLaunchKernelEx(&cfg, k, a.M, a.K, a.N, a.nnz, a.rowptr, a.colind,
                                        static_cast<const T *>(a.val), static_cast<const T *>(a.B),
                                        a.ldb, a.C, a.ldc, a.beta, a.status, list, ctx->d_long,
-                                       a.C16);
+                                       a.C16, a.relu);
     ctx->launches++;
     return check_cuda(e != cudaSuccess ? e : cudaGetLastError(), "spmm long rows launch");
 }

@@ -100,7 +100,7 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
               const T *__restrict__ B, long ldb, float *__restrict__ C, long ldc, float beta,
               float *__restrict__ carry, int *__restrict__ fix, unsigned *status,
               const T *__restrict__ F, long ldf, const int *__restrict__ perm,
-              float *__restrict__ dA, uint16_t *__restrict__ C16) {
+              float *__restrict__ dA, uint16_t *__restrict__ C16, bool relu) {
     using V = Vec<T, VB>;
     constexpr int E = V::E;
     constexpr int TILE = GROUP * E * CPL;
@@ -270,7 +270,7 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
             const int cc = tile0 + (j * GROUP + g) * E;
             if (cc < N) {
                 if (!split && C16) {
-                    store_bf16<E>(C16 + r * ldc + cc, acc[j]);
+                    store_bf16<E>(C16 + r * ldc + cc, acc[j], relu);
                 } else {
 #pragma unroll
                     for (int i = 0; i < E; ++i) dst[cc + i] = acc[j][i];
@@ -314,9 +314,10 @@ struct Lanes<1> {
 constexpr int kFixChunks = kThreads / 32;
 
 template <int VW>
-__device__ __forceinline__ void store_out(float *C, uint16_t *C16, long off, float beta, float v) {
+__device__ __forceinline__ void store_out(float *C, uint16_t *C16, long off, float beta, float v,
+                                          bool relu) {
     if (C16)
-        C16[off] = f32_to_bf16(v);
+        C16[off] = f32_to_bf16(relu_if(v, relu));
     else
         C[off] = beta == 0.0f ? v : fmaf(beta, C[off], v);
 }
@@ -325,7 +326,8 @@ template <int VW>
 __global__ void __launch_bounds__(kThreads)
 spmm_nnz_fixup(int M, int N, long nchunks, int CH, const int *__restrict__ rowptr,
                const float *__restrict__ carry, const int *__restrict__ fix,
-               float *__restrict__ C, long ldc, float beta, uint16_t *__restrict__ C16) {
+               float *__restrict__ C, long ldc, float beta, uint16_t *__restrict__ C16,
+               bool relu) {
     __shared__ float part[kThreads * VW];
     __shared__ int long_rows[kFixChunks];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -368,7 +370,7 @@ spmm_nnz_fixup(int M, int N, long nchunks, int CH, const int *__restrict__ rowpt
 #pragma unroll
                     for (int i = 1; i < kShortSpan; ++i)
                         if (i < n) acc += v[i][j];
-                    store_out<VW>(C, C16, r * ldc + col + j, beta, acc);
+                    store_out<VW>(C, C16, r * ldc + col + j, beta, acc, relu);
                 }
             }
         }
@@ -416,7 +418,7 @@ spmm_nnz_fixup(int M, int N, long nchunks, int CH, const int *__restrict__ rowpt
                 for (int j = 0; j < VW; ++j) {
                     float t = part[gi * VW + j];
                     for (int q = 1; q < R; ++q) t += part[(q * cgs + gi) * VW + j];
-                    store_out<VW>(C, C16, r * ldc + col + j, beta, t);
+                    store_out<VW>(C, C16, r * ldc + col + j, beta, t, relu);
                 }
             }
             __syncthreads();  // part[] is reused by the next column block or row
@@ -475,14 +477,14 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, const SddmmFuse *fu, cu
             a.M, a.K, a.N, a.nnz, CH, a.rowptr, a.colind, static_cast<const T *>(a.val),
             static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, carry, fix, a.status,
             FUSE ? static_cast<const T *>(fu->F) : nullptr, FUSE ? fu->ldf : 0,
-            FUSE ? fu->perm : nullptr, FUSE ? fu->dA : nullptr, a.C16);
+            FUSE ? fu->perm : nullptr, FUSE ? fu->dA : nullptr, a.C16, a.relu);
         dim3 g2(static_cast<unsigned>(ceil_div(nchunks, kFixChunks)));
         if (a.N % 4 == 0)  // carry rows are 16-byte aligned: whole-vector loads
             spmm_nnz_fixup<4><<<g2, kThreads, 0, s>>>(a.M, a.N, nchunks, CH, a.rowptr, carry, fix,
-                                                      a.C, a.ldc, a.beta, a.C16);
+                                                      a.C, a.ldc, a.beta, a.C16, a.relu);
         else
             spmm_nnz_fixup<1><<<g2, kThreads, 0, s>>>(a.M, a.N, nchunks, CH, a.rowptr, carry, fix,
-                                                      a.C, a.ldc, a.beta, a.C16);
+                                                      a.C, a.ldc, a.beta, a.C16, a.relu);
         ctx->launches += 2;
     }
     spmm_empty_rows<<<static_cast<unsigned>(ceil_div(a.M, kThreads)), kThreads, 0, s>>>(

@@ -160,12 +160,16 @@ struct Vec<uint16_t, 2> {
 };
 
 // v[0..E) rounded to bf16 (nearest even) and stored at p, in whole vectors of up to 16 bytes
-// (p aligned to min(2E, 16) bytes): the bf16 form of an fp32 output row segment.
+// (p aligned to min(2E, 16) bytes): the bf16 form of an fp32 output row segment. relu: negative
+// values are stored as 0 first (the epilogue of a layer followed by a ReLU).
 __device__ __forceinline__ unsigned pack_bf16x2(float lo, float hi) {
     return static_cast<unsigned>(f32_to_bf16(lo)) | (static_cast<unsigned>(f32_to_bf16(hi)) << 16);
 }
 template <int E>
-__device__ __forceinline__ void store_bf16(uint16_t *p, const float *v) {
+__device__ __forceinline__ void store_bf16(uint16_t *p, const float *vin, bool relu = false) {
+    float v[E];
+#pragma unroll
+    for (int i = 0; i < E; ++i) v[i] = relu_if(vin[i], relu);
     if constexpr (E % 8 == 0) {
 #pragma unroll
         for (int i = 0; i < E; i += 8)

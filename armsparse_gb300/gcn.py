@@ -26,19 +26,21 @@ from . import sparse as S
 from ._native import NativeError
 
 
-def _spmm(rowptr, colind, values, feat, variant=0):
-    """A * feat for fp32 / fp64 / bf16 features (bf16 values and features are multiplied in fp32;
-    the result is returned in the feature dtype)."""
+def _spmm(rowptr, colind, values, feat, variant=0, relu=False):
+    """A * feat (relu(A * feat) when relu) for fp32 / fp64 / bf16 features (bf16 values and
+    features are multiplied in fp32; the result is returned in the feature dtype)."""
     if feat.dtype == torch.bfloat16:
         vb = values.to(torch.bfloat16)
-        try:  # C written in bf16 by the kernel
+        try:  # C written in bf16 by the kernel, the ReLU applied in the same store
             return S.spmm(rowptr, colind, vb, feat.contiguous(), variant=variant,
-                          out_dtype=torch.bfloat16)
+                          out_dtype=torch.bfloat16, relu=relu)
         except NativeError as e:
             if e.status != 3:  # AS_ERR_UNSUPPORTED (a bulk variant): fp32 C, then rounded
                 raise
-        return S.spmm(rowptr, colind, vb, feat.contiguous(), variant=variant).to(torch.bfloat16)
-    return S.spmm(rowptr, colind, values.to(feat.dtype), feat.contiguous(), variant=variant)
+        out = S.spmm(rowptr, colind, vb, feat.contiguous(), variant=variant).to(torch.bfloat16)
+    else:
+        out = S.spmm(rowptr, colind, values.to(feat.dtype), feat.contiguous(), variant=variant)
+    return F.relu(out) if relu else out
 
 
 class SPMMFunction(torch.autograd.Function):
@@ -48,25 +50,29 @@ class SPMMFunction(torch.autograd.Function):
     product; 0 = library choice) and an optional ``csc_pos`` (the CSC position of each CSR
     entry, ``Graph.csc_pos``): given it, a backward that needs both gradients runs them in one
     pass over the CSC (``sparse.spmm_sddmm``: dOut's rows gathered once for dB and dA), the
-    edge gradient written in CSC order and then gathered into CSR order."""
+    edge gradient written in CSC order and then gathered into CSR order. ``relu=True`` returns
+    relu(A * feat), the ReLU applied in the SpMM's store (its backward masks the gradient by
+    the output, as F.relu's does)."""
 
     @staticmethod
     def forward(ctx, rowptr, colind, colptr, rowind, feat, edge_weight_csr=None,
-                edge_weight_csc=None, variants=None, csc_pos=None):
+                edge_weight_csc=None, variants=None, csc_pos=None, relu=False):
         if edge_weight_csr is None:
             raise ValueError("SPMMFunction needs edge values (pass ones for an unweighted graph)")
         fwd_v, bwd_v = variants if variants is not None else (0, 0)
-        out = _spmm(rowptr, colind, edge_weight_csr, feat, fwd_v)
+        out = _spmm(rowptr, colind, edge_weight_csr, feat, fwd_v, relu)
         ctx.save_for_backward(rowptr, colind, colptr, rowind, feat, edge_weight_csr,
-                              edge_weight_csc, csc_pos)
+                              edge_weight_csc, csc_pos, out if relu else None)
         ctx.bwd_variant = bwd_v
         return out
 
     @staticmethod
     def backward(ctx, grad_out):
-        rowptr, colind, colptr, rowind, feat, w_csr, w_csc, csc_pos = ctx.saved_tensors
+        rowptr, colind, colptr, rowind, feat, w_csr, w_csc, csc_pos, out = ctx.saved_tensors
         grad_feat = grad_w = None
         g = grad_out.contiguous()
+        if out is not None:  # the ReLU's backward: zero where the output was clamped
+            g = torch.ops.aten.threshold_backward(g, out, 0)
         if (csc_pos is not None and ctx.needs_input_grad[4] and ctx.needs_input_grad[5] and
                 w_csc is not None and w_csc.numel() == w_csr.numel() and g.dtype == feat.dtype
                 and g.dtype in (torch.float32, torch.bfloat16)):
@@ -75,7 +81,7 @@ class SPMMFunction(torch.autograd.Function):
             if fused is not None:
                 grad_feat, grad_w = fused
                 return (None, None, None, None, grad_feat, grad_w.to(w_csr.dtype), None, None,
-                        None)
+                        None, None)
         if ctx.needs_input_grad[4]:
             if w_csc is None or w_csc.numel() != w_csr.numel():
                 raise RuntimeError("backward of SPMMFunction needs the edge values in CSC order "
@@ -90,7 +96,7 @@ class SPMMFunction(torch.autograd.Function):
                 gf = g if g.dtype in (torch.float32, torch.float64) else g.float()
                 ff = feat if feat.dtype == gf.dtype else feat.to(gf.dtype)
                 grad_w = S.sddmm(rowptr, colind, gf, ff.contiguous()).to(w_csr.dtype)
-        return None, None, None, None, grad_feat, grad_w, None, None, None
+        return None, None, None, None, grad_feat, grad_w, None, None, None, None
 
 
 def _spmm_sddmm_t(colptr, rowind, w_csc, g, feat, csc_pos, variant):

@@ -65,11 +65,12 @@ def sync_status(device=None) -> None:
 
 
 def spmm(rowptr, colind, val, B, C=None, beta: float = 0.0, variant: int = 0,
-         out_dtype: torch.dtype = torch.float32):
+         out_dtype: torch.dtype = torch.float32, relu: bool = False):
     """C = A*B + beta*C with A (M x K) in CSR. fp32 val/B -> fp32 path (bit-identical to the
     reference's rowBaseSpmm3 for row-split variants); bf16 val/B -> bf16 storage with fp32
     accumulation. C is fp32 (allocated when None); with bf16 val/B, out_dtype=torch.bfloat16
-    gives C in bf16 (the fp32 result rounded to nearest even, beta 0) without a second pass."""
+    gives C in bf16 (the fp32 result rounded to nearest even, beta 0) without a second pass,
+    and relu=True (bf16 output only) stores max(C, 0) in the same pass."""
     dev = _dev(rowptr, colind, val, B, C)
     M, nnz = _csr(rowptr, colind)
     if B.dim() != 2:
@@ -80,9 +81,11 @@ def spmm(rowptr, colind, val, B, C=None, beta: float = 0.0, variant: int = 0,
     ldb = B.stride(0) if K > 1 else Ncols
     if out_dtype == torch.bfloat16:
         return _spmm_bf16_out16(rowptr, colind, val, B, C, beta, variant, dev, M, nnz, K, Ncols,
-                                ldb)
+                                ldb, relu)
     if out_dtype != torch.float32:
         raise TypeError("out_dtype must be float32 or bfloat16")
+    if relu:
+        raise ValueError("relu is an epilogue of the bf16 output")
     if val.dtype == torch.float32 and B.dtype == torch.float32:
         fn, dname = N.load().as_spmm_csr_f32, "as_spmm_csr_f32"
     elif val.dtype == torch.bfloat16 and B.dtype == torch.bfloat16:
@@ -108,7 +111,8 @@ def spmm(rowptr, colind, val, B, C=None, beta: float = 0.0, variant: int = 0,
     return C
 
 
-def _spmm_bf16_out16(rowptr, colind, val, B, C, beta, variant, dev, M, nnz, K, Ncols, ldb):
+def _spmm_bf16_out16(rowptr, colind, val, B, C, beta, variant, dev, M, nnz, K, Ncols, ldb,
+                     relu=False):
     if val.dtype != torch.bfloat16 or B.dtype != torch.bfloat16:
         raise TypeError("a bf16 output needs bf16 val and B")
     if beta != 0.0:
@@ -124,7 +128,7 @@ def _spmm_bf16_out16(rowptr, colind, val, B, C, beta, variant, dev, M, nnz, K, N
     ctx = N.context(dev.index)
     N.check(N.load().as_spmm_csr_bf16_out16(ctx.handle, M, K, Ncols, nnz, _ptr(rowptr),
                                             _ptr(colind), _ptr(val), _ptr(B), ldb, _ptr(C), ldc,
-                                            int(variant), _stream(dev)),
+                                            int(bool(relu)), int(variant), _stream(dev)),
             "as_spmm_csr_bf16_out16")
     return C
 

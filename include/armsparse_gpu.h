@@ -149,11 +149,13 @@ as_status as_sddmm_csr_bf16(as_ctx *ctx, int M, int N, int K, int nnz, const int
 /* bf16 output: C = bf16(A*B) (round to nearest even from the FP32 sums; beta is 0), so a bf16
  * pipeline stores half the bytes and needs no conversion pass. The FP32 sums are those of
  * as_spmm_csr_bf16 with the same variant, so C is that call's result rounded, bit for bit.
+ * relu != 0: negative sums are stored as 0 (a layer followed by a ReLU, in the same pass).
  * C (ldc elements per row) is aligned to the variant's vectors (min(2 x elements, 16) bytes);
  * the bulk-copy variants have no bf16 output (AS_ERR_UNSUPPORTED). */
 as_status as_spmm_csr_bf16_out16(as_ctx *ctx, int M, int K, int N, int nnz, const int *rowptr,
                                  const int *colind, const uint16_t *val, const uint16_t *B,
-                                 long ldb, uint16_t *C, long ldc, int variant, void *stream);
+                                 long ldb, uint16_t *C, long ldc, int relu, int variant,
+                                 void *stream);
 
 /* ---- Softmax cross-entropy of class scores (the GCN's loss) ----------------------------------
  * n rows of C class scores in bf16 (row stride lds >= C elements), int64 labels in [0, C).

@@ -141,6 +141,32 @@ def test_fused_backward_matches_separate(oracle):
     assert oracle.scaled_err(grads[1][1].cpu().numpy(), r64, ab).max() < 1e-5
 
 
+def test_relu_epilogue_matches_relu_after():
+    """SPMMFunction(relu=True) on bf16 features: the output is F.relu of the plain op's and the
+    gradients through it are the same bits (the backward masks by the output as F.relu's)."""
+    a = S.powerlaw_graph(4000, 30000, seed=8)
+    G = gcn.Graph.from_csr(a, dev())
+    colptr, rowind, vcsc = G.csc
+    gen = torch.Generator(device=dev()).manual_seed(9)
+    f0 = torch.randn(4000, 64, generator=gen, device=dev()).to(torch.bfloat16)
+    gy = torch.randn(4000, 64, generator=gen, device=dev()).to(torch.bfloat16)
+    res = []
+    for fused in (True, False):
+        f = f0.clone().requires_grad_(True)
+        w = G.values.clone().requires_grad_(True)
+        if fused:
+            out = gcn.SPMMFunction.apply(G.rowptr, G.colind, colptr, rowind, f, w, vcsc, None,
+                                         None, True)
+        else:
+            out = torch.nn.functional.relu(
+                gcn.SPMMFunction.apply(G.rowptr, G.colind, colptr, rowind, f, w, vcsc))
+        out.backward(gy)
+        res.append((out.detach(), f.grad, w.grad))
+    assert torch.equal(res[0][0], res[1][0])
+    assert torch.equal(res[0][1], res[1][1])
+    assert torch.equal(res[0][2], res[1][2])
+
+
 def test_gcn_training_is_reproducible():
     x, g, y, train, _ = gcn.synthetic_task(seed=0)
 

@@ -339,8 +339,8 @@ def test_nnzsplit_bf16_variants(oracle):
 @pytest.mark.parametrize("N_", [46, 64, 256])
 def test_bf16_output_is_rounded_fp32_output(N_):
     """C in bf16 (as_spmm_csr_bf16_out16) is the same variant's fp32 C rounded to nearest even,
-    bit for bit, through the row-split, long-row and entry-balanced kernels; the bulk-copy
-    variants have no bf16 output."""
+    bit for bit, through the row-split, long-row and entry-balanced kernels (and with the ReLU
+    epilogue, relu of it); the bulk-copy variants have no bf16 output."""
     a = _skewed(9, n_rows=2500, n_cols=20000, long_lens=(20000, 3000, 600, 257))
     rp, ci, v = csr_dev(a)
     vd = v.to(torch.bfloat16)
@@ -362,6 +362,8 @@ def test_bf16_output_is_rounded_fp32_output(N_):
         assert C16.dtype == torch.bfloat16
         assert torch.equal(C16.view(torch.int16), C32.to(torch.bfloat16).view(torch.int16)), \
             names[var - 1]
+        R16 = A.spmm(rp, ci, vd, Bd, variant=var, out_dtype=torch.bfloat16, relu=True)
+        assert torch.equal(R16, torch.relu(C16)), names[var - 1]  # the ReLU epilogue
     assert ran >= 20
     C0 = A.spmm(rp, ci, vd, Bd, out_dtype=torch.bfloat16)  # library choice
     assert torch.equal(C0.view(torch.int16), A.spmm(rp, ci, vd, Bd).to(torch.bfloat16).view(torch.int16))
