@@ -197,6 +197,8 @@ static as_status spmm_common(const char *fn, int dtype, as_ctx *c, int M, int K,
     if (st != AS_OK) return st;
     if (N < 0) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": negative N");
     if (M == 0 || N == 0) return AS_OK;
+    if (nnz > 0 && K == 0)  // every entry's column would be out of range (B has no rows)
+        return fail(AS_ERR_INVALID_CSR, std::string(fn) + ": entries in a matrix without columns");
     if (!C && !C16) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": C is NULL");
     if (K > 0 && nnz > 0 && !B) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": B is NULL");
     if (ldb < N || ldc < N)
@@ -247,6 +249,8 @@ static as_status spmm_sddmm_common(const char *fn, int dtype, as_ctx *c, int M, 
                                           static_cast<cudaStream_t>(stream)),
                           fn);
     }
+    if (nnz > 0 && K == 0)
+        return fail(AS_ERR_INVALID_CSR, std::string(fn) + ": entries in a matrix without columns");
     if (!C && !C16) return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": C is NULL");
     if (nnz > 0 && (!B || !F || !dA))
         return fail(AS_ERR_INVALID_VALUE, std::string(fn) + ": B, F or dA is NULL");

@@ -74,6 +74,9 @@ as_status xent_bwd_launch(as_ctx *ctx, int n, int C, const uint16_t *S, long lds
 as_status spmm_nnz_launch(as_ctx *ctx, int dtype, int vb, int group, int cpl, int chunk,
                           int unroll, const SpmmArgs &a, cudaStream_t s,
                           const SddmmFuse *fuse = nullptr);
+// Multi-entry nnz-split (narrow B rows): a warp per chunk, 32 / group sub-groups.
+as_status spmm_nnzme_launch(as_ctx *ctx, int dtype, int vb, int group, int chunk,
+                            const SpmmArgs &a, cudaStream_t s, const SddmmFuse *fuse = nullptr);
 as_status spmm_bulk_launch(as_ctx *ctx, int dtype, int lane_bytes, int stages, const SpmmArgs &a,
                            cudaStream_t s);
 // Long rows of the row-split kernels: the cp.async size (16 or 4 bytes) the layout allows,

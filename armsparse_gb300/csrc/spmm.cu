@@ -209,7 +209,8 @@ struct Variant {
     const char *name;
     int kind;  // 0 = row-split (registers), 1 = bulk-copy staged (spmm_bulk.cu: vb = bytes per
                // lane, unroll = ring stages), 2 = nnz-split (spmm_nnz.cu: unroll = chunk size,
-               // steps = entries per load batch)
+               // steps = entries per load batch), 3 = multi-entry nnz-split (spmm_nnz.cu, a warp
+               // per chunk in 32 / group sub-groups; unroll = chunk size)
     int steps = 4;
 };
 
@@ -230,14 +231,18 @@ struct Variant {
 // 32-entry chunks: many short chains for small graphs (N <= kSmallChunkMaxN: their carry
 // scratch, 2 x nnz/32 x N floats, stays modest)
 #define AS_NNZS32 AS_NNZ(4, 32, 1, 32), AS_NNZ(4, 32, 2, 32), AS_NNZ(16, 32, 1, 32)
+// multi-entry chunks for narrow rows of B (a row of B spans fewer than 32 lanes' vectors)
+#define AS_ME(vb, g, ch) {vb, g, 1, ch, "nnzme_v" #vb "_g" #g "_ch" #ch, 3}
+#define AS_MES AS_ME(16, 8, 256), AS_ME(16, 8, 1024), AS_ME(16, 16, 1024), AS_ME(8, 8, 1024), \
+    AS_ME(8, 16, 1024)
 constexpr int kSmallChunk = 32;
 constexpr int kSmallChunkMaxN = 64;
 const Variant kF32[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_BULKS, AS_NNZS(128),
-                        AS_NNZS(1024), AS_NNZS8(256), AS_NNZS8(1024), AS_NNZS32};
+                        AS_NNZS(1024), AS_NNZS8(256), AS_NNZS8(1024), AS_NNZS32, AS_MES};
 const Variant kBF16[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_VROW(2), AS_BULKS,
                          AS_NNZS(128), AS_NNZS(1024), AS_NNZS_BF16_SCALAR(128),
                          AS_NNZS_BF16_SCALAR(1024), AS_NNZS8(256), AS_NNZS8(1024),
-                         AS_NNZ8(2, 32, 2, 256), AS_NNZ8(2, 32, 2, 1024), AS_NNZS32};
+                         AS_NNZ8(2, 32, 2, 256), AS_NNZ8(2, 32, 2, 1024), AS_NNZS32, AS_MES};
 constexpr int kNF32 = sizeof(kF32) / sizeof(kF32[0]);
 constexpr int kNBF16 = sizeof(kBF16) / sizeof(kBF16[0]);
 
@@ -373,8 +378,8 @@ bool spmm_variant_supported(int dtype, int variant, int N, long ldb, long ldc, c
                pc % 16 == 0 && (static_cast<long>(N % tile) * esz) % 16 == 0 &&
                ceil_div(N, tile) <= 65535;
     }
-    const int E = v.vb / esz;  // nnz-split
-    if (v.unroll == kSmallChunk && N > kSmallChunkMaxN) return false;
+    const int E = v.vb / esz;  // nnz-split and multi-entry
+    if (v.kind == 2 && v.unroll == kSmallChunk && N > kSmallChunkMaxN) return false;
     return N % E == 0 && ldb % E == 0 && pb % (E * esz) == 0 &&
            ceil_div(N, E * v.group * v.cpl) <= 65535 && ceil_div(N, 32) <= 65535;
 }
@@ -397,6 +402,7 @@ as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cu
                                                 " needs the bf16 C aligned to its vectors");
     }
     if (v.kind == 1) return spmm_bulk_launch(ctx, dtype, v.vb, v.unroll, a, s);
+    if (v.kind == 3) return spmm_nnzme_launch(ctx, dtype, v.vb, v.group, v.unroll, a, s);
     if (v.kind == 2) {
         if (v.unroll == kSmallChunk && a.N > kSmallChunkMaxN)
             return fail(AS_ERR_UNSUPPORTED, std::string("spmm: variant ") + v.name +
@@ -467,12 +473,13 @@ as_status spmm_sddmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs 
             return fail(AS_ERR_UNSUPPORTED, "spmm+sddmm: no variant covers this N and layout");
     }
     const Variant &v = t[variant - 1];
-    if (v.kind != 2)
+    if (v.kind != 2 && v.kind != 3)
         return fail(AS_ERR_UNSUPPORTED, std::string("spmm+sddmm: variant ") + v.name +
                                             " is not an nnz-split variant");
     if (tile(v) < a.N)
         return fail(AS_ERR_UNSUPPORTED, std::string("spmm+sddmm: variant ") + v.name +
                                             " covers fewer than N columns");
+    if (v.kind == 3) return spmm_nnzme_launch(ctx, dtype, v.vb, v.group, v.unroll, a, s, &f);
     if (v.unroll == kSmallChunk && a.N > kSmallChunkMaxN)
         return fail(AS_ERR_UNSUPPORTED, std::string("spmm+sddmm: variant ") + v.name +
                                             " serves N <= 64 only");

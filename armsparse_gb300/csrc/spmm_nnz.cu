@@ -283,6 +283,172 @@ spmm_nnzsplit(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowp
     if (blockIdx.y == 0 && g == 0) fix[chunk] = fix_row;
 }
 
+// Multi-entry form, for narrow rows of B (GROUP * E < 32 lanes' worth): a warp takes a chunk,
+// and its S = 32 / GROUP sub-groups of GROUP lanes take every S-th entry of each row segment
+// (sub-group s: entries s, s + S, s + 2S, ... of each 32-entry block), so one load
+// instruction brings S entries' rows and the broadcasts, addresses and loop control are shared
+// by S entries. A sub-group chains its entries in CSR order; at the segment's end the S partial
+// sums are added by a butterfly over the sub-groups (lane l adds lane l ^ off, off = GROUP ..
+// 16), then beta * C. Deterministic, but not the single CSR chain of the other kernels. Carry
+// slots, fix-up and empty rows as in spmm_nnzsplit; FUSE as there (each dot product over one
+// sub-group's GROUP lanes), with one column tile.
+template <int U, int GROUP>
+__device__ __forceinline__ void write_dots_me(float (&d)[U], const int (&kk)[U], unsigned gmask,
+                                              int g, int e0, int stride, int nnz,
+                                              const int *__restrict__ perm, float *__restrict__ dA,
+                                              unsigned *status) {
+    unsigned ok = 0;
+#pragma unroll
+    for (int u = 0; u < U; ++u) ok |= (kk[u] >= 0 ? 1u : 0u) << u;
+    const float sum = reduce_entries<U, GROUP>(d, gmask, g);
+    constexpr int SUB = GROUP / U;
+    const int u = g / SUB;
+    if (g % SUB == 0 && ((ok >> u) & 1u)) store_dot(e0 + stride * u, sum, nnz, perm, dA, status);
+}
+
+template <typename T, int VB, int GROUP, int U, bool FUSE>
+__global__ void __launch_bounds__(kThreads)
+spmm_nnzme(int M, int K, int N, int nnz, int CH, const int *__restrict__ rowptr,
+           const int *__restrict__ colind, const T *__restrict__ val, const T *__restrict__ B,
+           long ldb, float *__restrict__ C, long ldc, float beta, float *__restrict__ carry,
+           int *__restrict__ fix, unsigned *status, const T *__restrict__ F, long ldf,
+           const int *__restrict__ perm, float *__restrict__ dA, uint16_t *__restrict__ C16,
+           bool relu) {
+    using V = Vec<T, VB>;
+    constexpr int E = V::E;
+    constexpr int S = 32 / GROUP;
+    constexpr int TILE = GROUP * E;
+    static_assert(S >= 1 && U <= GROUP, "shape");
+    const int lane = threadIdx.x & 31;
+    const int g = lane % GROUP, sg = lane / GROUP;
+    const unsigned gmask =
+        GROUP == 32 ? 0xffffffffu : (((1u << GROUP) - 1u) << (lane & ~(GROUP - 1)));
+    const long chunk = static_cast<long>(blockIdx.x) * (kThreads / 32) + threadIdx.x / 32;
+    const long e0l = chunk * CH;
+    if (e0l >= nnz) return;  // the whole warp leaves together
+    const int e0 = static_cast<int>(e0l);
+    const int e1 = static_cast<int>(e0l + CH < nnz ? e0l + CH : nnz);
+    const int cc = blockIdx.y * TILE + g * E;  // this lane's columns
+    const bool col_ok = cc < N;
+    int r = find_row(rowptr, M, e0);
+    int e = e0;
+    int fix_row = -1;
+    while (e < e1 && r < M) {  // uniform across the warp
+        const int rs = __ldg(rowptr + r), re = __ldg(rowptr + r + 1);
+        if (re <= e || rs > e) {
+            if (rs > e || re < rs) {
+                flag(status, kFlagBadRowptr);
+                break;
+            }
+            ++r;
+            continue;
+        }
+        const int se = re < e1 ? re : e1;
+        const bool split = rs < e0 || re > e1;
+        if (rs < e0 && re <= e1) fix_row = r;
+        typename V::Raw fr;  // FUSE: this row's slice of F
+        if constexpr (FUSE) fr = V::raw(F + static_cast<long>(r) * ldf + (col_ok ? cc : 0));
+        float acc[E];
+#pragma unroll
+        for (int i = 0; i < E; ++i) acc[i] = 0.0f;
+        for (int base = e; base < se; base += 32) {
+            const int ee = base + lane;
+            int k = -1;
+            float v = 0.0f;
+            if (ee < se) {
+                k = ld_stream(colind + ee);
+                v = to_f32(ld_stream(val + ee));
+                if (static_cast<unsigned>(k) >= static_cast<unsigned>(K)) {
+                    flag(status, kFlagBadColind);
+                    k = -1;
+                }
+            }
+            const int cnt = min(32, se - base);
+            for (int t = 0; t < cnt; t += S * U) {  // sub-group sg: entries t + sg + S*u
+                int kk[U];
+                float vv[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int j = t + sg + S * u;
+                    kk[u] = __shfl_sync(0xffffffffu, k, j & 31);
+                    vv[u] = __shfl_sync(0xffffffffu, v, j & 31);
+                    if (j >= cnt) kk[u] = -1;
+                }
+                if constexpr (sizeof(T) == 4) {
+                    float b[U][E];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        if (col_ok && kk[u] >= 0) {
+                            V::load(B + static_cast<long>(kk[u]) * ldb + cc, b[u]);
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < E; ++i) b[u][i] = 0.0f;
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; ++u)
+                        if (kk[u] >= 0) fma_vec_f32<E>(b[u], vv[u], acc);
+                    if constexpr (FUSE) {
+                        float d[U];
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            d[u] = 0.0f;
+                            if (col_ok)
+#pragma unroll
+                                for (int i = 0; i < E; ++i) d[u] = fmaf(b[u][i], V::at(fr, i), d[u]);
+                        }
+                        write_dots_me<U, GROUP>(d, kk, gmask, g, base + t + sg, S, nnz, perm, dA,
+                                                status);
+                    }
+                } else {
+                    typename V::Raw b[U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u)  // branch-free: a skipped entry reads row 0
+                        b[u] = V::raw(B + static_cast<long>(kk[u] < 0 ? 0 : kk[u]) * ldb +
+                                      (col_ok ? cc : 0));
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        if (kk[u] < 0) continue;
+                        const unsigned short vu =
+                            static_cast<unsigned short>(__float_as_uint(vv[u]) >> 16);
+                        V::fma(b[u], vu, acc);
+                    }
+                    if constexpr (FUSE) {
+                        float d[U];
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            d[u] = 0.0f;
+                            if (col_ok) V::dot(b[u], fr, d[u]);
+                        }
+                        write_dots_me<U, GROUP>(d, kk, gmask, g, base + t + sg, S, nnz, perm, dA,
+                                                status);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int off = GROUP; off < 32; off <<= 1)  // the sub-groups' partial sums
+#pragma unroll
+            for (int i = 0; i < E; ++i) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], off);
+        if (sg == 0 && col_ok) {
+            if (split) {
+                float *dst = carry + (2 * chunk + (e == e0 ? 0 : 1)) * static_cast<long>(N) + cc;
+#pragma unroll
+                for (int i = 0; i < E; ++i) dst[i] = acc[i];
+            } else if (C16) {
+                store_bf16<E>(C16 + r * ldc + cc, acc, relu);
+            } else {
+                float *dst = C + r * ldc + cc;
+#pragma unroll
+                for (int i = 0; i < E; ++i) dst[i] = beta != 0.0f ? fmaf(beta, dst[i], acc[i]) : acc[i];
+            }
+        }
+        e = se;
+        ++r;
+    }
+    if (blockIdx.y == 0 && lane == 0) fix[chunk] = fix_row;
+}
+
 constexpr int kShortSpan = 8;  // rows over at most this many chunks: the one-pass fix-up
 constexpr int kFixBatch = 8;  // partial loads in flight per thread on a long span (16 measured slower)
 
@@ -447,8 +613,10 @@ spmm_empty_rows(int M, int N, const int *__restrict__ rowptr, float *__restrict_
     }
 }
 
-template <typename T, int VB, int G, int CPL, int U, bool FUSE>
+// ME: the multi-entry kernel (spmm_nnzme, CPL 1); else spmm_nnzsplit.
+template <typename T, int VB, int G, int CPL, int U, bool FUSE, bool ME = false>
 as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, const SddmmFuse *fu, cudaStream_t s) {
+    static_assert(!ME || CPL == 1, "multi-entry kernels hold one vector per lane");
     constexpr int E = Vec<T, VB>::E;
     constexpr int TILE = G * E * CPL;
     const int esz = sizeof(T);
@@ -471,13 +639,23 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, int CH, const SddmmFuse *fu, cu
     float *carry = static_cast<float *>(w);
     int *fix = reinterpret_cast<int *>(static_cast<char *>(w) + carry_bytes);
     if (nchunks > 0) {
-        dim3 g1(static_cast<unsigned>(ceil_div(nchunks, kThreads / G)),
-                static_cast<unsigned>(ceil_div(a.N, TILE)));
-        spmm_nnzsplit<T, VB, G, CPL, U, FUSE><<<g1, kThreads, 0, s>>>(
-            a.M, a.K, a.N, a.nnz, CH, a.rowptr, a.colind, static_cast<const T *>(a.val),
-            static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, carry, fix, a.status,
-            FUSE ? static_cast<const T *>(fu->F) : nullptr, FUSE ? fu->ldf : 0,
-            FUSE ? fu->perm : nullptr, FUSE ? fu->dA : nullptr, a.C16, a.relu);
+        if constexpr (ME) {
+            dim3 g1(static_cast<unsigned>(ceil_div(nchunks, kThreads / 32)),
+                    static_cast<unsigned>(ceil_div(a.N, TILE)));
+            spmm_nnzme<T, VB, G, U, FUSE><<<g1, kThreads, 0, s>>>(
+                a.M, a.K, a.N, a.nnz, CH, a.rowptr, a.colind, static_cast<const T *>(a.val),
+                static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, carry, fix, a.status,
+                FUSE ? static_cast<const T *>(fu->F) : nullptr, FUSE ? fu->ldf : 0,
+                FUSE ? fu->perm : nullptr, FUSE ? fu->dA : nullptr, a.C16, a.relu);
+        } else {
+            dim3 g1(static_cast<unsigned>(ceil_div(nchunks, kThreads / G)),
+                    static_cast<unsigned>(ceil_div(a.N, TILE)));
+            spmm_nnzsplit<T, VB, G, CPL, U, FUSE><<<g1, kThreads, 0, s>>>(
+                a.M, a.K, a.N, a.nnz, CH, a.rowptr, a.colind, static_cast<const T *>(a.val),
+                static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, carry, fix, a.status,
+                FUSE ? static_cast<const T *>(fu->F) : nullptr, FUSE ? fu->ldf : 0,
+                FUSE ? fu->perm : nullptr, FUSE ? fu->dA : nullptr, a.C16, a.relu);
+        }
         dim3 g2(static_cast<unsigned>(ceil_div(nchunks, kFixChunks)));
         if (a.N % 4 == 0)  // carry rows are 16-byte aligned: whole-vector loads
             spmm_nnz_fixup<4><<<g2, kThreads, 0, s>>>(a.M, a.N, nchunks, CH, a.rowptr, carry, fix,
@@ -503,7 +681,28 @@ as_status launch_u(as_ctx *ctx, const SpmmArgs &a, int CH, int unroll, const Sdd
                        : launch<T, VB, G, CPL, 4, false>(ctx, a, CH, fu, s);
 }
 
+template <typename T, int VB, int G>
+as_status launch_me(as_ctx *ctx, const SpmmArgs &a, int CH, const SddmmFuse *fu, cudaStream_t s) {
+    return fu ? launch<T, VB, G, 1, 4, true, true>(ctx, a, CH, fu, s)
+              : launch<T, VB, G, 1, 4, false, true>(ctx, a, CH, fu, s);
+}
+
 }  // namespace
+
+as_status spmm_nnzme_launch(as_ctx *ctx, int dtype, int vb, int group, int chunk,
+                            const SpmmArgs &a, cudaStream_t s, const SddmmFuse *fuse) {
+#define AS_ME_CASE(T, VBV, G) \
+    if (vb == VBV && group == G) return launch_me<T, VBV, G>(ctx, a, chunk, fuse, s);
+    if (dtype == 0) {
+        AS_ME_CASE(float, 16, 8) AS_ME_CASE(float, 16, 16) AS_ME_CASE(float, 8, 8)
+        AS_ME_CASE(float, 8, 16)
+    } else {
+        AS_ME_CASE(uint16_t, 16, 8) AS_ME_CASE(uint16_t, 16, 16) AS_ME_CASE(uint16_t, 8, 8)
+        AS_ME_CASE(uint16_t, 8, 16)
+    }
+#undef AS_ME_CASE
+    return fail(AS_ERR_UNSUPPORTED, "spmm multi-entry: configuration not instantiated");
+}
 
 as_status spmm_nnz_launch(as_ctx *ctx, int dtype, int vb, int group, int cpl, int chunk,
                           int unroll, const SpmmArgs &a, cudaStream_t s, const SddmmFuse *fuse) {

@@ -125,9 +125,10 @@ def _time_pick(rowptr, colind, values, n_in: int, width: int, dtype) -> int:
 
 
 def _nnz_tile(name: str, esz: int) -> int:
-    """Column tile (vector elements x lanes x vectors per lane) of an nnz-split variant name."""
+    """Column tile (vector elements x lanes x vectors per lane) of an nnz-split or multi-entry
+    variant name."""
     f = {p[0]: int(p[1:]) for p in name.split("_")[1:] if p[:1] in "vgc" and p[1:].isdigit()}
-    return (f["v"] // esz) * f["g"] * f["c"]
+    return (f["v"] // esz) * f["g"] * f.get("c", 1)
 
 
 def _time_pick_fused(colptr, rowind, values, n_out: int, width: int, dtype) -> int:
@@ -144,7 +145,7 @@ def _time_pick_fused(colptr, rowind, values, n_out: int, width: int, dtype) -> i
     best, best_ms = 0, float("inf")
     for i, name in enumerate(S.spmm_variants(dtype)):
         v = i + 1
-        if (not name.startswith("nnzsplit") or _nnz_tile(name, esz) < width
+        if (not name.startswith(("nnzsplit", "nnzme")) or _nnz_tile(name, esz) < width
                 or not S.spmm_variant_supported(v, width, dtype)):
             continue
         fn = lambda: S.spmm_sddmm(colptr, rowind, vals, g, f, C=C, variant=v, dA=dA,

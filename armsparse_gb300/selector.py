@@ -48,6 +48,7 @@ CANDIDATES = [
     "rowsplit_v16_g32_c2_u8", "nnzsplit_v16_g32_c1_ch256_u8", "nnzsplit_v4_g32_c2_ch256_u8",
     "nnzsplit_v16_g32_c1_ch1024_u8", "nnzsplit_v4_g32_c2_ch1024_u8",
     "nnzsplit_v4_g32_c1_ch32", "nnzsplit_v4_g32_c2_ch32", "nnzsplit_v16_g32_c1_ch32",
+    "nnzme_v8_g16_ch1024", "nnzme_v16_g8_ch1024", "nnzme_v16_g16_ch1024",
 ]
 
 

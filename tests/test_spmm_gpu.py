@@ -37,8 +37,9 @@ def test_golden_rowbasespmm3_every_variant(golden, oracle):
         names = A.spmm_variants()
         C64, A64 = oracle.spmm_f64(g[f"c{i}_rowptr"], g[f"c{i}_colind"], g[f"c{i}_val"], g[f"c{i}_B"])
         for var, C in outs.items():
-            if names[var - 1].startswith("nnzsplit"):
-                # rows that cross a chunk boundary are summed in chunk order
+            if names[var - 1].startswith(("nnzsplit", "nnzme")):
+                # rows that cross a chunk boundary are summed in chunk order (the multi-entry
+                # kernels sum every row in sub-group order)
                 assert oracle.scaled_err(C.cpu().numpy(), C64, A64).max() < 1e-5, names[var - 1]
             else:
                 assert np.array_equal(bits(C), bits(g[f"c{i}_C"])), (i, names[var - 1])
@@ -369,4 +370,38 @@ def test_bf16_output_is_rounded_fp32_output(N_):
     assert torch.equal(C0.view(torch.int16), A.spmm(rp, ci, vd, Bd).to(torch.bfloat16).view(torch.int16))
     with pytest.raises(ValueError):
         A.spmm(rp, ci, vd, Bd, C=torch.empty_like(C0), beta=1.0, out_dtype=torch.bfloat16)
+    A.sync_status()
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("N_", [16, 48, 64, 128])
+def test_multi_entry_variants(oracle, dtype, N_):
+    """The multi-entry kernels (a warp per chunk, 32 / group sub-groups each taking every
+    sub-group-th entry): fp32 accumulation error only, deterministic, beta and the bf16
+    output as the others, rows that span many chunks included."""
+    a = _skewed(30 + N_, n_rows=2500, n_cols=20000, long_lens=(20000, 3000, 600, 257))
+    rp, ci, v = csr_dev(a)
+    B = S.dense_uniform((a.n_cols, N_), 31 + N_)
+    if dtype == torch.bfloat16:
+        vh, Bh = oracle.bf16_round(a.val), oracle.bf16_round(B)
+    else:
+        vh, Bh = a.val, B
+    R, Ab = oracle.spmm_f64(a.rowptr, a.colind, vh, Bh)
+    vd, Bd = to_dev(vh).to(dtype), to_dev(Bh).to(dtype)
+    ran = 0
+    for var in _variant_ids("nnzme", dtype):
+        if not A.spmm_variant_supported(var, N_, dtype):
+            continue
+        ran += 1
+        C = A.spmm(rp, ci, vd, Bd, variant=var)
+        assert oracle.scaled_err(C.cpu().numpy(), R, Ab).max() < 1e-5
+        assert torch.equal(C, A.spmm(rp, ci, vd, Bd, variant=var))
+        Cb = torch.full_like(C, 2.0)
+        A.spmm(rp, ci, vd, Bd, C=Cb, beta=0.5, variant=var)
+        assert oracle.scaled_err(Cb.cpu().numpy(), R + 1.0, Ab + 1.0).max() < 1e-5
+        assert (C[:5] == 0).all()  # empty rows
+        if dtype == torch.bfloat16:
+            C16 = A.spmm(rp, ci, vd, Bd, variant=var, out_dtype=torch.bfloat16)
+            assert torch.equal(C16.view(torch.int16), C.to(torch.bfloat16).view(torch.int16))
+    assert ran >= 3
     A.sync_status()

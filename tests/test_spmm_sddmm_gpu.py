@@ -27,16 +27,16 @@ def _skewed(seed, n_rows=1500, n_cols=3000, long_lens=(2500, 700)):
 
 
 def _shape(name):
-    """(vector bytes, group, vectors per lane) of an nnz-split variant name."""
+    """(vector bytes, group, vectors per lane) of an nnz-split or multi-entry variant name."""
     f = dict((p[0], p[1:]) for p in name.split("_")[1:] if p[0] in "vgc" and p[1:].isdigit())
-    return int(f["v"]), int(f["g"]), int(f["c"])
+    return int(f["v"]), int(f["g"]), int(f.get("c", 1))
 
 
 def _fusable(dtype, N_):
     esz = 4 if dtype == torch.float32 else 2
     out = []
     for i, name in enumerate(A.spmm_variants(dtype)):
-        if not name.startswith("nnzsplit") or not A.spmm_variant_supported(i + 1, N_, dtype):
+        if not name.startswith(("nnzsplit", "nnzme")) or not A.spmm_variant_supported(i + 1, N_, dtype):
             continue
         vb, g, c = _shape(name)
         if (vb // esz) * g * c >= N_:
