@@ -528,45 +528,64 @@ sddmm_tc_persistent(const __grid_constant__ CUtensorMap tmXhi, const __grid_cons
 }
 
 // One warp per row: flags rows whose columns do not ascend (or leave [0, N)), and sets
-// occ[tm * tiles_n + tn] = 1 for every output tile holding a pattern entry -- one store per
-// (row, tile) since the columns ascend (the first entry of the row in each tile stores). Each
+// occ[tm * tiles_n + tn] = 1 for every output tile holding a pattern entry -- one mark per
+// (row, tile) since the columns ascend (the first entry of the row in each tile marks). Each
 // lane issues four column loads before using them; a lane's predecessor column comes from
-// the lane below (lane 0: the last column of the previous batch).
+// the lane below (lane 0: the last column of the previous batch). SHARED: the CTA's 8 rows
+// (all in one 128-row band) mark a shared copy of the band's flags, which the CTA then writes
+// out once -- the 128 rows of a band otherwise store to the same few bytes, and those stores
+// serialise in L2.
+constexpr int kMarkSharedTiles = 16384;  // tiles per band held in shared memory
+
+template <bool SHARED>
 __global__ void __launch_bounds__(256)
 check_and_mark(int M, int N, int nnz, const int *__restrict__ rowptr,
                const int *__restrict__ colind, int BN, int tiles_n, unsigned char *__restrict__ occ,
                unsigned *status) {
+    extern __shared__ unsigned char sflag[];  // SHARED: tiles_n bytes
     const long w = (static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (w >= M) return;
-    int lo, hi;
-    row_range(rowptr, static_cast<int>(w), nnz, status, lo, hi);
-    unsigned char *rowocc = occ + (w / kBM) * static_cast<long>(tiles_n);
-    bool bad = false;
-    int carry = -1;  // column of the entry before this batch (-1 before the row's first)
-    for (int base = lo; base < hi; base += 128) {
-        int c[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = base + 32 * q + lane;
-            c[q] = e < hi ? __ldg(colind + e) : 0;
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = base + 32 * q + lane;
-            const int up = __shfl_up_sync(0xffffffffu, c[q], 1);
-            const int last = __shfl_sync(0xffffffffu, c[q], 31);
-            const int prev = lane == 0 ? carry : up;
-            if (e < hi) {
-                if (c[q] < 0 || c[q] >= N || prev >= c[q])
-                    bad = true;
-                else if (prev < 0 || prev / BN != c[q] / BN)
-                    rowocc[c[q] / BN] = 1;
-            }
-            carry = last;
-        }
+    const long band = (static_cast<long>(blockIdx.x) * (blockDim.x >> 5)) / kBM;
+    if (SHARED) {
+        for (int t = threadIdx.x; t < tiles_n; t += blockDim.x) sflag[t] = 0;
+        __syncthreads();
     }
-    if (__any_sync(0xffffffffu, bad) && lane == 0) flag(status, kFlagBadColind);
+    unsigned char *rowocc = SHARED ? sflag : occ + (w / kBM) * static_cast<long>(tiles_n);
+    bool bad = false;
+    if (w < M) {
+        int lo, hi;
+        row_range(rowptr, static_cast<int>(w), nnz, status, lo, hi);
+        int carry = -1;  // column of the entry before this batch (-1 before the row's first)
+        for (int base = lo; base < hi; base += 128) {
+            int c[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int e = base + 32 * q + lane;
+                c[q] = e < hi ? __ldg(colind + e) : 0;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int e = base + 32 * q + lane;
+                const int up = __shfl_up_sync(0xffffffffu, c[q], 1);
+                const int last = __shfl_sync(0xffffffffu, c[q], 31);
+                const int prev = lane == 0 ? carry : up;
+                if (e < hi) {
+                    if (c[q] < 0 || c[q] >= N || prev >= c[q])
+                        bad = true;
+                    else if (prev < 0 || prev / BN != c[q] / BN)
+                        rowocc[c[q] / BN] = 1;
+                }
+                carry = last;
+            }
+        }
+        if (__any_sync(0xffffffffu, bad) && lane == 0) flag(status, kFlagBadColind);
+    }
+    if (SHARED) {
+        __syncthreads();
+        unsigned char *bandocc = occ + band * static_cast<long>(tiles_n);
+        for (int t = threadIdx.x; t < tiles_n; t += blockDim.x)
+            if (sflag[t]) bandocc[t] = 1;
+    }
 }
 
 // X's rows then Y's rows -> bf16 hi/lo planes: hi = bf16(x), lo = bf16(x - hi), columns
@@ -751,8 +770,12 @@ as_status sddmm_bf16x3_launch(as_ctx *ctx, int M, int N, int K, int nnz, const i
     } else {
         cudaError_t e = cudaMemsetAsync(occ, 0, occ_bytes, s);
         if (e != cudaSuccess) return check_cuda(e, "sddmm_bf16x3: occupancy clear");
-        check_and_mark<<<rows_grid, 256, 0, s>>>(M, N, nnz, rowptr, colind, BN, tiles_n, occ,
-                                                 ctx->d_status);
+        if (tiles_n <= kMarkSharedTiles)
+            check_and_mark<true><<<rows_grid, 256, static_cast<size_t>(tiles_n), s>>>(
+                M, N, nnz, rowptr, colind, BN, tiles_n, occ, ctx->d_status);
+        else
+            check_and_mark<false><<<rows_grid, 256, 0, s>>>(M, N, nnz, rowptr, colind, BN,
+                                                            tiles_n, occ, ctx->d_status);
     }
     ctx->launches++;
     if (K == 0) {
