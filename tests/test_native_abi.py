@@ -131,3 +131,47 @@ def test_variant_feasibility_query(native_lib):
     for N_ in (1, 3, 47, 64, 4096):
         v = native_lib.as_spmm_default_variant(0, 100, 100, N_, 500, N_, N_, 256, 256)
         assert A.spmm_variant_supported(v, N_)
+
+
+def test_selector_model_names_known_variants(native_lib):
+    """Every candidate of the shipped selector model (and of the sweep list) is a kernel of
+    both variant tables, and the multi-entry family is in the tables."""
+    import json
+    import armsparse_gb300 as A
+    from armsparse_gb300 import selector as SEL
+    with open(SEL.DEFAULT_MODEL) as f:
+        model = json.load(f)
+    for dt in (torch.float32, torch.bfloat16):
+        names = set(A.spmm_variants(dt))
+        assert set(model["candidates"]) <= names
+        assert set(SEL.CANDIDATES) <= names
+        assert {n for n in names if n.startswith("nnzme_")}
+    assert len(model["weights"][-1]) == len(model["candidates"])  # one score per candidate
+
+
+def test_multi_entry_and_fused_feasibility(native_lib):
+    import armsparse_gb300 as A
+    from armsparse_gb300 import gcn
+    names = A.spmm_variants(torch.bfloat16)
+    idx = {n: i + 1 for i, n in enumerate(names)}
+    assert A.spmm_variant_supported(idx["nnzme_v8_g16_ch1024"], 48, torch.bfloat16)
+    assert not A.spmm_variant_supported(idx["nnzme_v8_g16_ch1024"], 46, torch.bfloat16)  # 4 | N
+    assert gcn._nnz_tile("nnzme_v8_g16_ch1024", 2) == 64
+    assert gcn._nnz_tile("nnzsplit_v16_g32_c2_ch1024_u8", 2) == 512
+    assert gcn._nnz_tile("nnzsplit_v4_g32_c1_ch128", 4) == 32
+
+
+def test_new_ops_validate_on_the_host():
+    """Argument errors of the fused, gather and loss wrappers are raised before any device
+    work (here, on CPU tensors)."""
+    import armsparse_gb300 as A
+    rp = torch.tensor([0, 1], dtype=torch.int32)
+    ci = torch.tensor([0], dtype=torch.int32)
+    with pytest.raises(ValueError, match="CUDA"):
+        A.spmm_sddmm(rp, ci, torch.ones(1), torch.ones(1, 4), torch.ones(1, 4))
+    with pytest.raises(ValueError, match="CUDA"):
+        A.gather(torch.ones(4), torch.zeros(2, dtype=torch.int32))
+    with pytest.raises(ValueError, match="CUDA"):
+        A.softmax_xent(torch.zeros(2, 8, dtype=torch.bfloat16), torch.zeros(2, dtype=torch.long), 8)
+    with pytest.raises(ValueError, match="CUDA"):
+        A.csr2csc_perm(rp, ci, 1)

@@ -122,6 +122,41 @@ def test_sddmm_oracles_agree(oracle):
     assert np.allclose(o64, dense, rtol=1e-12, atol=1e-12)
 
 
+def test_sddmm_slices_order(oracle):
+    """The fused pass's dot-product order (lane slices, then a butterfly): within FP32 error of
+    FP64, deterministic, placed through a permutation, and equal to a plain loop restatement."""
+    a = S.uniform_csr(60, 50, 500, 17)
+    for G, E, CPL, K in ((32, 2, 1, 48), (8, 8, 1, 48), (16, 4, 2, 100), (32, 8, 1, 256)):
+        X, Y = S.dense_normal((60, K), K), S.dense_normal((50, K), K + 1)
+        r64, ab = oracle.sddmm_f64(a.rowptr, a.colind, X, Y)
+        got = oracle.sddmm_f32_slices(a.rowptr, a.colind, X, Y, G, E, CPL)
+        assert oracle.scaled_err(got, r64, ab).max() < 1e-5
+        perm = np.random.default_rng(K).permutation(got.size).astype(np.int32)
+        placed = oracle.sddmm_f32_slices(a.rowptr, a.colind, X, Y, G, E, CPL, perm=perm)
+        assert np.array_equal(placed[perm].view(np.uint32), got.view(np.uint32))
+    # a plain restatement for one shape (fmaf = a product exact in double, then one rounding)
+    G, E, CPL, K = 8, 4, 2, 40
+    X, Y = S.dense_normal((60, K), 3), S.dense_normal((50, K), 4)
+    got = oracle.sddmm_f32_slices(a.rowptr, a.colind, X, Y, G, E, CPL)
+    rows = np.repeat(np.arange(60), np.diff(a.rowptr))
+    for e in range(0, a.colind.size, 37):
+        x, y = X[rows[e]], Y[a.colind[e]]
+        lanes = []
+        for l in range(G):
+            acc = np.float32(0)
+            for j in range(CPL):
+                c = (j * G + l) * E
+                for i in range(E):
+                    if c + i < K:
+                        acc = np.float32(np.float64(y[c + i]) * np.float64(x[c + i]) + np.float64(acc))
+            lanes.append(acc)
+        off = G // 2
+        while off:
+            lanes = [np.float32(lanes[l] + lanes[l ^ off]) for l in range(G)]
+            off //= 2
+        assert lanes[0] == got[e]
+
+
 def test_scaled_err_metric(oracle):
     ref = np.array([1.0, 0.0, -2.0])
     ab = np.array([1.0, 4.0, 2.0])
