@@ -11,8 +11,8 @@ gcn/pytorch-custom/spmm_kernel.cu:437-457). Here:
    t_v ~ exp(-(time_v / best - 1) / tau), on the GPU, with this project's own kernels
    (include/armsparse_mlp.h: linear forward/backward, softmax cross entropy, Adam);
 3. ``Selector.choose`` evaluates the network on the host (a few thousand multiply-adds) and
-   returns the variant id; the autotuner stays the fallback and the judge
-   (``evaluate`` reports picked time / best time).
+   returns the variant id; the autotuner stays the fallback and the yardstick the picks are
+   scored against (``evaluate`` reports picked time / best time).
 
 Model files are JSON (weights, feature normalisation, candidate names, format version).
 """

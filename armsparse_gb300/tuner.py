@@ -4,7 +4,7 @@ The nearest reference logic is a static dispatch on the dense width (k < 32 / k 
 in gcn/pytorch-custom/spmm_kernel.cu:437-457, and k % 4 / k % 2 in sddmm.cu:438-455). Here
 every variant that can run the arguments is timed with CUDA events on the current stream,
 L2 flushed before every repetition, and the median is kept. The tuner is the fallback when
-no learned selector is loaded and the judge the selector is scored against.
+no learned selector is loaded and the yardstick the selector is scored against.
 """
 from __future__ import annotations
 
