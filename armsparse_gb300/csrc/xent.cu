@@ -132,11 +132,12 @@ xent_bwd(int n, int C, const uint16_t *__restrict__ S, long lds,
             g[q] = (ok && j < C) ? (expf(x[q] - lse) - (j == t ? 1.0f : 0.0f)) * scale : 0.0f;
         }
         if (VEC) {
+            auto pk = [](float lo, float hi) {
+                return static_cast<unsigned>(f32_to_bf16(lo)) |
+                       (static_cast<unsigned>(f32_to_bf16(hi)) << 16);
+            };
             *reinterpret_cast<uint4 *>(grow + 8 * v) =
-                make_uint4(static_cast<unsigned>(f32_to_bf16(g[0])) | (static_cast<unsigned>(f32_to_bf16(g[1])) << 16),
-                           static_cast<unsigned>(f32_to_bf16(g[2])) | (static_cast<unsigned>(f32_to_bf16(g[3])) << 16),
-                           static_cast<unsigned>(f32_to_bf16(g[4])) | (static_cast<unsigned>(f32_to_bf16(g[5])) << 16),
-                           static_cast<unsigned>(f32_to_bf16(g[6])) | (static_cast<unsigned>(f32_to_bf16(g[7])) << 16));
+                make_uint4(pk(g[0], g[1]), pk(g[2], g[3]), pk(g[4], g[5]), pk(g[6], g[7]));
         } else {
 #pragma unroll
             for (int q = 0; q < 8; ++q)
