@@ -48,6 +48,94 @@ void or_spmm_fma_chain_f32(int M, int N, const int *rowptr, const int *colind,
     }
 }
 
+/* The entry-balanced GPU SpMM's summation order, restated (no reference counterpart: the
+ * reference's SpMM is the single chain of or_spmm_fma_chain_f32; this states how the GPU's
+ * entry-balanced kernels, spmm_nnz.cu, reorder it, so their results can be checked bit for bit).
+ * The entries are cut into chunks of CH. Per output element (r, j):
+ *  - each chunk's segment of row r is summed by S sub-chains: sub-chain s takes the segment's
+ *    entries s, s + S, s + 2S, ... in order, fmaf from 0; the S sums are added by a butterfly
+ *    (pairs s, s ^ 1, then s, s ^ 2, ...). S = 1 for the one-entry-per-step kernels (nnzsplit,
+ *    whose segment sum is then the plain chain), 32 / group for the multi-entry ones (nnzme).
+ *    For S = 1 a row inside one chunk starts its chain from beta * C instead of 0; for S > 1
+ *    it gets fmaf(beta, C, sum) (beta != 0) at the end;
+ *  - a row over n > 1 chunks: its chunk partials p_0 .. p_{n-1}, n <= 8: p_0 + p_1 + ... in
+ *    order; n > 8: R consecutive runs (R = 256 / G, G = the 256-wide block of column groups of
+ *    VW columns holding j: VW = 4 when N % 4 == 0, else 1), each summed from 0 in order, then
+ *    run 0 + run 1 + ...; then fmaf(beta, C, t) when beta != 0. */
+static float or_seg_sum(const int *colind, const float *val, const float *B, long ldb, int lo,
+                        int hi, int j, int S, float init) {
+    float sub[32];
+    for (int s = 0; s < S; ++s) sub[s] = 0.0f;
+    if (S == 1) sub[0] = init;
+    for (int e = lo; e < hi; ++e) {
+        const int s = (e - lo) % S;
+        sub[s] = fmaf(B[(long)colind[e] * ldb + j], val[e], sub[s]);
+    }
+    for (int off = 1; off < S; off <<= 1) {
+        float nxt[32];
+        for (int s = 0; s < S; ++s) nxt[s] = sub[s] + sub[s ^ off];
+        for (int s = 0; s < S; ++s) sub[s] = nxt[s];
+    }
+    return sub[0];
+}
+
+void or_spmm_nnz_order_f32(int M, int N, const int *rowptr, const int *colind, const float *val,
+                           const float *B, long ldb, float *C, long ldc, float beta, int CH,
+                           int S, int threads) {
+    const int VW = N % 4 == 0 ? 4 : 1;
+    const int ncg = N / VW;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 16)
+    for (int r = 0; r < M; ++r) {
+        const int rs = rowptr[r], re = rowptr[r + 1];
+        float *c = C + (long)r * ldc;
+        if (rs == re) {
+            for (int j = 0; j < N; ++j) c[j] = beta == 0.0f ? 0.0f : beta * c[j];
+            continue;
+        }
+        const long c_first = rs / CH, c_last = (re - 1) / CH;
+        const long n = c_last - c_first + 1;
+        for (int j = 0; j < N; ++j) {
+            if (n == 1) {
+                if (S == 1) {
+                    c[j] = or_seg_sum(colind, val, B, ldb, rs, re, j, 1,
+                                      beta != 0.0f ? beta * c[j] : 0.0f);
+                } else {
+                    const float t = or_seg_sum(colind, val, B, ldb, rs, re, j, S, 0.0f);
+                    c[j] = beta != 0.0f ? fmaf(beta, c[j], t) : t;
+                }
+                continue;
+            }
+            float t;
+            if (n <= 8) {
+                t = 0.0f;
+                for (long q = 0; q < n; ++q) {
+                    const long cc = c_first + q;
+                    const int lo = (int)(cc * CH > rs ? cc * CH : rs);
+                    const int hi = (int)((cc + 1) * CH < re ? (cc + 1) * CH : re);
+                    const float p = or_seg_sum(colind, val, B, ldb, lo, hi, j, S, 0.0f);
+                    t = q == 0 ? p : t + p;
+                }
+            } else {
+                const int cg = j / VW, cg0 = cg / 256 * 256;
+                const int cgs = ncg - cg0 < 256 ? ncg - cg0 : 256;
+                const int R = 256 / cgs;
+                t = 0.0f;
+                for (int q = 0; q < R; ++q) {
+                    const long b0 = c_first + n * q / R, b1 = c_first + n * (q + 1) / R;
+                    float run = 0.0f;
+                    for (long cc = b0; cc < b1; ++cc) {
+                        const int lo = (int)(cc * CH > rs ? cc * CH : rs);
+                        const int hi = (int)((cc + 1) * CH < re ? (cc + 1) * CH : re);
+                        run += or_seg_sum(colind, val, B, ldb, lo, hi, j, S, 0.0f);
+                    }
+                    t = q == 0 ? run : t + run;
+                }
+            }
+            c[j] = beta != 0.0f ? fmaf(beta, c[j], t) : t;
+        }
+    }
+}
+
 /* Sparse x sparse -> dense: C += A*B with A (M x K) and B (K x N) both CSR and C dense
  * row-major. For each row of A, its entries in CSR order, each contributing its B row's
  * entries in order, as the reference's sparse_matrix_mul3 does (SpMM.cpp:309-327, built with

@@ -62,6 +62,9 @@ def lib():
             L = ctypes.CDLL(path)
             L.or_spmm_fma_chain_f32.argtypes = [_c_int, _c_int, _i32p, _i32p, _f32p, _f32p,
                                                 _c_long, _f32p, _c_long, _c_int, _c_int]
+            L.or_spmm_nnz_order_f32.argtypes = [_c_int, _c_int, _i32p, _i32p, _f32p, _f32p,
+                                                _c_long, _f32p, _c_long, ctypes.c_float,
+                                                _c_int, _c_int, _c_int]
             L.or_spmm_f64.argtypes = [_c_int, _c_int, _i32p, _i32p, _f64p, _f64p, _c_long,
                                       _f64p, _f64p, _c_int]
             L.or_spmv_vcsr4_f32.argtypes = [_c_int, _i32p, _i32p, _f32p, _f32p, _f32p, _c_int,
@@ -121,6 +124,26 @@ def spmm_fma_chain_f32(rowptr, colind, val, B, C=None, threads=None):
     out = np.ascontiguousarray(C, dtype=np.float32).copy() if acc else np.empty((M, N), np.float32)
     lib().or_spmm_fma_chain_f32(M, N, rowptr, colind, np.ascontiguousarray(val, np.float32), B,
                                 N, out, N, int(acc), threads or max_threads())
+    return out
+
+
+def spmm_nnz_order_f32(rowptr, colind, val, B, chunk, subchains=1, C=None, beta=0.0,
+                       threads=None):
+    """C = A*B + beta*C in the summation order of the GPU's entry-balanced SpMM kernels:
+    chunks of `chunk` entries, `subchains` interleaved chains per chunk segment (1 for the
+    one-entry-per-step kernels, 32 / group for the multi-entry ones) and the fix-up's order
+    for rows over several chunks. Test infrastructure for bit-exact checks of those kernels."""
+    rowptr, colind = _csr(rowptr, colind)
+    M = rowptr.size - 1
+    B = np.ascontiguousarray(B, dtype=np.float32)
+    N = B.shape[1]
+    if subchains < 1 or subchains > 32 or subchains & (subchains - 1):
+        raise ValueError("subchains must be a power of two <= 32")
+    out = (np.ascontiguousarray(C, dtype=np.float32).copy() if C is not None
+           else np.zeros((M, N), np.float32))
+    lib().or_spmm_nnz_order_f32(M, N, rowptr, colind, np.ascontiguousarray(val, np.float32), B,
+                                N, out, N, float(beta), int(chunk), int(subchains),
+                                threads or max_threads())
     return out
 
 

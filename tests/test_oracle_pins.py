@@ -157,6 +157,35 @@ def test_sddmm_slices_order(oracle):
         assert lanes[0] == got[e]
 
 
+def test_entry_balanced_order(oracle):
+    """The entry-balanced kernels' order: one sub-chain is the plain chain for rows inside a
+    chunk, every form stays within FP32 error of FP64 (short and long spans, beta), and
+    sub-chains of 2 and 4 reorder only within a segment."""
+    rng = np.random.default_rng(5)
+    lens = rng.integers(0, 12, 900)
+    lens[10], lens[400], lens[401] = 5000, 700, 129  # spans > 8 chunks, 2-8 chunks, a boundary
+    rp = np.zeros(901, np.int32)
+    np.cumsum(lens, out=rp[1:])
+    ci = np.concatenate([np.sort(rng.choice(6000, l, replace=False)) for l in lens]).astype(np.int32)
+    val = rng.uniform(-1, 1, ci.size).astype(np.float32)
+    for N_ in (8, 6, 40):
+        B = S.dense_uniform((6000, N_), N_)
+        chain = oracle.spmm_fma_chain_f32(rp, ci, val, B)
+        r64, ab = oracle.spmm_f64(rp, ci, val, B)
+        for ch in (128, 1024):
+            c_first, c_last = rp[:-1] // ch, np.maximum(rp[1:] - 1, rp[:-1]) // ch
+            inside = c_first == c_last
+            for sub in (1, 2, 4):
+                got = oracle.spmm_nnz_order_f32(rp, ci, val, B, ch, sub)
+                assert oracle.scaled_err(got, r64, ab).max() < 1e-5
+                if sub == 1:
+                    assert np.array_equal(got[inside].view(np.uint32),
+                                          chain[inside].view(np.uint32))
+            C0 = S.dense_uniform((900, N_), 7)
+            got = oracle.spmm_nnz_order_f32(rp, ci, val, B, ch, 1, C=C0, beta=0.5)
+            assert oracle.scaled_err(got, r64 + 0.5 * C0, ab + 0.5 * np.abs(C0)).max() < 1e-5
+
+
 def test_scaled_err_metric(oracle):
     ref = np.array([1.0, 0.0, -2.0])
     ab = np.array([1.0, 4.0, 2.0])
