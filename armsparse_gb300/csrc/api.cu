@@ -325,7 +325,7 @@ as_status as_spmm_csr_reduce_f32(as_ctx *c, int M, int K, int N, int nnz, const 
     if (!c) return fail(AS_ERR_INVALID_VALUE, "as_spmm_csr_reduce_f32: ctx is NULL");
     as_status st = check_csr_args("as_spmm_csr_reduce_f32", M, K, nnz, rowptr, colind, nullptr, false);
     if (st != AS_OK) return st;
-    if (op != AS_REDUCE_SUM && op != AS_REDUCE_MAX)
+    if (op != AS_REDUCE_SUM && op != AS_REDUCE_MAX && op != AS_REDUCE_MAX_DGL)
         return fail(AS_ERR_INVALID_VALUE, "as_spmm_csr_reduce_f32: unknown reduction");
     if (N < 0) return fail(AS_ERR_INVALID_VALUE, "as_spmm_csr_reduce_f32: negative N");
     if (M == 0 || N == 0) return AS_OK;

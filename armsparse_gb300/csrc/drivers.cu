@@ -291,6 +291,10 @@ void as_drv_rowBaseSpmm3(int *rowPtr, int *colInd, float *val, float *B, float *
                          int N, int threads) {
     rowBaseSpmm3(rowPtr, colInd, val, B, C, M, K, N, threads);
 }
+void as_drv_rowBaseSpmm2(int *rowPtr, int *colInd, float *val, float *B, float *C, int M, int K,
+                         int N, int threads) {
+    rowBaseSpmm2(rowPtr, colInd, val, B, C, M, K, N, threads);
+}
 void as_drv_origin(int *rowPtr, int *colInd, float *val, float *B, float *C, int M, int K, int N,
                    int threads) {
     origin(rowPtr, colInd, val, B, C, M, K, N, threads);

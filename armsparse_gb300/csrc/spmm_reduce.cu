@@ -3,8 +3,10 @@
 // aggregation of the reference's topo*SPMMKernel family (gcn/pytorch-custom/spmm_kernel.cu:
 // 31-207; each output is acc += B[...] in CSR order, reproduced here add for add); the
 // weighted sum is the FMA chain of the SpMM; max is the copy-max aggregation of the DGL
-// kernels (binary_reduce_max.cu:26-168). Rows without entries give 0 (what those kernels
-// leave for isolated nodes).
+// kernels (binary_reduce_max.cu:26-168). OP 0 = sum, 1 = max from -inf (fmaxf), both giving 0
+// for rows without entries; OP 2 = the DGL kernels' own max: the accumulator starts at -10000
+// (max_init, binary_reduce_max.cu:22-24) and takes acc = acc > x ? acc : x (max_reduce, :18-20)
+// in CSR order, so an empty row stays at -10000.
 //
 // One warp per row; lane l owns columns l, l+32, ... of a 32*CPL-column tile (scalar loads,
 // any N); 4 entries per step.
@@ -30,7 +32,7 @@ spmm_reduce(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
     const int tile0 = blockIdx.y * 32 * CPL;
     float acc[CPL];
 #pragma unroll
-    for (int j = 0; j < CPL; ++j) acc[j] = OP == 0 ? 0.0f : -INFINITY;
+    for (int j = 0; j < CPL; ++j) acc[j] = OP == 0 ? 0.0f : OP == 1 ? -INFINITY : -10000.0f;
     for (int base = lo; base < hi; base += 32) {
         const int e = base + lane;
         int k = -1;
@@ -56,8 +58,12 @@ spmm_reduce(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                     const float b = __ldg(brow + c);
                     if (OP == 0)  // weighted: the FMA chain of the SpMM; unweighted: plain adds
                         acc[j] = WEIGHTED ? fmaf(b, ww, acc[j]) : __fadd_rn(acc[j], b);
-                    else
+                    else if (OP == 1)
                         acc[j] = fmaxf(acc[j], WEIGHTED ? __fmul_rn(ww, b) : b);
+                    else {
+                        const float x = WEIGHTED ? __fmul_rn(ww, b) : b;
+                        acc[j] = acc[j] > x ? acc[j] : x;
+                    }
                 }
             }
         }
@@ -65,7 +71,7 @@ spmm_reduce(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
 #pragma unroll
     for (int j = 0; j < CPL; ++j) {
         const int c = tile0 + j * 32 + lane;
-        if (c < N) C[row * ldc + c] = (hi == lo) ? 0.0f : acc[j];
+        if (c < N) C[row * ldc + c] = (hi == lo && OP != 2) ? 0.0f : acc[j];
     }
 }
 
@@ -86,7 +92,8 @@ as_status spmm_reduce_launch(as_ctx *ctx, int op, const SpmmArgs &a, cudaStream_
     if (ceil_div(a.N, 128) > 65535) return fail(AS_ERR_UNSUPPORTED, "spmm reduce: N too large");
     const bool w = a.val != nullptr;
     if (op == 0) w ? launch<0, true>(a, s) : launch<0, false>(a, s);
-    else w ? launch<1, true>(a, s) : launch<1, false>(a, s);
+    else if (op == 1) w ? launch<1, true>(a, s) : launch<1, false>(a, s);
+    else w ? launch<2, true>(a, s) : launch<2, false>(a, s);
     ctx->launches++;
     return check_cuda(cudaGetLastError(), "spmm reduce launch");
 }

@@ -192,7 +192,7 @@ def spmm_reduce(rowptr, colind, B, val=None, op: str = "sum", C=None):
                                             _ptr(colind), _ptr(val), _ptr(B),
                                             B.stride(0) if K > 1 else Ncols, _ptr(C),
                                             C.stride(0) if M > 1 else Ncols,
-                                            {"sum": 0, "max": 1}[op], _stream(dev)),
+                                            {"sum": 0, "max": 1, "max_dgl": 2}[op], _stream(dev)),
             "as_spmm_csr_reduce_f32")
     return C
 

@@ -53,6 +53,9 @@ extern "C" {
 /* C-linkage aliases of the shims above, for FFI callers (ctypes, cgo, JNI). */
 void as_drv_rowBaseSpmm3(int *rowPtr, int *colInd, float *val, float *B, float *C, int M, int K,
                          int N, int threads);
+/* SDMM.cpp:65 -- rowBaseSpmm2, the cblas_saxpy variant; same contract and result as above. */
+void as_drv_rowBaseSpmm2(int *rowPtr, int *colInd, float *val, float *B, float *C, int M, int K,
+                         int N, int threads);
 void as_drv_origin(int *rowPtr, int *colInd, float *val, float *B, float *C, int M, int K, int N,
                    int threads);
 void as_drv_sparse_dense_vector(float *B, float *C, int *rowPtr, int *colInd, float *val, int M,

@@ -78,12 +78,21 @@ as_status as_spmm_csr_bf16(as_ctx *ctx, int M, int K, int N, int nnz, const int 
                            void *stream);
 
 /* Other reductions: C[i,:] = reduce_{e in row i} w_e * B[col(e),:], reduce = sum or max,
- * w_e = val[e] (val may be NULL: every w_e = 1, the unweighted "copy" aggregation). Rows
- * without entries give 0. Unweighted sum adds in CSR order exactly as the reference's
- * topo*SPMMKernel family (gcn/pytorch-custom/spmm_kernel.cu:31-207); max is the copy-max
- * aggregation of its DGL kernels (binary_reduce_max.cu:26-168). Overwrites C. */
+ * w_e = val[e] (val may be NULL: every w_e = 1, the unweighted "copy" aggregation). Overwrites C.
+ *  - AS_REDUCE_SUM: unweighted sum adds in CSR order exactly as the reference's
+ *    topo*SPMMKernel family (gcn/pytorch-custom/spmm_kernel.cu:31-207); rows without entries
+ *    give 0.
+ *  - AS_REDUCE_MAX: max starting from -inf (fmaxf, NaN entries ignored); rows without entries
+ *    give 0.
+ *  - AS_REDUCE_MAX_DGL: the reference's copy-max aggregation as its DGL kernels compute it
+ *    (gcn/dgl-custom/binary_reduce_max.cu:18-24, :41-54, :151-166): the accumulator starts at
+ *    -10000 and each entry applies acc = (acc > x) ? acc : x in CSR order. So values below
+ *    -10000 never show, a NaN entry sets the accumulator to NaN and the entry after it
+ *    replaces that NaN (no comparison with NaN is true), and rows without entries give
+ *    -10000. */
 #define AS_REDUCE_SUM 0
 #define AS_REDUCE_MAX 1
+#define AS_REDUCE_MAX_DGL 2
 as_status as_spmm_csr_reduce_f32(as_ctx *ctx, int M, int K, int N, int nnz, const int *rowptr,
                                  const int *colind, const float *val, const float *B, long ldb,
                                  float *C, long ldc, int op, void *stream);

@@ -416,23 +416,31 @@ int or_max_threads(void) {
 /* Unweighted / weighted sum or max aggregation: C[i,:] = reduce over row i of w_e * B[col,:]
  * (w_e = val[e] or 1 when val is NULL), in CSR order: the unweighted sum adds acc += B[...] as
  * the reference's copy-sum kernels do (gcn/pytorch-custom/spmm_kernel.cu:156-173), the
- * weighted sum is the fused chain of rowBaseSpmm3, max takes the rounded product. Rows without
- * entries give 0. op: 0 = sum, 1 = max. */
+ * weighted sum is the fused chain of rowBaseSpmm3, max takes the rounded product.
+ * op: 0 = sum, 1 = max from -inf (fmaxf); both give 0 for rows without entries.
+ * op 2 = the reference's DGL copy-max (gcn/dgl-custom/binary_reduce_max.cu): max_init() returns
+ * -10000 (:22-24), max_reduce(acc, x) is acc > x ? acc : x (:18-20), applied to each entry of
+ * the row in CSR order (topoSimpleSPMMMaxKernel :151-166; the tiled kernels :26-149 apply the
+ * same two functions in the same order), and an empty row keeps -10000. */
 void or_spmm_reduce_f32(int M, int N, const int *rowptr, const int *colind, const float *val,
                         const float *B, long ldb, float *C, int op) {
     for (int m = 0; m < M; ++m) {
         float *c = C + (long)m * N;
-        for (int j = 0; j < N; ++j) c[j] = op == 0 ? 0.0f : -INFINITY;
+        for (int j = 0; j < N; ++j) c[j] = op == 0 ? 0.0f : op == 1 ? -INFINITY : -10000.0f;
         for (int e = rowptr[m]; e < rowptr[m + 1]; ++e) {
             const float *b = B + (long)colind[e] * ldb;
             for (int j = 0; j < N; ++j) {
-                if (op == 0)
+                if (op == 0) {
                     c[j] = val ? fmaf(b[j], val[e], c[j]) : c[j] + b[j];
-                else
+                } else if (op == 1) {
                     c[j] = fmaxf(c[j], val ? val[e] * b[j] : b[j]);
+                } else {
+                    const float x = val ? val[e] * b[j] : b[j];
+                    c[j] = c[j] > x ? c[j] : x;
+                }
             }
         }
-        if (rowptr[m] == rowptr[m + 1])
+        if (rowptr[m] == rowptr[m + 1] && op != 2)
             for (int j = 0; j < N; ++j) c[j] = 0.0f;
     }
 }

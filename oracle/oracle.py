@@ -180,7 +180,7 @@ def spmm_reduce_f32(rowptr, colind, B, val=None, op="sum"):
     out = np.empty((M, B.shape[1]), np.float32)
     v = None if val is None else np.ascontiguousarray(val, np.float32)
     lib().or_spmm_reduce_f32(M, B.shape[1], rowptr, colind, None if v is None else v.ctypes.data,
-                             B, B.shape[1], out, {"sum": 0, "max": 1}[op])
+                             B, B.shape[1], out, {"sum": 0, "max": 1, "max_dgl": 2}[op])
     return out
 
 
@@ -382,3 +382,29 @@ def mlp_adam(p, g, m, v, lr, b1, b2, eps, wd, step):
     mh = m / (1 - b1 ** step)
     vh = v / (1 - b2 ** step)
     return p - lr * mh / (np.sqrt(vh) + eps), m, v
+
+
+def ref_read_mtx(path: str):
+    """The reference's own readMtx<float> (gcn/util/util.hpp:286-333) run on ``path`` through
+    ``oracle/_ref/libref_mtx.so``: (nrows, ncols, rows, cols, vals) as it leaves its vectors,
+    or None when the library was not built (no reference sources)."""
+    L = ref_lib("mtx")
+    if L is None:
+        return None
+    ip = ctypes.POINTER(ctypes.c_int)
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.ref_read_mtx.argtypes = [ctypes.c_char_p, ip, ip, ip, ctypes.POINTER(ip),
+                               ctypes.POINTER(ip), ctypes.POINTER(fp)]
+    L.ref_read_mtx.restype = ctypes.c_int
+    L.ref_mtx_free.argtypes = [ctypes.c_void_p]
+    m, n, nv = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    r, c, v = ip(), ip(), fp()
+    L.ref_read_mtx(path.encode(), ctypes.byref(m), ctypes.byref(n), ctypes.byref(nv),
+                   ctypes.byref(r), ctypes.byref(c), ctypes.byref(v))
+    k = nv.value
+    out = (np.ctypeslib.as_array(r, (max(k, 1),))[:k].copy(),
+           np.ctypeslib.as_array(c, (max(k, 1),))[:k].copy(),
+           np.ctypeslib.as_array(v, (max(k, 1),))[:k].copy())
+    for p in (r, c, v):
+        L.ref_mtx_free(ctypes.cast(p, ctypes.c_void_p))
+    return (m.value, n.value) + out

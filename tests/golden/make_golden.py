@@ -1,8 +1,8 @@
 """Generate the golden vectors in this folder from the reference's own kernels.
 
-Run in a checkout that has the reference sources (REF, default /root/reference):
+Run with the path of a reference checkout (REF, required):
 
-    python tests/golden/make_golden.py [REF] [--only NAME]
+    python tests/golden/make_golden.py REF [--only NAME]
 
 It compiles the reference's SDMM.cpp, SpMV.cpp and sparseTranspose.cpp unmodified through
 oracle/Makefile (target ``ref``; on x86_64 a scalar NEON shim stands in for <arm_neon.h>),
@@ -10,7 +10,8 @@ runs them on small seeded inputs and saves inputs and outputs as .npz files:
 
 * spmm_rowbasespmm3.npz -- rowBaseSpmm3 (SDMM.cpp:90-114) from a zeroed C, and after a
   second call (the driver's accumulate pattern, SDMM.cpp:277-283), plus origin
-  (SDMM.cpp:422-448); A built by the reference's toCSR (SDMM.cpp:355-370) from a dense
+  (SDMM.cpp:422-448) and rowBaseSpmm2 (SDMM.cpp:65-89, its cblas_saxpy restated as
+  OpenBLAS's fused kernels compute it: oracle/ref_bridge/cblas_saxpy.c); A built by the reference's toCSR (SDMM.cpp:355-370) from a dense
   matrix;
 * spmv_vcsr4.npz -- toVectorAwareCSR (SpMV.cpp:15-38) and sparse_dense_vector
   (SpMV.cpp:155-179);
@@ -18,6 +19,10 @@ runs them on small seeded inputs and saves inputs and outputs as .npz files:
   scan, ascending columns, as toCSR writes them), C dense, accumulated over two calls;
 * transpose_triplets.npz -- convert (sparseTranspose.cpp:71-92) and fast_transpose
   (sparseTranspose.cpp:95-142) run on one thread (stable order);
+* mtx_reader.npz -- the reference's Matrix Market reader readMtx<float> (gcn/util/util.hpp:
+  286-333, with makeSymmetric :218-284) on small seeded .mtx texts (stored in the file):
+  symmetric real and pattern files with self-loops and duplicates, general real with
+  duplicates, integer with upper-case qualifiers, skew-symmetric;
 * gcn_op.npz -- the reference's own gcn/pytorch-custom/op.py imported as is: its
   SPMMFunction forward and backward and one GCNConv forward+backward on a small seeded graph.
   The module's ``spmm = load(name='spmm', ...)`` (op.py:6) is served by the reference's
@@ -81,9 +86,12 @@ def spmm_cases(ref):
         ref.ref_rowBaseSpmm3(_p(rowptr), _p(colind), _p(val), _p(B), _p(C2), M, K, N, 4)
         Co = np.zeros((M, N), np.float32)
         ref.ref_origin(_p(rowptr), _p(colind), _p(val), _p(B), _p(Co), M, K, N, 4)
+        Cs = np.zeros((M, N), np.float32)
+        ref.ref_rowBaseSpmm2(_p(rowptr), _p(colind), _p(val), _p(B), _p(Cs), M, K, N, 4)
         out.update({f"c{i}_shape": np.array([M, K, N], np.int32), f"c{i}_rowptr": rowptr,
                     f"c{i}_colind": colind[:nnz], f"c{i}_val": val[:nnz], f"c{i}_B": B,
-                    f"c{i}_C": C1, f"c{i}_C_twice": C2, f"c{i}_C_origin": Co})
+                    f"c{i}_C": C1, f"c{i}_C_twice": C2, f"c{i}_C_origin": Co,
+                    f"c{i}_C_saxpy": Cs})
     out["n_cases"] = np.array(len(cases), np.int32)
     np.savez_compressed(os.path.join(HERE, "spmm_rowbasespmm3.npz"), **out)
 
@@ -166,6 +174,71 @@ def transpose_cases(ref):
     np.savez_compressed(os.path.join(HERE, "transpose_triplets.npz"), **out)
 
 
+def mtx_texts():
+    """Small seeded Matrix Market files covering what the reference's reader distinguishes:
+    symmetric (mirrors, self-loops, duplicates, real values that the compaction misaligns),
+    symmetric pattern, general with duplicates kept, integer, skew-symmetric (read as stored),
+    upper-case qualifiers and comment lines."""
+    rng = np.random.default_rng(4242)
+    texts = {}
+
+    def body(n, m, entries, field):
+        lines = [f"{n} {m} {len(entries)}"]
+        for r, c, v in entries:
+            lines.append(f"{r + 1} {c + 1}" + ("" if field == "pattern" else f" {v}"))
+        return "\n".join(lines) + "\n"
+
+    def entries(n, m, k, field, diag=0, dups=0, lower=False):
+        # symmetric (lower) files get distinct keys plus exact duplicate lines: the value that
+        # survives a run of equal keys follows std::sort's unspecified order of equal elements,
+        # so only same-valued duplicates give a result that does not depend on it
+        out, seen = [], set()
+        for _ in range(k):
+            r, c = int(rng.integers(0, n)), int(rng.integers(0, m))
+            if lower and c > r:
+                r, c = c, r
+            if lower and ((r, c) in seen or r == c):
+                continue
+            seen.add((r, c))
+            v = int(rng.integers(-9, 10)) if field == "integer" else float(np.float32(rng.normal()))
+            out.append((r, c, v))
+        for i in rng.choice(min(n, m), diag, replace=False):
+            out.append((int(i), int(i), 1.5))
+        for _ in range(dups):
+            out.append(out[int(rng.integers(0, len(out)))])
+        order = rng.permutation(len(out))
+        return [out[i] for i in order]
+
+    texts["sym_real"] = ("%%MatrixMarket matrix coordinate real symmetric\n% seeded\n" +
+                         body(40, 40, entries(40, 40, 120, "real", diag=6, dups=5, lower=True), "real"))
+    texts["sym_pattern"] = ("%%MatrixMarket matrix coordinate pattern symmetric\n" +
+                            body(60, 60, entries(60, 60, 200, "pattern", diag=4, dups=7, lower=True), "pattern"))
+    texts["general_real"] = ("%%MatrixMarket matrix coordinate real general\n%\n% two comments\n" +
+                             body(30, 45, entries(30, 45, 150, "real", diag=3, dups=6), "real"))
+    texts["general_int"] = ("%%MatrixMarket MATRIX Coordinate INTEGER General\n" +
+                            body(25, 25, entries(25, 25, 90, "integer"), "integer"))
+    texts["skew_real"] = ("%%MatrixMarket matrix coordinate real skew-symmetric\n" +
+                          body(20, 20, entries(20, 20, 50, "real", lower=True), "real"))
+    return texts
+
+
+def mtx_cases():
+    import tempfile
+    out = {}
+    names = sorted(mtx_texts().items())
+    with tempfile.TemporaryDirectory() as td:
+        for i, (name, text) in enumerate(names):
+            path = os.path.join(td, name + ".mtx")
+            with open(path, "w") as f:
+                f.write(text)
+            m, n, r, c, v = O.ref_read_mtx(path)
+            out.update({f"c{i}_name": np.array(name), f"c{i}_text": np.array(text),
+                        f"c{i}_shape": np.array([m, n], np.int32), f"c{i}_rows": r,
+                        f"c{i}_cols": c, f"c{i}_vals": v})
+    out["n_cases"] = np.array(len(names), np.int32)
+    np.savez_compressed(os.path.join(HERE, "mtx_reader.npz"), **out)
+
+
 def gcn_cases(ref_dir):
     import types
 
@@ -242,13 +315,16 @@ def main():
     only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
     if only:
         args = [a for a in args if a != only]
-    ref_dir = args[0] if args else "/root/reference"
+    if not args:
+        raise SystemExit("usage: make_golden.py REF [--only NAME] (REF: the reference checkout)")
+    ref_dir = args[0]
     if not O.build_ref(ref_dir):
         raise SystemExit("could not build the reference kernels from " + ref_dir)
     makers = {"spmm": lambda: spmm_cases(O.ref_lib("sdmm")),
               "spmv": lambda: spmv_cases(O.ref_lib("spmv")),
               "transpose": lambda: transpose_cases(O.ref_lib("transpose")),
-              "spgemm": lambda: spgemm_cases(O.ref_lib("spgemm"))}
+              "spgemm": lambda: spgemm_cases(O.ref_lib("spgemm")),
+              "mtx": mtx_cases}
     for name, make in makers.items():
         if only in (None, name):
             make()

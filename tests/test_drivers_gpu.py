@@ -32,6 +32,11 @@ def test_spmm_shims(drv, golden):
         assert np.array_equal(C.view(np.uint32), g[f"c{i}_C"].view(np.uint32))
         drv.as_drv_rowBaseSpmm3(_p(rp), _p(ci), _p(v), _p(B), _p(C), M, K, N, 32)
         assert np.array_equal(C.view(np.uint32), g[f"c{i}_C_twice"].view(np.uint32))
+        Cs = np.zeros((M, N), np.float32)
+        drv.as_drv_rowBaseSpmm2(_p(rp), _p(ci), _p(v), _p(B), _p(Cs), M, K, N, 32)
+        assert drv.as_drv_last_status() == 0
+        # SDMM.cpp:65-89 (cblas_saxpy per entry) compiled from the reference, golden C_saxpy
+        assert np.array_equal(Cs.view(np.uint32), g[f"c{i}_C_saxpy"].view(np.uint32))
         Co = np.full((M, N), 7.0, np.float32)
         drv.as_drv_origin(_p(rp), _p(ci), _p(v), _p(B), _p(Co), M, K, N, 32)
         assert np.array_equal(Co.view(np.uint32), g[f"c{i}_C"].view(np.uint32))

@@ -21,6 +21,9 @@ def test_spmm_chain_matches_rowbasespmm3_golden(oracle, golden):
         assert np.array_equal(C.view(np.uint32), g[f"c{i}_C"].view(np.uint32)), i
         C2 = oracle.spmm_fma_chain_f32(rp, ci, v, B, C=C, threads=2)
         assert np.array_equal(C2.view(np.uint32), g[f"c{i}_C_twice"].view(np.uint32)), i
+        # rowBaseSpmm2 (SDMM.cpp:65-89): one fused saxpy step per entry and column, in CSR
+        # order -- the same chain
+        assert np.array_equal(C.view(np.uint32), g[f"c{i}_C_saxpy"].view(np.uint32)), i
         # origin() (SDMM.cpp:422-448): same terms, its own compiled summation; agrees to
         # FP32 rounding
         C64, A64 = oracle.spmm_f64(rp, ci, v, B, threads=1)
@@ -239,3 +242,31 @@ def test_spgemm_dense_against_compiled_reference(oracle):
     arrs = [x.copy() for x in (a.rowptr, a.colind, a.val, b.rowptr, b.colind, b.val)]
     ref.ref_sparse_matrix_mul3(*[_p(x) for x in arrs], _p(C), 120, 90, 70, 2)
     assert np.array_equal(mine.view(np.uint32), C.view(np.uint32))
+
+
+def _dgl_copy_max(rowptr, colind, B):
+    """The reference's copy-max kernel read line by line (gcn/dgl-custom/binary_reduce_max.cu):
+    acc1 = max_init() = -10000 (:22-24, :158); for ptr in [lb, hb): acc1 = max_reduce(acc1,
+    B[A_indices[ptr]*k + col]) with max_reduce(acc, x) = acc > x ? acc : x (:18-20, :160-165);
+    C = acc1 (:166). Pure Python over float32 scalars, for small cases."""
+    M, N = rowptr.size - 1, B.shape[1]
+    C = np.empty((M, N), np.float32)
+    for r in range(M):
+        for j in range(N):
+            acc = np.float32(-10000)
+            for p in range(rowptr[r], rowptr[r + 1]):
+                x = B[colind[p], j]
+                acc = acc if acc > x else x
+            C[r, j] = acc
+    return C
+
+
+def test_reduce_max_dgl_restates_reference_loop(oracle):
+    a = S.powerlaw_csr(300, 2.0, 5.0, seed=71, n_cols=200)
+    rng = np.random.default_rng(72)
+    B = (rng.uniform(-30000, 20000, (200, 5))).astype(np.float32)
+    B[rng.integers(0, 200, 12), rng.integers(0, 5, 12)] = np.nan
+    got = oracle.spmm_reduce_f32(a.rowptr, a.colind, B, op="max_dgl")
+    ref = _dgl_copy_max(a.rowptr, a.colind, B)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+    assert (np.diff(a.rowptr) == 0).any()

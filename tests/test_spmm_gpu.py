@@ -246,6 +246,27 @@ def test_reduce_aggregations(oracle, op):
     A.sync_status()
 
 
+def test_reduce_max_dgl(oracle):
+    """The reference's DGL copy-max (binary_reduce_max.cu: start at -10000, acc > x ? acc : x):
+    empty rows give -10000, values below -10000 never show, a NaN entry is replaced by the entry
+    after it. Bit-exact against the oracle, NaN payloads included."""
+    a = S.powerlaw_csr(2000, 2.0, 7.0, seed=61, n_cols=1500)
+    rng = np.random.default_rng(62)
+    for N_ in (1, 31, 64, 130):
+        B = S.dense_uniform((1500, N_), 63) * 30000.0 - 15000.0  # about half below -10000
+        B[rng.integers(0, 1500, 40), rng.integers(0, N_, 40)] = np.nan
+        B = B.astype(np.float32)
+        rp, ci, v = csr_dev(a)
+        for val in (None, a.val):
+            got = A.spmm_reduce(rp, ci, to_dev(B), val=None if val is None else v, op="max_dgl")
+            ref = oracle.spmm_reduce_f32(a.rowptr, a.colind, B, val=val, op="max_dgl")
+            assert np.array_equal(bits(got), bits(ref)), (N_, val is None)
+            empty = np.diff(a.rowptr) == 0
+            assert empty.any() and (got.cpu().numpy()[empty] == -10000.0).all()
+            assert (np.nan_to_num(got.cpu().numpy(), nan=0.0) >= -10000.0).all()
+    A.sync_status()
+
+
 def _skewed(seed, n_rows=3000, n_cols=40000, long_lens=(50000, 4097, 2048, 257, 256, 300)):
     """Short rows plus rows at and past the long-row threshold (256 entries): one long enough
     to cross many (colind, val) chunks of 2048 entries."""
