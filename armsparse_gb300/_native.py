@@ -28,6 +28,7 @@ SIGNATURES = {
     "as_last_error": (ctypes.c_char_p, []),
     "as_status_string": (ctypes.c_char_p, [_I]),
     "as_ctx_launch_count": (_U64, [_P]),
+    "as_ctx_set_spin_limit": (_I, [_P, ctypes.c_uint]),
     "as_csr_validate": (_I, [_P, _I, _I, _I, _P, _P, _I, _P]),
     "as_spmm_csr_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _F, _I, _P]),
     "as_spmm_csr_bf16": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _F, _I, _P]),

@@ -139,6 +139,12 @@ as_status as_ctx_destroy(as_ctx *c) {
 
 uint64_t as_ctx_launch_count(const as_ctx *c) { return c ? c->launches : 0; }
 
+as_status as_ctx_set_spin_limit(as_ctx *c, unsigned polls) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_ctx_set_spin_limit: ctx is NULL");
+    c->spin_limit = polls;
+    return AS_OK;
+}
+
 as_status as_ctx_sync_status(as_ctx *c, void *stream) {
     if (!c) return fail(AS_ERR_INVALID_VALUE, "as_ctx_sync_status: ctx is NULL");
     DeviceGuard g(c->device);

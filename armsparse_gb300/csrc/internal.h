@@ -21,6 +21,8 @@ struct as_ctx {
     std::vector<void *> retired;   // outgrown arenas: kept until the context is destroyed, since
                                    // kernels in flight or recorded in a CUDA graph may use them
     uint64_t launches = 0;         // kernels this library launched through the context
+    unsigned spin_limit = 1u << 22;  // polls of a coordination wait before it gives up
+                                     // (as_ctx_set_spin_limit); copy-drain waits keep 1 << 22
 };
 
 namespace as {

@@ -13,7 +13,10 @@
 //
 // (colind, val) arrive in coalesced batches of 32 (current and next batch held in lane
 // registers) and are broadcast with shuffles. Every wait is bounded: a timeout sets the status
-// word, lane 0 waits (bounded) for the copies it issued, and the warp leaves.
+// word, lane 0 waits (bounded) for the copies it issued, and the warp leaves. The warp's wait
+// for a ring slot polls at most `spin_limit` times (the context's setting, as_ctx_set_spin_limit:
+// a test sets it to 0 to take the timeout path); the drain of its issued copies before it
+// leaves always polls up to kSpinLimit times per copy, so no copy is in flight when it exits.
 #include "common.cuh"
 #include "internal.h"
 
@@ -39,8 +42,8 @@ __device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
-__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
-    for (unsigned i = 0; i < kSpinLimit; ++i)
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, unsigned limit = kSpinLimit) {
+    for (unsigned i = 0; i < limit; ++i)
         if (bar_try(bar, parity)) return true;
     return false;
 }
@@ -99,7 +102,8 @@ template <typename T, int LB, int STAGES>
 __global__ void __launch_bounds__(kWarps * 32)
 spmm_bulk(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
           const int *__restrict__ colind, const T *__restrict__ val, const T *__restrict__ B,
-          long ldb, float *__restrict__ C, long ldc, float beta, unsigned *status) {
+          long ldb, float *__restrict__ C, long ldc, float beta, unsigned *status,
+          unsigned spin_limit) {
     using L = Lane<T, LB>;
     using S = BulkSmem<T, LB, STAGES>;
     constexpr int E = L::E;
@@ -176,7 +180,8 @@ spmm_bulk(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
             ++issued;
         }
         const int slot = done % STAGES;
-        const bool got = __all_sync(0xffffffffu, bar_wait(bar0 + 8 * slot, (done / STAGES) & 1));
+        const bool got =
+            __all_sync(0xffffffffu, bar_wait(bar0 + 8 * slot, (done / STAGES) & 1, spin_limit));
         if (!got) {
             ok = false;
             break;
@@ -237,7 +242,7 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, cudaStream_t s) {
     dim3 grid(static_cast<unsigned>(ceil_div(a.M, kWarps)), static_cast<unsigned>(ceil_div(a.N, TILE)));
     spmm_bulk<T, LB, STAGES><<<grid, kWarps * 32, S::kBytes, s>>>(
         a.M, a.K, a.N, a.nnz, a.rowptr, a.colind, static_cast<const T *>(a.val),
-        static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, a.status);
+        static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, a.status, ctx->spin_limit);
     ctx->launches++;
     return check_cuda(cudaGetLastError(), "spmm bulk launch");
 }

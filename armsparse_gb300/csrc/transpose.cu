@@ -118,8 +118,9 @@ scan_downsweep(const int *__restrict__ in, long n, const int *__restrict__ block
 // ---- transpose kernels -----------------------------------------------------------------
 // rowidx[e] = row of entry e. Each thread takes kExpand consecutive entries: one binary
 // search over rowptr for its first entry, then it steps the row forward -- so one row with
-// millions of entries is spread over many threads. Rows with malformed pointers flag and
-// write nothing.
+// millions of entries is spread over many threads. An entry that no well-formed row holds
+// (malformed pointers) is flagged and given row 0, so every row index written stays in [0, M)
+// and no slot keeps data from an earlier call.
 constexpr int kExpand = 8;
 __global__ void __launch_bounds__(kThreads)
 expand_rows(int M, int nnz, const int *__restrict__ rowptr, int *__restrict__ rowidx,
@@ -145,7 +146,8 @@ expand_rows(int M, int nnz, const int *__restrict__ rowptr, int *__restrict__ ro
         }
         if (rs < 0 || re < rs || re > nnz || e < rs || e >= re) {
             flag(status, kFlagBadRowptr);
-            continue;  // malformed pointers: the slot keeps its value (check_rowptr_ends)
+            rowidx[e] = 0;  // malformed pointers: an in-range row, never stale scratch
+            continue;
         }
         rowidx[e] = r;
     }
@@ -506,7 +508,7 @@ as_status f32_to_bf16_launch(as_ctx *ctx, long n, const float *src, uint16_t *ds
 // AS_CSR2CSC_STATIC_MAX_NNZ entries; every GPU that loads this library holds it until the
 // process exits. Host code only knows the array through the address cudaGetSymbolAddress
 // returns for the current device (the symbol itself is a host-side stand-in), fetched once
-// per device by the first call on that device.
+// per device by the first call on that device and kept for the life of the process.
 #include <mutex>
 
 namespace as {
@@ -619,11 +621,14 @@ extern "C" as_status as_csr2csc_static(int M, int N, int nnz, const int *rowptr,
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return AS_ERR_CUDA;
     if (dev < 0 || dev >= kStaticMaxDevices) return AS_ERR_UNSUPPORTED;
+    // a launch error left pending by earlier, unrelated work would otherwise be returned as this
+    // call's: take it off first, so the status below belongs to this call's own launches
+    (void)cudaGetLastError();
     StaticSlot slot;
     if (static_slot(dev, &slot) != cudaSuccess) return AS_ERR_CUDA;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    // the status word keeps the previous call's flags: start each call from zero
-    if (cudaMemsetAsync(slot.status, 0, sizeof(unsigned), s) != cudaSuccess) return AS_ERR_CUDA;
+    // slot.status only gives the kernels a word to flag malformed input into; nothing reads it
+    // (the entry point reports argument errors only), so it is not reset between calls
     if (nnz == 0) {
         return cudaMemsetAsync(colptr, 0, sizeof(int) * (static_cast<size_t>(N) + 1), s) ==
                        cudaSuccess

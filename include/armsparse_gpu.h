@@ -47,6 +47,14 @@ const char *as_last_error(void);
 const char *as_status_string(as_status s);
 /* Number of this library's kernels launched through `ctx` since creation. */
 uint64_t as_ctx_launch_count(const as_ctx *ctx);
+/* How many times a kernel polls a coordination wait (the bulk-copy SpMM variants' wait for a
+ * gathered row to land in shared memory) before it gives up: it then sets AS_ERR_TIMEOUT in
+ * the status word, waits for the copies it issued (that drain always polls up to 2^22 times
+ * per copy, whatever this setting), and leaves its outputs unwritten. Default 2^22 (a few
+ * seconds). 0 makes every such wait give up at once: tests use it to take the timeout path
+ * without a fault or a hang. Applies to launches issued after the call. No counterpart in the
+ * reference, which has no device-side waits. */
+as_status as_ctx_set_spin_limit(as_ctx *ctx, unsigned polls);
 
 /* ---- CSR validation (synchronous) --------------------------------------------------------
  * rowptr[0] == 0, rowptr non-decreasing, rowptr[n_rows] == nnz, 0 <= colind < n_cols.
@@ -265,11 +273,17 @@ as_status as_gather_f32(as_ctx *ctx, long n, long n_src, const float *src, const
  *    nothing. Other argument errors return AS_ERR_INVALID_VALUE (AS_ERR_INVALID_CSR for entries
  *    without rows or columns); these statuses are the whole report (as_last_error() is not set).
  *  - The first call on a device looks up the array's device address (cudaGetSymbolAddress)
- *    with that device current; make that first call before any stream capture.
+ *    with that device current; make that first call before any stream capture. The address is
+ *    kept for the life of the process: after cudaDeviceReset (or anything else that tears down
+ *    and recreates the device's primary context) this entry point must not be called again on
+ *    that device.
+ *  - A launch error that earlier, unrelated work left pending in the CUDA runtime is cleared
+ *    at entry (cudaGetLastError), so that the status returned is this call's own.
  *  - All calls share the one array: calls whose work overlaps on the GPU (different streams or
  *    threads, no ordering between them) race and corrupt each other's results. Serialise them.
  *  - Malformed CSR is handled memory-safely but not reported (there is no context to hold the
- *    flag); validate with as_csr_validate beforehand where that matters.
+ *    flag): every row index written is still in [0, M), but the result is meaningless.
+ *    Validate with as_csr_validate beforehand where that matters.
  * Same output contract as as_csr2csc (rows ascending within columns, bit-exact). */
 #define AS_CSR2CSC_STATIC_MAX_NNZ (1 << 18)
 as_status as_csr2csc_static(int M, int N, int nnz, const int *rowptr, const int *colind,
