@@ -8,12 +8,23 @@
 //
 // Each output element is still one fused-FMA chain over the row's entries in CSR order (the
 // order cannot be split without changing the bits), so the speed comes from feeding the
-// chains: a CTA takes one (long row, 64-byte column slice) at a time; all 256 threads copy B
-// segments
-// of upcoming entries into a shared-memory ring with cp.async (kStages stages of kStage
-// entries in flight), and the slice's columns -- one per consumer thread -- run their chains
-// out of shared memory. Column indices and values are staged a chunk of kChunk entries ahead
-// in registers (plain coalesced loads) and parked in shared memory half a chunk later.
+// chains. A CTA takes one (long row, 64-byte column slice) at a time and splits its warps by
+// role:
+//  - warp 0 is the consumer: one lane per column of the slice runs the chain out of shared
+//    memory, stage after stage, and never waits on anything but the stage it needs next;
+//  - warps 1..7 are producers: for each stage of kStage entries they read the entries'
+//    column indices and values, copy each entry's B segment into the stage's ring slot with
+//    cp.async (one commit group per stage) and write its value next to it. A producer thread
+//    announces stage s on the slot's `full` mbarrier once its copies of that stage have
+//    landed, which it checks after issuing stage s + kLag (cp.async.wait_group kLag), so kLag
+//    stages of copies stay in flight per thread; every arrival is the thread's own, none is
+//    left pending when the CTA moves on. A slot is refilled only after the consumer arrives
+//    on its `empty` mbarrier.
+// The producers run up to kStages stages ahead of the consumer, which covers the index load
+// and the gather latency. Every wait is bounded; a wait that gives up sets the timeout flag
+// and an abort flag that makes the other role leave too; each thread waits for its own copies
+// before the CTA moves on, and a row whose wait gave up is left unwritten. A malformed column
+// index is flagged and its entry reads B row 0 with value 0.
 //
 // The list counter and a CTA-done counter live in the context's device words; the last CTA
 // to finish resets both, so the next call starts from zero without a memset.
@@ -26,32 +37,53 @@ namespace as {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kSliceBytes = 64;   // B bytes per entry per stage (16 fp32 / 32 bf16 columns)
-constexpr int kStage = 64;        // entries per pipeline stage
-constexpr int kStages = 12;       // stages in the B ring: 704 entries in flight cover the
-                                  // gather latency at the chain's ~4 cycles per entry
-constexpr int kChunk = 2048;      // entries per (colind, val) chunk; a multiple of kStage
-constexpr int kChunkPerThread = kChunk / kThreads;
-constexpr int kSmemBytes = kStages * kStage * kSliceBytes + 2 * kChunk * 8;
-// the next chunk's (colind, val) reach shared memory half a chunk in, before the B lookahead
-// of kStages - 1 stages first needs them
-static_assert(kStages - 1 < kChunk / kStage / 2, "B lookahead must not outrun the chunk staging");
+constexpr int kProducers = kThreads - 32;  // warps 1..7
+constexpr int kSliceBytes = 64;            // B bytes per entry per stage (16 fp32 / 32 bf16 columns)
+constexpr int kStage = 64;                 // entries per pipeline stage
+constexpr int kStages = 24;                // ring slots
+constexpr int kLag = 12;                   // stages of copies in flight per producer thread
+static_assert(kLag < kStages, "a producer must announce stage s before it waits to refill its slot");
+constexpr unsigned kSpinLimit = 1u << 22;  // polls of a bounded wait (a few seconds at most)
+constexpr int kRingBytes = kStages * kStage * kSliceBytes;
+constexpr int kVringBytes = kStages * kStage * 4;
+constexpr int kSmemBytes = kRingBytes + kVringBytes + 2 * kStages * 8 + 16;
 
 __device__ __forceinline__ float to_f32(float v) { return v; }
 __device__ __forceinline__ float to_f32(uint16_t v) { return bf16_to_f32(v); }
 
-template <int GB>
-__device__ __forceinline__ void cp_async(void *smem, const void *gmem) {
-    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
-    if constexpr (GB == 16)
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-    else
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+
+template <int GB>
+__device__ __forceinline__ void cp_async(uint32_t dst, const void *gmem) {
+    if constexpr (GB == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for `parity` of the mbarrier at `bar`; false when `limit` polls pass or the
+// other role has given up.
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, unsigned limit,
+                                         const volatile int *abort_flag) {
+    for (unsigned i = 0; i < limit; ++i) {
+        if (bar_try(bar, parity)) return true;
+        if (*abort_flag) return false;
+    }
+    return false;
 }
 
 // T: storage type of val and B (float or uint16_t = bf16); GB: cp.async size in bytes.
@@ -61,17 +93,20 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
           const int *__restrict__ colind, const T *__restrict__ val, const T *__restrict__ B,
           long ldb, float *__restrict__ C, long ldc, float beta, unsigned *status,
           const int *__restrict__ list, unsigned *counters, uint16_t *__restrict__ C16,
-          bool relu) {
+          bool relu, unsigned spin_limit) {
     constexpr int W = kSliceBytes / static_cast<int>(sizeof(T));  // columns per slice
-    extern __shared__ __align__(16) unsigned char smem[];
-    unsigned char *ring = smem;  // [kStages][kStage][kSliceBytes]
-    int *kbuf = reinterpret_cast<int *>(smem + kStages * kStage * kSliceBytes);  // [2][kChunk]
-    float *vbuf = reinterpret_cast<float *>(kbuf + 2 * kChunk);                  // [2][kChunk]
+    constexpr int P = kSliceBytes / GB;                            // copy pieces of a full slice
+    extern __shared__ __align__(128) unsigned char smem[];
+    unsigned char *ring = smem;                                       // [kStages][kStage][64 B]
+    float *vring = reinterpret_cast<float *>(smem + kRingBytes);      // [kStages][kStage]
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + kRingBytes + kVringBytes);
+    uint64_t *empty = full + kStages;
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(empty + kStages);
 
     // launched as a programmatic dependent of the row-split kernel: wait for it to finish
     // (and its list writes to be visible) before reading the list
     asm volatile("griddepcontrol.wait;\n" ::: "memory");
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int n_long = static_cast<int>(
         min(*reinterpret_cast<volatile unsigned *>(counters), static_cast<unsigned>(M)));
     const int n_slices = static_cast<int>(ceil_div(N, W));
@@ -82,159 +117,151 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         const int item = static_cast<int>(u / n_slices);
         const int slice0 = static_cast<int>(u - static_cast<long>(item) * n_slices) * W;
         const int w = min(W, N - slice0);                  // columns of this slice
-        const int seg = w * static_cast<int>(sizeof(T));   // bytes of B per entry in this slice
-        const int pieces = seg / GB;                       // cp.async pieces per entry
+        const int pieces = w * static_cast<int>(sizeof(T)) / GB;  // copy pieces per entry
         const int r = list[item];
         if (r < 0 || r >= M) continue;
         int lo, hi;
         row_range(rowptr, r, nnz, status, lo, hi);
         const int L = hi - lo;
         const int n_stages = static_cast<int>(ceil_div(L, kStage));
-        const int n_chunks = static_cast<int>(ceil_div(L, kChunk));
 
-        // chunk 0 of (colind, val), straight into shared memory
-        for (int i = tid; i < kChunk; i += kThreads) {
-            int k = -1;
-            float v = 0.0f;
-            if (i < L) {
-                k = ld_stream(colind + lo + i);
-                v = to_f32(ld_stream(val + lo + i));
-                if (static_cast<unsigned>(k) >= static_cast<unsigned>(K)) {
-                    flag(status, kFlagBadColind);
-                    k = -1;
-                    v = 0.0f;
-                }
+        if (tid == 0) {
+            for (int s = 0; s < kStages; ++s) {
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(full + s)),
+                             "r"(kProducers));
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)));
             }
-            kbuf[i] = k;
-            vbuf[i] = v;
+            *abort_flag = 0;
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
         __syncthreads();
 
-        // B segments of stage st into ring slot st % kStages. Warp w copies entries 8w..8w+7 of
-        // the stage; lane l takes piece l % P of entry l / P (P pieces per full slice), so a
-        // full warp instruction moves 512 bytes (a copy instruction costs the same issue slot
-        // however few lanes it carries). Entries past the row are not copied (never read); a
-        // flagged entry gets zeros (its value is 0 as well).
-        const int warp = tid >> 5, lane = tid & 31;
-        auto issue = [&](int st) {
-            if (st < n_stages) {
-                const int base = st * kStage;  // first entry of the stage, relative to lo
-                const int *kb = kbuf + ((base / kChunk) & 1) * kChunk + base % kChunk;
-                unsigned char *dst = ring + (st % kStages) * kStage * kSliceBytes;
-                constexpr int P = kSliceBytes / GB;           // pieces of a full slice (4 or 16)
-                constexpr int kPerWarp = kStage / (kThreads / 32);
-#pragma unroll
-                for (int t = 0; t < kPerWarp * P / 32; ++t) {
-                    const int p = lane + 32 * t;
-                    const int j = warp * kPerWarp + p / P, q = p % P;
-                    if (q >= pieces || base + j >= L) continue;
-                    const int k = kb[j];
-                    unsigned char *d = dst + j * kSliceBytes + q * GB;
-                    if (k >= 0) {
-                        const unsigned char *src = reinterpret_cast<const unsigned char *>(
-                            B + static_cast<long>(k) * ldb + slice0);
-                        cp_async<GB>(d, src + q * GB);
-                    } else if constexpr (GB == 16) {
-                        *reinterpret_cast<uint4 *>(d) = make_uint4(0, 0, 0, 0);
-                    } else {
-                        *reinterpret_cast<unsigned *>(d) = 0u;
-                    }
-                }
-            }
-            cp_async_commit();  // one group per stage, empty or not, to keep the counting uniform
-        };
-
         float acc = 0.0f;
         float *crow = C + static_cast<long>(r) * ldc + slice0;
-        if (tid < w && beta != 0.0f) acc = crow[tid] * beta;
-
-        for (int st = 0; st < kStages - 1; ++st) issue(st);
-
-        int kreg[kChunkPerThread];
-        float vreg[kChunkPerThread];
-        for (int st = 0; st < n_stages; ++st) {
-            const int c = st / (kChunk / kStage), sc = st % (kChunk / kStage);
-            // stage the next chunk: registers at its start, shared memory at its middle
-            if (sc == 0 && c + 1 < n_chunks) {
-#pragma unroll
-                for (int i = 0; i < kChunkPerThread; ++i) {
-                    const int e = (c + 1) * kChunk + i * kThreads + tid;
-                    kreg[i] = -1;
-                    vreg[i] = 0.0f;
-                    if (e < L) {
-                        kreg[i] = ld_stream(colind + lo + e);
-                        vreg[i] = to_f32(ld_stream(val + lo + e));
+        if (warp == 0) {
+            // ---- consumer: the chains ----
+            if (lane < w && beta != 0.0f) acc = crow[lane] * beta;
+            for (int s = 0; s < n_stages; ++s) {
+                const int slot = s % kStages;
+                const bool ok = __all_sync(
+                    0xffffffffu, bar_wait(smem_u32(full + slot), (s / kStages) & 1, spin_limit,
+                                          abort_flag));
+                if (!ok) {
+                    if (lane == 0) {
+                        flag(status, kFlagTimeout);
+                        *abort_flag = 1;
                     }
+                    break;
                 }
-            }
-            if (sc == kChunk / kStage / 2 && c + 1 < n_chunks) {
-                int *kd = kbuf + ((c + 1) & 1) * kChunk;
-                float *vd = vbuf + ((c + 1) & 1) * kChunk;
+                if (lane < w) {
+                    const int n = min(kStage, L - s * kStage);
+                    const float *vs = vring + slot * kStage;
+                    const T *bs = reinterpret_cast<const T *>(ring + slot * kStage * kSliceBytes) + lane;
+                    int j = 0;
+                    if (n >= 8) {  // the next 8 entries' loads are in flight during this 8's chain
+                        float b[8], bn[8];
+                        float4 v0 = *reinterpret_cast<const float4 *>(vs);
+                        float4 v1 = *reinterpret_cast<const float4 *>(vs + 4);
 #pragma unroll
-                for (int i = 0; i < kChunkPerThread; ++i) {
-                    int k = kreg[i];
-                    float v = vreg[i];
-                    if (k != -1 && static_cast<unsigned>(k) >= static_cast<unsigned>(K)) {
-                        flag(status, kFlagBadColind);
-                        k = -1;
-                        v = 0.0f;
+                        for (int i = 0; i < 8; ++i) b[i] = to_f32(bs[i * W]);
+                        for (; j + 8 <= n; j += 8) {
+                            const bool more = j + 16 <= n;
+                            float4 n0 = v0, n1 = v1;
+                            if (more) {
+                                n0 = *reinterpret_cast<const float4 *>(vs + j + 8);
+                                n1 = *reinterpret_cast<const float4 *>(vs + j + 12);
+#pragma unroll
+                                for (int i = 0; i < 8; ++i) bn[i] = to_f32(bs[(j + 8 + i) * W]);
+                            }
+                            acc = fmaf(b[0], v0.x, acc);
+                            acc = fmaf(b[1], v0.y, acc);
+                            acc = fmaf(b[2], v0.z, acc);
+                            acc = fmaf(b[3], v0.w, acc);
+                            acc = fmaf(b[4], v1.x, acc);
+                            acc = fmaf(b[5], v1.y, acc);
+                            acc = fmaf(b[6], v1.z, acc);
+                            acc = fmaf(b[7], v1.w, acc);
+                            if (more) {
+                                v0 = n0;
+                                v1 = n1;
+#pragma unroll
+                                for (int i = 0; i < 8; ++i) b[i] = bn[i];
+                            }
+                        }
                     }
-                    kd[i * kThreads + tid] = k;
-                    vd[i * kThreads + tid] = v;
+                    for (; j < n; ++j) acc = fmaf(to_f32(bs[j * W]), vs[j], acc);
                 }
+                __syncwarp();
+                if (lane == 0)
+                    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(
+                                     smem_u32(empty + slot))
+                                 : "memory");
             }
-            __syncthreads();  // slot (st - 1) % kStages is free; staged (colind, val) visible
-            issue(st + kStages - 1);
-            cp_async_wait<kStages - 1>();  // stage st has landed (this thread's copies)
-            __syncthreads();               // ... and every thread's
-            if (tid < w) {
-                const int base = st * kStage;
+        } else {
+            // ---- producers: indices, values and B segments of upcoming stages ----
+            const int p = tid - 32;
+            auto announce = [&](int st) {  // stage st's copies and stores by this thread are done
+                asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(
+                                 smem_u32(full + st % kStages))
+                             : "memory");
+            };
+            int issued = 0;
+            for (int s = 0; s < n_stages; ++s) {
+                const int slot = s % kStages;
+                if (s >= kStages &&
+                    !bar_wait(smem_u32(empty + slot), ((s / kStages) - 1) & 1, kSpinLimit,
+                              abort_flag)) {
+                    if (!*abort_flag) {
+                        flag(status, kFlagTimeout);
+                        *abort_flag = 1;
+                    }
+                    break;
+                }
+                const int base = s * kStage;
                 const int n = min(kStage, L - base);
-                const float *vs = vbuf + ((base / kChunk) & 1) * kChunk + base % kChunk;
-                const T *bs = reinterpret_cast<const T *>(ring + (st % kStages) * kStage * kSliceBytes) + tid;
-                int j = 0;
-                if (n >= 8) {  // the next 8 entries' loads are in flight during this 8's chain
-                    float b[8], bn[8];
-                    float4 v0 = *reinterpret_cast<const float4 *>(vs);
-                    float4 v1 = *reinterpret_cast<const float4 *>(vs + 4);
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) b[i] = to_f32(bs[i * W]);
-                    for (; j + 8 <= n; j += 8) {
-                        const bool more = j + 16 <= n;
-                        float4 n0 = v0, n1 = v1;
-                        if (more) {
-                            n0 = *reinterpret_cast<const float4 *>(vs + j + 8);
-                            n1 = *reinterpret_cast<const float4 *>(vs + j + 12);
-#pragma unroll
-                            for (int i = 0; i < 8; ++i) bn[i] = to_f32(bs[(j + 8 + i) * W]);
-                        }
-                        acc = fmaf(b[0], v0.x, acc);
-                        acc = fmaf(b[1], v0.y, acc);
-                        acc = fmaf(b[2], v0.z, acc);
-                        acc = fmaf(b[3], v0.w, acc);
-                        acc = fmaf(b[4], v1.x, acc);
-                        acc = fmaf(b[5], v1.y, acc);
-                        acc = fmaf(b[6], v1.z, acc);
-                        acc = fmaf(b[7], v1.w, acc);
-                        if (more) {
-                            v0 = n0;
-                            v1 = n1;
-#pragma unroll
-                            for (int i = 0; i < 8; ++i) b[i] = bn[i];
-                        }
+                const uint32_t dst0 = smem_u32(ring + slot * kStage * kSliceBytes);
+                for (int q = p; q < kStage * P; q += kProducers) {
+                    const int j = q / P, piece = q % P;
+                    if (j >= n || piece >= pieces) continue;
+                    const int e = lo + base + j;
+                    int k = ld_stream(colind + e);
+                    const bool bad = static_cast<unsigned>(k) >= static_cast<unsigned>(K);
+                    if (bad) k = 0;
+                    const unsigned char *src =
+                        reinterpret_cast<const unsigned char *>(B + static_cast<long>(k) * ldb + slice0);
+                    cp_async<GB>(dst0 + j * kSliceBytes + piece * GB, src + piece * GB);
+                    if (piece == 0) {
+                        if (bad) flag(status, kFlagBadColind);
+                        vring[slot * kStage + j] = bad ? 0.0f : to_f32(ld_stream(val + e));
                     }
                 }
-                for (; j < n; ++j) acc = fmaf(to_f32(bs[j * W]), vs[j], acc);
+                asm volatile("cp.async.commit_group;\n" ::: "memory");
+                issued = s + 1;
+                if (s >= kLag) {
+                    asm volatile("cp.async.wait_group %0;\n" ::"n"(kLag) : "memory");
+                    announce(s - kLag);
+                }
+            }
+            if (!*abort_flag) {  // the last stages: all copies landed
+                asm volatile("cp.async.wait_all;\n" ::: "memory");
+                for (int st = issued > kLag ? issued - kLag : 0; st < issued; ++st) announce(st);
             }
         }
-        cp_async_wait<0>();
-        if (tid < w) {
+        asm volatile("cp.async.wait_all;\n" ::: "memory");  // this thread's copies have landed
+        __syncthreads();
+        if (warp == 0 && lane < w && !*abort_flag) {
             if (C16)
-                C16[static_cast<long>(r) * ldc + slice0 + tid] = f32_to_bf16(relu_if(acc, relu));
+                C16[static_cast<long>(r) * ldc + slice0 + lane] = f32_to_bf16(relu_if(acc, relu));
             else
-                crow[tid] = acc;
+                crow[lane] = acc;
         }
-        __syncthreads();  // shared memory is reused by the next row
+        if (tid == 0) {
+            for (int s = 0; s < kStages; ++s) {
+                asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(full + s)));
+                asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(empty + s)));
+            }
+        }
+        __syncthreads();  // shared memory and barriers are reused by the next unit
     }
 
     // the last CTA out resets the list counter and the done counter for the next call
@@ -282,7 +309,7 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, const int *list, cudaStream_t s
     cudaError_t e = cudaLaunchKernelEx(&cfg, k, a.M, a.K, a.N, a.nnz, a.rowptr, a.colind,
                                        static_cast<const T *>(a.val), static_cast<const T *>(a.B),
                                        a.ldb, a.C, a.ldc, a.beta, a.status, list, ctx->d_long,
-                                       a.C16, a.relu);
+                                       a.C16, a.relu, ctx->spin_limit);
     ctx->launches++;
     return check_cuda(e != cudaSuccess ? e : cudaGetLastError(), "spmm long rows launch");
 }

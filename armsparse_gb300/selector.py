@@ -197,22 +197,25 @@ class MLP:
         return [p.detach().cpu().numpy().astype(np.float64) for p in self.params]
 
 
-def train(records, epochs=3000, hidden=64, lr=3e-3, seed=0, tau=0.1, device=None, log=None):
-    """Fit the selector on sweep records (full batch); returns a model dict."""
+def train(records, epochs=3000, hidden=64, lr=3e-3, seed=0, tau=0.1, device=None, log=None,
+          candidates=None, fmt=FORMAT):
+    """Fit the selector on sweep records (full batch); returns a model dict. ``candidates``
+    (default: the SpMM CANDIDATES) names the network's outputs, one per timed path."""
+    candidates = candidates or CANDIDATES
     device = device or torch.device("cuda", 0)
     X = np.array([r["features"] for r in records], np.float64)
     mu, sd = X.mean(axis=0), X.std(axis=0) + 1e-6
     Xn = torch.tensor((X - mu) / sd, dtype=torch.float32, device=device)
     T = torch.tensor(np.stack([soft_targets(r["times_ms"], tau) for r in records]),
                      dtype=torch.float32, device=device)
-    net = MLP(X.shape[1], len(CANDIDATES), hidden, seed, device)
+    net = MLP(X.shape[1], len(candidates), hidden, seed, device)
     for ep in range(epochs):
         loss, grads = net.loss_and_grads(Xn, T)
         net.adam_step(grads, lr=lr)
         if log and (ep % 500 == 0 or ep == epochs - 1):
             log(f"epoch {ep:5d} loss {float(loss):.4f}")
     W = net.host_weights()
-    return {"format": FORMAT, "candidates": CANDIDATES, "mu": mu.tolist(), "sd": sd.tolist(),
+    return {"format": fmt, "candidates": list(candidates), "mu": mu.tolist(), "sd": sd.tolist(),
             "weights": [w.tolist() for w in W], "hidden": hidden, "tau": tau,
             "n_train": len(records)}
 
@@ -313,3 +316,136 @@ class Selector:
         if key is not None:
             self._cache[(key, N, dtype)] = v
         return v
+
+
+
+# ------------------------------------------------------------------------------------------
+# SDDMM path choice: CUDA cores (exact FP32 dot products) or the tcgen05 split-bf16 kernels
+# ------------------------------------------------------------------------------------------
+SDDMM_FORMAT = "armsparse-sddmm-selector-1"
+DEFAULT_SDDMM_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                                   "sddmm_selector_model.json")
+
+
+def sddmm_sweep_configs(n_patterns=160, seed=0, max_nnz=6_000_000, max_dense_bytes=1 << 30):
+    """Seeded SDDMM problems: uniform patterns (density log-uniform in [1e-4, 0.3]), banded
+    and power-law ones; rows and columns log-uniform in [512, 16384]; K in {32, ..., 2048}.
+    Entries are capped at max_nnz and the dense operands at max_dense_bytes (sweep time)."""
+    rng = np.random.default_rng(seed)
+    kinds = ["uniform", "uniform", "banded", "powerlaw"]
+    out = []
+    for i in range(n_patterns):
+        M = int(2 ** rng.uniform(9, 14))
+        Nc = int(2 ** rng.uniform(9, 14))
+        K = int(rng.choice([32, 64, 128, 256, 512, 1024, 2048]))
+        while (M + Nc) * K * 4 > max_dense_bytes and K > 32:
+            K //= 2
+        cfg = {"id": i, "kind": kinds[i % 4], "M": M, "N": Nc, "K": K, "seed": 5000 + i}
+        if cfg["kind"] == "uniform":
+            cfg["density"] = float(min(10 ** rng.uniform(-4, math.log10(0.3)), max_nnz / (M * Nc)))
+        elif cfg["kind"] == "banded":
+            cfg["bandwidth"] = int(min(rng.integers(3, 257), max(3, max_nnz // M)))
+        else:
+            cfg["exponent"] = float(rng.uniform(1.8, 2.5))
+            cfg["mean"] = float(min(rng.uniform(2, 300), max_nnz / M, Nc / 4))
+        out.append(cfg)
+    return out
+
+
+def make_sddmm_pattern(cfg, device):
+    """(rowptr, colind) of a sweep problem on the device, columns ascending in each row."""
+    from . import synthetic as syn
+    M, Nc = cfg["M"], cfg["N"]
+    if cfg["kind"] == "powerlaw":
+        rp, ci, _ = syn.powerlaw_csr_device(M, cfg["exponent"], cfg["mean"], cfg["seed"], device,
+                                            n_cols=Nc)
+        return rp, ci
+    if cfg["kind"] == "banded":
+        g = torch.Generator(device=device).manual_seed(cfg["seed"])
+        bw = cfg["bandwidth"]
+        rows = torch.arange(M, device=device).repeat_interleave(bw)
+        off = torch.randint(-bw, bw + 1, (M * bw,), generator=g, device=device)
+        cols = (rows * Nc // M + off).clamp_(0, Nc - 1)
+        keys = torch.unique(rows * Nc + cols)
+    else:
+        g = torch.Generator(device=device).manual_seed(cfg["seed"])
+        n = max(1, int(cfg["density"] * M * Nc))
+        keys = torch.unique(torch.randint(0, M * Nc, (n,), generator=g, device=device))
+    rows, cols = keys // Nc, (keys % Nc).to(torch.int32)
+    rowptr = torch.zeros(M + 1, dtype=torch.int64, device=device)
+    rowptr[1:] = torch.cumsum(torch.bincount(rows, minlength=M), 0)
+    return rowptr.to(torch.int32), cols.contiguous()
+
+
+def sddmm_sweep(configs, device=None, reps=3, log=None):
+    """Time every SDDMM path (tuner.sddmm_paths) on each problem; returns records."""
+    device = device or torch.device("cuda", 0)
+    paths = tuner.sddmm_paths()
+    records = []
+    for cfg in configs:
+        rowptr, colind = make_sddmm_pattern(cfg, device)
+        g = torch.Generator(device=device).manual_seed(cfg["seed"] + 1)
+        X = torch.randn(cfg["M"], cfg["K"], generator=g, device=device)
+        Y = torch.randn(cfg["N"], cfg["K"], generator=g, device=device)
+        t = tuner.autotune_sddmm(rowptr, colind, X, Y, paths=paths, reps=reps, max_ratio=4.0)
+        feats = tuner.sddmm_features(rowptr, colind, cfg["N"], cfg["K"])
+        rec = {"cfg": cfg, "features": feats.tolist(), "nnz": int(colind.numel()),
+               "times_ms": [x.ms for x in t]}
+        records.append(rec)
+        if log:
+            ok = [x for x in t if x.ms is not None]
+            b = min(ok, key=lambda x: x.ms)
+            log(f"{cfg['id']:4d} {cfg['kind']:8s} {cfg['M']}x{cfg['N']} K={cfg['K']} "
+                f"nnz={rec['nnz']} best={b.name} {b.ms * 1e3:.1f}us "
+                f"simt={t[0].ms if t[0].ms is None else round(t[0].ms * 1e3, 1)}us")
+        del rowptr, colind, X, Y
+    return records
+
+
+def evaluate_sddmm(model, records):
+    """Picked time / best time of the network over records (mean, geometric mean, worst),
+    against always taking the CUDA-core path -- the reference's only kind of SDDMM kernel
+    (gcn/pytorch-custom/sddmm.cu:438-455 chooses among them by K % 4 and K % 2 alone) -- and
+    against always taking the library's default tensor-core variant."""
+    picked, simt, tc = [], [], []
+    names = model["candidates"]
+    for r in records:
+        t = np.array([np.inf if x is None else x for x in r["times_ms"]])
+        best = t.min()
+        scores = np.where(np.isfinite(t), host_forward(model, r["features"]), -np.inf)
+        picked.append(t[int(np.argmax(scores))] / best)
+        simt.append(t[names.index("simt")] / best)
+        tc_best = [t[i] for i, n in enumerate(names) if n.startswith("tc")]
+        tc.append(tc_best[-1] / best if np.isfinite(tc_best[-1]) else np.nan)
+    gm = lambda a: float(np.exp(np.nanmean(np.log(np.asarray(a)))))
+    return {"mlp_geomean": gm(picked), "mlp_mean": float(np.mean(picked)),
+            "mlp_worst": float(np.max(picked)), "simt_geomean": gm(simt),
+            "tc_default_geomean": gm(tc), "n": len(records)}
+
+
+class SddmmSelector:
+    """The learned choice of SDDMM path for a pattern and K: "simt" or "tc<variant>"."""
+
+    def __init__(self, model: dict):
+        if model.get("format") != SDDMM_FORMAT:
+            raise ValueError("unknown SDDMM selector model format")
+        self.model = model
+
+    @classmethod
+    def load(cls, path: str = DEFAULT_SDDMM_MODEL) -> "SddmmSelector":
+        with open(path) as f:
+            return cls(json.load(f))
+
+    def save(self, path: str) -> None:
+        with open(path, "w") as f:
+            json.dump(self.model, f)
+
+    def choose(self, rowptr, colind, n_cols: int, K: int) -> str:
+        feats = tuner.sddmm_features(rowptr, colind, n_cols, K)
+        scores = host_forward(self.model, feats)
+        names = self.model["candidates"]
+        known = set(tuner.sddmm_paths())
+        for i in np.argsort(-scores):
+            if names[int(i)] in known:
+                return names[int(i)]
+        return "simt"

@@ -8,6 +8,7 @@ no learned selector is loaded and the yardstick the selector is scored against.
 """
 from __future__ import annotations
 
+import math
 import statistics
 from dataclasses import dataclass
 
@@ -118,3 +119,81 @@ def features(rowptr: np.ndarray, n_cols: int, N: int, dtype_bf16: bool) -> np.nd
 
 
 N_FEATURES = 11 + HIST_BINS
+
+
+# ------------------------------------------------------------------------------------------
+# SDDMM paths
+# ------------------------------------------------------------------------------------------
+def sddmm_paths() -> list[str]:
+    """Names of the SDDMM paths a fp32 call can take: "simt" (CUDA-core FP32 dot products,
+    as_sddmm_csr_f32) and "tc1".."tcN" (the tcgen05 split-bf16 kernel variants,
+    as_sddmm_csr_bf16x3_v). The reference has one kind only, picked by K % 4 / K % 2
+    (gcn/pytorch-custom/sddmm.cu:438-455)."""
+    n = int(N.load().as_sddmm_bf16x3_variant_count())
+    return ["simt"] + [f"tc{v}" for v in range(1, n + 1)]
+
+
+def run_sddmm_path(name: str, rowptr, colind, X, Y, aval=None, out=None):
+    """One SDDMM through the named path (see sddmm_paths)."""
+    if name == "simt":
+        return S.sddmm(rowptr, colind, X, Y, aval=aval, out=out)
+    return S.sddmm(rowptr, colind, X, Y, aval=aval, out=out, tensor_cores=True,
+                   variant=int(name[2:]))
+
+
+def autotune_sddmm(rowptr, colind, X, Y, aval=None, paths=None, reps: int = 5,
+                   flush: bool = True, max_ratio: float | None = None) -> list[Timing]:
+    """Time every SDDMM path on these arguments (median of reps, L2 flushed); the Timing's
+    ``variant`` is the index into sddmm_paths()."""
+    names = sddmm_paths()
+    paths = paths or names
+    out = torch.empty(colind.numel(), dtype=torch.float32, device=X.device)
+    res, best_ms = [], None
+    for name in paths:
+        fn = lambda: run_sddmm_path(name, rowptr, colind, X, Y, aval, out)
+        try:
+            fn()
+        except N.NativeError as e:
+            if e.status == 3:  # AS_ERR_UNSUPPORTED
+                res.append(Timing(names.index(name), name, None))
+                continue
+            raise
+        ms = time_cuda(fn, reps=1, warmup=0, flush=flush, device=X.device)
+        if not (max_ratio and best_ms is not None and ms > max_ratio * best_ms):
+            ms = time_cuda(fn, reps=reps, warmup=0, flush=flush, device=X.device)
+        best_ms = ms if best_ms is None else min(best_ms, ms)
+        res.append(Timing(names.index(name), name, ms))
+    return res
+
+
+SDDMM_TILE = (128, 256)  # output tile of the tcgen05 kernels (rows x columns)
+N_SDDMM_FEATURES = 10
+
+
+def sddmm_features(rowptr: torch.Tensor, colind: torch.Tensor, n_cols: int, K: int) -> np.ndarray:
+    """Inputs of the learned SDDMM path choice: log2 of rows, columns, K and entries; density;
+    mean and coefficient of variation of the row lengths; the fraction of 128 x 256 output
+    tiles that hold an entry and the work those tiles carry per entry (the dense tiles the
+    tensor-core path computes divided by the entries it keeps: its wasted-work factor) -- the
+    last two from one pass over the pattern on the device."""
+    M = rowptr.numel() - 1
+    nnz = int(colind.numel())
+    lens = (rowptr[1:] - rowptr[:-1]).double()
+    mean = float(lens.mean()) if M else 0.0
+    cv = float(lens.std(unbiased=False) / (lens.mean() + 1e-9)) if M else 0.0
+    tr, tc = SDDMM_TILE
+    n_tiles_c = (n_cols + tc - 1) // tc
+    n_tiles = max(1, ((M + tr - 1) // tr) * n_tiles_c)
+    if nnz:
+        rows = torch.repeat_interleave(torch.arange(M, device=rowptr.device),
+                                       (rowptr[1:] - rowptr[:-1]).long())
+        tiles = (rows // tr) * n_tiles_c + (colind.long() // tc)
+        occupied = int(torch.unique(tiles).numel())
+    else:
+        occupied = 0
+    density = nnz / max(1.0, float(M) * n_cols)
+    waste = occupied * tr * tc / max(1, nnz)
+    f = [math.log2(M + 1), math.log2(n_cols + 1), math.log2(K + 1), math.log2(nnz + 1),
+         density, math.log2(mean + 1), cv, occupied / n_tiles, math.log2(waste + 1),
+         math.log2(K * nnz + 1)]
+    return np.asarray(f, np.float32)

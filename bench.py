@@ -137,6 +137,12 @@ class SpmmF32(Workload):
             raise RuntimeError("e2e call failed")
 
     # --- CPU: the reference algorithm (oracle restatement of rowBaseSpmm3) ---
+    def extra(self):
+        """The other headline figures, measured in the same process (capped at about a
+        minute): bf16-storage SpMM on this matrix, both SDDMM paths on the 4096^3 density 0.1
+        case with their error against FP64, and the GCN epoch tuned vs plain."""
+        return default_extras(self)
+
     def cpu_step(self, threads, rows=None):
         from oracle import oracle as O
         a = self.a
@@ -147,6 +153,96 @@ class SpmmF32(Workload):
         O.spmm_fma_chain_f32(rp, a.colind, a.val, self.B, threads=threads)
         nnz = int(rp[-1])
         return 4 * (rows + 1) + 8 * nnz + 4 * self.K * self.N + 4 * rows * self.N
+
+
+def _scaled_err_max(got, ref64, scale64):
+    """max |got - ref| / max(|ref|, sum |terms|) over the outputs (FP64 reference)."""
+    import torch
+    d = (got.double() - ref64).abs() / torch.maximum(ref64.abs(), scale64).clamp_min(1e-300)
+    return float(d.max())
+
+
+def default_extras(wl, budget_s: float = 60.0):
+    """Time-capped figures beside the default SpMM line. FP64 references are computed on the
+    GPU with torch (sparse fp64 products and this library's fp64 SDDMM), not by the oracle."""
+    import torch
+    import armsparse_gb300 as A
+    from armsparse_gb300 import tuner
+    t_start = time.perf_counter()
+    dev = wl.Bd.device
+    out = {"budget_s": budget_s}
+
+    def left():
+        return budget_s - (time.perf_counter() - t_start)
+
+    # SpMM bf16 storage, fp32 accumulate: same matrix and B, rounded
+    try:
+        v16, B16 = wl.v.to(torch.bfloat16), wl.Bd.to(torch.bfloat16)
+        C16 = torch.empty_like(wl.C)
+        f32_ms = tuner.time_cuda(lambda: A.spmm(wl.rp, wl.ci, wl.v, wl.Bd, C=wl.C), reps=20)
+        bf_ms = tuner.time_cuda(lambda: A.spmm(wl.rp, wl.ci, v16, B16, C=C16), reps=20)
+        Acsr = torch.sparse_csr_tensor(wl.rp.long(), wl.ci.long(), wl.v.double(),
+                                       size=(wl.M, wl.K))
+        Aabs = torch.sparse_csr_tensor(wl.rp.long(), wl.ci.long(), wl.v.double().abs(),
+                                       size=(wl.M, wl.K))
+        B64 = wl.Bd.double()
+        ref, scale = Acsr @ B64, Aabs @ B64.abs()
+        err_f32 = _scaled_err_max(wl.C, ref, scale)
+        err_bf = _scaled_err_max(C16, ref, scale)
+        del ref, scale, Acsr, Aabs, B64
+        bytes16 = 4 * (wl.M + 1) + 6 * wl.a.nnz + 2 * wl.K * wl.N + 4 * wl.M * wl.N
+        out["spmm_bf16"] = {"ms": round(bf_ms, 5), "gbs": round(bytes16 / (bf_ms * 1e-3) / 1e9, 1),
+                            "speedup_vs_f32": round(f32_ms / bf_ms, 3), "f32_ms": round(f32_ms, 5),
+                            "max_scaled_err_vs_fp64": err_bf,
+                            "f32_max_scaled_err_vs_fp64": err_f32,
+                            "error_metric": "|C - C64| / max(|C64|, sum|a*b|), fp64 of the "
+                                            "fp32 inputs"}
+    except Exception as e:  # noqa: BLE001 -- a failed extra is reported, not fatal
+        out["spmm_bf16"] = {"error": repr(e)[:200]}
+
+    # SDDMM 4096^3 density 0.1, both paths
+    if left() > 20:
+        try:
+            sd = SddmmTc()
+            sd.to_device(dev)
+            res = {}
+            for name, tc in (("tc", True), ("f32", False)):
+                fn = lambda: A.sddmm(sd.rp, sd.ci, sd.Xd, sd.Yd, aval=sd.v, out=sd.out,
+                                     tensor_cores=tc)
+                ms = tuner.time_cuda(fn, reps=10)
+                fn()
+                res[name] = (ms, sd.out.clone())
+            X64, Y64, v64 = sd.Xd.double(), sd.Yd.double(), sd.v.double()
+            r64 = A.sddmm(sd.rp, sd.ci, X64, Y64, aval=v64)
+            s64 = A.sddmm(sd.rp, sd.ci, X64.abs(), Y64.abs(), aval=v64.abs())
+            del X64, Y64
+            for name, (ms, o) in res.items():
+                out[f"sddmm_{name}"] = {
+                    "us": round(ms * 1e3, 1),
+                    "gflops_algorithmic": round(sd.flops / (ms * 1e-3) / 1e9, 1),
+                    "max_scaled_err_vs_fp64": _scaled_err_max(o, r64, s64)}
+            out["sddmm_tc"]["executed_tflops"] = round(sd.exec_flops / (res["tc"][0] * 1e-3) / 1e12, 1)
+            del sd, r64, s64, res
+        except Exception as e:  # noqa: BLE001
+            out["sddmm"] = {"error": repr(e)[:200]}
+    # GCN epoch: tuned (captured graph, selector kernels) vs plain (eager, library default)
+    if left() > 15:
+        try:
+            g = GcnEpoch()
+            g.to_device(dev)
+            for _ in range(3):
+                g.step()
+            graph_ms = tuner.time_cuda(g.step, reps=20, warmup=2, flush=False)
+            plain_ms = tuner.time_cuda(g.plain_step, reps=10, warmup=2, flush=False)
+            out["gcn_epoch"] = {"tuned_graph_ms": round(graph_ms, 4),
+                                "plain_eager_ms": round(plain_ms, 4),
+                                "speedup": round(plain_ms / graph_ms, 2)}
+            del g
+        except Exception as e:  # noqa: BLE001
+            out["gcn_epoch"] = {"error": repr(e)[:200]}
+    torch.cuda.empty_cache()
+    out["elapsed_s"] = round(time.perf_counter() - t_start, 1)
+    return out
 
 
 class _Generic(Workload):
@@ -987,7 +1083,7 @@ def run_reference(args, wl_cls):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": wl.higher_is_better,
         "scaling": "weak", "vs_baseline": None, "dtype": wl.dtype, "data": "synthetic (seeded)",
-        "config": wl.config,
+        "config": dict(wl.config, parallelism=f"replicas x{ws}"),
         "cpu_baseline": {"value": round(value, 3), "unit": wl.unit, "cores": threads,
                          "kind": "port",
                          "sample": f"the whole workload per step, {args.steps} steps, "

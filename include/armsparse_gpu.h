@@ -48,9 +48,10 @@ const char *as_status_string(as_status s);
 /* Number of this library's kernels launched through `ctx` since creation. */
 uint64_t as_ctx_launch_count(const as_ctx *ctx);
 /* How many times a kernel polls a coordination wait (the bulk-copy SpMM variants' wait for a
- * gathered row to land in shared memory) before it gives up: it then sets AS_ERR_TIMEOUT in
- * the status word, waits for the copies it issued (that drain always polls up to 2^22 times
- * per copy, whatever this setting), and leaves its outputs unwritten. Default 2^22 (a few
+ * gathered row to land in shared memory; the long-row SpMM kernel's wait for a pipeline
+ * stage) before it gives up: it then sets AS_ERR_TIMEOUT in the status word, waits for the
+ * copies it issued (that drain always completes, whatever this setting), and leaves its
+ * outputs unwritten. Default 2^22 (a few
  * seconds). 0 makes every such wait give up at once: tests use it to take the timeout path
  * without a fault or a hang. Applies to launches issued after the call. No counterpart in the
  * reference, which has no device-side waits. */
