@@ -600,6 +600,48 @@ as_status as_csr_to_vcsr4_fill(as_ctx *c, int M, int nnz, const int *rowptr, con
                                     static_cast<cudaStream_t>(stream));
 }
 
+as_status as_csr_to_rowpair_count(as_ctx *c, int M, int nnz, const int *rowptr,
+                                  const int *colind, int *rowptr2, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_csr_to_rowpair_count: ctx is NULL");
+    as_status st = check_csr_args("as_csr_to_rowpair_count", M, 0, nnz, rowptr, colind, nullptr,
+                                  false);
+    if (st != AS_OK) return st;
+    if (!rowptr2) return fail(AS_ERR_INVALID_VALUE, "as_csr_to_rowpair_count: rowptr2 is NULL");
+    DeviceGuard g(c->device);
+    return csr_to_rowpair_count_launch(c, M, nnz, rowptr, colind, rowptr2,
+                                       static_cast<cudaStream_t>(stream));
+}
+
+as_status as_csr_to_rowpair_fill(as_ctx *c, int M, int nnz, const int *rowptr, const int *colind,
+                                 const float *val, const int *rowptr2, int *colind2, float *val2,
+                                 uint8_t *flag2, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_csr_to_rowpair_fill: ctx is NULL");
+    as_status st = check_csr_args("as_csr_to_rowpair_fill", M, 0, nnz, rowptr, colind, val, true);
+    if (st != AS_OK) return st;
+    if (!rowptr2 || (nnz > 0 && (!colind2 || !val2 || !flag2)))
+        return fail(AS_ERR_INVALID_VALUE, "as_csr_to_rowpair_fill: NULL output");
+    if (M == 0) return AS_OK;
+    DeviceGuard g(c->device);
+    return csr_to_rowpair_fill_launch(c, M, nnz, rowptr, colind, val, rowptr2, colind2, val2,
+                                      flag2, static_cast<cudaStream_t>(stream));
+}
+
+as_status as_spmm_rowpair_f32(as_ctx *c, int M, int K, int N, int nnz, const int *rowptr2,
+                              const int *colind2, const float *val2, const uint8_t *flag2,
+                              const float *B, long ldb, float *C, long ldc, float beta,
+                              void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_spmm_rowpair_f32: ctx is NULL");
+    as_status st = check_csr_args("as_spmm_rowpair_f32", M, K, nnz, rowptr2, colind2, val2, true);
+    if (st != AS_OK) return st;
+    if (N < 0) return fail(AS_ERR_INVALID_VALUE, "as_spmm_rowpair_f32: negative N");
+    if (M == 0 || N == 0) return AS_OK;
+    if (!C || (nnz > 0 && (!B || !flag2)) || ldb < N || ldc < N)
+        return fail(AS_ERR_INVALID_VALUE, "as_spmm_rowpair_f32: bad dense operand");
+    DeviceGuard g(c->device);
+    SpmmArgs a{M, K, N, nnz, rowptr2, colind2, val2, B, ldb, C, ldc, beta, c->d_status};
+    return spmm_rowpair_launch(c, a, flag2, static_cast<cudaStream_t>(stream));
+}
+
 as_status as_gather_f32(as_ctx *c, long n, long n_src, const float *src, const int *idx,
                         float *dst, void *stream) {
     if (!c) return fail(AS_ERR_INVALID_VALUE, "as_gather_f32: ctx is NULL");

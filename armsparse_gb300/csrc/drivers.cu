@@ -225,6 +225,113 @@ void sparse_dense_vector(float *B, float *C, int rowPtr[], int colInd[], float v
     report(s, run(), "sparse_dense_vector");
 }
 
+void DataReuseSpmm(int rowPtr[], int colInd[], float val[], float B[], float C[], int M, int K,
+                   int N, int threads, bool *flag) {
+    (void)threads;
+    State &s = state();
+    std::lock_guard<std::mutex> g(s.mu);
+    auto run = [&]() -> as_status {
+        if (M < 0 || K < 0 || N < 0 || !rowPtr) return AS_ERR_INVALID_VALUE;
+        const int nnz = rowPtr[M];
+        if (nnz < 0) return AS_ERR_INVALID_CSR;
+        const size_t bytes = al(sizeof(int) * (M + 1)) + 2 * al(sizeof(int) * nnz) + al(nnz) +
+                             al(sizeof(float) * size_t(K) * N) + al(sizeof(float) * size_t(M) * N);
+        char *base = nullptr;
+        as_status st = prepare(s, bytes, &base);
+        if (st != AS_OK) return st;
+        Arena a{base};
+        int *drp = a.take<int>(M + 1);
+        int *dci = a.take<int>(nnz);
+        float *dv = a.take<float>(nnz);
+        uint8_t *df = a.take<uint8_t>(nnz);
+        float *dB = a.take<float>(size_t(K) * N);
+        float *dC = a.take<float>(size_t(M) * N);
+        static_assert(sizeof(bool) == 1, "the reference's flag array is one byte per entry");
+        if ((st = h2d(s, drp, rowPtr, sizeof(int) * (M + 1))) != AS_OK) return st;
+        if ((st = h2d(s, dci, colInd, sizeof(int) * nnz)) != AS_OK) return st;
+        if ((st = h2d(s, dv, val, sizeof(float) * nnz)) != AS_OK) return st;
+        if ((st = h2d(s, df, flag, size_t(nnz))) != AS_OK) return st;
+        if ((st = h2d(s, dB, B, sizeof(float) * size_t(K) * N)) != AS_OK) return st;
+        if ((st = h2d(s, dC, C, sizeof(float) * size_t(M) * N)) != AS_OK) return st;
+        st = as_spmm_rowpair_f32(s.ctx, M, K, N, nnz, drp, dci, dv, df, dB, N, dC, N, 1.0f,
+                                 s.stream);
+        if (st != AS_OK) return st;
+        return finish(s, C, dC, sizeof(float) * size_t(M) * N);
+    };
+    report(s, run(), "DataReuseSpmm");
+}
+
+void toDataReuseFormat(float *matrix, int rows, int cols, int *rowPtr, int *colInd, float *val,
+                       bool *flag) {
+    State &s = state();
+    std::lock_guard<std::mutex> g(s.mu);
+    auto run = [&]() -> as_status {
+        if (rows < 0 || cols < 0 || !matrix || !rowPtr) return AS_ERR_INVALID_VALUE;
+        const size_t dense = sizeof(float) * size_t(rows) * cols;
+        // dense -> CSR (count, then fill once nnz is known) -> row-pair layout
+        const size_t head = al(dense) + 2 * al(sizeof(int) * (size_t(rows) + 1));
+        char *base = nullptr;
+        as_status st = prepare(s, head, &base);
+        if (st != AS_OK) return st;
+        Arena a{base};
+        float *dD = a.take<float>(size_t(rows) * cols);
+        int *drp = a.take<int>(size_t(rows) + 1);
+        int *drp2 = a.take<int>(size_t(rows) + 1);
+        if ((st = h2d(s, dD, matrix, dense)) != AS_OK) return st;
+        if ((st = as_dense_to_csr_count(s.ctx, rows, cols, dD, cols, drp, s.stream)) != AS_OK)
+            return st;
+        int nnz = 0;
+        if (cudaMemcpyAsync(&nnz, drp + rows, sizeof(int), cudaMemcpyDeviceToHost, s.stream) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(s.stream) != cudaSuccess)
+            return AS_ERR_CUDA;
+        // the arena may grow: keep the dense matrix and row pointers by recopying into it
+        const size_t need = head + 4 * al(sizeof(int) * size_t(nnz)) + al(size_t(nnz));
+        if (need > s.cap) {
+            std::vector<int> hrp(size_t(rows) + 1);
+            if (cudaMemcpy(hrp.data(), drp, sizeof(int) * hrp.size(), cudaMemcpyDeviceToHost) !=
+                cudaSuccess)
+                return AS_ERR_CUDA;
+            if ((st = prepare(s, need, &base)) != AS_OK) return st;
+            a = Arena{base};
+            dD = a.take<float>(size_t(rows) * cols);
+            drp = a.take<int>(size_t(rows) + 1);
+            drp2 = a.take<int>(size_t(rows) + 1);
+            if ((st = h2d(s, dD, matrix, dense)) != AS_OK) return st;
+            if ((st = h2d(s, drp, hrp.data(), sizeof(int) * hrp.size())) != AS_OK) return st;
+        }
+        int *dci = a.take<int>(nnz);
+        float *dv = a.take<float>(nnz);
+        int *dci2 = a.take<int>(nnz);
+        float *dv2 = a.take<float>(nnz);
+        uint8_t *df = a.take<uint8_t>(nnz);
+        if ((st = as_dense_to_csr_fill(s.ctx, rows, cols, dD, cols, drp, dci, dv, s.stream)) != AS_OK)
+            return st;
+        if ((st = as_csr_to_rowpair_count(s.ctx, rows, nnz, drp, dci, drp2, s.stream)) != AS_OK)
+            return st;
+        if ((st = as_csr_to_rowpair_fill(s.ctx, rows, nnz, drp, dci, dv, drp2, dci2, dv2, df,
+                                         s.stream)) != AS_OK)
+            return st;
+        if (cudaMemcpyAsync(rowPtr, drp2, sizeof(int) * (size_t(rows) + 1), cudaMemcpyDeviceToHost,
+                            s.stream) != cudaSuccess ||
+            (nnz && (cudaMemcpyAsync(colInd, dci2, sizeof(int) * nnz, cudaMemcpyDeviceToHost,
+                                     s.stream) != cudaSuccess ||
+                     cudaMemcpyAsync(val, dv2, sizeof(float) * nnz, cudaMemcpyDeviceToHost,
+                                     s.stream) != cudaSuccess ||
+                     cudaMemcpyAsync(flag, df, size_t(nnz), cudaMemcpyDeviceToHost, s.stream) !=
+                         cudaSuccess)))
+            return AS_ERR_CUDA;
+        if ((st = finish(s, nullptr, nullptr, 0)) != AS_OK) return st;
+        // as the reference does, the entries moved into the previous row's segment are zeroed
+        // in the dense matrix
+        for (int r = 0; r + 1 < rows; r += 2)
+            for (int e = rowPtr[r]; e < rowPtr[r + 1]; ++e)
+                if (flag[e]) matrix[size_t(r + 1) * cols + colInd[e]] = 0.0f;
+        return AS_OK;
+    };
+    report(s, run(), "toDataReuseFormat");
+}
+
 static as_status transpose_host(int *sm, int *res) {
     State &s = state();
     if (!sm || !res) return AS_ERR_INVALID_VALUE;
@@ -313,5 +420,13 @@ void as_drv_csr_spmm_kernel(int A_nrows, int B_ncols, int *rowptr, int *colind, 
     csr_spmm_kernel(A_nrows, B_ncols, rowptr, colind, val, B, C);
 }
 void as_drv_fast_transpose(int *sm, int *res) { fast_transpose(sm, res, nullptr); }
+void as_drv_DataReuseSpmm(int *rowPtr, int *colInd, float *val, float *B, float *C, int M, int K,
+                          int N, int threads, unsigned char *flag) {
+    DataReuseSpmm(rowPtr, colInd, val, B, C, M, K, N, threads, reinterpret_cast<bool *>(flag));
+}
+void as_drv_toDataReuseFormat(float *matrix, int rows, int cols, int *rowPtr, int *colInd,
+                              float *val, unsigned char *flag) {
+    toDataReuseFormat(matrix, rows, cols, rowPtr, colInd, val, reinterpret_cast<bool *>(flag));
+}
 as_status as_drv_last_status(void) { return state().last; }
 }

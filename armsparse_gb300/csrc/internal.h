@@ -142,6 +142,13 @@ as_status dense_to_csr_count_launch(as_ctx *ctx, int M, int K, const float *D, l
                                     int *rowptr, cudaStream_t s);
 as_status dense_to_csr_fill_launch(as_ctx *ctx, int M, int K, const float *D, long ld,
                                    const int *rowptr, int *colind, float *val, cudaStream_t s);
+as_status csr_to_rowpair_count_launch(as_ctx *ctx, int M, int nnz, const int *rowptr,
+                                      const int *colind, int *rowptr2, cudaStream_t s);
+as_status csr_to_rowpair_fill_launch(as_ctx *ctx, int M, int nnz, const int *rowptr,
+                                     const int *colind, const float *val, const int *rowptr2,
+                                     int *colind2, float *val2, uint8_t *flag2, cudaStream_t s);
+as_status spmm_rowpair_launch(as_ctx *ctx, const SpmmArgs &a, const uint8_t *flag2,
+                              cudaStream_t s);
 as_status csr_to_vcsr4_count_launch(as_ctx *ctx, int M, int nnz, const int *rowptr,
                                     const int *colind, int *vrowptr, cudaStream_t s);
 as_status csr_to_vcsr4_fill_launch(as_ctx *ctx, int M, int nnz, const int *rowptr,

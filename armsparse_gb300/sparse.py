@@ -542,3 +542,47 @@ def csr_to_vcsr4(rowptr, colind, val):
                                           _ptr(val), _ptr(vrowptr), _ptr(vcolind), _ptr(vval),
                                           _stream(dev)), "as_csr_to_vcsr4_fill")
     return vrowptr, vcolind, vval
+
+
+def csr_to_rowpair(rowptr, colind, val):
+    """The reference's row-pair reuse layout (toDataReuseFormat, suitesparse_sdmm.cpp:150-179)
+    from CSR with ascending columns: (rowptr2, colind2, val2, flag2 as uint8). The entry count
+    is unchanged, so nothing synchronises."""
+    dev = _dev(rowptr, colind, val)
+    M, nnz = _csr(rowptr, colind)
+    _need(val, torch.float32, "val", 1)
+    rowptr2 = torch.empty(M + 1, dtype=torch.int32, device=dev)
+    colind2 = torch.empty(nnz, dtype=torch.int32, device=dev)
+    val2 = torch.empty(nnz, dtype=torch.float32, device=dev)
+    flag2 = torch.empty(nnz, dtype=torch.uint8, device=dev)
+    ctx = N.context(dev.index)
+    N.check(N.load().as_csr_to_rowpair_count(ctx.handle, M, nnz, _ptr(rowptr), _ptr(colind),
+                                             _ptr(rowptr2), _stream(dev)),
+            "as_csr_to_rowpair_count")
+    N.check(N.load().as_csr_to_rowpair_fill(ctx.handle, M, nnz, _ptr(rowptr), _ptr(colind),
+                                            _ptr(val), _ptr(rowptr2), _ptr(colind2), _ptr(val2),
+                                            _ptr(flag2), _stream(dev)), "as_csr_to_rowpair_fill")
+    return rowptr2, colind2, val2, flag2
+
+
+def spmm_rowpair(rowptr2, colind2, val2, flag2, B, C=None, beta: float = 0.0):
+    """C = A*B + beta*C over the row-pair layout, bit for bit the reference's DataReuseSpmm
+    (suitesparse_sdmm.cpp:25-44): even rows are their CSR chains, odd rows chain over the
+    columns they share with the row above first."""
+    dev = _dev(rowptr2, colind2, val2, flag2, B, C)
+    M, nnz = _csr(rowptr2, colind2)
+    _need(val2, torch.float32, "val2", 1)
+    if flag2.dtype != torch.uint8 or flag2.numel() != nnz:
+        raise ValueError("flag2 must be uint8 with one byte per entry")
+    if B.dtype != torch.float32 or B.dim() != 2 or B.stride(1) != 1:
+        raise ValueError("B must be float32, 2-D, row-major")
+    K, Ncols = B.shape
+    if C is None:
+        C = torch.empty((M, Ncols), dtype=torch.float32, device=dev)
+    ctx = N.context(dev.index)
+    N.check(N.load().as_spmm_rowpair_f32(ctx.handle, M, K, Ncols, nnz, _ptr(rowptr2),
+                                         _ptr(colind2), _ptr(val2), _ptr(flag2), _ptr(B),
+                                         B.stride(0) if K > 1 else Ncols, _ptr(C),
+                                         C.stride(0) if M > 1 else Ncols, float(beta),
+                                         _stream(dev)), "as_spmm_rowpair_f32")
+    return C

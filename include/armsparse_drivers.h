@@ -45,6 +45,15 @@ void csr_spmm_kernel(int A_nrows, int B_ncols, int *A_csrRowPtr, int *A_csrColIn
  * (row, col, value) rows). The input must be in row-major order (what convert() writes); the
  * output lists each column's entries with rows ascending. mtx is not used. */
 void fast_transpose(int *sm, int *res, std::mutex mtx[]);
+/* suitesparse_sdmm.cpp:25 -- C[M x N] += A * B over the row-pair reuse layout (rowPtr[M+1],
+ * colInd/val/flag[rowPtr[M]]), bit-identical to the reference with its saxpy fused. */
+void DataReuseSpmm(int rowPtr[], int colInd[], float val[], float B[], float C[], int M, int K,
+                   int N, int threads, bool *flag);
+/* suitesparse_sdmm.cpp:150 -- dense matrix (rows x cols, row-major) -> the row-pair reuse
+ * layout; rowPtr needs rows + 1 ints, the other arrays one slot per nonzero. As in the
+ * reference, the entries that move into the previous row's segment are zeroed in `matrix`. */
+void toDataReuseFormat(float *matrix, int rows, int cols, int *rowPtr, int *colInd, float *val,
+                       bool *flag);
 #endif
 
 #ifdef __cplusplus
@@ -66,6 +75,10 @@ void as_drv_sparse_matrix_mul3(int *rowPtr1, int *colInd1, float *val1, int *row
 void as_drv_csr_spmm_kernel(int A_nrows, int B_ncols, int *rowptr, int *colind, float *val,
                             float *B, float *C);
 void as_drv_fast_transpose(int *sm, int *res);
+void as_drv_DataReuseSpmm(int *rowPtr, int *colInd, float *val, float *B, float *C, int M, int K,
+                          int N, int threads, unsigned char *flag);
+void as_drv_toDataReuseFormat(float *matrix, int rows, int cols, int *rowPtr, int *colInd,
+                              float *val, unsigned char *flag);
 /* Status of the last shim call on any thread (AS_OK when it succeeded). */
 as_status as_drv_last_status(void);
 #ifdef __cplusplus

@@ -320,6 +320,28 @@ as_status as_csr_to_vcsr4_fill(as_ctx *ctx, int M, int nnz, const int *rowptr, c
                                const float *val, const int *vrowptr, int *vcolind, float *vval,
                                void *stream);
 
+/* CSR (columns ascending in rows) -> the reference's row-pair reuse layout, toDataReuseFormat
+ * (suitesparse_sdmm.cpp:150-179): rows are paired (2p, 2p+1); row 2p's segment lists its
+ * entries in column order, each followed by row 2p+1's entry in the same column when there is
+ * one (flag2 = 1: it belongs to the next row); row 2p+1's segment keeps its other entries; an
+ * unpaired last row is copied. The total stays nnz. _count writes rowptr2[0..M]; _fill writes
+ * colind2, val2 and flag2 (one byte per entry). Rows that are not sorted give a memory-safe
+ * layout that is not the reference's. */
+as_status as_csr_to_rowpair_count(as_ctx *ctx, int M, int nnz, const int *rowptr,
+                                  const int *colind, int *rowptr2, void *stream);
+as_status as_csr_to_rowpair_fill(as_ctx *ctx, int M, int nnz, const int *rowptr, const int *colind,
+                                 const float *val, const int *rowptr2, int *colind2, float *val2,
+                                 uint8_t *flag2, void *stream);
+/* C = A*B + beta*C over the row-pair layout, bit-identical to DataReuseSpmm
+ * (suitesparse_sdmm.cpp:25-44, its saxpy fused per element as OpenBLAS computes it): row 2p is
+ * its CSR chain; row 2p+1 chains over the entries it shares with row 2p first (column order),
+ * then over its own segment. A flagged entry reuses the B segment of the entry before it (the
+ * same column) instead of gathering it again. beta = 1 is the reference's accumulate. */
+as_status as_spmm_rowpair_f32(as_ctx *ctx, int M, int K, int N, int nnz, const int *rowptr2,
+                              const int *colind2, const float *val2, const uint8_t *flag2,
+                              const float *B, long ldb, float *C, long ldc, float beta,
+                              void *stream);
+
 /* ---- small dense helpers used around the hot path ---------------------------------------- */
 /* dst[i] = bf16(src[i]) (round to nearest even). */
 as_status as_f32_to_bf16(as_ctx *ctx, long n, const float *src, uint16_t *dst, void *stream);

@@ -444,3 +444,76 @@ void or_spmm_reduce_f32(int M, int N, const int *rowptr, const int *colind, cons
             for (int j = 0; j < N; ++j) c[j] = 0.0f;
     }
 }
+
+/* Row-pair reuse format of the reference's suitesparse_sdmm.cpp (toDataReuseFormat, :150-179),
+ * built from CSR with ascending columns instead of from a dense matrix (the same layout): rows
+ * are paired (2p, 2p+1); row 2p's segment lists its entries in column order, each followed by
+ * row 2p+1's entry in the same column when there is one (flag 1: it belongs to the next row);
+ * row 2p+1's segment keeps its entries in columns row 2p does not have. An unpaired last row is
+ * copied. Total entries are unchanged. rowptr2[M+1], colind2/val2/flag2[nnz]. */
+void or_csr_to_rowpair(int M, const int *rowptr, const int *colind, const float *val,
+                       int *rowptr2, int *colind2, float *val2, unsigned char *flag2) {
+    int size = 0;
+    for (int r = 0; r < M; ++r) {
+        rowptr2[r] = size;
+        const int a0 = rowptr[r], a1 = rowptr[r + 1];
+        if (r % 2 == 0 && r + 1 < M) {
+            const int b1 = rowptr[r + 2];
+            int b = rowptr[r + 1];
+            for (int e = a0; e < a1; ++e) {
+                colind2[size] = colind[e];
+                val2[size] = val[e];
+                flag2[size] = 0;
+                ++size;
+                while (b < b1 && colind[b] < colind[e]) ++b;
+                if (b < b1 && colind[b] == colind[e]) {
+                    colind2[size] = colind[b];
+                    val2[size] = val[b];
+                    flag2[size] = 1;
+                    ++size;
+                }
+            }
+        } else if (r % 2 == 1) {
+            const int p0 = rowptr[r - 1], p1 = rowptr[r];
+            int q = p0;
+            for (int e = a0; e < a1; ++e) {
+                while (q < p1 && colind[q] < colind[e]) ++q;
+                if (q < p1 && colind[q] == colind[e]) continue; /* moved into row r-1's segment */
+                colind2[size] = colind[e];
+                val2[size] = val[e];
+                flag2[size] = 0;
+                ++size;
+            }
+        } else { /* unpaired last row */
+            for (int e = a0; e < a1; ++e) {
+                colind2[size] = colind[e];
+                val2[size] = val[e];
+                flag2[size] = 0;
+                ++size;
+            }
+        }
+    }
+    rowptr2[M] = size;
+}
+
+/* DataReuseSpmm (suitesparse_sdmm.cpp:25-44): for each row m and each entry of its segment,
+ * C[m + flag] += val * B[col] by a fused saxpy (one fmaf per column, as OpenBLAS computes
+ * it), rows of a pair handled in order (schedule(static, 2)). So row 2p's outputs are the CSR
+ * chain, and row 2p+1's chain runs over the entries it shares with row 2p first (in column
+ * order), then over its own segment. C is accumulated (the caller zeroes it). */
+void or_spmm_rowpair_f32(int M, int N, const int *rowptr2, const int *colind2, const float *val2,
+                         const unsigned char *flag2, const float *B, long ldb, float *C, long ldc,
+                         int threads) {
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(static, 2)
+#endif
+    for (int m = 0; m < M; ++m) {
+        for (int e = rowptr2[m]; e < rowptr2[m + 1]; ++e) {
+            float *c = C + (long)(m + flag2[e]) * ldc;
+            const float *b = B + (long)colind2[e] * ldb;
+            const float v = val2[e];
+            for (int j = 0; j < N; ++j) c[j] = fmaf(v, b[j], c[j]);
+        }
+    }
+}

@@ -88,6 +88,13 @@ def lib():
                                               _f32p, _f32p, _c_long, _c_int]
             L.or_spmm_reduce_f32.argtypes = [_c_int, _c_int, _i32p, _i32p, ctypes.c_void_p, _f32p,
                                              _c_long, _f32p, _c_int]
+            L.or_csr_to_rowpair.argtypes = [_c_int, _i32p, _i32p, _f32p, _i32p, _i32p, _f32p,
+                                            np.ctypeslib.ndpointer(dtype=np.uint8,
+                                                                   flags="C_CONTIGUOUS")]
+            L.or_spmm_rowpair_f32.argtypes = [_c_int, _c_int, _i32p, _i32p, _f32p,
+                                              np.ctypeslib.ndpointer(dtype=np.uint8,
+                                                                     flags="C_CONTIGUOUS"),
+                                              _f32p, _c_long, _f32p, _c_long, _c_int]
             _LIB = L
     return _LIB
 
@@ -408,3 +415,30 @@ def ref_read_mtx(path: str):
     for p in (r, c, v):
         L.ref_mtx_free(ctypes.cast(p, ctypes.c_void_p))
     return (m.value, n.value) + out
+
+
+def csr_to_rowpair(rowptr, colind, val):
+    """The reference's row-pair reuse layout (suitesparse_sdmm.cpp:150-179) from CSR with
+    ascending columns: (rowptr2, colind2, val2, flag2)."""
+    rowptr, colind = _csr(rowptr, colind)
+    M, nnz = rowptr.size - 1, colind.size
+    val = np.ascontiguousarray(val, np.float32)
+    rp2 = np.zeros(M + 1, np.int32)
+    ci2 = np.zeros(max(nnz, 1), np.int32)
+    v2 = np.zeros(max(nnz, 1), np.float32)
+    f2 = np.zeros(max(nnz, 1), np.uint8)
+    lib().or_csr_to_rowpair(M, rowptr, colind, val, rp2, ci2, v2, f2)
+    return rp2, ci2[:nnz], v2[:nnz], f2[:nnz]
+
+
+def spmm_rowpair_f32(rowptr2, colind2, val2, flag2, B, C=None, threads=None):
+    """DataReuseSpmm (suitesparse_sdmm.cpp:25-44) over the row-pair layout: C += A*B."""
+    rowptr2, colind2 = _csr(rowptr2, colind2)
+    M = rowptr2.size - 1
+    B = np.ascontiguousarray(B, np.float32)
+    C = np.zeros((M, B.shape[1]), np.float32) if C is None else np.ascontiguousarray(C, np.float32).copy()
+    lib().or_spmm_rowpair_f32(M, B.shape[1], rowptr2, colind2,
+                              np.ascontiguousarray(val2, np.float32),
+                              np.ascontiguousarray(flag2, np.uint8), B, B.shape[1], C,
+                              B.shape[1], threads or 0)
+    return C

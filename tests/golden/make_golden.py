@@ -19,6 +19,8 @@ runs them on small seeded inputs and saves inputs and outputs as .npz files:
   scan, ascending columns, as toCSR writes them), C dense, accumulated over two calls;
 * transpose_triplets.npz -- convert (sparseTranspose.cpp:71-92) and fast_transpose
   (sparseTranspose.cpp:95-142) run on one thread (stable order);
+* rowpair_reuse.npz -- the row-pair reuse layout toDataReuseFormat (suitesparse_sdmm.cpp:
+  150-179) and DataReuseSpmm (:25-44) over it, A built by that file's toCSR;
 * mtx_reader.npz -- the reference's Matrix Market reader readMtx<float> (gcn/util/util.hpp:
   286-333, with makeSymmetric :218-284) on small seeded .mtx texts (stored in the file):
   symmetric real and pattern files with self-loops and duplicates, general real with
@@ -174,6 +176,41 @@ def transpose_cases(ref):
     np.savez_compressed(os.path.join(HERE, "transpose_triplets.npz"), **out)
 
 
+def rowpair_cases(ref):
+    """The reference's row-pair reuse layout (toDataReuseFormat) and DataReuseSpmm on small
+    seeded matrices whose paired rows share columns (half of each odd row's columns copied from
+    the even row above it), an odd row count included."""
+    cases = [(64, 80, 32, 0.1, 41), (33, 40, 7, 0.2, 42), (50, 64, 130, 0.15, 43),
+             (16, 16, 1, 0.3, 44)]
+    out = {}
+    for i, (M, K, N, dens, seed) in enumerate(cases):
+        rng = np.random.default_rng(6000 + seed)
+        dense = dense_sparse(rng, M, K, dens)
+        for r in range(1, M, 2):  # let pairs share columns
+            share = (dense[r - 1] != 0) & (rng.random(K) < 0.5)
+            dense[r, share] = rng.uniform(-1, 1, int(share.sum())).astype(np.float32) + 2.0
+        nnz = int((dense != 0).sum())
+        rowptr = np.zeros(M + 1, np.int32)
+        colind = np.zeros(max(nnz, 1), np.int32)
+        val = np.zeros(max(nnz, 1), np.float32)
+        ref.ref_toCSR_rp(_p(dense), M, K, _p(rowptr), _p(colind), _p(val))
+        work = dense.copy()
+        rp2 = np.zeros(M + 1, np.int32)
+        ci2 = np.zeros(max(nnz, 1), np.int32)
+        v2 = np.zeros(max(nnz, 1), np.float32)
+        f2 = np.zeros(max(nnz, 1), np.uint8)
+        ref.ref_toDataReuseFormat(_p(work), M, K, _p(rp2), _p(ci2), _p(v2), _p(f2))
+        B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+        C = np.zeros((M, N), np.float32)
+        ref.ref_DataReuseSpmm(_p(rp2), _p(ci2), _p(v2), _p(B), _p(C), M, K, N, 4, _p(f2))
+        out.update({f"c{i}_shape": np.array([M, K, N], np.int32), f"c{i}_rowptr": rowptr,
+                    f"c{i}_colind": colind[:nnz], f"c{i}_val": val[:nnz], f"c{i}_B": B,
+                    f"c{i}_rowptr2": rp2, f"c{i}_colind2": ci2[:nnz], f"c{i}_val2": v2[:nnz],
+                    f"c{i}_flag2": f2[:nnz], f"c{i}_C": C})
+    out["n_cases"] = np.array(len(cases), np.int32)
+    np.savez_compressed(os.path.join(HERE, "rowpair_reuse.npz"), **out)
+
+
 def mtx_texts():
     """Small seeded Matrix Market files covering what the reference's reader distinguishes:
     symmetric (mirrors, self-loops, duplicates, real values that the compaction misaligns),
@@ -324,7 +361,8 @@ def main():
               "spmv": lambda: spmv_cases(O.ref_lib("spmv")),
               "transpose": lambda: transpose_cases(O.ref_lib("transpose")),
               "spgemm": lambda: spgemm_cases(O.ref_lib("spgemm")),
-              "mtx": mtx_cases}
+              "mtx": mtx_cases,
+              "rowpair": lambda: rowpair_cases(O.ref_lib("rowpair"))}
     for name, make in makers.items():
         if only in (None, name):
             make()

@@ -54,7 +54,8 @@ def test_drivers_library_exports_reference_signatures():
     out = os.popen("nm -D --defined-only " + build.os.path.join(build.PKG, build.DRIVERS_NAME)).read()
     for mangled in ["_Z12rowBaseSpmm3PiS_PfS0_S0_iiii", "_Z12rowBaseSpmm2PiS_PfS0_S0_iiii",
                     "_Z6originPiS_PfS0_S0_iiii", "_Z19sparse_dense_vectorPfS_PiS0_S_ii",
-                    "_Z15csr_spmm_kerneliiPiS_PfS0_S0_", "_Z14fast_transposePiS_PSt5mutex"]:
+                    "_Z15csr_spmm_kerneliiPiS_PfS0_S0_", "_Z14fast_transposePiS_PSt5mutex",
+                    "_Z13DataReuseSpmmPiS_PfS0_S0_iiiiPb", "_Z17toDataReuseFormatPfiiPiS0_S_Pb"]:
         assert mangled in out, mangled
 
 

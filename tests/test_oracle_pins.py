@@ -270,3 +270,24 @@ def test_reduce_max_dgl_restates_reference_loop(oracle):
     ref = _dgl_copy_max(a.rowptr, a.colind, B)
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
     assert (np.diff(a.rowptr) == 0).any()
+
+
+def test_rowpair_layout_and_spmm_match_reference_golden(oracle, golden):
+    """The oracle's row-pair layout (built from CSR) and its DataReuseSpmm order against what
+    the reference's own toDataReuseFormat / DataReuseSpmm (suitesparse_sdmm.cpp) produced from
+    the dense matrices -- bit for bit."""
+    g = golden["rowpair_reuse"]
+    for i in range(int(g["n_cases"])):
+        rp2, ci2, v2, f2 = oracle.csr_to_rowpair(g[f"c{i}_rowptr"], g[f"c{i}_colind"],
+                                                 g[f"c{i}_val"])
+        assert np.array_equal(rp2, g[f"c{i}_rowptr2"]), i
+        assert np.array_equal(ci2, g[f"c{i}_colind2"]), i
+        assert np.array_equal(v2.view(np.uint32), g[f"c{i}_val2"].view(np.uint32)), i
+        assert np.array_equal(f2, g[f"c{i}_flag2"]), i
+        assert f2.any()  # the cases do share columns within pairs
+        C = oracle.spmm_rowpair_f32(rp2, ci2, v2, f2, g[f"c{i}_B"], threads=3)
+        assert np.array_equal(C.view(np.uint32), g[f"c{i}_C"].view(np.uint32)), i
+        # even rows keep the CSR chain; odd rows that share a column generally do not
+        chain = oracle.spmm_fma_chain_f32(g[f"c{i}_rowptr"], g[f"c{i}_colind"], g[f"c{i}_val"],
+                                          g[f"c{i}_B"])
+        assert np.array_equal(C[0::2].view(np.uint32), chain[0::2].view(np.uint32)), i
