@@ -13,10 +13,14 @@
 
 namespace {
 
+constexpr int kRowBlocks = 8;  // SpMM row blocks whose copies back overlap the next blocks
+
 struct State {
     std::mutex mu;
     as_ctx *ctx = nullptr;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // device -> host copies of finished row blocks
+    cudaEvent_t done[kRowBlocks] = {};   // row block b's kernels have finished
     void *buf = nullptr;
     size_t cap = 0;
     as_status last = AS_OK;
@@ -40,8 +44,12 @@ as_status prepare(State &s, size_t bytes, char **base) {
         cudaGetDevice(&dev);
         as_status st = as_ctx_create(&s.ctx, dev);
         if (st != AS_OK) return st;
-        if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess)
+        if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&s.copy_stream, cudaStreamNonBlocking) != cudaSuccess)
             return AS_ERR_CUDA;
+        for (cudaEvent_t &e : s.done)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+                return AS_ERR_CUDA;
     }
     if (bytes > s.cap) {
         if (s.buf) cudaFree(s.buf);
@@ -104,9 +112,41 @@ as_status spmm_host(const int *rowPtr, const int *colInd, const float *val, cons
     if ((st = h2d(s, dv, val, sizeof(float) * nnz)) != AS_OK) return st;
     if ((st = h2d(s, dB, B, sizeof(float) * size_t(K) * N)) != AS_OK) return st;
     if (beta != 0.0f && (st = h2d(s, dC, C, sizeof(float) * size_t(M) * N)) != AS_OK) return st;
-    st = as_spmm_csr_f32(s.ctx, M, K, N, nnz, drp, dci, dv, dB, N, dC, N, beta, 0, s.stream);
-    if (st != AS_OK) return st;
-    return finish(s, C, dC, sizeof(float) * size_t(M) * N);
+    // Row blocks: block b's result goes back to the host on the copy stream while the kernels
+    // of blocks b+1.. run, so only the first block's compute adds to the copies. Each block is
+    // the same library call on a slice of rows (rowptr offset, C offset), so every output is
+    // the same fused chain as in one call.
+    const int blocks = (M >= kRowBlocks * 512 && N > 0) ? kRowBlocks : 1;
+    const int rows_per = (M + blocks - 1) / blocks;
+    int issued = 0;
+    for (int b = 0; b < blocks; ++b) {
+        const int r0 = b * rows_per, r1 = std::min(M, r0 + rows_per);
+        if (r0 >= r1) break;
+        st = as_spmm_csr_f32(s.ctx, r1 - r0, K, N, nnz, drp + r0, dci, dv, dB, N,
+                             dC + size_t(r0) * N, N, beta, 0, s.stream);
+        if (st != AS_OK) break;
+        if (cudaEventRecord(s.done[b], s.stream) != cudaSuccess) {
+            st = AS_ERR_CUDA;
+            break;
+        }
+        issued = b + 1;
+    }
+    for (int b = 0; b < issued && st == AS_OK; ++b) {
+        const int r0 = b * rows_per, r1 = std::min(M, r0 + rows_per);
+        if (cudaStreamWaitEvent(s.copy_stream, s.done[b], 0) != cudaSuccess ||
+            cudaMemcpyAsync(C + size_t(r0) * N, dC + size_t(r0) * N,
+                            sizeof(float) * size_t(r1 - r0) * N, cudaMemcpyDeviceToHost,
+                            s.copy_stream) != cudaSuccess)
+            st = AS_ERR_CUDA;
+    }
+    // both streams drain before the call returns, whatever happened
+    const bool synced = cudaStreamSynchronize(s.copy_stream) == cudaSuccess;
+    if (st != AS_OK) {
+        cudaStreamSynchronize(s.stream);
+        return st;
+    }
+    if (!synced) return AS_ERR_CUDA;
+    return finish(s, nullptr, nullptr, 0);
 }
 
 as_status spgemm_host(const int *rp1, const int *ci1, const float *v1, const int *rp2,

@@ -24,7 +24,7 @@
 // and the gather latency. Every wait is bounded; a wait that gives up sets the timeout flag
 // and an abort flag that makes the other role leave too; each thread waits for its own copies
 // before the CTA moves on, and a row whose wait gave up is left unwritten. A malformed column
-// index is flagged and its entry reads B row 0 with value 0.
+// index is flagged and its entry gets a zero segment and value 0 (nothing is read for it).
 //
 // The list counter and a CTA-done counter live in the context's device words; the last CTA
 // to finish resets both, so the next call starts from zero without a memset.
@@ -224,12 +224,18 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                     const int j = q / P, piece = q % P;
                     if (j >= n || piece >= pieces) continue;
                     const int e = lo + base + j;
-                    int k = ld_stream(colind + e);
+                    const int k = ld_stream(colind + e);
                     const bool bad = static_cast<unsigned>(k) >= static_cast<unsigned>(K);
-                    if (bad) k = 0;
-                    const unsigned char *src =
-                        reinterpret_cast<const unsigned char *>(B + static_cast<long>(k) * ldb + slice0);
-                    cp_async<GB>(dst0 + j * kSliceBytes + piece * GB, src + piece * GB);
+                    unsigned char *d = ring + slot * kStage * kSliceBytes + j * kSliceBytes + piece * GB;
+                    if (!bad) {
+                        const unsigned char *src = reinterpret_cast<const unsigned char *>(
+                            B + static_cast<long>(k) * ldb + slice0);
+                        cp_async<GB>(dst0 + j * kSliceBytes + piece * GB, src + piece * GB);
+                    } else if constexpr (GB == 16) {  // nothing is read for a malformed entry
+                        *reinterpret_cast<uint4 *>(d) = make_uint4(0, 0, 0, 0);
+                    } else {
+                        *reinterpret_cast<unsigned *>(d) = 0u;
+                    }
                     if (piece == 0) {
                         if (bad) flag(status, kFlagBadColind);
                         vring[slot * kStage + j] = bad ? 0.0f : to_f32(ld_stream(val + e));

@@ -143,6 +143,14 @@ class SpmmF32(Workload):
         case with their error against FP64, and the GCN epoch tuned vs plain."""
         return default_extras(self)
 
+    # --- reference arm on the GPU: the reference's own spmm_cuda kernels ---
+    ref_cuda_kernel = ("spmm_cuda (gcn/pytorch-custom/spmm_kernel.cu:425-458: spmm_test2 at this "
+                       "width), compiled for sm_103a from the reference's source")
+
+    def ref_cuda_step(self):
+        from oracle import ref_gpu
+        ref_gpu.spmm_cuda(self.rp, self.ci, self.v, self.Bd, out=self.C)
+
     def cpu_step(self, threads, rows=None):
         from oracle import oracle as O
         a = self.a
@@ -404,7 +412,24 @@ class SpgemmDense(_Generic):
         return self.bytes
 
 
-class SddmmTc(_Generic):
+class _SddmmRefCuda:
+    ref_cuda_kernel = ("sddmm_cuda_csr (gcn/pytorch-custom/sddmm.cu:459-483: sddmmCSR2Scale), "
+                       "compiled for sm_103a from the reference's source; unscaled, on the "
+                       "pattern cut to a multiple of 16 entries (its tail blocks read past row "
+                       "ends otherwise)")
+
+    def ref_cuda_step(self):
+        from oracle import ref_gpu
+        if not hasattr(self, "_ref16"):
+            import torch
+            n16 = self.a.nnz - self.a.nnz % 16
+            self._ref16 = (torch.clamp(self.rp, max=n16), self.ci[:n16],
+                           torch.empty(n16, device=self.Xd.device))
+        rp, ci, out = self._ref16
+        ref_gpu.sddmm_cuda_csr(rp, ci, self.Xd, self.Yd, out=out)
+
+
+class SddmmTc(_Generic, _SddmmRefCuda):
     name = "sddmm_tc"
     metric = "SDDMM GB/s (algorithmic bytes), tensor-core split-bf16 path"
     unit = "GB/s"
@@ -1091,8 +1116,33 @@ def run_reference(args, wl_cls):
         "e2e": {"value": round(value, 3), "unit": wl.unit, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+    gpu = reference_cuda(args, wl)
+    if gpu is not None:
+        line["reference_cuda"] = gpu
     print(json.dumps(line), flush=True)
     return 0
+
+
+def reference_cuda(args, wl):
+    """The reference's own CUDA kernels for this workload on this machine's GPU (where the
+    workload has them and their cubins were built): K timed steps after W warm-ups, L2
+    flushed between steps, CUDA events; None otherwise."""
+    if not hasattr(wl, "ref_cuda_step"):
+        return None
+    try:
+        import torch
+        from oracle import ref_gpu
+        if not (torch.cuda.is_available() and ref_gpu.available()):
+            return {"unavailable": "no GPU or reference cubins not built"}
+        from armsparse_gb300 import tuner
+        dev = torch.device("cuda", 0)
+        wl.to_device(dev)
+        ms = tuner.time_cuda(wl.ref_cuda_step, reps=max(3, args.steps), warmup=max(3, args.warmup))
+        return {"kernel": wl.ref_cuda_kernel, "ms_per_step": round(ms, 5),
+                "value": round(wl.value(ms * 1e-3), 3), "unit": wl.unit,
+                "l2": "flushed between steps"}
+    except Exception as e:  # noqa: BLE001 -- the CPU line stands without it
+        return {"unavailable": repr(e)[:200]}
 
 
 def cpu_baseline(wl, budget_s=10.0):
