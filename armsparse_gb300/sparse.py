@@ -257,11 +257,37 @@ def spmv_vcsr4(vrowptr, vcolind, vval, x, y=None, beta: float = 0.0):
     return y
 
 
-def sddmm(rowptr, colind, X, Y, aval=None, out=None, tensor_cores: bool = False,
-          variant: int = 0):
+_SDDMM_SELECTOR = []
+
+
+def sddmm_path(rowptr, colind, n_cols: int, K: int) -> str:
+    """The learned choice of SDDMM path for this pattern and K ("simt" or "tc<variant>", see
+    tuner.sddmm_paths), from armsparse_gb300/sddmm_selector_model.json; "simt" when no model
+    file is present. Computes the pattern's features on the device (one pass over it): cache
+    the answer when the same pattern is used again."""
+    if not _SDDMM_SELECTOR:
+        from . import selector
+        try:
+            _SDDMM_SELECTOR.append(selector.SddmmSelector.load())
+        except (OSError, ValueError):
+            _SDDMM_SELECTOR.append(None)
+    sel = _SDDMM_SELECTOR[0]
+    return "simt" if sel is None else sel.choose(rowptr, colind, n_cols, K)
+
+
+def sddmm(rowptr, colind, X, Y, aval=None, out=None, tensor_cores=False, variant: int = 0):
     """out[e] = aval[e] * <X[row(e)], Y[col(e)]> (aval None -> unscaled, the reference's
     sddmm_cuda_csr). X: M x K, Y: N x K, fp32 -- or both bf16 (fp32 products and sums, fp32
-    out). tensor_cores selects the tcgen05 split-bf16 path (fp32 inputs)."""
+    out). tensor_cores=True selects the tcgen05 split-bf16 path (fp32 inputs; ``variant`` its
+    kernel), False the CUDA-core FP32 path, "auto" the learned choice between them
+    (``sddmm_path``) for fp32 inputs."""
+    if tensor_cores == "auto":
+        if X.dtype == torch.float32 and Y.dtype == torch.float32:
+            path = sddmm_path(rowptr, colind, Y.shape[0], X.shape[1])
+            tensor_cores = path != "simt"
+            variant = int(path[2:]) if tensor_cores else 0
+        else:
+            tensor_cores = False
     dev = _dev(rowptr, colind, X, Y, aval, out)
     M, nnz = _csr(rowptr, colind)
     if X.dtype == torch.float64:

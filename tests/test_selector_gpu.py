@@ -114,3 +114,35 @@ def test_trained_selector_beats_width_rule():
     ev = SEL.evaluate(model, test)
     assert ev["mlp_geomean"] <= ev["rule_geomean"], ev
     assert ev["mlp_geomean"] < 1.6, ev
+
+
+def test_sddmm_path_choice_against_autotuner():
+    """The learned SDDMM path choice (CUDA-core FP32 or a tcgen05 split-bf16 variant) on
+    held-out seeded patterns the model was not trained on (another seed): its pick's time
+    within 1.1x of the exhaustive autotuner's best (geometric mean), and at least as good as
+    always taking the CUDA-core path -- the only kind the reference has, chosen by K % 4 and
+    K % 2 alone (gcn/pytorch-custom/sddmm.cu:438-455). Every path agrees with FP64."""
+    if not os.path.exists(SEL.DEFAULT_SDDMM_MODEL):
+        pytest.skip("no SDDMM selector model file")
+    from armsparse_gb300 import sparse as S
+    from armsparse_gb300 import tuner
+    sel = SEL.SddmmSelector.load()
+    cfgs = SEL.sddmm_sweep_configs(16, seed=777, max_nnz=3_000_000,
+                                   max_dense_bytes=256 << 20)
+    recs = SEL.sddmm_sweep(cfgs, reps=3)
+    ev = SEL.evaluate_sddmm(sel.model, recs)
+    assert ev["mlp_geomean"] <= 1.1, ev
+    assert ev["mlp_geomean"] <= ev["simt_geomean"] + 1e-9, ev
+    # the API's "auto" takes the model's pick and stays within the accuracy of either path
+    d = torch.device("cuda", 0)
+    cfg = cfgs[0]
+    rp, ci = SEL.make_sddmm_pattern(cfg, d)
+    g = torch.Generator(device=d).manual_seed(5)
+    X = torch.randn(cfg["M"], cfg["K"], generator=g, device=d)
+    Y = torch.randn(cfg["N"], cfg["K"], generator=g, device=d)
+    out = S.sddmm(rp, ci, X, Y, tensor_cores="auto")
+    r64 = S.sddmm(rp, ci, X.double(), Y.double())
+    s64 = S.sddmm(rp, ci, X.double().abs(), Y.double().abs())
+    err = ((out.double() - r64).abs() / torch.maximum(r64.abs(), s64)).max().item()
+    assert err < 3e-5
+    assert S.sddmm_path(rp, ci, cfg["N"], cfg["K"]) in tuner.sddmm_paths()
