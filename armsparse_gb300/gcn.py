@@ -114,12 +114,14 @@ def _spmm_sddmm_t(colptr, rowind, w_csc, g, feat, csc_pos, variant):
     return C, S.gather(dA_csc, csc_pos)
 
 
-def _time_pick(rowptr, colind, values, n_in: int, width: int, dtype) -> int:
-    """The fastest of the selector's candidate SpMM kernels on these arrays (timed once)."""
+def _time_pick(rowptr, colind, values, n_in: int, width: int, dtype, exact: bool = False) -> int:
+    """The fastest of the selector's candidate SpMM kernels on these arrays (timed once);
+    with ``exact`` only the bit-exact families (selector.is_exact)."""
     from . import selector as SEL
     from . import tuner
     B = torch.zeros(n_in, width, device=rowptr.device, dtype=dtype)
-    ids = SEL.variant_ids(SEL.CANDIDATES, dtype)
+    names = [n for n in SEL.CANDIDATES if not exact or SEL.is_exact(n)]
+    ids = SEL.variant_ids(names, dtype)
     return tuner.best(tuner.autotune_spmm(rowptr, colind, values.to(dtype), B, variants=ids,
                                           reps=3, max_ratio=3.0)).variant
 
@@ -200,6 +202,11 @@ class Graph:
         self._perm = None
         self._csc_pos = None
         self.selector = None  # a selector.Selector: per-width kernel choice (None = library choice)
+        # with a selector: True restricts the choice to kernels whose outputs are the CSR-order
+        # chains (so training is bit-for-bit the library default's), False lets it take the
+        # entry-balanced kernels too (their sums differ in the last bits for rows that cross a
+        # chunk, and over hundreds of epochs the losses drift apart by up to ~1e-3)
+        self.exact = False
         self._plans = {}
 
     @property
@@ -237,23 +244,26 @@ class Graph:
         that carries the SDDMM, timed once."""
         if self.selector is None or dtype == torch.float64:
             return (0, 0)
-        if fused:
+        if fused and not self.exact:
             key = (N, dtype, "fused")
             if key not in self._plans:
                 colptr, rowind, vcsc = self.csc
                 bwd = _time_pick_fused(colptr, rowind, vcsc, self.n_rows, N, dtype)
                 self._plans[key] = (self.plan(N, dtype)[0], bwd or self.plan(N, dtype)[1])
             return self._plans[key]
-        key = (N, dtype)
+        key = (N, dtype, self.exact)
         if key not in self._plans:
             colptr, rowind, vcsc = self.csc
+            ex = self.exact
             if N < 16:
                 self._plans[key] = (_time_pick(self.rowptr, self.colind, self.values,
-                                               self.n_cols, N, dtype),
-                                    _time_pick(colptr, rowind, vcsc, self.n_rows, N, dtype))
+                                               self.n_cols, N, dtype, ex),
+                                    _time_pick(colptr, rowind, vcsc, self.n_rows, N, dtype, ex))
             else:
-                self._plans[key] = (self.selector.choose(self.rowptr, self.n_cols, N, dtype),
-                                    self.selector.choose(colptr, self.n_rows, N, dtype))
+                self._plans[key] = (self.selector.choose(self.rowptr, self.n_cols, N, dtype,
+                                                         exact=ex),
+                                    self.selector.choose(colptr, self.n_rows, N, dtype,
+                                                         exact=ex))
         return self._plans[key]
 
     @classmethod

@@ -52,6 +52,13 @@ CANDIDATES = [
 ]
 
 
+def is_exact(name: str) -> bool:
+    """Whether a variant's outputs are each the CSR-order fused chain (bit-identical to the
+    reference's rowBaseSpmm3 and to the library default): the row-split and bulk-copy
+    families. The entry-balanced ones reorder the sums of rows that cross a chunk."""
+    return name.startswith(("rowsplit", "bulk"))
+
+
 def variant_ids(names, dtype):
     table = {n: i + 1 for i, n in enumerate(S.spmm_variants(dtype))}
     return [table[n] for n in names]
@@ -292,10 +299,13 @@ class Selector:
         with open(path, "w") as f:
             json.dump(self.model, f)
 
-    def choose(self, rowptr, n_cols: int, N: int, dtype=torch.float32, key=None) -> int:
-        """Variant id for an SpMM with this matrix and dense width (cached by ``key``)."""
-        if key is not None and (key, N, dtype) in self._cache:
-            return self._cache[(key, N, dtype)]
+    def choose(self, rowptr, n_cols: int, N: int, dtype=torch.float32, key=None,
+               exact: bool = False) -> int:
+        """Variant id for an SpMM with this matrix and dense width (cached by ``key``). With
+        ``exact`` only kernels whose every output is the reference's CSR-order chain are
+        considered (the row-split and bulk families: bit-identical to the library default)."""
+        if key is not None and (key, N, dtype, exact) in self._cache:
+            return self._cache[(key, N, dtype, exact)]
         rp = rowptr.cpu().numpy() if isinstance(rowptr, torch.Tensor) else np.asarray(rowptr)
         feats = tuner.features(rp, n_cols, N, dtype == torch.bfloat16)
         order = np.argsort(-host_forward(self.model, feats))
@@ -306,6 +316,8 @@ class Selector:
         names = S.spmm_variants(dtype)
         for i in order:
             cand = ids[int(i)]
+            if exact and not is_exact(self.model["candidates"][int(i)]):
+                continue
             if S.spmm_variant_supported(cand, N, dtype):
                 v = cand
                 break
@@ -314,7 +326,7 @@ class Selector:
                 v = alt
                 break
         if key is not None:
-            self._cache[(key, N, dtype)] = v
+            self._cache[(key, N, dtype, exact)] = v
         return v
 
 
