@@ -10,7 +10,7 @@ behind the C ABI in include/armsparse_gpu.h. The ops need the CUDA library built
 GPU; there is no CPU fallback.
 """
 from .sparse import (csr2csc, csr2csc_perm, csr_to_rowpair, csr_to_vcsr4, dense_to_csr,
-                     gather, sddmm, spmm_rowpair,
+                     gather, sddmm, spmm_rowpair, spmm_vcsr4,
                      sddmm_coo, softmax_xent, softmax_xent_grad, spgemm_dense, spmm,
                      spmm_default_variant, spmm_reduce, spmm_sddmm, spmm_variant_supported,
                      spmm_variants, spmv, spmv_vcsr4, sync_status, to_bf16, validate_csr)
@@ -18,6 +18,7 @@ from ._native import NativeError, Context, context
 
 __all__ = ["spmm", "spmm_reduce", "spmm_sddmm", "spgemm_dense", "spmv", "spmv_vcsr4", "sddmm",
            "sddmm_coo", "csr2csc", "csr2csc_perm", "gather", "softmax_xent", "softmax_xent_grad",
-           "csr_to_vcsr4", "csr_to_rowpair", "spmm_rowpair", "dense_to_csr", "validate_csr", "sync_status", "to_bf16",
+           "csr_to_vcsr4", "csr_to_rowpair", "spmm_rowpair", "spmm_vcsr4", "dense_to_csr",
+           "validate_csr", "sync_status", "to_bf16",
            "spmm_variants", "spmm_default_variant", "spmm_variant_supported", "NativeError",
            "Context", "context"]

@@ -65,6 +65,7 @@ SIGNATURES = {
     "as_f32_to_bf16": (_I, [_P, _L, _P, _P, _P]),
     "as_dense_to_csr_count": (_I, [_P, _I, _I, _P, _L, _P, _P]),
     "as_dense_to_csr_fill": (_I, [_P, _I, _I, _P, _L, _P, _P, _P, _P]),
+    "as_spmm_vcsr4_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _L, _P, _L, _F, _P]),
     "as_csr_to_rowpair_count": (_I, [_P, _I, _I, _P, _P, _P, _P]),
     "as_csr_to_rowpair_fill": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
     "as_spmm_rowpair_f32": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _P, _L, _P, _L, _F, _P]),

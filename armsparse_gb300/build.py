@@ -32,6 +32,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-I" + INCLUDE, "-I" + CSRC]
 CU_SOURCES = ["api.cu", "spmm.cu", "spmm_bulk.cu", "spmm_nnz.cu", "spmm_long.cu", "spmv.cu", "sddmm_simt.cu", "sddmm_tc.cu", "transpose.cu",
               "fp64.cu", "mlp.cu", "formats.cu", "spmm_reduce.cu", "spgemm_dense.cu", "spmm_rowpair.cu",
+              "spmm_vcsr4.cu",
               "xent.cu"]
 LIB_NAME = "libarmsparse_gpu.so"
 DRIVERS_NAME = "libarmsparse_drivers.so"

@@ -642,6 +642,21 @@ as_status as_spmm_rowpair_f32(as_ctx *c, int M, int K, int N, int nnz, const int
     return spmm_rowpair_launch(c, a, flag2, static_cast<cudaStream_t>(stream));
 }
 
+as_status as_spmm_vcsr4_f32(as_ctx *c, int M, int K, int N, int nslots, const int *vrowptr,
+                            const int *vcolind, const float *vval, const float *B, long ldb,
+                            float *C, long ldc, float beta, void *stream) {
+    if (!c) return fail(AS_ERR_INVALID_VALUE, "as_spmm_vcsr4_f32: ctx is NULL");
+    as_status st = check_csr_args("as_spmm_vcsr4_f32", M, K, nslots, vrowptr, vcolind, vval, true);
+    if (st != AS_OK) return st;
+    if (N < 0) return fail(AS_ERR_INVALID_VALUE, "as_spmm_vcsr4_f32: negative N");
+    if (M == 0 || N == 0) return AS_OK;
+    if (!C || (nslots > 0 && K > 0 && !B) || ldb < N || ldc < N)
+        return fail(AS_ERR_INVALID_VALUE, "as_spmm_vcsr4_f32: bad dense operand");
+    DeviceGuard g(c->device);
+    return spmm_vcsr4_launch(c, M, K, N, nslots, vrowptr, vcolind, vval, B, ldb, C, ldc, beta,
+                             static_cast<cudaStream_t>(stream));
+}
+
 as_status as_gather_f32(as_ctx *c, long n, long n_src, const float *src, const int *idx,
                         float *dst, void *stream) {
     if (!c) return fail(AS_ERR_INVALID_VALUE, "as_gather_f32: ctx is NULL");

@@ -149,6 +149,9 @@ as_status csr_to_rowpair_fill_launch(as_ctx *ctx, int M, int nnz, const int *row
                                      int *colind2, float *val2, uint8_t *flag2, cudaStream_t s);
 as_status spmm_rowpair_launch(as_ctx *ctx, const SpmmArgs &a, const uint8_t *flag2,
                               cudaStream_t s);
+as_status spmm_vcsr4_launch(as_ctx *ctx, int M, int K, int N, int nslots, const int *vrowptr,
+                            const int *vcolind, const float *vval, const float *B, long ldb,
+                            float *C, long ldc, float beta, cudaStream_t s);
 as_status csr_to_vcsr4_count_launch(as_ctx *ctx, int M, int nnz, const int *rowptr,
                                     const int *colind, int *vrowptr, cudaStream_t s);
 as_status csr_to_vcsr4_fill_launch(as_ctx *ctx, int M, int nnz, const int *rowptr,

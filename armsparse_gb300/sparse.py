@@ -612,3 +612,22 @@ def spmm_rowpair(rowptr2, colind2, val2, flag2, B, C=None, beta: float = 0.0):
                                          C.stride(0) if M > 1 else Ncols, float(beta),
                                          _stream(dev)), "as_spmm_rowpair_f32")
     return C
+
+
+def spmm_vcsr4(vrowptr, vcolind, vval, B, C=None, beta: float = 0.0):
+    """C = A*B + beta*C with A in the reference's 1x4-blocked layout (``csr_to_vcsr4``); slots
+    holding 0 are skipped, so the result is the CSR SpMM's, bit for bit."""
+    dev = _dev(vrowptr, vcolind, vval, B, C)
+    M, ns = _csr(vrowptr, vcolind)
+    _need(vval, torch.float32, "vval", 1)
+    if B.dtype != torch.float32 or B.dim() != 2 or B.stride(1) != 1:
+        raise ValueError("B must be float32, 2-D, row-major")
+    K, Ncols = B.shape
+    if C is None:
+        C = torch.empty((M, Ncols), dtype=torch.float32, device=dev)
+    ctx = N.context(dev.index)
+    N.check(N.load().as_spmm_vcsr4_f32(ctx.handle, M, K, Ncols, ns, _ptr(vrowptr), _ptr(vcolind),
+                                       _ptr(vval), _ptr(B), B.stride(0) if K > 1 else Ncols,
+                                       _ptr(C), C.stride(0) if M > 1 else Ncols, float(beta),
+                                       _stream(dev)), "as_spmm_vcsr4_f32")
+    return C

@@ -197,3 +197,34 @@ def sddmm_features(rowptr: torch.Tensor, colind: torch.Tensor, n_cols: int, K: i
          density, math.log2(mean + 1), cv, occupied / n_tiles, math.log2(waste + 1),
          math.log2(K * nnz + 1)]
     return np.asarray(f, np.float32)
+
+
+# ------------------------------------------------------------------------------------------
+# Storage formats
+# ------------------------------------------------------------------------------------------
+def autotune_formats(rowptr, colind, val, B, reps: int = 5, exact: bool = True,
+                     variant: int = 0) -> dict:
+    """Time one SpMM (fp32) in each storage format the library has, the conversion from CSR
+    done once beforehand and timed separately:
+      "csr"     -- the CSR kernels (``variant``, 0 = library default);
+      "vcsr4"   -- the reference's 1x4-blocked layout (toVectorAwareCSR, SpMV.cpp:15-38);
+      "rowpair" -- the reference's row-pair reuse layout (toDataReuseFormat,
+                   suitesparse_sdmm.cpp:150-179), only when ``exact`` is False: its odd rows
+                   sum in DataReuseSpmm's order, not the CSR order.
+    "csr" and "vcsr4" give the same bits. Returns {"times": {format: {"ms", "convert_ms"}},
+    "pick": fastest format}; a caller that reuses the matrix converts once and keeps the pick."""
+    out = {}
+    C = torch.empty((rowptr.numel() - 1, B.shape[1]), dtype=torch.float32, device=B.device)
+    out["csr"] = {"ms": time_cuda(lambda: S.spmm(rowptr, colind, val, B, C=C, variant=variant),
+                                  reps=reps), "convert_ms": 0.0}
+    conv_ms = time_cuda(lambda: S.csr_to_vcsr4(rowptr, colind, val), reps=1, warmup=1)
+    vr, vc, vv = S.csr_to_vcsr4(rowptr, colind, val)
+    out["vcsr4"] = {"ms": time_cuda(lambda: S.spmm_vcsr4(vr, vc, vv, B, C=C), reps=reps),
+                    "convert_ms": conv_ms, "slots_per_entry": vc.numel() / max(1, colind.numel())}
+    if not exact:
+        conv_ms = time_cuda(lambda: S.csr_to_rowpair(rowptr, colind, val), reps=1, warmup=1)
+        r2, c2, v2, f2 = S.csr_to_rowpair(rowptr, colind, val)
+        out["rowpair"] = {"ms": time_cuda(lambda: S.spmm_rowpair(r2, c2, v2, f2, B, C=C), reps=reps),
+                          "convert_ms": conv_ms,
+                          "shared_fraction": float(f2.float().mean()) if f2.numel() else 0.0}
+    return {"times": out, "pick": min(out, key=lambda k: out[k]["ms"])}

@@ -1245,7 +1245,7 @@ def run_ours(args, wl_cls):
         "clocks": clk.summary(),
         "wall_s_timed_region": round(wall, 4),
     }
-    if hasattr(wl, "extra"):
+    if hasattr(wl, "extra") and not args.no_extra:
         line["extra"] = wl.extra()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
@@ -1284,6 +1284,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="spmm_f32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the extra figures (profiler runs of the headline step alone)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--tc-variant", type=int, default=0,
                     help="tensor-core SDDMM kernel variant (0 = library choice)")

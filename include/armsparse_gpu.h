@@ -320,6 +320,15 @@ as_status as_csr_to_vcsr4_fill(as_ctx *ctx, int M, int nnz, const int *rowptr, c
                                const float *val, const int *vrowptr, int *vcolind, float *vval,
                                void *stream);
 
+/* C = A*B + beta*C with A in the reference's 1x4-blocked layout (vrowptr[M+1], vcolind and vval
+ * [nslots], as as_csr_to_vcsr4_* write it): the SpMM counterpart of sparse_dense_vector
+ * (SpMV.cpp:155-179). Slots holding 0 are skipped (the layout does not tell a stored zero from
+ * an empty slot), so each output is the fused chain over the row's nonzero entries in column
+ * order -- bit for bit the CSR SpMM of the matrix without stored zeros. */
+as_status as_spmm_vcsr4_f32(as_ctx *ctx, int M, int K, int N, int nslots, const int *vrowptr,
+                            const int *vcolind, const float *vval, const float *B, long ldb,
+                            float *C, long ldc, float beta, void *stream);
+
 /* CSR (columns ascending in rows) -> the reference's row-pair reuse layout, toDataReuseFormat
  * (suitesparse_sdmm.cpp:150-179): rows are paired (2p, 2p+1); row 2p's segment lists its
  * entries in column order, each followed by row 2p+1's entry in the same column when there is

@@ -83,3 +83,24 @@ def test_rowpair_host_shims(golden):
         drv.as_drv_DataReuseSpmm(_p(rp2), _p(ci2), _p(v2), _p(B), _p(C), M, K, N, 8, _p(f2))
         assert drv.as_drv_last_status() == 0
         assert np.array_equal(C.view(np.uint32), g[f"c{i}_C"].view(np.uint32))
+
+
+@pytest.mark.parametrize("N", [3, 8, 64, 300])
+def test_vcsr4_spmm_is_the_csr_chain(oracle, N):
+    """The SpMM over the reference's 1x4-blocked layout, built on the GPU from CSR, gives the
+    CSR chain bit for bit (empty slots skipped), with accumulate; and the format tuner times
+    all three layouts and reports one of them."""
+    from armsparse_gb300 import tuner
+    for a in (S.banded_csr(5000, 11, seed=95), S.powerlaw_csr(3000, 2.0, 9.0, seed=96)):
+        rp, ci, v = to_dev(a.rowptr), to_dev(a.colind), to_dev(a.val)
+        vr, vc, vv = A.csr_to_vcsr4(rp, ci, v)
+        B = S.dense_uniform((a.n_cols, N), 97)
+        C0 = S.dense_uniform((a.n_rows, N), 98)
+        C = to_dev(C0)
+        A.spmm_vcsr4(vr, vc, vv, to_dev(B), C=C, beta=1.0)
+        ref = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, B, C=C0)
+        assert np.array_equal(bits(C), bits(ref)), N
+        res = tuner.autotune_formats(rp, ci, v, to_dev(B), reps=2, exact=False)
+        assert res["pick"] in ("csr", "vcsr4", "rowpair")
+        assert all(t["ms"] > 0 for t in res["times"].values())
+    A.sync_status()
