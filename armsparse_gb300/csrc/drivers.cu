@@ -13,7 +13,9 @@
 
 namespace {
 
-constexpr int kRowBlocks = 8;  // SpMM row blocks whose copies back overlap the next blocks
+constexpr int kRowBlocks = 8;  // at most this many SpMM row blocks, whose copies back overlap
+                               // the next blocks' kernels
+constexpr size_t kMinBlockBytes = size_t(16) << 20;  // each block's copy back: >= 16 MB
 
 struct State {
     std::mutex mu;
@@ -116,7 +118,8 @@ as_status spmm_host(const int *rowPtr, const int *colInd, const float *val, cons
     // of blocks b+1.. run, so only the first block's compute adds to the copies. Each block is
     // the same library call on a slice of rows (rowptr offset, C offset), so every output is
     // the same fused chain as in one call.
-    const int blocks = (M >= kRowBlocks * 512 && N > 0) ? kRowBlocks : 1;
+    const size_t c_bytes = sizeof(float) * size_t(M) * N;
+    const int blocks = int(std::max<size_t>(1, std::min<size_t>(kRowBlocks, c_bytes / kMinBlockBytes)));
     const int rows_per = (M + blocks - 1) / blocks;
     int issued = 0;
     for (int b = 0; b < blocks; ++b) {
