@@ -104,12 +104,10 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         }
     }
 
-    // (colind, val) of GROUP entries per batch, one per lane; the next batch is loaded while
-    // the current one is consumed, so a row longer than one batch does not wait for its
-    // indices between batches
-    auto load_entry = [&](int e, int &k, float &v) {
-        k = -1;
-        v = 0.0f;
+    for (int base = lo; base < hi; base += GROUP) {
+        const int e = base + g;
+        int k = -1;
+        float v = 0.0f;
         if (e < hi) {
             k = ld_stream(colind + e);
             v = to_f32(ld_stream(val + e));
@@ -118,12 +116,6 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 k = -1;
             }
         }
-    };
-    int k, kn;
-    float v, vn;
-    load_entry(lo + g, k, v);
-    for (int base = lo; base < hi; base += GROUP) {
-        load_entry(base + GROUP + g, kn, vn);
         const int cnt = min(GROUP, hi - base);
         int t = 0;
         // U entries per step: their B loads are issued before the FMAs, which then run in
@@ -197,8 +189,6 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 }
             }
         }
-        k = kn;
-        v = vn;
     }
 
 #pragma unroll

@@ -11,20 +11,20 @@
 // chains. A CTA takes one (long row, 64-byte column slice) at a time and splits its warps by
 // role:
 //  - warp 0 is the consumer: one lane per column of the slice runs the chain out of shared
-//    memory, stage after stage, and never waits on anything but the stage it needs next;
-//  - warps 1..7 are producers: for each stage of kStage entries they read the entries'
-//    column indices and values, copy each entry's B segment into the stage's ring slot with
-//    cp.async (one commit group per stage) and write its value next to it. A producer thread
-//    announces stage s on the slot's `full` mbarrier once its copies of that stage have
-//    landed, which it checks after issuing stage s + kLag (cp.async.wait_group kLag), so kLag
-//    stages of copies stay in flight per thread; every arrival is the thread's own, none is
-//    left pending when the CTA moves on. A slot is refilled only after the consumer arrives
-//    on its `empty` mbarrier.
-// The producers run up to kStages stages ahead of the consumer, which covers the index load
-// and the gather latency. Every wait is bounded; a wait that gives up sets the timeout flag
-// and an abort flag that makes the other role leave too; each thread waits for its own copies
-// before the CTA moves on, and a row whose wait gave up is left unwritten. A malformed column
-// index is flagged and its entry gets a zero segment and value 0 (nothing is read for it).
+//    memory, stage after stage. The entries' values it loads itself, three stages ahead, into
+//    registers (lane l holds entries l and 32 + l of a stage) and broadcasts them by shuffles;
+//  - warps 1-2 are producers, one thread per entry of a stage of kStage entries: the thread
+//    copies its entry's B segment into the stage's ring slot with cp.async, and the entry's
+//    column index for the stage kLag ahead into its own slot of a small index ring (cp.async
+//    too), one commit group per stage. Before stage s it waits for its group of stage s - kLag
+//    (cp.async.wait_group): that gives it stage s's index and tells it that its copies of stage
+//    s - kLag have landed, which it then announces on that slot's `full` mbarrier. A slot is
+//    refilled only after the consumer arrives on its `empty` mbarrier.
+// Every arrival is the arriving thread's own (none is left pending when the CTA moves on).
+// Every wait is bounded; a wait that gives up sets the timeout flag and an abort flag that makes
+// the other role leave too; each thread waits for its own copies before the CTA moves on, and a
+// row whose wait gave up is left unwritten. A malformed column index is flagged and its entry
+// gets a zero segment (nothing is read for it).
 //
 // The list counter and a CTA-done counter live in the context's device words; the last CTA
 // to finish resets both, so the next call starts from zero without a memset.
@@ -36,17 +36,19 @@
 namespace as {
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kProducers = kThreads - 32;  // warps 1..7
-constexpr int kSliceBytes = 64;            // B bytes per entry per stage (16 fp32 / 32 bf16 columns)
 constexpr int kStage = 64;                 // entries per pipeline stage
-constexpr int kStages = 24;                // ring slots
+constexpr int kProducers = kStage;         // warps 1-2: one thread per entry of a stage
+constexpr int kThreads = 32 + kProducers;
+constexpr int kSliceBytes = 64;            // B bytes per entry per stage (16 fp32 / 32 bf16 columns)
+constexpr int kStages = 24;                // B ring slots
 constexpr int kLag = 12;                   // stages of copies in flight per producer thread
+constexpr int kIdx = kLag + 1;             // index ring slots (a thread reads slot s, refills s + kLag)
+constexpr int kVAhead = 3;                 // stages of values the consumer loads ahead
 static_assert(kLag < kStages, "a producer must announce stage s before it waits to refill its slot");
 constexpr unsigned kSpinLimit = 1u << 22;  // polls of a bounded wait (a few seconds at most)
 constexpr int kRingBytes = kStages * kStage * kSliceBytes;
-constexpr int kVringBytes = kStages * kStage * 4;
-constexpr int kSmemBytes = kRingBytes + kVringBytes + 2 * kStages * 8 + 16;
+constexpr int kIdxBytes = kIdx * kStage * 4;
+constexpr int kSmemBytes = kRingBytes + kIdxBytes + 2 * kStages * 8 + 16;
 
 __device__ __forceinline__ float to_f32(float v) { return v; }
 __device__ __forceinline__ float to_f32(uint16_t v) { return bf16_to_f32(v); }
@@ -95,11 +97,10 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
           const int *__restrict__ list, unsigned *counters, uint16_t *__restrict__ C16,
           bool relu, unsigned spin_limit) {
     constexpr int W = kSliceBytes / static_cast<int>(sizeof(T));  // columns per slice
-    constexpr int P = kSliceBytes / GB;                            // copy pieces of a full slice
     extern __shared__ __align__(128) unsigned char smem[];
-    unsigned char *ring = smem;                                       // [kStages][kStage][64 B]
-    float *vring = reinterpret_cast<float *>(smem + kRingBytes);      // [kStages][kStage]
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + kRingBytes + kVringBytes);
+    unsigned char *ring = smem;                                    // [kStages][kStage][64 B]
+    int *kring = reinterpret_cast<int *>(smem + kRingBytes);       // [kIdx][kStage]
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + kRingBytes + kIdxBytes);
     uint64_t *empty = full + kStages;
     volatile int *abort_flag = reinterpret_cast<volatile int *>(empty + kStages);
 
@@ -140,8 +141,20 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         float *crow = C + static_cast<long>(r) * ldc + slice0;
         if (warp == 0) {
             // ---- consumer: the chains ----
+            const int col = lane < W ? lane : lane & (W - 1);  // lanes past the slice mirror
             if (lane < w && beta != 0.0f) acc = crow[lane] * beta;
+            float vq[kVAhead + 1][2];  // values of stages s .. s + kVAhead
+            auto loadv = [&](int st, float *d) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int e = st * kStage + h * 32 + lane;
+                    d[h] = (st < n_stages && e < L) ? to_f32(ld_stream(val + lo + e)) : 0.0f;
+                }
+            };
+#pragma unroll
+            for (int a = 0; a < kVAhead; ++a) loadv(a, vq[a]);
             for (int s = 0; s < n_stages; ++s) {
+                loadv(s + kVAhead, vq[kVAhead]);
                 const int slot = s % kStages;
                 const bool ok = __all_sync(
                     0xffffffffu, bar_wait(smem_u32(full + slot), (s / kStages) & 1, spin_limit,
@@ -153,60 +166,81 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                     }
                     break;
                 }
-                if (lane < w) {
-                    const int n = min(kStage, L - s * kStage);
-                    const float *vs = vring + slot * kStage;
-                    const T *bs = reinterpret_cast<const T *>(ring + slot * kStage * kSliceBytes) + lane;
-                    int j = 0;
-                    if (n >= 8) {  // the next 8 entries' loads are in flight during this 8's chain
-                        float b[8], bn[8];
-                        float4 v0 = *reinterpret_cast<const float4 *>(vs);
-                        float4 v1 = *reinterpret_cast<const float4 *>(vs + 4);
+                const int n = min(kStage, L - s * kStage);
+                const T *bs = reinterpret_cast<const T *>(ring + slot * kStage * kSliceBytes) + col;
+                int j = 0;
+                // eight entries per step: the next eight's loads and broadcasts are issued
+                // during this eight's chain
+                if (n >= 8) {
+                    float b[8], v[8], bn[8], vn[8];
 #pragma unroll
-                        for (int i = 0; i < 8; ++i) b[i] = to_f32(bs[i * W]);
-                        for (; j + 8 <= n; j += 8) {
-                            const bool more = j + 16 <= n;
-                            float4 n0 = v0, n1 = v1;
-                            if (more) {
-                                n0 = *reinterpret_cast<const float4 *>(vs + j + 8);
-                                n1 = *reinterpret_cast<const float4 *>(vs + j + 12);
+                    for (int i = 0; i < 8; ++i) {
+                        b[i] = to_f32(bs[i * W]);
+                        v[i] = __shfl_sync(0xffffffffu, vq[0][0], i);
+                    }
+                    for (; j + 8 <= n; j += 8) {
+                        const bool more = j + 16 <= n;
+                        if (more) {
 #pragma unroll
-                                for (int i = 0; i < 8; ++i) bn[i] = to_f32(bs[(j + 8 + i) * W]);
+                            for (int i = 0; i < 8; ++i) {
+                                const int jj = j + 8 + i;
+                                bn[i] = to_f32(bs[jj * W]);
+                                vn[i] = __shfl_sync(0xffffffffu, jj < 32 ? vq[0][0] : vq[0][1],
+                                                    jj & 31);
                             }
-                            acc = fmaf(b[0], v0.x, acc);
-                            acc = fmaf(b[1], v0.y, acc);
-                            acc = fmaf(b[2], v0.z, acc);
-                            acc = fmaf(b[3], v0.w, acc);
-                            acc = fmaf(b[4], v1.x, acc);
-                            acc = fmaf(b[5], v1.y, acc);
-                            acc = fmaf(b[6], v1.z, acc);
-                            acc = fmaf(b[7], v1.w, acc);
-                            if (more) {
-                                v0 = n0;
-                                v1 = n1;
+                        }
 #pragma unroll
-                                for (int i = 0; i < 8; ++i) b[i] = bn[i];
+                        for (int i = 0; i < 8; ++i) acc = fmaf(b[i], v[i], acc);
+                        if (more) {
+#pragma unroll
+                            for (int i = 0; i < 8; ++i) {
+                                b[i] = bn[i];
+                                v[i] = vn[i];
                             }
                         }
                     }
-                    for (; j < n; ++j) acc = fmaf(to_f32(bs[j * W]), vs[j], acc);
+                }
+                for (; j < n; ++j) {
+                    const float vv = __shfl_sync(0xffffffffu, j < 32 ? vq[0][0] : vq[0][1], j & 31);
+                    acc = fmaf(to_f32(bs[j * W]), vv, acc);
                 }
                 __syncwarp();
                 if (lane == 0)
                     asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(
                                      smem_u32(empty + slot))
                                  : "memory");
+#pragma unroll
+                for (int a = 0; a < kVAhead; ++a) {
+                    vq[a][0] = vq[a + 1][0];
+                    vq[a][1] = vq[a + 1][1];
+                }
             }
         } else {
-            // ---- producers: indices, values and B segments of upcoming stages ----
+            // ---- producers: thread p owns entry p of every stage ----
             const int p = tid - 32;
-            auto announce = [&](int st) {  // stage st's copies and stores by this thread are done
+            auto announce = [&](int st) {  // this thread's copies of stage st have landed
                 asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(
                                  smem_u32(full + st % kStages))
                              : "memory");
             };
+            auto copy_index = [&](int st) {  // column index of stage st's entry p, into the ring
+                const int e = st * kStage + p;
+                if (st < n_stages && e < L)
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(
+                                     smem_u32(kring + (st % kIdx) * kStage + p)),
+                                 "l"(colind + lo + e)
+                                 : "memory");
+            };
+            for (int t = 0; t < kLag; ++t) {  // the first kLag stages' indices, a group each
+                copy_index(t);
+                asm volatile("cp.async.commit_group;\n" ::: "memory");
+            }
             int issued = 0;
             for (int s = 0; s < n_stages; ++s) {
+                // this thread's group kLag back has landed: stage s's index, and its copies of
+                // stage s - kLag (announced now)
+                asm volatile("cp.async.wait_group %0;\n" ::"n"(kLag - 1) : "memory");
+                if (s >= kLag) announce(s - kLag);
                 const int slot = s % kStages;
                 if (s >= kStages &&
                     !bar_wait(smem_u32(empty + slot), ((s / kStages) - 1) & 1, kSpinLimit,
@@ -217,36 +251,27 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                     }
                     break;
                 }
-                const int base = s * kStage;
-                const int n = min(kStage, L - base);
-                const uint32_t dst0 = smem_u32(ring + slot * kStage * kSliceBytes);
-                for (int q = p; q < kStage * P; q += kProducers) {
-                    const int j = q / P, piece = q % P;
-                    if (j >= n || piece >= pieces) continue;
-                    const int e = lo + base + j;
-                    const int k = ld_stream(colind + e);
-                    const bool bad = static_cast<unsigned>(k) >= static_cast<unsigned>(K);
-                    unsigned char *d = ring + slot * kStage * kSliceBytes + j * kSliceBytes + piece * GB;
-                    if (!bad) {
+                const int e = s * kStage + p;
+                if (e < L) {
+                    const int k = kring[(s % kIdx) * kStage + p];
+                    unsigned char *d = ring + (slot * kStage + p) * kSliceBytes;
+                    if (static_cast<unsigned>(k) < static_cast<unsigned>(K)) {
                         const unsigned char *src = reinterpret_cast<const unsigned char *>(
                             B + static_cast<long>(k) * ldb + slice0);
-                        cp_async<GB>(dst0 + j * kSliceBytes + piece * GB, src + piece * GB);
-                    } else if constexpr (GB == 16) {  // nothing is read for a malformed entry
-                        *reinterpret_cast<uint4 *>(d) = make_uint4(0, 0, 0, 0);
-                    } else {
-                        *reinterpret_cast<unsigned *>(d) = 0u;
-                    }
-                    if (piece == 0) {
-                        if (bad) flag(status, kFlagBadColind);
-                        vring[slot * kStage + j] = bad ? 0.0f : to_f32(ld_stream(val + e));
+                        for (int q = 0; q < pieces; ++q) cp_async<GB>(smem_u32(d + q * GB), src + q * GB);
+                    } else {  // malformed: a zero segment, nothing read
+                        flag(status, kFlagBadColind);
+                        for (int q = 0; q < pieces; ++q) {
+                            if constexpr (GB == 16)
+                                *reinterpret_cast<uint4 *>(d + q * GB) = make_uint4(0, 0, 0, 0);
+                            else
+                                *reinterpret_cast<unsigned *>(d + q * GB) = 0u;
+                        }
                     }
                 }
+                copy_index(s + kLag);
                 asm volatile("cp.async.commit_group;\n" ::: "memory");
                 issued = s + 1;
-                if (s >= kLag) {
-                    asm volatile("cp.async.wait_group %0;\n" ::"n"(kLag) : "memory");
-                    announce(s - kLag);
-                }
             }
             if (!*abort_flag) {  // the last stages: all copies landed
                 asm volatile("cp.async.wait_all;\n" ::: "memory");

@@ -279,8 +279,9 @@ def sddmm(rowptr, colind, X, Y, aval=None, out=None, tensor_cores=False, variant
     """out[e] = aval[e] * <X[row(e)], Y[col(e)]> (aval None -> unscaled, the reference's
     sddmm_cuda_csr). X: M x K, Y: N x K, fp32 -- or both bf16 (fp32 products and sums, fp32
     out). tensor_cores=True selects the tcgen05 split-bf16 path (fp32 inputs; ``variant`` its
-    kernel), False the CUDA-core FP32 path, "auto" the learned choice between them
-    (``sddmm_path``) for fp32 inputs."""
+    kernel; columns must ascend within each row), False the CUDA-core FP32 path, "auto" the
+    learned choice between them (``sddmm_path``) for fp32 inputs -- which may be the
+    tensor-core path, so it too needs ascending columns."""
     if tensor_cores == "auto":
         if X.dtype == torch.float32 and Y.dtype == torch.float32:
             path = sddmm_path(rowptr, colind, Y.shape[0], X.shape[1])
