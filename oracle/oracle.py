@@ -43,9 +43,10 @@ def build(quiet: bool = True) -> str:
     return os.path.join(_HERE, "_build", "liboracle.so")
 
 
-def build_ref(ref_dir: str | None = None, gcn: bool = False) -> bool:
-    """Compile the reference's own kernels into ``oracle/_ref`` when its sources exist."""
-    args = ["make", "-C", _HERE, "ref"] + (["ref-gcn"] if gcn else [])
+def build_ref(ref_dir: str | None = None, gcn: bool = False, cuda: bool = False) -> bool:
+    """Compile the reference's own kernels into ``oracle/_ref`` when its sources exist (with
+    ``cuda``, also its CUDA kernels as sm_103a cubins for oracle/ref_gpu.py)."""
+    args = ["make", "-C", _HERE, "ref"] + (["ref-gcn"] if gcn else []) + (["ref-cuda"] if cuda else [])
     if ref_dir:
         args.append(f"REF={ref_dir}")
     out = subprocess.run(args, capture_output=True, text=True)
