@@ -56,8 +56,8 @@ __device__ __forceinline__ void load_c(const float *p, float *v) {
 constexpr int kThreads = 256;
 constexpr int kLongRow = 256;  // entries; longer rows are handed to spmm_long.cu
 
-template <typename T, int VB, int GROUP, int CPL, int U>
-__global__ void __launch_bounds__(kThreads)
+template <typename T, int VB, int GROUP, int CPL, int U, bool PF>
+__global__ void __launch_bounds__(kThreads, PF ? 4 : 1)
 spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
               const int *__restrict__ colind, const T *__restrict__ val,
               const T *__restrict__ B, long ldb, float *__restrict__ C, long ldc, float beta,
@@ -104,10 +104,11 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         }
     }
 
-    for (int base = lo; base < hi; base += GROUP) {
-        const int e = base + g;
-        int k = -1;
-        float v = 0.0f;
+    // (colind, val) of GROUP entries per batch, one per lane. PF: the next batch is loaded while
+    // the current one is consumed (registers capped so that four CTAs stay resident)
+    auto load_entry = [&](int e, int &k, float &v) {
+        k = -1;
+        v = 0.0f;
         if (e < hi) {
             k = ld_stream(colind + e);
             v = to_f32(ld_stream(val + e));
@@ -115,6 +116,20 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 flag(status, kFlagBadColind);
                 k = -1;
             }
+        }
+    };
+    int kn = -1;
+    float vn = 0.0f;
+    if (PF) load_entry(lo + g, kn, vn);
+    for (int base = lo; base < hi; base += GROUP) {
+        int k;
+        float v;
+        if (PF) {
+            k = kn;
+            v = vn;
+            load_entry(base + GROUP + g, kn, vn);
+        } else {
+            load_entry(base + g, k, v);
         }
         const int cnt = min(GROUP, hi - base);
         int t = 0;
@@ -212,9 +227,12 @@ struct Variant {
                // steps = entries per load batch), 3 = multi-entry nnz-split (spmm_nnz.cu, a warp
                // per chunk in 32 / group sub-groups; unroll = chunk size)
     int steps = 4;
+    int pf = 0;  // row-split: 1 = next index batch prefetched (64 registers at most)
 };
 
 #define AS_V(vb, g, c, u) {vb, g, c, u, "rowsplit_v" #vb "_g" #g "_c" #c "_u" #u, 0}
+#define AS_VPF(vb, g, c, u) {vb, g, c, u, "rowsplit_v" #vb "_g" #g "_c" #c "_u" #u "_pf", 0, 4, 1}
+#define AS_VPFS AS_VPF(8, 32, 4, 4), AS_VPF(16, 32, 2, 4), AS_VPF(16, 32, 4, 4)
 #define AS_BULK(lb, st) {lb, 32, 1, st, "bulk_lb" #lb "_s" #st, 1}
 #define AS_BULKS AS_BULK(16, 8), AS_BULK(32, 8), AS_BULK(16, 16), AS_BULK(32, 4)
 #define AS_NNZ(vb, g, c, ch) {vb, g, c, ch, "nnzsplit_v" #vb "_g" #g "_c" #c "_ch" #ch, 2}
@@ -238,11 +256,13 @@ struct Variant {
 constexpr int kSmallChunk = 32;
 constexpr int kSmallChunkMaxN = 64;
 const Variant kF32[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_BULKS, AS_NNZS(128),
-                        AS_NNZS(1024), AS_NNZS8(256), AS_NNZS8(1024), AS_NNZS32, AS_MES};
+                        AS_NNZS(1024), AS_NNZS8(256), AS_NNZS8(1024), AS_NNZS32, AS_MES,
+                        AS_VPFS};
 const Variant kBF16[] = {AS_VROW(16), AS_VROW(8), AS_VROW(4), AS_VROW(2), AS_BULKS,
                          AS_NNZS(128), AS_NNZS(1024), AS_NNZS_BF16_SCALAR(128),
                          AS_NNZS_BF16_SCALAR(1024), AS_NNZS8(256), AS_NNZS8(1024),
-                         AS_NNZ8(2, 32, 2, 256), AS_NNZ8(2, 32, 2, 1024), AS_NNZS32, AS_MES};
+                         AS_NNZ8(2, 32, 2, 256), AS_NNZ8(2, 32, 2, 1024), AS_NNZS32, AS_MES,
+                         AS_VPFS};
 constexpr int kNF32 = sizeof(kF32) / sizeof(kF32[0]);
 constexpr int kNBF16 = sizeof(kBF16) / sizeof(kBF16[0]);
 
@@ -252,13 +272,13 @@ struct LongRows {
     unsigned *count;  // list length (context device word)
 };
 
-template <typename T, int VB, int G, int CPL, int U>
+template <typename T, int VB, int G, int CPL, int U, bool PF = false>
 void launch_one(const SpmmArgs &a, const LongRows &lr, cudaStream_t s) {
     constexpr int E = Vec<T, VB>::E;
     constexpr int TILE = G * E * CPL;
     dim3 grid(static_cast<unsigned>(ceil_div(a.M, kThreads / G)),
               static_cast<unsigned>(ceil_div(a.N, TILE)));
-    spmm_rowsplit<T, VB, G, CPL, U><<<grid, kThreads, 0, s>>>(
+    spmm_rowsplit<T, VB, G, CPL, U, PF><<<grid, kThreads, 0, s>>>(
         a.M, a.K, a.N, a.nnz, a.rowptr, a.colind, static_cast<const T *>(a.val),
         static_cast<const T *>(a.B), a.ldb, a.C, a.ldc, a.beta, a.status, lr.thresh, lr.list,
         lr.count, a.C16, a.relu);
@@ -278,6 +298,15 @@ bool dispatch_cpl(int cpl, int u, const SpmmArgs &a, const LongRows &lr, cudaStr
             case 2: launch_one<T, VB, G, 2, 8>(a, lr, s); return true;
         }
     }
+    return false;
+}
+
+// the prefetching row-split kernels: full warps, four entries per step
+template <typename T>
+bool dispatch_pf(int vb, int cpl, const SpmmArgs &a, const LongRows &lr, cudaStream_t s) {
+    if (vb == 8 && cpl == 4) { launch_one<T, 8, 32, 4, 4, true>(a, lr, s); return true; }
+    if (vb == 16 && cpl == 2) { launch_one<T, 16, 32, 2, 4, true>(a, lr, s); return true; }
+    if (vb == 16 && cpl == 4) { launch_one<T, 16, 32, 4, 4, true>(a, lr, s); return true; }
     return false;
 }
 
@@ -323,7 +352,7 @@ static int find_variant(int dtype, int vb, int g, int cpl, int u) {
     const Variant *t = dtype == 0 ? kF32 : kBF16;
     const int n = spmm_variant_count(dtype);
     for (int i = 0; i < n; ++i)
-        if (t[i].kind == 0 && t[i].vb == vb && t[i].group == g && t[i].cpl == cpl &&
+        if (t[i].kind == 0 && !t[i].pf && t[i].vb == vb && t[i].group == g && t[i].cpl == cpl &&
             t[i].unroll == u)
             return i + 1;
     return 0;
@@ -426,7 +455,10 @@ as_status spmm_launch(as_ctx *ctx, int dtype, int variant, const SpmmArgs &a, cu
         lr.list = static_cast<int *>(p);
     }
     bool ok = false;
-    if (dtype == 0) {
+    if (v.pf) {
+        ok = dtype == 0 ? dispatch_pf<float>(v.vb, v.cpl, a, lr, s)
+                        : dispatch_pf<uint16_t>(v.vb, v.cpl, a, lr, s);
+    } else if (dtype == 0) {
         switch (v.vb) {
             case 16: ok = dispatch_group<float, 16>(v.group, v.cpl, v.unroll, a, lr, s); break;
             case 8: ok = dispatch_group<float, 8>(v.group, v.cpl, v.unroll, a, lr, s); break;
