@@ -11,7 +11,7 @@
 // chains. A CTA takes one (long row, 64-byte column slice) at a time and splits its warps by
 // role:
 //  - warp 0 is the consumer: one lane per column of the slice runs the chain out of shared
-//    memory, stage after stage. The entries' values it loads itself, three stages ahead, into
+//    memory, stage after stage. The entries' values it loads itself, kVAhead stages ahead, into
 //    registers (lane l holds entries l and 32 + l of a stage) and broadcasts them by shuffles;
 //  - warps 1-2 are producers, one thread per entry of a stage of kStage entries: the thread
 //    copies its entry's B segment into the stage's ring slot with cp.async, and the entry's
@@ -43,7 +43,8 @@ constexpr int kSliceBytes = 64;            // B bytes per entry per stage (16 fp
 constexpr int kStages = 24;                // B ring slots
 constexpr int kLag = 12;                   // stages of copies in flight per producer thread
 constexpr int kIdx = kLag + 1;             // index ring slots (a thread reads slot s, refills s + kLag)
-constexpr int kVAhead = 3;                 // stages of values the consumer loads ahead
+constexpr int kVAhead = 12;                // stages of values the consumer loads ahead (about
+                                           // 4,000 cycles: a DRAM round trip under load)
 static_assert(kLag < kStages, "a producer must announce stage s before it waits to refill its slot");
 constexpr unsigned kSpinLimit = 1u << 22;  // polls of a bounded wait (a few seconds at most)
 constexpr int kRingBytes = kStages * kStage * kSliceBytes;
