@@ -348,11 +348,11 @@ const char *spmm_variant_name(int dtype, int variant) {
     return dtype == 0 ? kF32[variant - 1].name : kBF16[variant - 1].name;
 }
 
-static int find_variant(int dtype, int vb, int g, int cpl, int u) {
+static int find_variant(int dtype, int vb, int g, int cpl, int u, int pf = 0) {
     const Variant *t = dtype == 0 ? kF32 : kBF16;
     const int n = spmm_variant_count(dtype);
     for (int i = 0; i < n; ++i)
-        if (t[i].kind == 0 && !t[i].pf && t[i].vb == vb && t[i].group == g && t[i].cpl == cpl &&
+        if (t[i].kind == 0 && t[i].pf == pf && t[i].vb == vb && t[i].group == g && t[i].cpl == cpl &&
             t[i].unroll == u)
             return i + 1;
     return 0;
@@ -360,7 +360,8 @@ static int find_variant(int dtype, int vb, int g, int cpl, int u) {
 
 // Library choice among the bit-identical row-split kernels, from the variant sweep on GB300:
 // wide rows of B (N >= 512) want full warps with two or four vectors per lane (fp32:
-// float2 x 4, bf16: 8 x bf16 x 2); narrow B wants full warps of scalar lanes with 8 entries
+// float4 x 2 with the next index batch prefetched, then float2 x 4; bf16: 8 x bf16 x 2);
+// narrow B wants full warps of scalar lanes with 8 entries
 // per step (the batch of 32 (colind, val) pairs amortises the index loads). The entry-balanced
 // kernels, which win on skewed rows, are not picked here: they change the summation order of
 // rows that cross a chunk, and the library cannot see the row lengths without reading rowptr
@@ -369,23 +370,23 @@ int spmm_default_variant(int dtype, int M, int K, int N, int nnz, long ldb, long
                          const void *B, const void *C) {
     (void)M; (void)K; (void)nnz;
     const int esz = dtype == 0 ? 4 : 2;
-    struct Pick { int vb, g, cpl, u; };
-    const Pick wide_f32[] = {{8, 32, 4, 4}, {16, 32, 2, 4}, {4, 32, 2, 8}};
-    const Pick wide_bf16[] = {{16, 32, 2, 4}, {8, 32, 2, 4}, {4, 32, 4, 4}, {2, 32, 2, 8}};
-    const Pick narrow_f32[] = {{4, 32, 2, 8}};
-    const Pick narrow_bf16[] = {{4, 32, 2, 8}, {2, 32, 2, 8}};
+    struct Pick { int vb, g, cpl, u, pf; };
+    const Pick wide_f32[] = {{16, 32, 2, 4, 1}, {8, 32, 4, 4, 0}, {16, 32, 2, 4, 0}, {4, 32, 2, 8, 0}};
+    const Pick wide_bf16[] = {{16, 32, 2, 4, 0}, {8, 32, 2, 4, 0}, {4, 32, 4, 4, 0}, {2, 32, 2, 8, 0}};
+    const Pick narrow_f32[] = {{4, 32, 2, 8, 0}};
+    const Pick narrow_bf16[] = {{4, 32, 2, 8, 0}, {2, 32, 2, 8, 0}};
     const Pick *list;
     int n;
     if (N >= 512) {
         list = dtype == 0 ? wide_f32 : wide_bf16;
-        n = dtype == 0 ? 3 : 4;
+        n = 4;
     } else {
         list = dtype == 0 ? narrow_f32 : narrow_bf16;
         n = dtype == 0 ? 1 : 2;
     }
     for (int i = 0; i < n; ++i)
         if (vb_ok(dtype, list[i].vb, N, ldb, ldc, B, C))
-            return find_variant(dtype, list[i].vb, list[i].g, list[i].cpl, list[i].u);
+            return find_variant(dtype, list[i].vb, list[i].g, list[i].cpl, list[i].u, list[i].pf);
     // any layout: scalar lanes
     return find_variant(dtype, esz, 32, N > 32 ? 2 : 1, 8);
 }

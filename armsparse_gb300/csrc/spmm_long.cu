@@ -11,15 +11,17 @@
 // chains. A CTA takes one (long row, 64-byte column slice) at a time and splits its warps by
 // role:
 //  - warp 0 is the consumer: one lane per column of the slice runs the chain out of shared
-//    memory, stage after stage. The entries' values it loads itself, kVAhead stages ahead, into
-//    registers (lane l holds entries l and 32 + l of a stage) and broadcasts them by shuffles;
+//    memory, stage after stage, reading each entry's B segment and value from the stage's slot;
 //  - warps 1-2 are producers, one thread per entry of a stage of kStage entries: the thread
 //    copies its entry's B segment into the stage's ring slot with cp.async, and the entry's
 //    column index for the stage kLag ahead into its own slot of a small index ring (cp.async
 //    too), one commit group per stage. Before stage s it waits for its group of stage s - kLag
 //    (cp.async.wait_group): that gives it stage s's index and tells it that its copies of stage
-//    s - kLag have landed, which it then announces on that slot's `full` mbarrier. A slot is
-//    refilled only after the consumer arrives on its `empty` mbarrier.
+//    s - kLag have landed, which it then announces on that slot's `full` mbarrier. The entry's
+//    value it loads kLag stages ahead into a ring of kLag registers (the stage loop is unrolled
+//    kLag times, so each register is named statically and none is read before its load is kLag
+//    stages old) and stores it beside the B segment. A slot is refilled only after the consumer
+//    arrives on its `empty` mbarrier.
 // Every arrival is the arriving thread's own (none is left pending when the CTA moves on).
 // Every wait is bounded; a wait that gives up sets the timeout flag and an abort flag that makes
 // the other role leave too; each thread waits for its own copies before the CTA moves on, and a
@@ -43,13 +45,12 @@ constexpr int kSliceBytes = 64;            // B bytes per entry per stage (16 fp
 constexpr int kStages = 24;                // B ring slots
 constexpr int kLag = 12;                   // stages of copies in flight per producer thread
 constexpr int kIdx = kLag + 1;             // index ring slots (a thread reads slot s, refills s + kLag)
-constexpr int kVAhead = 12;                // stages of values the consumer loads ahead (about
-                                           // 4,000 cycles: a DRAM round trip under load)
 static_assert(kLag < kStages, "a producer must announce stage s before it waits to refill its slot");
 constexpr unsigned kSpinLimit = 1u << 22;  // polls of a bounded wait (a few seconds at most)
 constexpr int kRingBytes = kStages * kStage * kSliceBytes;
 constexpr int kIdxBytes = kIdx * kStage * 4;
-constexpr int kSmemBytes = kRingBytes + kIdxBytes + 2 * kStages * 8 + 16;
+constexpr int kVringBytes = kStages * kStage * 4;  // each entry's value, beside its B segment
+constexpr int kSmemBytes = kRingBytes + kIdxBytes + kVringBytes + 2 * kStages * 8 + 16;
 
 __device__ __forceinline__ float to_f32(float v) { return v; }
 __device__ __forceinline__ float to_f32(uint16_t v) { return bf16_to_f32(v); }
@@ -101,7 +102,8 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned char *ring = smem;                                    // [kStages][kStage][64 B]
     int *kring = reinterpret_cast<int *>(smem + kRingBytes);       // [kIdx][kStage]
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + kRingBytes + kIdxBytes);
+    float *vring = reinterpret_cast<float *>(smem + kRingBytes + kIdxBytes);  // [kStages][kStage]
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + kRingBytes + kIdxBytes + kVringBytes);
     uint64_t *empty = full + kStages;
     volatile int *abort_flag = reinterpret_cast<volatile int *>(empty + kStages);
 
@@ -144,18 +146,7 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
             // ---- consumer: the chains ----
             const int col = lane < W ? lane : lane & (W - 1);  // lanes past the slice mirror
             if (lane < w && beta != 0.0f) acc = crow[lane] * beta;
-            float vq[kVAhead + 1][2];  // values of stages s .. s + kVAhead
-            auto loadv = [&](int st, float *d) {
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int e = st * kStage + h * 32 + lane;
-                    d[h] = (st < n_stages && e < L) ? to_f32(ld_stream(val + lo + e)) : 0.0f;
-                }
-            };
-#pragma unroll
-            for (int a = 0; a < kVAhead; ++a) loadv(a, vq[a]);
             for (int s = 0; s < n_stages; ++s) {
-                loadv(s + kVAhead, vq[kVAhead]);
                 const int slot = s % kStages;
                 const bool ok = __all_sync(
                     0xffffffffu, bar_wait(smem_u32(full + slot), (s / kStages) & 1, spin_limit,
@@ -168,53 +159,46 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                     break;
                 }
                 const int n = min(kStage, L - s * kStage);
+                const float *vs = vring + slot * kStage;
                 const T *bs = reinterpret_cast<const T *>(ring + slot * kStage * kSliceBytes) + col;
                 int j = 0;
-                // eight entries per step: the next eight's loads and broadcasts are issued
-                // during this eight's chain
-                if (n >= 8) {
-                    float b[8], v[8], bn[8], vn[8];
+                if (n >= 8) {  // the next 8 entries' loads are in flight during this 8's chain
+                    float b[8], bn[8];
+                    float4 v0 = *reinterpret_cast<const float4 *>(vs);
+                    float4 v1 = *reinterpret_cast<const float4 *>(vs + 4);
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        b[i] = to_f32(bs[i * W]);
-                        v[i] = __shfl_sync(0xffffffffu, vq[0][0], i);
-                    }
+                    for (int i = 0; i < 8; ++i) b[i] = to_f32(bs[i * W]);
                     for (; j + 8 <= n; j += 8) {
                         const bool more = j + 16 <= n;
+                        float4 n0 = v0, n1 = v1;
                         if (more) {
+                            n0 = *reinterpret_cast<const float4 *>(vs + j + 8);
+                            n1 = *reinterpret_cast<const float4 *>(vs + j + 12);
 #pragma unroll
-                            for (int i = 0; i < 8; ++i) {
-                                const int jj = j + 8 + i;
-                                bn[i] = to_f32(bs[jj * W]);
-                                vn[i] = __shfl_sync(0xffffffffu, jj < 32 ? vq[0][0] : vq[0][1],
-                                                    jj & 31);
-                            }
+                            for (int i = 0; i < 8; ++i) bn[i] = to_f32(bs[(j + 8 + i) * W]);
                         }
-#pragma unroll
-                        for (int i = 0; i < 8; ++i) acc = fmaf(b[i], v[i], acc);
+                        acc = fmaf(b[0], v0.x, acc);
+                        acc = fmaf(b[1], v0.y, acc);
+                        acc = fmaf(b[2], v0.z, acc);
+                        acc = fmaf(b[3], v0.w, acc);
+                        acc = fmaf(b[4], v1.x, acc);
+                        acc = fmaf(b[5], v1.y, acc);
+                        acc = fmaf(b[6], v1.z, acc);
+                        acc = fmaf(b[7], v1.w, acc);
                         if (more) {
+                            v0 = n0;
+                            v1 = n1;
 #pragma unroll
-                            for (int i = 0; i < 8; ++i) {
-                                b[i] = bn[i];
-                                v[i] = vn[i];
-                            }
+                            for (int i = 0; i < 8; ++i) b[i] = bn[i];
                         }
                     }
                 }
-                for (; j < n; ++j) {
-                    const float vv = __shfl_sync(0xffffffffu, j < 32 ? vq[0][0] : vq[0][1], j & 31);
-                    acc = fmaf(to_f32(bs[j * W]), vv, acc);
-                }
+                for (; j < n; ++j) acc = fmaf(to_f32(bs[j * W]), vs[j], acc);
                 __syncwarp();
                 if (lane == 0)
                     asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(
                                      smem_u32(empty + slot))
                                  : "memory");
-#pragma unroll
-                for (int a = 0; a < kVAhead; ++a) {
-                    vq[a][0] = vq[a + 1][0];
-                    vq[a][1] = vq[a + 1][1];
-                }
             }
         } else {
             // ---- producers: thread p owns entry p of every stage ----
@@ -236,8 +220,16 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 copy_index(t);
                 asm volatile("cp.async.commit_group;\n" ::: "memory");
             }
-            int issued = 0;
-            for (int s = 0; s < n_stages; ++s) {
+            // value of stage st's entry p (0 past the row)
+            auto load_value = [&](int st) {
+                const int e = st * kStage + p;
+                return (st < n_stages && e < L) ? to_f32(ld_stream(val + lo + e)) : 0.0f;
+            };
+            float vr[kLag];  // vr[s % kLag]: the value of stage s, loaded at stage s - kLag
+#pragma unroll
+            for (int t = 0; t < kLag; ++t) vr[t] = load_value(t);
+            // one stage; false when the wait for its slot gave up
+            auto stage = [&](int s, float &vreg) {
                 // this thread's group kLag back has landed: stage s's index, and its copies of
                 // stage s - kLag (announced now)
                 asm volatile("cp.async.wait_group %0;\n" ::"n"(kLag - 1) : "memory");
@@ -250,7 +242,7 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                         flag(status, kFlagTimeout);
                         *abort_flag = 1;
                     }
-                    break;
+                    return false;
                 }
                 const int e = s * kStage + p;
                 if (e < L) {
@@ -260,7 +252,8 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                         const unsigned char *src = reinterpret_cast<const unsigned char *>(
                             B + static_cast<long>(k) * ldb + slice0);
                         for (int q = 0; q < pieces; ++q) cp_async<GB>(smem_u32(d + q * GB), src + q * GB);
-                    } else {  // malformed: a zero segment, nothing read
+                        vring[slot * kStage + p] = vreg;
+                    } else {  // malformed: a zero segment and value, nothing read
                         flag(status, kFlagBadColind);
                         for (int q = 0; q < pieces; ++q) {
                             if constexpr (GB == 16)
@@ -268,11 +261,22 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                             else
                                 *reinterpret_cast<unsigned *>(d + q * GB) = 0u;
                         }
+                        vring[slot * kStage + p] = 0.0f;
                     }
                 }
+                vreg = load_value(s + kLag);  // read again kLag stages from now
                 copy_index(s + kLag);
                 asm volatile("cp.async.commit_group;\n" ::: "memory");
-                issued = s + 1;
+                return true;
+            };
+            int issued = 0;
+            bool go = true;
+            for (int s0 = 0; go && s0 < n_stages; s0 += kLag) {
+#pragma unroll
+                for (int u = 0; u < kLag; ++u) {
+                    if (s0 + u >= n_stages || !(go = stage(s0 + u, vr[u]))) break;
+                    issued = s0 + u + 1;
+                }
             }
             if (!*abort_flag) {  // the last stages: all copies landed
                 asm volatile("cp.async.wait_all;\n" ::: "memory");

@@ -83,8 +83,11 @@ def test_variant_table(native_lib):
     names = [native_lib.as_spmm_variant_name(0, i).decode() for i in range(1, n32 + 1)]
     assert len(set(names)) == n32
     assert native_lib.as_spmm_variant_name(0, 0) == b"unknown"
-    # the default pick for the 4096-wide fp32 case uses 128-bit loads and full warps
+    # the default pick for the 4096-wide fp32 case: full warps, 128-bit loads, the next index
+    # batch prefetched; with B only 8-byte aligned, 64-bit loads
     v = native_lib.as_spmm_default_variant(0, 4096, 4096, 4096, 167772, 4096, 4096, 256, 256)
+    assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v16_g32_c2_u4_pf"
+    v = native_lib.as_spmm_default_variant(0, 4096, 4096, 4096, 167772, 4096, 4096, 264, 256)
     assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v8_g32_c4_u4"
     v = native_lib.as_spmm_default_variant(0, 100, 100, 3, 500, 3, 3, 256, 256)
     assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v4_g32_c2_u8"
