@@ -17,12 +17,14 @@
 //    column index for the stage kLag ahead into its own slot of a small index ring (cp.async
 //    too), one commit group per stage. Before stage s it waits for its group of stage s - kLag
 //    (cp.async.wait_group): that gives it stage s's index and tells it that its copies of stage
-//    s - kLag have landed, which it then announces on that slot's `full` mbarrier. The entry's
+//    s - kLag have landed, which its warp then announces on that slot's `full` mbarrier (one
+//    arrival per warp after __syncwarp; one lane per warp polls `empty`). The entry's
 //    value it loads kLag stages ahead into a ring of kLag registers (the stage loop is unrolled
 //    kLag times, so each register is named statically and none is read before its load is kLag
 //    stages old) and stores it beside the B segment. A slot is refilled only after the consumer
 //    arrives on its `empty` mbarrier.
-// Every arrival is the arriving thread's own (none is left pending when the CTA moves on).
+// Every arrival is a synchronous one by the arriving thread (none is left pending when the CTA
+// moves on).
 // Every wait is bounded; a wait that gives up sets the timeout flag and an abort flag that makes
 // the other role leave too; each thread waits for its own copies before the CTA moves on, and a
 // row whose wait gave up is left unwritten. A malformed column index is flagged and its entry
@@ -132,7 +134,7 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         if (tid == 0) {
             for (int s = 0; s < kStages; ++s) {
                 asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(full + s)),
-                             "r"(kProducers));
+                             "r"(kProducers / 32));
                 asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)));
             }
             *abort_flag = 0;
@@ -203,10 +205,14 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         } else {
             // ---- producers: thread p owns entry p of every stage ----
             const int p = tid - 32;
-            auto announce = [&](int st) {  // this thread's copies of stage st have landed
-                asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(
-                                 smem_u32(full + st % kStages))
-                             : "memory");
+            // the warp's copies and stores of stage st are done: __syncwarp orders every lane's
+            // (each waited for its own copies) before lane 0's release arrival, one per warp
+            auto announce = [&](int st) {
+                __syncwarp();
+                if (lane == 0)
+                    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(
+                                     smem_u32(full + st % kStages))
+                                 : "memory");
             };
             auto copy_index = [&](int st) {  // column index of stage st's entry p, into the ring
                 const int e = st * kStage + p;
@@ -235,14 +241,20 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 asm volatile("cp.async.wait_group %0;\n" ::"n"(kLag - 1) : "memory");
                 if (s >= kLag) announce(s - kLag);
                 const int slot = s % kStages;
-                if (s >= kStages &&
-                    !bar_wait(smem_u32(empty + slot), ((s / kStages) - 1) & 1, kSpinLimit,
-                              abort_flag)) {
-                    if (!*abort_flag) {
-                        flag(status, kFlagTimeout);
-                        *abort_flag = 1;
+                if (s >= kStages) {
+                    // lane 0 waits for the consumer to free the slot; the shuffle orders the
+                    // other lanes' writes after its acquire
+                    int ok = 1;
+                    if (lane == 0)
+                        ok = bar_wait(smem_u32(empty + slot), ((s / kStages) - 1) & 1, kSpinLimit,
+                                      abort_flag);
+                    if (!__shfl_sync(0xffffffffu, ok, 0)) {
+                        if (lane == 0 && !*abort_flag) {
+                            flag(status, kFlagTimeout);
+                            *abort_flag = 1;
+                        }
+                        return false;
                     }
-                    return false;
                 }
                 const int e = s * kStage + p;
                 if (e < L) {
@@ -278,7 +290,8 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                     issued = s0 + u + 1;
                 }
             }
-            if (!*abort_flag) {  // the last stages: all copies landed
+            // the last stages: all copies landed (the decision is the warp's, as announce syncs it)
+            if (__shfl_sync(0xffffffffu, static_cast<int>(!*abort_flag), 0)) {
                 asm volatile("cp.async.wait_all;\n" ::: "memory");
                 for (int st = issued > kLag ? issued - kLag : 0; st < issued; ++st) announce(st);
             }
