@@ -13,7 +13,8 @@
 struct as_ctx {
     int device = 0;
     unsigned *d_status = nullptr;  // device words: [0] status (bit flags from common.cuh),
-                                   // [1..2] long-row list length and CTA-done count
+                                   // [1..3] long-row list: rows listed from the front, CTA-done
+                                   // count, huge rows listed from the end
     unsigned *d_long = nullptr;    // = d_status + 1
     int sms = 1;                   // multiprocessors of the device
     void *scratch = nullptr;       // scratch arena

@@ -4,34 +4,37 @@
 // (a hub of a power-law graph) keeps a single group busy long after the rest of the grid has
 // finished. The row-split kernels therefore leave every row longer than a threshold to this
 // kernel: they append the row number to a list (one atomic per long row) and skip it; this
-// kernel, launched right after on the same stream, takes the listed rows.
+// kernel, launched right after on the same stream, takes the listed rows. Rows longer than
+// kHugeRow entries are listed from the other end of the list and taken first, so the longest
+// chains start at once instead of behind shorter rows.
 //
 // Each output element is still one fused-FMA chain over the row's entries in CSR order (the
 // order cannot be split without changing the bits), so the speed comes from feeding the
-// chains. A CTA takes one (long row, 64-byte column slice) at a time and splits its warps by
-// role:
-//  - warp 0 is the consumer: one lane per column of the slice runs the chain out of shared
-//    memory, stage after stage, reading each entry's B segment and value from the stage's slot;
-//  - warps 1-2 are producers, one thread per entry of a stage of kStage entries: the thread
-//    copies its entry's B segment into the stage's ring slot with cp.async, and the entry's
-//    column index for the stage kLag ahead into its own slot of a small index ring (cp.async
-//    too), one commit group per stage. Before stage s it waits for its group of stage s - kLag
-//    (cp.async.wait_group): that gives it stage s's index and tells it that its copies of stage
-//    s - kLag have landed, which its warp then announces on that slot's `full` mbarrier (one
-//    arrival per warp after __syncwarp; one lane per warp polls `empty`). The entry's
-//    value it loads kLag stages ahead into a ring of kLag registers (the stage loop is unrolled
-//    kLag times, so each register is named statically and none is read before its load is kLag
-//    stages old) and stores it beside the B segment. A slot is refilled only after the consumer
-//    arrives on its `empty` mbarrier.
-// Every arrival is a synchronous one by the arriving thread (none is left pending when the CTA
-// moves on).
-// Every wait is bounded; a wait that gives up sets the timeout flag and an abort flag that makes
-// the other role leave too; each thread waits for its own copies before the CTA moves on, and a
-// row whose wait gave up is left unwritten. A malformed column index is flagged and its entry
-// gets a zero segment (nothing is read for it).
+// chains. A CTA takes one (long row, 64-column slice) at a time; its warps split by role:
+//  - warp 0 is the consumer: lane l runs the chains of columns 2l and 2l+1 of the slice out of
+//    shared memory, stage after stage (kStage entries per stage), reading each entry's two B
+//    values with one 64-bit (fp32) or 32-bit (bf16) load and the entry's value from the
+//    stage's value slot. At the start of a stage it probes the next stage's `full` mbarrier
+//    without blocking, so a stage that is already complete costs no blocking wait;
+//  - eight producer warps take the stages in turn (warp p owns stages p, p + 8, ...). For its
+//    stage a warp waits for the slot's `empty` mbarrier, stores the entries' values (loaded
+//    into registers one turn earlier) into the value slot, and copies each entry's B segment
+//    into the ring slot with cp.async, eight lanes per entry; the entries' column indices,
+//    also loaded one turn earlier, reach those lanes by shuffle. Every lane then makes a
+//    cp.async.mbarrier.arrive.noinc on the slot's `full` mbarrier (it lands when the lane's
+//    copies have), and lane 0 a release arrival after __syncwarp for the value stores.
+// The consumer warp sits alone on its SM sub-partition (warps 4 and 8 are idle): the chains
+// issue one FMA every few cycles and lose a large share of that rate when two busy producer
+// warps share its scheduler.
 //
-// The list counter and a CTA-done counter live in the context's device words; the last CTA
-// to finish resets both, so the next call starts from zero without a memset.
+// Every wait is bounded; a wait that gives up sets the timeout flag and an abort flag that makes
+// the other role leave too. Before the CTA moves on, each producer warp waits (bounded) for the
+// `full` phases of its last stages, so no copy or arrival is in flight when the barriers are
+// invalidated; a row whose wait gave up is left unwritten. A malformed column index is flagged
+// and its entry gets a zero segment (nothing is read for it).
+//
+// The list counters and a CTA-done counter live in the context's device words; the last CTA
+// to finish resets them, so the next call starts from zero without a memset.
 #include <algorithm>
 
 #include "common.cuh"
@@ -40,33 +43,35 @@
 namespace as {
 namespace {
 
-constexpr int kStage = 64;                 // entries per pipeline stage
-constexpr int kProducers = kStage;         // warps 1-2: one thread per entry of a stage
-constexpr int kThreads = 32 + kProducers;
-constexpr int kSliceBytes = 64;            // B bytes per entry per stage (16 fp32 / 32 bf16 columns)
-constexpr int kStages = 24;                // B ring slots
-constexpr int kLag = 12;                   // stages of copies in flight per producer thread
-constexpr int kIdx = kLag + 1;             // index ring slots (a thread reads slot s, refills s + kLag)
-static_assert(kLag < kStages, "a producer must announce stage s before it waits to refill its slot");
-constexpr unsigned kSpinLimit = 1u << 22;  // polls of a bounded wait (a few seconds at most)
-constexpr int kRingBytes = kStages * kStage * kSliceBytes;
-constexpr int kIdxBytes = kIdx * kStage * 4;
-constexpr int kVringBytes = kStages * kStage * 4;  // each entry's value, beside its B segment
-constexpr int kSmemBytes = kRingBytes + kIdxBytes + kVringBytes + 2 * kStages * 8 + 16;
+constexpr int kCols = 64;                   // columns per slice (two per consumer lane)
+constexpr int kStage = 64;                  // entries per pipeline stage
+constexpr int kStages = 8;                  // ring slots
+constexpr int kProducers = 8;               // producer warps, one stage each in turn
+constexpr int kWarps = 12;                  // warp 0 consumer; 4, 8 and 11 idle
+constexpr int kThreads = 32 * kWarps;
+constexpr int kFullCount = 33;              // 32 cp.async arrivals + lane 0's release
+constexpr unsigned kSpinLimit = 1u << 22;   // polls of a bounded wait (a few seconds at most)
+static_assert(kStages % kProducers == 0, "a slot is always refilled by the same producer warp");
+static_assert(kStage == 64, "each producer lane holds two entries' index and value");
+
+template <typename T>
+struct Layout {
+    static constexpr int kSlice = kCols * static_cast<int>(sizeof(T));  // B bytes per entry
+    static constexpr int kRing = kStages * kStage * kSlice;
+    static constexpr int kVals = kStages * kStage * 4;                  // values as fp32
+    static constexpr int kBytes = kRing + kVals + 2 * kStages * 8 + 16;
+};
+
+// producer index (0-7) of a warp, or -1 for the consumer and the idle warps
+__device__ __forceinline__ int producer_of(int warp) {
+    return (warp & 3) != 0 && warp <= 10 ? warp - 1 - (warp >> 2) : -1;
+}
 
 __device__ __forceinline__ float to_f32(float v) { return v; }
 __device__ __forceinline__ float to_f32(uint16_t v) { return bf16_to_f32(v); }
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-template <int GB>
-__device__ __forceinline__ void cp_async(uint32_t dst, const void *gmem) {
-    if constexpr (GB == 16)
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(gmem) : "memory");
-    else
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(gmem) : "memory");
 }
 
 __device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
@@ -81,31 +86,79 @@ __device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
+// non-blocking probe of a phase
+__device__ __forceinline__ bool bar_test(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
 // Bounded wait for `parity` of the mbarrier at `bar`; false when `limit` polls pass or the
-// other role has given up.
+// other role has given up. `nap` > 0 sleeps that many ns between polls (producers, which
+// are ahead and must not take issue slots from the consumer).
 __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, unsigned limit,
-                                         const volatile int *abort_flag) {
+                                         const volatile int *abort_flag, unsigned nap = 0) {
     for (unsigned i = 0; i < limit; ++i) {
         if (bar_try(bar, parity)) return true;
         if (*abort_flag) return false;
+        if (nap) __nanosleep(nap);
     }
     return false;
 }
 
+// Two consecutive B columns of one entry from shared memory, as fp32.
+__device__ __forceinline__ float2 lds_pair(uint32_t a, float) {
+    float2 r;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(r.x), "=f"(r.y) : "r"(a));
+    return r;
+}
+__device__ __forceinline__ float2 lds_pair(uint32_t a, uint16_t) {
+    uint32_t u;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(u) : "r"(a));
+    return make_float2(__uint_as_float(u << 16), __uint_as_float(u & 0xffff0000u));
+}
+__device__ __forceinline__ float4 lds_vals(uint32_t a) {
+    float4 r;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+                 : "r"(a));
+    return r;
+}
+
+template <int GB>
+__device__ __forceinline__ void cp_async_zfill(uint32_t dst, const void *gmem, int src_bytes) {
+    if constexpr (GB == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(gmem),
+                     "r"(src_bytes)
+                     : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(dst), "l"(gmem),
+                     "r"(src_bytes)
+                     : "memory");
+}
+
 // T: storage type of val and B (float or uint16_t = bf16); GB: cp.async size in bytes.
 template <typename T, int GB>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 1)
 spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
           const int *__restrict__ colind, const T *__restrict__ val, const T *__restrict__ B,
           long ldb, float *__restrict__ C, long ldc, float beta, unsigned *status,
           const int *__restrict__ list, unsigned *counters, uint16_t *__restrict__ C16,
           bool relu, unsigned spin_limit) {
-    constexpr int W = kSliceBytes / static_cast<int>(sizeof(T));  // columns per slice
-    extern __shared__ __align__(128) unsigned char smem[];
-    unsigned char *ring = smem;                                    // [kStages][kStage][64 B]
-    int *kring = reinterpret_cast<int *>(smem + kRingBytes);       // [kIdx][kStage]
-    float *vring = reinterpret_cast<float *>(smem + kRingBytes + kIdxBytes);  // [kStages][kStage]
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + kRingBytes + kIdxBytes + kVringBytes);
+    using Lay = Layout<T>;
+    constexpr int kSlice = Lay::kSlice;
+    constexpr int kEsz = static_cast<int>(sizeof(T));
+    constexpr unsigned kAll = 0xffffffffu;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *ring = smem;                                  // [kStages][kStage][kSlice]
+    float *vals = reinterpret_cast<float *>(smem + Lay::kRing);  // [kStages][kStage]
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + Lay::kRing + Lay::kVals);
     uint64_t *empty = full + kStages;
     volatile int *abort_flag = reinterpret_cast<volatile int *>(empty + kStages);
 
@@ -113,18 +166,25 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
     // (and its list writes to be visible) before reading the list
     asm volatile("griddepcontrol.wait;\n" ::: "memory");
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int n_long = static_cast<int>(
-        min(*reinterpret_cast<volatile unsigned *>(counters), static_cast<unsigned>(M)));
-    const int n_slices = static_cast<int>(ceil_div(N, W));
-    const long units = static_cast<long>(n_long) * n_slices;
+    const unsigned cap = static_cast<unsigned>(M);
+    const int n_long = static_cast<int>(min(*reinterpret_cast<volatile unsigned *>(counters), cap));
+    const int n_huge =
+        static_cast<int>(min(*reinterpret_cast<volatile unsigned *>(counters + 2), cap));
+    const int n_slices = static_cast<int>(ceil_div(N, kCols));
+    const long units_huge = static_cast<long>(n_huge) * n_slices;
+    const long units = units_huge + static_cast<long>(n_long) * n_slices;
+    const int pw = producer_of(warp);
 
-    // work units (long row, column slice), the slices of one row on consecutive CTAs
+    // work units (row, column slice): the huge rows (listed from the end) first, the slices of
+    // one row on consecutive CTAs
     for (long u = blockIdx.x; u < units; u += gridDim.x) {
-        const int item = static_cast<int>(u / n_slices);
-        const int slice0 = static_cast<int>(u - static_cast<long>(item) * n_slices) * W;
-        const int w = min(W, N - slice0);                  // columns of this slice
-        const int pieces = w * static_cast<int>(sizeof(T)) / GB;  // copy pieces per entry
-        const int r = list[item];
+        const bool huge = u < units_huge;
+        const long v = huge ? u : u - units_huge;
+        const int item = static_cast<int>(v / n_slices);
+        const int slice0 = static_cast<int>(v - static_cast<long>(item) * n_slices) * kCols;
+        const int w = min(kCols, N - slice0);        // columns of this slice
+        const int pieces = w * kEsz / GB;            // copy pieces per entry
+        const int r = huge ? list[M - 1 - item] : list[item];
         if (r < 0 || r >= M) continue;
         int lo, hi;
         row_range(rowptr, r, nnz, status, lo, hi);
@@ -134,7 +194,7 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         if (tid == 0) {
             for (int s = 0; s < kStages; ++s) {
                 asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(full + s)),
-                             "r"(kProducers / 32));
+                             "r"(kFullCount));
                 asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)));
             }
             *abort_flag = 0;
@@ -142,167 +202,166 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         }
         __syncthreads();
 
-        float acc = 0.0f;
+        float acc0 = 0.0f, acc1 = 0.0f;
+        const int c0 = 2 * lane;  // this lane's first column within the slice
         float *crow = C + static_cast<long>(r) * ldc + slice0;
         if (warp == 0) {
-            // ---- consumer: the chains ----
-            const int col = lane < W ? lane : lane & (W - 1);  // lanes past the slice mirror
-            if (lane < w && beta != 0.0f) acc = crow[lane] * beta;
+            // ---- consumer: the chains of columns c0 and c0 + 1 ----
+            if (beta != 0.0f) {
+                if (c0 < w) acc0 = crow[c0] * beta;
+                if (c0 + 1 < w) acc1 = crow[c0 + 1] * beta;
+            }
+            bool ready = false;  // the stage's `full` phase was seen complete by the last probe
             for (int s = 0; s < n_stages; ++s) {
                 const int slot = s % kStages;
-                const bool ok = __all_sync(
-                    0xffffffffu, bar_wait(smem_u32(full + slot), (s / kStages) & 1, spin_limit,
-                                          abort_flag));
-                if (!ok) {
-                    if (lane == 0) {
-                        flag(status, kFlagTimeout);
-                        *abort_flag = 1;
+                if (!ready) {
+                    const bool ok = __all_sync(kAll, bar_wait(smem_u32(full + slot), (s / kStages) & 1,
+                                                              spin_limit, abort_flag));
+                    if (!ok) {
+                        if (lane == 0) {
+                            flag(status, kFlagTimeout);
+                            *abort_flag = 1;
+                        }
+                        break;
                     }
-                    break;
                 }
+                // the next stage's probe; its answer is needed only after this stage's chain
+                const bool next = s + 1 < n_stages &&
+                                  bar_test(smem_u32(full + (s + 1) % kStages), ((s + 1) / kStages) & 1);
                 const int n = min(kStage, L - s * kStage);
-                const float *vs = vring + slot * kStage;
-                const T *bs = reinterpret_cast<const T *>(ring + slot * kStage * kSliceBytes) + col;
-                int j = 0;
-                if (n >= 8) {  // the next 8 entries' loads are in flight during this 8's chain
-                    float b[8], bn[8];
-                    float4 v0 = *reinterpret_cast<const float4 *>(vs);
-                    float4 v1 = *reinterpret_cast<const float4 *>(vs + 4);
+                const uint32_t bs = smem_u32(ring + slot * kStage * kSlice) + c0 * kEsz;
+                const uint32_t vs = smem_u32(vals + slot * kStage);
+                if (n == kStage) {
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) b[i] = to_f32(bs[i * W]);
-                    for (; j + 8 <= n; j += 8) {
-                        const bool more = j + 16 <= n;
-                        float4 n0 = v0, n1 = v1;
-                        if (more) {
-                            n0 = *reinterpret_cast<const float4 *>(vs + j + 8);
-                            n1 = *reinterpret_cast<const float4 *>(vs + j + 12);
+                    for (int q = 0; q < kStage; q += 16) {
+                        float2 b[16];
+                        float4 v[4];
 #pragma unroll
-                            for (int i = 0; i < 8; ++i) bn[i] = to_f32(bs[(j + 8 + i) * W]);
-                        }
-                        acc = fmaf(b[0], v0.x, acc);
-                        acc = fmaf(b[1], v0.y, acc);
-                        acc = fmaf(b[2], v0.z, acc);
-                        acc = fmaf(b[3], v0.w, acc);
-                        acc = fmaf(b[4], v1.x, acc);
-                        acc = fmaf(b[5], v1.y, acc);
-                        acc = fmaf(b[6], v1.z, acc);
-                        acc = fmaf(b[7], v1.w, acc);
-                        if (more) {
-                            v0 = n0;
-                            v1 = n1;
+                        for (int i = 0; i < 16; ++i) b[i] = lds_pair(bs + (q + i) * kSlice, T());
 #pragma unroll
-                            for (int i = 0; i < 8; ++i) b[i] = bn[i];
+                        for (int i = 0; i < 4; ++i) v[i] = lds_vals(vs + (q + 4 * i) * 4);
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            acc0 = fmaf(b[4 * i].x, v[i].x, acc0);
+                            acc1 = fmaf(b[4 * i].y, v[i].x, acc1);
+                            acc0 = fmaf(b[4 * i + 1].x, v[i].y, acc0);
+                            acc1 = fmaf(b[4 * i + 1].y, v[i].y, acc1);
+                            acc0 = fmaf(b[4 * i + 2].x, v[i].z, acc0);
+                            acc1 = fmaf(b[4 * i + 2].y, v[i].z, acc1);
+                            acc0 = fmaf(b[4 * i + 3].x, v[i].w, acc0);
+                            acc1 = fmaf(b[4 * i + 3].y, v[i].w, acc1);
                         }
                     }
+                } else {
+                    for (int j = 0; j < n; ++j) {
+                        const float2 b = lds_pair(bs + j * kSlice, T());
+                        const float x = vals[slot * kStage + j];
+                        acc0 = fmaf(b.x, x, acc0);
+                        acc1 = fmaf(b.y, x, acc1);
+                    }
                 }
-                for (; j < n; ++j) acc = fmaf(to_f32(bs[j * W]), vs[j], acc);
+                ready = __all_sync(kAll, next);
                 __syncwarp();
                 if (lane == 0)
                     asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(
                                      smem_u32(empty + slot))
                                  : "memory");
             }
-        } else {
-            // ---- producers: thread p owns entry p of every stage ----
-            const int p = tid - 32;
-            // the warp's copies and stores of stage st are done: __syncwarp orders every lane's
-            // (each waited for its own copies) before lane 0's release arrival, one per warp
-            auto announce = [&](int st) {
-                __syncwarp();
-                if (lane == 0)
-                    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(
-                                     smem_u32(full + st % kStages))
-                                 : "memory");
+        } else if (pw >= 0) {
+            // ---- producer pw: stages pw, pw + kProducers, ... (all in slot pw % kStages) ----
+            const int sub = lane >> 3, pl = lane & 7;  // entry of a group of four, lane in it
+            // column index and value of this lane's entries (lane, lane + 32) of stage st
+            auto load = [&](int st, int &k0, int &k1, float &x0, float &x1) {
+                k0 = k1 = 0;
+                x0 = x1 = 0.0f;
+                const int e0 = st * kStage + lane, e1 = e0 + 32;
+                if (st < n_stages && e0 < L) {
+                    k0 = ld_stream(colind + lo + e0);
+                    x0 = to_f32(ld_stream(val + lo + e0));
+                }
+                if (st < n_stages && e1 < L) {
+                    k1 = ld_stream(colind + lo + e1);
+                    x1 = to_f32(ld_stream(val + lo + e1));
+                }
             };
-            auto copy_index = [&](int st) {  // column index of stage st's entry p, into the ring
-                const int e = st * kStage + p;
-                if (st < n_stages && e < L)
-                    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(
-                                     smem_u32(kring + (st % kIdx) * kStage + p)),
-                                 "l"(colind + lo + e)
-                                 : "memory");
-            };
-            for (int t = 0; t < kLag; ++t) {  // the first kLag stages' indices, a group each
-                copy_index(t);
-                asm volatile("cp.async.commit_group;\n" ::: "memory");
-            }
-            // value of stage st's entry p (0 past the row)
-            auto load_value = [&](int st) {
-                const int e = st * kStage + p;
-                return (st < n_stages && e < L) ? to_f32(ld_stream(val + lo + e)) : 0.0f;
-            };
-            float vr[kLag];  // vr[s % kLag]: the value of stage s, loaded at stage s - kLag
-#pragma unroll
-            for (int t = 0; t < kLag; ++t) vr[t] = load_value(t);
-            // one stage; false when the wait for its slot gave up
-            auto stage = [&](int s, float &vreg) {
-                // this thread's group kLag back has landed: stage s's index, and its copies of
-                // stage s - kLag (announced now)
-                asm volatile("cp.async.wait_group %0;\n" ::"n"(kLag - 1) : "memory");
-                if (s >= kLag) announce(s - kLag);
+            int k0, k1;
+            float x0, x1;
+            load(pw, k0, k1, x0, x1);
+            int last = -1;  // the last stage this warp issued
+            for (int s = pw; s < n_stages; s += kProducers) {
                 const int slot = s % kStages;
-                if (s >= kStages) {
-                    // lane 0 waits for the consumer to free the slot; the shuffle orders the
-                    // other lanes' writes after its acquire
+                if (s >= kStages) {  // the consumer is done with stage s - kStages
                     int ok = 1;
                     if (lane == 0)
                         ok = bar_wait(smem_u32(empty + slot), ((s / kStages) - 1) & 1, kSpinLimit,
-                                      abort_flag);
-                    if (!__shfl_sync(0xffffffffu, ok, 0)) {
-                        if (lane == 0 && !*abort_flag) {
-                            flag(status, kFlagTimeout);
-                            *abort_flag = 1;
-                        }
-                        return false;
-                    }
+                                      abort_flag, 64);
+                    if (!__shfl_sync(kAll, ok, 0)) break;
                 }
-                const int e = s * kStage + p;
-                if (e < L) {
-                    const int k = kring[(s % kIdx) * kStage + p];
-                    unsigned char *d = ring + (slot * kStage + p) * kSliceBytes;
-                    if (static_cast<unsigned>(k) < static_cast<unsigned>(K)) {
+                int nk0, nk1;
+                float nx0, nx1;
+                load(s + kProducers, nk0, nk1, nx0, nx1);  // the next turn's, in flight meanwhile
+                vals[slot * kStage + lane] = x0;
+                vals[slot * kStage + lane + 32] = x1;
+                const uint32_t dst0 = smem_u32(ring + slot * kStage * kSlice);
+#pragma unroll 4
+                for (int g = 0; g < kStage / 4; ++g) {
+                    const int j = 4 * g + sub;
+                    int k = __shfl_sync(kAll, g < 8 ? k0 : k1, j & 31);
+                    if (s * kStage + j < L) {
+                        const bool bad = static_cast<unsigned>(k) >= static_cast<unsigned>(K);
+                        if (bad) {
+                            flag(status, kFlagBadColind);
+                            k = 0;
+                        }
                         const unsigned char *src = reinterpret_cast<const unsigned char *>(
                             B + static_cast<long>(k) * ldb + slice0);
-                        for (int q = 0; q < pieces; ++q) cp_async<GB>(smem_u32(d + q * GB), src + q * GB);
-                        vring[slot * kStage + p] = vreg;
-                    } else {  // malformed: a zero segment and value, nothing read
-                        flag(status, kFlagBadColind);
-                        for (int q = 0; q < pieces; ++q) {
-                            if constexpr (GB == 16)
-                                *reinterpret_cast<uint4 *>(d + q * GB) = make_uint4(0, 0, 0, 0);
-                            else
-                                *reinterpret_cast<unsigned *>(d + q * GB) = 0u;
+                        const uint32_t dst = dst0 + j * kSlice;
+#pragma unroll
+                        for (int q = 0; q < kSlice / GB / 8; ++q) {
+                            const int piece = pl + 8 * q;
+                            if (piece < pieces)
+                                cp_async_zfill<GB>(dst + piece * GB, src + piece * GB, bad ? 0 : GB);
                         }
-                        vring[slot * kStage + p] = 0.0f;
                     }
                 }
-                vreg = load_value(s + kLag);  // read again kLag stages from now
-                copy_index(s + kLag);
-                asm volatile("cp.async.commit_group;\n" ::: "memory");
-                return true;
-            };
-            int issued = 0;
-            bool go = true;
-            for (int s0 = 0; go && s0 < n_stages; s0 += kLag) {
-#pragma unroll
-                for (int u = 0; u < kLag; ++u) {
-                    if (s0 + u >= n_stages || !(go = stage(s0 + u, vr[u]))) break;
-                    issued = s0 + u + 1;
-                }
+                // the slot is full when every lane's copies have landed and the values are out
+                asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(
+                                 smem_u32(full + slot))
+                             : "memory");
+                __syncwarp();
+                if (lane == 0)
+                    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(
+                                     smem_u32(full + slot))
+                                 : "memory");
+                k0 = nk0;
+                k1 = nk1;
+                x0 = nx0;
+                x1 = nx1;
+                last = s;
             }
-            // the last stages: all copies landed (the decision is the warp's, as announce syncs it)
-            if (__shfl_sync(0xffffffffu, static_cast<int>(!*abort_flag), 0)) {
-                asm volatile("cp.async.wait_all;\n" ::: "memory");
-                for (int st = issued > kLag ? issued - kLag : 0; st < issued; ++st) announce(st);
+            asm volatile("cp.async.wait_all;\n" ::: "memory");
+            // the arrivals this warp's copies owe have landed before the barriers are reused:
+            // wait for the phase of its last stage (the slot's latest; earlier ones completed
+            // before the slot was refilled)
+            if (lane == 0 && last >= 0) {
+                unsigned i = 0;
+                while (i < kSpinLimit &&
+                       !bar_try(smem_u32(full + last % kStages), (last / kStages) & 1))
+                    ++i;
+                if (i == kSpinLimit) flag(status, kFlagTimeout);
             }
+            __syncwarp();
         }
-        asm volatile("cp.async.wait_all;\n" ::: "memory");  // this thread's copies have landed
         __syncthreads();
-        if (warp == 0 && lane < w && !*abort_flag) {
-            if (C16)
-                C16[static_cast<long>(r) * ldc + slice0 + lane] = f32_to_bf16(relu_if(acc, relu));
-            else
-                crow[lane] = acc;
+        if (warp == 0 && !*abort_flag) {
+            if (C16) {
+                uint16_t *orow = C16 + static_cast<long>(r) * ldc + slice0;
+                if (c0 < w) orow[c0] = f32_to_bf16(relu_if(acc0, relu));
+                if (c0 + 1 < w) orow[c0 + 1] = f32_to_bf16(relu_if(acc1, relu));
+            } else {
+                if (c0 < w) crow[c0] = acc0;
+                if (c0 + 1 < w) crow[c0 + 1] = acc1;
+            }
         }
         if (tid == 0) {
             for (int s = 0; s < kStages; ++s) {
@@ -313,7 +372,7 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         __syncthreads();  // shared memory and barriers are reused by the next unit
     }
 
-    // the last CTA out resets the list counter and the done counter for the next call
+    // the last CTA out resets the list counters and the done counter for the next call
     __syncthreads();
     if (tid == 0) {
         __threadfence();
@@ -321,6 +380,7 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         if (atomicAdd(counters + 1, 1u) == total - 1) {
             counters[0] = 0;
             counters[1] = 0;
+            counters[2] = 0;
             __threadfence();
         }
     }
@@ -329,18 +389,22 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
 template <typename T, int GB>
 as_status launch(as_ctx *ctx, const SpmmArgs &a, const int *list, cudaStream_t s) {
     auto k = spmm_long<T, GB>;
-    static bool attr_set[64] = {};
+    constexpr int kBytes = Layout<T>::kBytes;
+    static int per_sm[64] = {};  // resident CTAs per multiprocessor, per device
     const int dev = ctx->device;
     if (dev < 0 || dev >= 64) return fail(AS_ERR_INVALID_VALUE, "spmm long rows: device index");
-    if (!attr_set[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             kSmemBytes);
+    if (!per_sm[dev]) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kBytes);
         if (e != cudaSuccess) return check_cuda(e, "spmm long rows: shared memory attribute");
-        attr_set[dev] = true;
+        int n = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kThreads, kBytes);
+        if (e != cudaSuccess) return check_cuda(e, "spmm long rows: occupancy");
+        per_sm[dev] = std::max(1, n);
     }
-    // two CTAs per multiprocessor (one wave), striding over the (row, slice) units
-    const long max_units = static_cast<long>(a.M) * ceil_div(a.N, kSliceBytes / static_cast<int>(sizeof(T)));
-    dim3 grid(static_cast<unsigned>(std::max(1L, std::min(max_units, 2L * ctx->sms))));
+    // one wave of CTAs striding over the (row, slice) units
+    const long max_units = static_cast<long>(a.M) * ceil_div(a.N, kCols);
+    dim3 grid(static_cast<unsigned>(
+        std::max(1L, std::min(max_units, static_cast<long>(per_sm[dev]) * ctx->sms))));
     // programmatic dependent launch (outside stream capture): the CTAs are scheduled while
     // the row-split kernel drains, hiding this launch when there are no long rows
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -348,7 +412,7 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, const int *list, cudaStream_t s
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = dim3(kThreads);
-    cfg.dynamicSmemBytes = kSmemBytes;
+    cfg.dynamicSmemBytes = kBytes;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -368,7 +432,6 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, const int *list, cudaStream_t s
 int spmm_long_granule(int dtype, int N, long ldb, const void *B) {
     const int esz = dtype == 0 ? 4 : 2;
     const uintptr_t pb = reinterpret_cast<uintptr_t>(B);
-    if (ceil_div(N, kSliceBytes / esz) > 65535) return 0;
     if ((static_cast<long>(N) * esz) % 16 == 0 && (ldb * esz) % 16 == 0 && pb % 16 == 0) return 16;
     if ((static_cast<long>(N) * esz) % 4 == 0 && (ldb * esz) % 4 == 0 && pb % 4 == 0) return 4;
     return 0;

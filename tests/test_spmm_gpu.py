@@ -319,6 +319,32 @@ def test_long_rows_row_split_bit_exact(oracle, N_):
     A.sync_status()
 
 
+def test_huge_rows_first_bit_exact(oracle):
+    """Rows past 16,384 entries are listed from the end of the long-row list and taken first,
+    among many rows just past the long-row threshold: bit-identical for fp32 and bf16 storage,
+    two 64-column slices per row, and the list counters start from zero on the next call."""
+    rng = np.random.default_rng(11)
+    n_rows, n_cols = 400, 60000
+    lens = rng.integers(200, 320, n_rows)
+    lens[[3, 50, 51, 399]] = [60000, 16385, 20000, 33333]
+    rp_h = np.zeros(n_rows + 1, np.int32)
+    np.cumsum(lens, out=rp_h[1:])
+    ci_h = np.concatenate([np.sort(rng.choice(n_cols, l, replace=False)) for l in lens]).astype(np.int32)
+    a = S.CSR(rp_h, ci_h, rng.uniform(-1, 1, ci_h.size).astype(np.float32), n_rows, n_cols)
+    B = S.dense_uniform((n_cols, 128), 12)
+    ref = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, B)
+    rp, ci, v = csr_dev(a)
+    Bd = to_dev(B)
+    for _ in range(2):
+        C = A.spmm(rp, ci, v, Bd)
+        assert np.array_equal(bits(C), bits(ref))
+    vb, Bb = oracle.bf16_round(a.val), oracle.bf16_round(B)
+    refb = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, vb, Bb)
+    C = A.spmm(rp, ci, v.to(torch.bfloat16), Bd.to(torch.bfloat16))
+    assert np.array_equal(bits(C), bits(refb))
+    A.sync_status()
+
+
 def test_long_rows_strided_and_bf16(oracle):
     a = _skewed(99)
     rp, ci, v = csr_dev(a)
