@@ -110,7 +110,7 @@ def build_drivers(verbose: bool = False) -> str:
     src = os.path.join(CSRC, "drivers.cu")
     out = os.path.join(PKG, DRIVERS_NAME)
     cmd = ([nvcc()] + NVCC_FLAGS + ["-shared", src, "-L" + PKG, "-larmsparse_gpu",
-                                    "-lcudart_static", "-Xlinker", "-rpath,$ORIGIN",
+                                    "-lcudart_static", "-lpthread", "-Xlinker", "-rpath,$ORIGIN",
                                     "-o", out + ".tmp"])
     stamp = _stamp(src, cmd)
     sf = os.path.join(BUILD, "drivers.stamp")

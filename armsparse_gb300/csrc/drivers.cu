@@ -6,23 +6,29 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "armsparse_drivers.h"
 
 namespace {
 
-constexpr int kRowBlocks = 8;  // at most this many SpMM row blocks, whose copies back overlap
-                               // the next blocks' kernels
-constexpr size_t kMinBlockBytes = size_t(16) << 20;  // each block's copy back: >= 16 MB
+constexpr int kColBlocks = 8;  // at most this many SpMM column blocks (B in, kernel, C out)
+constexpr size_t kMinBlockBytes = size_t(16) << 20;  // each block's columns of B: >= 16 MB
+                                                     // (4 blocks at 4096 x 4096: 0.74 ms a
+                                                     // call, against 0.78 with 2 or 8)
+constexpr int kColAlign = 32;  // block widths in columns (128-byte aligned fp32 starts)
 
 struct State {
     std::mutex mu;
     as_ctx *ctx = nullptr;
     cudaStream_t stream = nullptr;
-    cudaStream_t copy_stream = nullptr;  // device -> host copies of finished row blocks
-    cudaEvent_t done[kRowBlocks] = {};   // row block b's kernels have finished
+    cudaStream_t in_stream = nullptr;    // host -> device copies of column blocks
+    cudaStream_t copy_stream = nullptr;  // device -> host copies of finished column blocks
+    cudaEvent_t in_done[kColBlocks] = {};  // column block j's inputs are on the device
+    cudaEvent_t done[kColBlocks] = {};     // column block j's kernels have finished
     void *buf = nullptr;
     size_t cap = 0;
     as_status last = AS_OK;
@@ -47,10 +53,12 @@ as_status prepare(State &s, size_t bytes, char **base) {
         as_status st = as_ctx_create(&s.ctx, dev);
         if (st != AS_OK) return st;
         if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&s.in_stream, cudaStreamNonBlocking) != cudaSuccess ||
             cudaStreamCreateWithFlags(&s.copy_stream, cudaStreamNonBlocking) != cudaSuccess)
             return AS_ERR_CUDA;
-        for (cudaEvent_t &e : s.done)
-            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+        for (int j = 0; j < kColBlocks; ++j)
+            if (cudaEventCreateWithFlags(&s.in_done[j], cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&s.done[j], cudaEventDisableTiming) != cudaSuccess)
                 return AS_ERR_CUDA;
     }
     if (bytes > s.cap) {
@@ -109,46 +117,85 @@ as_status spmm_host(const int *rowPtr, const int *colInd, const float *val, cons
     float *dv = a.take<float>(nnz);
     float *dB = a.take<float>(size_t(K) * N);
     float *dC = a.take<float>(size_t(M) * N);
-    if ((st = h2d(s, drp, rowPtr, sizeof(int) * (M + 1))) != AS_OK) return st;
-    if ((st = h2d(s, dci, colInd, sizeof(int) * nnz)) != AS_OK) return st;
-    if ((st = h2d(s, dv, val, sizeof(float) * nnz)) != AS_OK) return st;
-    if ((st = h2d(s, dB, B, sizeof(float) * size_t(K) * N)) != AS_OK) return st;
-    if (beta != 0.0f && (st = h2d(s, dC, C, sizeof(float) * size_t(M) * N)) != AS_OK) return st;
-    // Row blocks: block b's result goes back to the host on the copy stream while the kernels
-    // of blocks b+1.. run, so only the first block's compute adds to the copies. Each block is
-    // the same library call on a slice of rows (rowptr offset, C offset), so every output is
-    // the same fused chain as in one call.
-    const size_t c_bytes = sizeof(float) * size_t(M) * N;
-    const int blocks = int(std::max<size_t>(1, std::min<size_t>(kRowBlocks, c_bytes / kMinBlockBytes)));
-    const int rows_per = (M + blocks - 1) / blocks;
-    int issued = 0;
-    for (int b = 0; b < blocks; ++b) {
-        const int r0 = b * rows_per, r1 = std::min(M, r0 + rows_per);
-        if (r0 >= r1) break;
-        st = as_spmm_csr_f32(s.ctx, r1 - r0, K, N, nnz, drp + r0, dci, dv, dB, N,
-                             dC + size_t(r0) * N, N, beta, 0, s.stream);
-        if (st != AS_OK) break;
-        if (cudaEventRecord(s.done[b], s.stream) != cudaSuccess) {
-            st = AS_ERR_CUDA;
-            break;
+    // Column blocks. Block j's columns of B (and of C, when accumulating) go in, its kernel
+    // runs, and its columns of C come back; copies of pageable memory hold the calling thread
+    // until they finish, so the copies back run on a helper thread while this one copies the
+    // next blocks in: the link then carries both directions at once. Each block is the same
+    // library call on a column slice (B and C offsets, ldb = ldc = N), so every output is the
+    // same fused chain as in one call.
+    const size_t b_bytes = sizeof(float) * size_t(K) * N;
+    int blocks = int(std::max<size_t>(1, std::min<size_t>(kColBlocks, b_bytes / kMinBlockBytes)));
+    const int width = std::max(kColAlign, (N + blocks - 1) / blocks + kColAlign - 1) / kColAlign * kColAlign;
+    blocks = N > 0 ? (N + width - 1) / width : 1;
+    auto copy2d = [&](float *dst, const float *src, int c0, int w, int rows, cudaMemcpyKind kind,
+                      cudaStream_t str) {
+        return cudaMemcpy2DAsync(dst + c0, sizeof(float) * size_t(N), src + c0,
+                                 sizeof(float) * size_t(N), sizeof(float) * size_t(w), rows, kind,
+                                 str) == cudaSuccess;
+    };
+    auto in = [&](void *d, const void *h, size_t bytes) {
+        return bytes == 0 || cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s.in_stream) ==
+                                 cudaSuccess;
+    };
+    if (!in(drp, rowPtr, sizeof(int) * (M + 1)) || !in(dci, colInd, sizeof(int) * nnz) ||
+        !in(dv, val, sizeof(float) * nnz)) {
+        cudaStreamSynchronize(s.in_stream);
+        return AS_ERR_CUDA;
+    }
+    // the helper: copies block j back once its kernel was enqueued (`enqueued` > j); stops
+    // after `enqueued` blocks once `last` is set
+    std::atomic<int> enqueued{0};
+    std::atomic<bool> last{false};
+    std::atomic<bool> out_ok{true};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    auto copy_back = [&]() {
+        cudaSetDevice(dev);
+        for (int j = 0;; ++j) {
+            while (enqueued.load() <= j && !last.load()) std::this_thread::yield();
+            if (enqueued.load() <= j) break;
+            const int c0 = j * width, w = std::min(width, N - c0);
+            if (cudaStreamWaitEvent(s.copy_stream, s.done[j], 0) != cudaSuccess ||
+                (M > 0 && w > 0 && !copy2d(C, dC, c0, w, M, cudaMemcpyDeviceToHost, s.copy_stream)))
+                out_ok = false;
         }
-        issued = b + 1;
+        if (cudaStreamSynchronize(s.copy_stream) != cudaSuccess) out_ok = false;
+    };
+    std::thread helper;
+    if (blocks > 1) {
+        try {
+            helper = std::thread(copy_back);
+        } catch (...) {  // no thread: the copies back run after the loop, on this thread
+        }
     }
-    for (int b = 0; b < issued && st == AS_OK; ++b) {
-        const int r0 = b * rows_per, r1 = std::min(M, r0 + rows_per);
-        if (cudaStreamWaitEvent(s.copy_stream, s.done[b], 0) != cudaSuccess ||
-            cudaMemcpyAsync(C + size_t(r0) * N, dC + size_t(r0) * N,
-                            sizeof(float) * size_t(r1 - r0) * N, cudaMemcpyDeviceToHost,
-                            s.copy_stream) != cudaSuccess)
+    for (int j = 0; j < blocks && st == AS_OK; ++j) {
+        const int c0 = j * width, w = std::min(width, N - c0);
+        if (K > 0 && w > 0 && !copy2d(dB, B, c0, w, K, cudaMemcpyHostToDevice, s.in_stream)) st = AS_ERR_CUDA;
+        if (st == AS_OK && beta != 0.0f && M > 0 && w > 0 &&
+            !copy2d(dC, C, c0, w, M, cudaMemcpyHostToDevice, s.in_stream))
             st = AS_ERR_CUDA;
+        if (st == AS_OK && (cudaEventRecord(s.in_done[j], s.in_stream) != cudaSuccess ||
+                            cudaStreamWaitEvent(s.stream, s.in_done[j], 0) != cudaSuccess))
+            st = AS_ERR_CUDA;
+        if (st == AS_OK)
+            st = as_spmm_csr_f32(s.ctx, M, K, w, nnz, drp, dci, dv, dB + c0, N, dC + c0, N, beta,
+                                 0, s.stream);
+        if (st == AS_OK && cudaEventRecord(s.done[j], s.stream) != cudaSuccess) st = AS_ERR_CUDA;
+        if (st == AS_OK) enqueued = j + 1;
     }
-    // both streams drain before the call returns, whatever happened
-    const bool synced = cudaStreamSynchronize(s.copy_stream) == cudaSuccess;
+    last = true;
+    if (helper.joinable()) {
+        helper.join();
+    } else {
+        copy_back();  // one block: the copy back on this thread
+    }
+    // all three streams drain before the call returns, whatever happened
+    const bool in_synced = cudaStreamSynchronize(s.in_stream) == cudaSuccess;
     if (st != AS_OK) {
         cudaStreamSynchronize(s.stream);
         return st;
     }
-    if (!synced) return AS_ERR_CUDA;
+    if (!in_synced || !out_ok.load()) return AS_ERR_CUDA;
     return finish(s, nullptr, nullptr, 0);
 }
 

@@ -46,6 +46,27 @@ def test_spmm_shims(drv, golden):
         assert np.array_equal(Cg.view(np.uint32), g[f"c{i}_C"].view(np.uint32))
 
 
+def test_spmm_shims_column_blocks(drv, oracle):
+    """B of 49 MB: the shim runs the SpMM in column blocks (B in, kernel, C out, the copies
+    back on a second host thread), here 1024 + 1024 + 952 columns; origin (C = A*B) and
+    rowBaseSpmm3 (C += A*B) stay bit-identical to the reference's chain, call after call."""
+    from armsparse_gb300 import synthetic as S
+    M, K, N = 1500, 4096, 3000
+    a = S.uniform_csr(M, K, 30000, seed=91)
+    B = S.dense_uniform((K, N), 92)
+    ref = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, B)
+    ref2 = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, B, C=ref)
+    rp, ci, v = (np.ascontiguousarray(x) for x in (a.rowptr, a.colind, a.val))
+    for _ in range(2):
+        C = np.full((M, N), 5.0, np.float32)
+        drv.as_drv_origin(_p(rp), _p(ci), _p(v), _p(B), _p(C), M, K, N, 16)
+        assert drv.as_drv_last_status() == 0
+        assert np.array_equal(C.view(np.uint32), ref.view(np.uint32))
+        drv.as_drv_rowBaseSpmm3(_p(rp), _p(ci), _p(v), _p(B), _p(C), M, K, N, 16)
+        assert drv.as_drv_last_status() == 0
+        assert np.array_equal(C.view(np.uint32), ref2.view(np.uint32))
+
+
 def test_spmv_shim(drv, golden):
     g = golden["spmv_vcsr4"]
     for i in range(int(g["n_cases"])):
