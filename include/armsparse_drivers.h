@@ -7,11 +7,13 @@
  * reference) is accepted and ignored. Semantics follow the replaced function: the SpMM and
  * SpMV shims ACCUMULATE into C / y exactly like the reference (the caller zeroes them), and
  * their results are bit-identical to the reference kernels (fused-FMA chains in CSR order).
- * The reference functions have no error path; a failure here prints one line to stderr,
- * leaves the output untouched, and is readable through as_drv_last_status().
+ * The reference functions have no error path; a failure here prints one line to stderr and
+ * is readable through as_drv_last_status(); the output is left untouched, except that an
+ * SpMM shim may already have written the column blocks finished before the failure.
  *
  * Calls are serialised by a process-wide lock; device buffers are cached between calls and
- * grown on demand.
+ * grown on demand. The SpMM shims run in column blocks and copy each block's C back from a
+ * helper thread (started and joined within the call) while the next blocks' B goes in.
  */
 #ifndef ARMSPARSE_DRIVERS_H
 #define ARMSPARSE_DRIVERS_H
