@@ -14,24 +14,24 @@
 //  - warp 0 is the consumer: lane l runs the chains of columns 2l and 2l+1 of the slice out of
 //    shared memory, stage after stage (kStage entries per stage), reading each entry's two B
 //    values with one 64-bit (fp32) or 32-bit (bf16) load and the entry's value from the
-//    stage's value slot. At the start of a stage it probes the next stage's `full` mbarrier
-//    without blocking, so a stage that is already complete costs no blocking wait;
-//  - eight producer warps take the stages in turn (warp p owns stages p, p + 8, ...). For its
-//    stage a warp waits for the slot's `empty` mbarrier, stores the entries' values (loaded
-//    into registers one turn earlier) into the value slot, and copies each entry's B segment
-//    into the ring slot with cp.async, eight lanes per entry; the entries' column indices,
-//    also loaded one turn earlier, reach those lanes by shuffle. Every lane then makes a
-//    cp.async.mbarrier.arrive.noinc on the slot's `full` mbarrier (it lands when the lane's
-//    copies have), and lane 0 a release arrival after __syncwarp for the value stores.
+//    stage's value slot. It waits for a stage on the slot's `full` flag (an acquire load of a
+//    shared word) and frees the slot by a release store to its `empty` flag;
+//  - eight producer warps take the stages in turn (warp p owns stages p, p + 8, ..., all in
+//    slot p). For its stage a warp waits for the slot's `empty` flag, stores the entries'
+//    values (loaded into registers one turn earlier) into the value slot, and copies each
+//    entry's B segment into the ring slot with cp.async, eight lanes per entry; the entries'
+//    column indices, also loaded one turn earlier, reach those lanes by shuffle. It then waits
+//    for its own copies (cp.async.wait_group 0; its next stage is a whole turn away) and
+//    lane 0 publishes the stage with a release store to the slot's `full` flag after
+//    __syncwarp.
 // The consumer warp sits alone on its SM sub-partition (warps 4 and 8 are idle): the chains
 // issue one FMA every few cycles and lose a large share of that rate when two busy producer
 // warps share its scheduler.
 //
 // Every wait is bounded; a wait that gives up sets the timeout flag and an abort flag that makes
-// the other role leave too. Before the CTA moves on, each producer warp waits (bounded) for the
-// `full` phases of its last stages, so no copy or arrival is in flight when the barriers are
-// invalidated; a row whose wait gave up is left unwritten. A malformed column index is flagged
-// and its entry gets a zero segment (nothing is read for it).
+// the other role leave too. No copy is ever in flight when a warp leaves (a stage is published
+// only after its copies landed); a row whose wait gave up is left unwritten. A malformed column
+// index is flagged and its entry gets a zero segment (nothing is read for it).
 //
 // The list counters and a CTA-done counter live in the context's device words; the last CTA
 // to finish resets them, so the next call starts from zero without a memset.
@@ -49,7 +49,6 @@ constexpr int kStages = 8;                  // ring slots
 constexpr int kProducers = 8;               // producer warps, one stage each in turn
 constexpr int kWarps = 12;                  // warp 0 consumer; 4, 8 and 11 idle
 constexpr int kThreads = 32 * kWarps;
-constexpr int kFullCount = 33;              // 32 cp.async arrivals + lane 0's release
 constexpr unsigned kSpinLimit = 1u << 22;   // polls of a bounded wait (a few seconds at most)
 static_assert(kStages % kProducers == 0, "a slot is always refilled by the same producer warp");
 static_assert(kStage == 64, "each producer lane holds two entries' index and value");
@@ -59,7 +58,7 @@ struct Layout {
     static constexpr int kSlice = kCols * static_cast<int>(sizeof(T));  // B bytes per entry
     static constexpr int kRing = kStages * kStage * kSlice;
     static constexpr int kVals = kStages * kStage * 4;                  // values as fp32
-    static constexpr int kBytes = kRing + kVals + 2 * kStages * 8 + 16;
+    static constexpr int kBytes = kRing + kVals + 2 * kStages * 4 + 16;
 };
 
 // producer index (0-7) of a warp, or -1 for the consumer and the idle warps
@@ -74,38 +73,21 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
+__device__ __forceinline__ int ld_acquire(uint32_t a) {
+    int v;
+    asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+    return v;
 }
-
-// non-blocking probe of a phase
-__device__ __forceinline__ bool bar_test(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
+__device__ __forceinline__ void st_release(uint32_t a, int v) {
+    asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
-
-// Bounded wait for `parity` of the mbarrier at `bar`; false when `limit` polls pass or the
-// other role has given up. `nap` > 0 sleeps that many ns between polls (producers, which
-// are ahead and must not take issue slots from the consumer).
-__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, unsigned limit,
+// Bounded wait until the flag at `a` reaches `target`; false when `limit` polls pass or the
+// other role has given up. `nap` > 0 sleeps that many ns between polls (producers, which are
+// ahead and must not take issue slots from the consumer).
+__device__ __forceinline__ bool wait_seq(uint32_t a, int target, unsigned limit,
                                          const volatile int *abort_flag, unsigned nap = 0) {
     for (unsigned i = 0; i < limit; ++i) {
-        if (bar_try(bar, parity)) return true;
+        if (ld_acquire(a) >= target) return true;
         if (*abort_flag) return false;
         if (nap) __nanosleep(nap);
     }
@@ -158,9 +140,9 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *ring = smem;                                  // [kStages][kStage][kSlice]
     float *vals = reinterpret_cast<float *>(smem + Lay::kRing);  // [kStages][kStage]
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + Lay::kRing + Lay::kVals);
-    uint64_t *empty = full + kStages;
-    volatile int *abort_flag = reinterpret_cast<volatile int *>(empty + kStages);
+    int *full_seq = reinterpret_cast<int *>(smem + Lay::kRing + Lay::kVals);  // stage filled + 1
+    int *empty_seq = full_seq + kStages;                                       // stage consumed + 1
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(empty_seq + kStages);
 
     // launched as a programmatic dependent of the row-split kernel: wait for it to finish
     // (and its list writes to be visible) before reading the list
@@ -193,12 +175,10 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
 
         if (tid == 0) {
             for (int s = 0; s < kStages; ++s) {
-                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(full + s)),
-                             "r"(kFullCount));
-                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)));
+                full_seq[s] = 0;
+                empty_seq[s] = 0;
             }
             *abort_flag = 0;
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
         __syncthreads();
 
@@ -211,23 +191,17 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 if (c0 < w) acc0 = crow[c0] * beta;
                 if (c0 + 1 < w) acc1 = crow[c0 + 1] * beta;
             }
-            bool ready = false;  // the stage's `full` phase was seen complete by the last probe
             for (int s = 0; s < n_stages; ++s) {
                 const int slot = s % kStages;
-                if (!ready) {
-                    const bool ok = __all_sync(kAll, bar_wait(smem_u32(full + slot), (s / kStages) & 1,
-                                                              spin_limit, abort_flag));
-                    if (!ok) {
-                        if (lane == 0) {
-                            flag(status, kFlagTimeout);
-                            *abort_flag = 1;
-                        }
-                        break;
+                const bool ok = __all_sync(kAll, wait_seq(smem_u32(full_seq + slot), s + 1,
+                                                          spin_limit, abort_flag));
+                if (!ok) {
+                    if (lane == 0) {
+                        flag(status, kFlagTimeout);
+                        *abort_flag = 1;
                     }
+                    break;
                 }
-                // the next stage's probe; its answer is needed only after this stage's chain
-                const bool next = s + 1 < n_stages &&
-                                  bar_test(smem_u32(full + (s + 1) % kStages), ((s + 1) / kStages) & 1);
                 const int n = min(kStage, L - s * kStage);
                 const uint32_t bs = smem_u32(ring + slot * kStage * kSlice) + c0 * kEsz;
                 const uint32_t vs = smem_u32(vals + slot * kStage);
@@ -260,12 +234,8 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                         acc1 = fmaf(b.y, x, acc1);
                     }
                 }
-                ready = __all_sync(kAll, next);
                 __syncwarp();
-                if (lane == 0)
-                    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(
-                                     smem_u32(empty + slot))
-                                 : "memory");
+                if (lane == 0) st_release(smem_u32(empty_seq + slot), s + 1);
             }
         } else if (pw >= 0) {
             // ---- producer pw: stages pw, pw + kProducers, ... (all in slot pw % kStages) ----
@@ -287,13 +257,12 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
             int k0, k1;
             float x0, x1;
             load(pw, k0, k1, x0, x1);
-            int last = -1;  // the last stage this warp issued
             for (int s = pw; s < n_stages; s += kProducers) {
                 const int slot = s % kStages;
                 if (s >= kStages) {  // the consumer is done with stage s - kStages
                     int ok = 1;
                     if (lane == 0)
-                        ok = bar_wait(smem_u32(empty + slot), ((s / kStages) - 1) & 1, kSpinLimit,
+                        ok = wait_seq(smem_u32(empty_seq + slot), s - kStages + 1, kSpinLimit,
                                       abort_flag, 64);
                     if (!__shfl_sync(kAll, ok, 0)) break;
                 }
@@ -324,32 +293,17 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                         }
                     }
                 }
-                // the slot is full when every lane's copies have landed and the values are out
-                asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(
-                                 smem_u32(full + slot))
-                             : "memory");
+                // the slot is full once every lane's copies have landed
+                asm volatile("cp.async.commit_group;\n" ::: "memory");
+                asm volatile("cp.async.wait_group 0;\n" ::: "memory");
                 __syncwarp();
-                if (lane == 0)
-                    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(
-                                     smem_u32(full + slot))
-                                 : "memory");
+                if (lane == 0) st_release(smem_u32(full_seq + slot), s + 1);
                 k0 = nk0;
                 k1 = nk1;
                 x0 = nx0;
                 x1 = nx1;
-                last = s;
             }
             asm volatile("cp.async.wait_all;\n" ::: "memory");
-            // the arrivals this warp's copies owe have landed before the barriers are reused:
-            // wait for the phase of its last stage (the slot's latest; earlier ones completed
-            // before the slot was refilled)
-            if (lane == 0 && last >= 0) {
-                unsigned i = 0;
-                while (i < kSpinLimit &&
-                       !bar_try(smem_u32(full + last % kStages), (last / kStages) & 1))
-                    ++i;
-                if (i == kSpinLimit) flag(status, kFlagTimeout);
-            }
             __syncwarp();
         }
         __syncthreads();
@@ -363,13 +317,7 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 if (c0 + 1 < w) crow[c0 + 1] = acc1;
             }
         }
-        if (tid == 0) {
-            for (int s = 0; s < kStages; ++s) {
-                asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(full + s)));
-                asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(empty + s)));
-            }
-        }
-        __syncthreads();  // shared memory and barriers are reused by the next unit
+        __syncthreads();  // shared memory and flags are reused by the next unit
     }
 
     // the last CTA out resets the list counters and the done counter for the next call
