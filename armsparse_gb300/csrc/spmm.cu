@@ -362,35 +362,50 @@ static int find_variant(int dtype, int vb, int g, int cpl, int u, int pf = 0) {
     return 0;
 }
 
-// Library choice among the bit-identical row-split kernels, from the variant sweep on GB300:
-// wide rows of B (N >= 512) want full warps with two or four vectors per lane (fp32:
-// float4 x 2 with the next index batch prefetched, then float2 x 4; bf16: 8 x bf16 x 2);
-// narrow B wants full warps of scalar lanes with 8 entries
-// per step (the batch of 32 (colind, val) pairs amortises the index loads). The entry-balanced
-// kernels, which win on skewed rows, are not picked here: they change the summation order of
-// rows that cross a chunk, and the library cannot see the row lengths without reading rowptr
-// (the learned selector does that on the host).
+// Library choice among the bit-identical row-split kernels, from variant sweeps on GB300 (a
+// uniform 100k x 100k matrix with 2M entries and a power-law 200k one, N from 16 to 384, and
+// the 4096-square C1 matrix): the fastest kernel's column tile matches the width of B, with
+// 16- or 8-byte vectors, and the one tile of a wide row wants full warps with two or four
+// vectors per lane (fp32: float4 x 2 with the next index batch prefetched, then float2 x 4;
+// bf16: 8 x bf16 x 2). Each width class lists its pick first, then narrower vectors for B and
+// C layouts the wider ones cannot serve. The entry-balanced kernels, which win on skewed rows,
+// are not picked here: they change the summation order of rows that cross a chunk, and the
+// library cannot see the row lengths without reading rowptr (the learned selector does that on
+// the host).
 int spmm_default_variant(int dtype, int M, int K, int N, int nnz, long ldb, long ldc,
                          const void *B, const void *C) {
     (void)M; (void)K; (void)nnz;
     const int esz = dtype == 0 ? 4 : 2;
     struct Pick { int vb, g, cpl, u, pf; };
-    const Pick wide_f32[] = {{16, 32, 2, 4, 1}, {8, 32, 4, 4, 0}, {16, 32, 2, 4, 0}, {4, 32, 2, 8, 0}};
-    const Pick wide_bf16[] = {{16, 32, 2, 4, 0}, {8, 32, 2, 4, 0}, {4, 32, 4, 4, 0}, {2, 32, 2, 8, 0}};
-    const Pick narrow_f32[] = {{4, 32, 2, 8, 0}};
-    const Pick narrow_bf16[] = {{4, 32, 2, 8, 0}, {2, 32, 2, 8, 0}};
-    const Pick *list;
-    int n;
-    if (N >= 512) {
-        list = dtype == 0 ? wide_f32 : wide_bf16;
-        n = 4;
-    } else {
-        list = dtype == 0 ? narrow_f32 : narrow_bf16;
-        n = dtype == 0 ? 1 : 2;
+    struct Class { int max_n; Pick picks[4]; int n; };
+    // fp32 (tile = vb / 4 * g * cpl columns)
+    static const Class f32[] = {
+        {16, {{16, 2, 2, 4, 0}, {8, 4, 2, 4, 0}, {4, 8, 2, 4, 0}}, 3},
+        {32, {{16, 4, 2, 8, 0}, {8, 8, 2, 4, 0}, {4, 16, 2, 4, 0}}, 3},
+        {64, {{8, 16, 2, 4, 0}, {4, 16, 4, 4, 0}, {4, 32, 2, 8, 0}}, 3},
+        {128, {{8, 32, 2, 4, 0}, {4, 32, 4, 4, 0}, {4, 32, 2, 8, 0}}, 3},
+        {256, {{16, 32, 2, 4, 1}, {8, 32, 4, 4, 1}, {8, 32, 2, 4, 0}, {4, 32, 4, 4, 0}}, 4},
+        {511, {{8, 32, 2, 4, 0}, {4, 32, 4, 4, 0}, {4, 32, 2, 8, 0}}, 3},
+        {INT_MAX, {{16, 32, 2, 4, 1}, {8, 32, 4, 4, 0}, {16, 32, 2, 4, 0}, {4, 32, 2, 8, 0}}, 4},
+    };
+    // bf16 (tile = vb / 2 * g * cpl columns)
+    static const Class bf16[] = {
+        {16, {{8, 4, 1, 4, 0}, {4, 8, 1, 4, 0}, {2, 16, 1, 4, 0}}, 3},
+        {32, {{16, 4, 1, 4, 0}, {8, 8, 1, 4, 0}, {4, 16, 1, 4, 0}}, 3},
+        {64, {{16, 8, 1, 4, 0}, {8, 16, 1, 4, 0}, {4, 16, 2, 4, 0}}, 3},
+        {128, {{16, 8, 2, 4, 0}, {8, 16, 2, 4, 0}, {4, 32, 2, 4, 0}}, 3},
+        {256, {{16, 32, 1, 4, 0}, {16, 16, 2, 4, 0}, {8, 32, 2, 4, 0}, {4, 32, 4, 4, 0}}, 4},
+        {511, {{16, 32, 2, 4, 1}, {16, 32, 2, 4, 0}, {8, 32, 2, 4, 0}, {4, 32, 4, 4, 0}}, 4},
+        {INT_MAX, {{16, 32, 2, 4, 0}, {8, 32, 2, 4, 0}, {4, 32, 4, 4, 0}, {2, 32, 2, 8, 0}}, 4},
+    };
+    const Class *cls = dtype == 0 ? f32 : bf16;
+    while (N > cls->max_n) ++cls;
+    for (int i = 0; i < cls->n; ++i) {
+        const Pick &p = cls->picks[i];
+        if (!vb_ok(dtype, p.vb, N, ldb, ldc, B, C)) continue;
+        const int v = find_variant(dtype, p.vb, p.g, p.cpl, p.u, p.pf);
+        if (v) return v;
     }
-    for (int i = 0; i < n; ++i)
-        if (vb_ok(dtype, list[i].vb, N, ldb, ldc, B, C))
-            return find_variant(dtype, list[i].vb, list[i].g, list[i].cpl, list[i].u, list[i].pf);
     // any layout: scalar lanes
     return find_variant(dtype, esz, 32, N > 32 ? 2 : 1, 8);
 }

@@ -89,8 +89,15 @@ def test_variant_table(native_lib):
     assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v16_g32_c2_u4_pf"
     v = native_lib.as_spmm_default_variant(0, 4096, 4096, 4096, 167772, 4096, 4096, 264, 256)
     assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v8_g32_c4_u4"
-    v = native_lib.as_spmm_default_variant(0, 100, 100, 3, 500, 3, 3, 256, 256)
-    assert native_lib.as_spmm_variant_name(0, v).decode() == "rowsplit_v4_g32_c2_u8"
+    # narrower B: the column tile matched to the width (16-byte vectors where the layout
+    # allows them, scalar lanes for N = 3)
+    for n_, name in ((3, "rowsplit_v4_g8_c2_u4"), (16, "rowsplit_v16_g2_c2_u4"),
+                     (64, "rowsplit_v8_g16_c2_u4"), (128, "rowsplit_v8_g32_c2_u4"),
+                     (256, "rowsplit_v16_g32_c2_u4_pf"), (384, "rowsplit_v8_g32_c2_u4")):
+        v = native_lib.as_spmm_default_variant(0, 100, 100, n_, 500, n_, n_, 256, 256)
+        assert native_lib.as_spmm_variant_name(0, v).decode() == name, n_
+    v = native_lib.as_spmm_default_variant(1, 100, 100, 128, 500, 128, 128, 256, 256)
+    assert native_lib.as_spmm_variant_name(1, v).decode() == "rowsplit_v16_g8_c2_u4"
 
 
 @pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU error path")
