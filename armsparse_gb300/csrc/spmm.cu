@@ -398,6 +398,12 @@ int spmm_default_variant(int dtype, int M, int K, int N, int nnz, long ldb, long
         {511, {{16, 32, 2, 4, 1}, {16, 32, 2, 4, 0}, {8, 32, 2, 4, 0}, {4, 32, 4, 4, 0}}, 4},
         {INT_MAX, {{16, 32, 2, 4, 0}, {8, 32, 2, 4, 0}, {4, 32, 4, 4, 0}, {2, 32, 2, 8, 0}}, 4},
     };
+    // bf16 rows wider than one 512-column tile that do not fill whole tiles: the 256-column
+    // tile (no half-empty last tile; 0.313 against 0.385 ms at N = 768 on the sweep matrix)
+    if (dtype == 1 && N > 511 && N % 512 != 0 && vb_ok(dtype, 16, N, ldb, ldc, B, C)) {
+        const int v = find_variant(dtype, 16, 32, 1, 4, 0);
+        if (v) return v;
+    }
     const Class *cls = dtype == 0 ? f32 : bf16;
     while (N > cls->max_n) ++cls;
     for (int i = 0; i < cls->n; ++i) {

@@ -96,8 +96,10 @@ def test_variant_table(native_lib):
                      (256, "rowsplit_v16_g32_c2_u4_pf"), (384, "rowsplit_v8_g32_c2_u4")):
         v = native_lib.as_spmm_default_variant(0, 100, 100, n_, 500, n_, n_, 256, 256)
         assert native_lib.as_spmm_variant_name(0, v).decode() == name, n_
-    v = native_lib.as_spmm_default_variant(1, 100, 100, 128, 500, 128, 128, 256, 256)
-    assert native_lib.as_spmm_variant_name(1, v).decode() == "rowsplit_v16_g8_c2_u4"
+    for n_, name in ((128, "rowsplit_v16_g8_c2_u4"), (768, "rowsplit_v16_g32_c1_u4"),
+                     (1024, "rowsplit_v16_g32_c2_u4")):
+        v = native_lib.as_spmm_default_variant(1, 100, 100, n_, 500, n_, n_, 256, 256)
+        assert native_lib.as_spmm_variant_name(1, v).decode() == name, n_
 
 
 @pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU error path")
