@@ -45,6 +45,25 @@ __device__ __forceinline__ uint16_t f32_to_bf16(float f) {
 // A ReLU applied at an output store when `relu` is set (negative -> 0; -0 and NaN pass).
 __device__ __forceinline__ float relu_if(float v, bool relu) { return relu && v < 0.0f ? 0.0f : v; }
 
+// Rows with more than kLongRow entries are left by the row kernels to the long-row kernel
+// (spmm_long.cu); rows with more than kHugeRow are listed from the end of its list, which it
+// takes first.
+constexpr int kLongRow = 256;
+constexpr int kHugeRow = 16384;
+
+// Lists row `row` (of `len` entries) for the long-row kernel: counters [0] rows listed from the
+// front, [2] huge rows listed from the end of the M-entry list.
+__device__ __forceinline__ void list_long_row(long row, int len, int M, int *long_list,
+                                              unsigned *long_count, unsigned *status) {
+    const bool huge = len > kHugeRow;
+    const unsigned idx = atomicAdd(long_count + (huge ? 2 : 0), 1u);
+    if (idx < static_cast<unsigned>(M))
+        long_list[huge ? M - 1 - static_cast<int>(idx) : static_cast<int>(idx)] =
+            static_cast<int>(row);
+    else
+        flag(status, kFlagLongList);
+}
+
 // Valid row range [lo, hi) of row r; rows with malformed pointers become empty and flag.
 __device__ __forceinline__ void row_range(const int *rowptr, int r, int nnz, unsigned *status,
                                           int &lo, int &hi) {

@@ -85,8 +85,10 @@ as_status spmm_bulk_launch(as_ctx *ctx, int dtype, int lane_bytes, int stages, c
 // Long rows of the row-split kernels: the cp.async size (16 or 4 bytes) the layout allows,
 // 0 when none does; the launch of the kernel that takes the listed rows.
 int spmm_long_granule(int dtype, int N, long ldb, const void *B);
+// `op` is the chain's step: 0 the SpMM's fused multiply-add, 1 the unweighted sum, 2 max from
+// -inf, 3 the DGL max (spmm_reduce.cu's reductions, fp32).
 as_status spmm_long_launch(as_ctx *ctx, int dtype, int granule, const SpmmArgs &a,
-                           const int *list, cudaStream_t s);
+                           const int *list, cudaStream_t s, int op = 0);
 as_status spgemm_dense_launch(as_ctx *ctx, int M, int K, int N, int nnz_a, const int *rp1,
                               const int *ci1, const float *v1, int nnz_b, const int *rp2,
                               const int *ci2, const float *v2, float *C, long ldc, float beta,

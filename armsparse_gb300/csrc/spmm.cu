@@ -54,8 +54,6 @@ __device__ __forceinline__ void load_c(const float *p, float *v) {
 }
 
 constexpr int kThreads = 256;
-constexpr int kLongRow = 256;  // entries; longer rows are handed to spmm_long.cu
-constexpr int kHugeRow = 16384;  // entries; such long rows are listed from the end, taken first
 
 template <typename T, int VB, int GROUP, int CPL, int U, bool PF>
 __global__ void __launch_bounds__(kThreads, PF ? 4 : 1)
@@ -79,16 +77,7 @@ spmm_rowsplit(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
     int lo, hi;
     row_range(rowptr, static_cast<int>(row), nnz, status, lo, hi);
     if (hi - lo > long_thresh) {  // left to the long-row kernel (spmm_long.cu)
-        if (blockIdx.y == 0 && g == 0) {
-            // counters: [0] rows listed from the front, [2] huge rows listed from the end
-            const bool huge = hi - lo > kHugeRow;
-            const unsigned idx = atomicAdd(long_count + (huge ? 2 : 0), 1u);
-            if (idx < static_cast<unsigned>(M))
-                long_list[huge ? M - 1 - static_cast<int>(idx) : static_cast<int>(idx)] =
-                    static_cast<int>(row);
-            else
-                flag(status, kFlagLongList);
-        }
+        if (blockIdx.y == 0 && g == 0) list_long_row(row, hi - lo, M, long_list, long_count, status);
         return;
     }
 

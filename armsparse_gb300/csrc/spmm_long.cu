@@ -125,8 +125,21 @@ __device__ __forceinline__ void cp_async_zfill(uint32_t dst, const void *gmem, i
                      : "memory");
 }
 
-// T: storage type of val and B (float or uint16_t = bf16); GB: cp.async size in bytes.
-template <typename T, int GB>
+// The per-entry step of a chain: OP 0 the SpMM's fused multiply-add (acc = fma(b, v, acc)),
+// 1 the unweighted copy-sum (acc + b), 2 max from -inf (fmaxf(acc, v * b)), 3 the DGL max
+// (acc > v * b ? acc : v * b); the max forms use b alone when the row has no values.
+template <int OP>
+__device__ __forceinline__ float step(float acc, float b, float v, bool weighted) {
+    if constexpr (OP == 0) return fmaf(b, v, acc);
+    if constexpr (OP == 1) return __fadd_rn(acc, b);
+    const float x = weighted ? __fmul_rn(v, b) : b;
+    if constexpr (OP == 2) return fmaxf(acc, x);
+    return acc > x ? acc : x;
+}
+
+// T: storage type of val and B (float or uint16_t = bf16); GB: cp.async size in bytes; OP: the
+// reduction (step above; the reductions other than 0 take fp32 only).
+template <typename T, int GB, int OP>
 __global__ void __launch_bounds__(kThreads, 1)
 spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
           const int *__restrict__ colind, const T *__restrict__ val, const T *__restrict__ B,
@@ -182,7 +195,9 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         }
         __syncthreads();
 
-        float acc0 = 0.0f, acc1 = 0.0f;
+        constexpr float kInit = OP == 2 ? -INFINITY : OP == 3 ? -10000.0f : 0.0f;
+        const bool weighted = val != nullptr;
+        float acc0 = kInit, acc1 = kInit;
         const int c0 = 2 * lane;  // this lane's first column within the slice
         float *crow = C + static_cast<long>(r) * ldc + slice0;
         if (warp == 0) {
@@ -216,22 +231,22 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                         for (int i = 0; i < 4; ++i) v[i] = lds_vals(vs + (q + 4 * i) * 4);
 #pragma unroll
                         for (int i = 0; i < 4; ++i) {
-                            acc0 = fmaf(b[4 * i].x, v[i].x, acc0);
-                            acc1 = fmaf(b[4 * i].y, v[i].x, acc1);
-                            acc0 = fmaf(b[4 * i + 1].x, v[i].y, acc0);
-                            acc1 = fmaf(b[4 * i + 1].y, v[i].y, acc1);
-                            acc0 = fmaf(b[4 * i + 2].x, v[i].z, acc0);
-                            acc1 = fmaf(b[4 * i + 2].y, v[i].z, acc1);
-                            acc0 = fmaf(b[4 * i + 3].x, v[i].w, acc0);
-                            acc1 = fmaf(b[4 * i + 3].y, v[i].w, acc1);
+                            acc0 = step<OP>(acc0, b[4 * i].x, v[i].x, weighted);
+                            acc1 = step<OP>(acc1, b[4 * i].y, v[i].x, weighted);
+                            acc0 = step<OP>(acc0, b[4 * i + 1].x, v[i].y, weighted);
+                            acc1 = step<OP>(acc1, b[4 * i + 1].y, v[i].y, weighted);
+                            acc0 = step<OP>(acc0, b[4 * i + 2].x, v[i].z, weighted);
+                            acc1 = step<OP>(acc1, b[4 * i + 2].y, v[i].z, weighted);
+                            acc0 = step<OP>(acc0, b[4 * i + 3].x, v[i].w, weighted);
+                            acc1 = step<OP>(acc1, b[4 * i + 3].y, v[i].w, weighted);
                         }
                     }
                 } else {
                     for (int j = 0; j < n; ++j) {
                         const float2 b = lds_pair(bs + j * kSlice, T());
                         const float x = vals[slot * kStage + j];
-                        acc0 = fmaf(b.x, x, acc0);
-                        acc1 = fmaf(b.y, x, acc1);
+                        acc0 = step<OP>(acc0, b.x, x, weighted);
+                        acc1 = step<OP>(acc1, b.y, x, weighted);
                     }
                 }
                 __syncwarp();
@@ -247,11 +262,11 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 const int e0 = st * kStage + lane, e1 = e0 + 32;
                 if (st < n_stages && e0 < L) {
                     k0 = ld_stream(colind + lo + e0);
-                    x0 = to_f32(ld_stream(val + lo + e0));
+                    x0 = weighted ? to_f32(ld_stream(val + lo + e0)) : 1.0f;
                 }
                 if (st < n_stages && e1 < L) {
                     k1 = ld_stream(colind + lo + e1);
-                    x1 = to_f32(ld_stream(val + lo + e1));
+                    x1 = weighted ? to_f32(ld_stream(val + lo + e1)) : 1.0f;
                 }
             };
             int k0, k1;
@@ -334,9 +349,9 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
     }
 }
 
-template <typename T, int GB>
+template <typename T, int GB, int OP = 0>
 as_status launch(as_ctx *ctx, const SpmmArgs &a, const int *list, cudaStream_t s) {
-    auto k = spmm_long<T, GB>;
+    auto k = spmm_long<T, GB, OP>;
     constexpr int kBytes = Layout<T>::kBytes;
     static int per_sm[64] = {};  // resident CTAs per multiprocessor, per device
     const int dev = ctx->device;
@@ -386,7 +401,16 @@ int spmm_long_granule(int dtype, int N, long ldb, const void *B) {
 }
 
 as_status spmm_long_launch(as_ctx *ctx, int dtype, int granule, const SpmmArgs &a,
-                           const int *list, cudaStream_t s) {
+                           const int *list, cudaStream_t s, int op) {
+    if (op != 0) {  // the reductions: fp32
+        if (dtype != 0) return fail(AS_ERR_UNSUPPORTED, "spmm long rows: reductions take fp32");
+        switch (op) {
+            case 1: return granule == 16 ? launch<float, 16, 1>(ctx, a, list, s) : launch<float, 4, 1>(ctx, a, list, s);
+            case 2: return granule == 16 ? launch<float, 16, 2>(ctx, a, list, s) : launch<float, 4, 2>(ctx, a, list, s);
+            case 3: return granule == 16 ? launch<float, 16, 3>(ctx, a, list, s) : launch<float, 4, 3>(ctx, a, list, s);
+        }
+        return fail(AS_ERR_INVALID_VALUE, "spmm long rows: unknown reduction");
+    }
     if (dtype == 0)
         return granule == 16 ? launch<float, 16>(ctx, a, list, s) : launch<float, 4>(ctx, a, list, s);
     return granule == 16 ? launch<uint16_t, 16>(ctx, a, list, s) : launch<uint16_t, 4>(ctx, a, list, s);

@@ -9,7 +9,11 @@
 // in CSR order, so an empty row stays at -10000.
 //
 // One warp per row; lane l owns columns l, l+32, ... of a 32*CPL-column tile (scalar loads,
-// any N); 4 entries per step.
+// any N). Rows with more than kLongRow entries are left to the long-row kernel (spmm_long.cu,
+// launched next with the same reduction as its chain step), as in the row-split SpMM: a hub
+// row would otherwise keep one warp busy for the whole call.
+#include <limits.h>
+
 #include "common.cuh"
 #include "internal.h"
 
@@ -23,12 +27,19 @@ __global__ void __launch_bounds__(kThreads)
 spmm_reduce(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
             const int *__restrict__ colind, const float *__restrict__ val,
             const float *__restrict__ B, long ldb, float *__restrict__ C, long ldc,
-            unsigned *status) {
+            unsigned *status, int long_thresh, int *long_list, unsigned *long_count) {
+    // let the long-row kernel (a programmatic dependent) be scheduled early; it waits for this
+    // grid to complete before it reads the list
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
     const int lane = threadIdx.x & 31;
     const long row = static_cast<long>(blockIdx.x) * (kThreads / 32) + (threadIdx.x >> 5);
     if (row >= M) return;
     int lo, hi;
     row_range(rowptr, static_cast<int>(row), nnz, status, lo, hi);
+    if (hi - lo > long_thresh) {  // left to the long-row kernel
+        if (blockIdx.y == 0 && lane == 0) list_long_row(row, hi - lo, M, long_list, long_count, status);
+        return;
+    }
     const int tile0 = blockIdx.y * 32 * CPL;
     float acc[CPL];
 #pragma unroll
@@ -76,14 +87,15 @@ spmm_reduce(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
 }
 
 template <int OP, bool W>
-void launch(const SpmmArgs &a, cudaStream_t s) {
+void launch(const SpmmArgs &a, int thresh, int *list, unsigned *counters, cudaStream_t s) {
     constexpr int CPL = 4;
     dim3 grid(static_cast<unsigned>(ceil_div(a.M, kThreads / 32)),
               static_cast<unsigned>(ceil_div(a.N, 32 * CPL)));
     spmm_reduce<OP, W, CPL><<<grid, kThreads, 0, s>>>(a.M, a.K, a.N, a.nnz, a.rowptr, a.colind,
                                                       static_cast<const float *>(a.val),
                                                       static_cast<const float *>(a.B), a.ldb,
-                                                      a.C, a.ldc, a.status);
+                                                      a.C, a.ldc, a.status, thresh, list,
+                                                      counters);
 }
 
 }  // namespace
@@ -91,11 +103,29 @@ void launch(const SpmmArgs &a, cudaStream_t s) {
 as_status spmm_reduce_launch(as_ctx *ctx, int op, const SpmmArgs &a, cudaStream_t s) {
     if (ceil_div(a.N, 128) > 65535) return fail(AS_ERR_UNSUPPORTED, "spmm reduce: N too large");
     const bool w = a.val != nullptr;
-    if (op == 0) w ? launch<0, true>(a, s) : launch<0, false>(a, s);
-    else if (op == 1) w ? launch<1, true>(a, s) : launch<1, false>(a, s);
-    else w ? launch<2, true>(a, s) : launch<2, false>(a, s);
+    // rows longer than kLongRow entries go to the long-row kernel when its copies can serve
+    // the layout
+    int thresh = INT_MAX;
+    int *list = nullptr;
+    const int granule = a.nnz > kLongRow && a.M > 0 ? spmm_long_granule(0, a.N, a.ldb, a.B) : 0;
+    if (granule) {
+        void *p = nullptr;
+        as_status st = scratch(ctx, static_cast<size_t>(a.M) * sizeof(int), &p);
+        if (st != AS_OK) return st;
+        thresh = kLongRow;
+        list = static_cast<int *>(p);
+    }
+    if (op == 0) w ? launch<0, true>(a, thresh, list, ctx->d_long, s) : launch<0, false>(a, thresh, list, ctx->d_long, s);
+    else if (op == 1) w ? launch<1, true>(a, thresh, list, ctx->d_long, s) : launch<1, false>(a, thresh, list, ctx->d_long, s);
+    else w ? launch<2, true>(a, thresh, list, ctx->d_long, s) : launch<2, false>(a, thresh, list, ctx->d_long, s);
     ctx->launches++;
-    return check_cuda(cudaGetLastError(), "spmm reduce launch");
+    as_status st = check_cuda(cudaGetLastError(), "spmm reduce launch");
+    if (st != AS_OK || !granule) return st;
+    // the long rows' chain step: the weighted sum is the SpMM's fused multiply-add
+    const int step = op == 0 ? (w ? 0 : 1) : op == 1 ? 2 : 3;
+    st = spmm_long_launch(ctx, 0, granule, a, list, s, step);
+    if (st != AS_OK) cudaMemsetAsync(ctx->d_long, 0, 3 * sizeof(unsigned), s);
+    return st;
 }
 
 }  // namespace as

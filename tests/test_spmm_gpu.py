@@ -246,6 +246,24 @@ def test_reduce_aggregations(oracle, op):
     A.sync_status()
 
 
+def test_reduce_long_rows(oracle):
+    """Rows past 256 entries (one past 16,384) go to the long-row kernel with the reduction as
+    its chain step: sum, weighted sum, max and the DGL max stay bit-exact against the CSR-order
+    restatement, for 16-byte (N = 64, 300) and 4-byte (N = 47) copies."""
+    a = _skewed(41)
+    rp, ci, v = csr_dev(a)
+    for N_ in (47, 64, 300):
+        B = S.dense_uniform((a.n_cols, N_), 42 + N_) * 30000.0 - 15000.0  # some below -10000
+        B = B.astype(np.float32)
+        Bd = to_dev(B)
+        for op in ("sum", "max", "max_dgl"):
+            for val in (None, a.val):
+                got = A.spmm_reduce(rp, ci, Bd, val=None if val is None else v, op=op)
+                ref = oracle.spmm_reduce_f32(a.rowptr, a.colind, B, val=val, op=op)
+                assert np.array_equal(bits(got), bits(ref)), (op, N_, val is None)
+    A.sync_status()
+
+
 def test_reduce_max_dgl(oracle):
     """The reference's DGL copy-max (binary_reduce_max.cu: start at -10000, acc > x ? acc : x):
     empty rows give -10000, values below -10000 never show unless they follow a NaN entry (which
