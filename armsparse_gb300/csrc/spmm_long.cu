@@ -127,11 +127,13 @@ __device__ __forceinline__ void cp_async_zfill(uint32_t dst, const void *gmem, i
 
 // The per-entry step of a chain: OP 0 the SpMM's fused multiply-add (acc = fma(b, v, acc)),
 // 1 the unweighted copy-sum (acc + b), 2 max from -inf (fmaxf(acc, v * b)), 3 the DGL max
-// (acc > v * b ? acc : v * b); the max forms use b alone when the row has no values.
+// (acc > v * b ? acc : v * b), 4 the fused multiply-add skipping zero values (the 1x4-blocked
+// layout's empty slots); the max forms use b alone when the row has no values.
 template <int OP>
 __device__ __forceinline__ float step(float acc, float b, float v, bool weighted) {
     if constexpr (OP == 0) return fmaf(b, v, acc);
     if constexpr (OP == 1) return __fadd_rn(acc, b);
+    if constexpr (OP == 4) return v != 0.0f ? fmaf(b, v, acc) : acc;
     const float x = weighted ? __fmul_rn(v, b) : b;
     if constexpr (OP == 2) return fmaxf(acc, x);
     return acc > x ? acc : x;
@@ -291,10 +293,13 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 for (int g = 0; g < kStage / 4; ++g) {
                     const int j = 4 * g + sub;
                     int k = __shfl_sync(kAll, g < 8 ? k0 : k1, j & 31);
+                    // OP 4: an empty slot (value 0) may point past K; only a filled one is bad
+                    bool filled = true;
+                    if constexpr (OP == 4) filled = __shfl_sync(kAll, g < 8 ? x0 : x1, j & 31) != 0.0f;
                     if (s * kStage + j < L) {
                         const bool bad = static_cast<unsigned>(k) >= static_cast<unsigned>(K);
                         if (bad) {
-                            flag(status, kFlagBadColind);
+                            if (filled) flag(status, kFlagBadColind);
                             k = 0;
                         }
                         const unsigned char *src = reinterpret_cast<const unsigned char *>(
@@ -402,12 +407,13 @@ int spmm_long_granule(int dtype, int N, long ldb, const void *B) {
 
 as_status spmm_long_launch(as_ctx *ctx, int dtype, int granule, const SpmmArgs &a,
                            const int *list, cudaStream_t s, int op) {
-    if (op != 0) {  // the reductions: fp32
-        if (dtype != 0) return fail(AS_ERR_UNSUPPORTED, "spmm long rows: reductions take fp32");
+    if (op != 0) {  // the reductions and the 1x4-blocked layout: fp32
+        if (dtype != 0) return fail(AS_ERR_UNSUPPORTED, "spmm long rows: this step takes fp32");
         switch (op) {
             case 1: return granule == 16 ? launch<float, 16, 1>(ctx, a, list, s) : launch<float, 4, 1>(ctx, a, list, s);
             case 2: return granule == 16 ? launch<float, 16, 2>(ctx, a, list, s) : launch<float, 4, 2>(ctx, a, list, s);
             case 3: return granule == 16 ? launch<float, 16, 3>(ctx, a, list, s) : launch<float, 4, 3>(ctx, a, list, s);
+            case 4: return granule == 16 ? launch<float, 16, 4>(ctx, a, list, s) : launch<float, 4, 4>(ctx, a, list, s);
         }
         return fail(AS_ERR_INVALID_VALUE, "spmm long rows: unknown reduction");
     }

@@ -8,7 +8,10 @@
 // skipped (the layout cannot tell a stored zero from an empty slot), so every output is one
 // fused chain over the row's nonzero entries in column order: bit for bit the CSR SpMM of the
 // same matrix without stored zeros. The four rows of a block are adjacent in B, which the
-// gathers see as one run of 4 * ldb elements.
+// gathers see as one run of 4 * ldb elements. Rows with more than kLongRow slots are left to
+// the long-row kernel (spmm_long.cu, its zero-skipping step), as in the row-split SpMM.
+#include <limits.h>
+
 #include "common.cuh"
 #include "internal.h"
 #include "spmm_vec.cuh"
@@ -23,7 +26,10 @@ __global__ void __launch_bounds__(kThreads)
 spmm_vcsr4(int M, int K, int N, int nslots, const int *__restrict__ vrowptr,
            const int *__restrict__ vcolind, const float *__restrict__ vval,
            const float *__restrict__ B, long ldb, float *__restrict__ C, long ldc, float beta,
-           unsigned *status) {
+           unsigned *status, int long_thresh, int *long_list, unsigned *long_count) {
+    // let the long-row kernel (a programmatic dependent) be scheduled early; it waits for this
+    // grid to complete before it reads the list
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
     using V = Vec<float, VB>;
     constexpr int E = V::E;
     constexpr int TILE = 32 * E * CPL;
@@ -32,6 +38,10 @@ spmm_vcsr4(int M, int K, int N, int nslots, const int *__restrict__ vrowptr,
     if (row >= M) return;
     int lo, hi;
     row_range(vrowptr, static_cast<int>(row), nslots, status, lo, hi);
+    if (hi - lo > long_thresh) {  // left to the long-row kernel
+        if (blockIdx.y == 0 && lane == 0) list_long_row(row, hi - lo, M, long_list, long_count, status);
+        return;
+    }
     const int tile0 = blockIdx.y * TILE;
     float acc[CPL][E];
 #pragma unroll
@@ -80,15 +90,22 @@ spmm_vcsr4(int M, int K, int N, int nslots, const int *__restrict__ vrowptr,
     }
 }
 
+struct LongList {
+    int thresh;
+    int *list;
+    unsigned *counters;
+};
+
 template <int VB, int CPL>
 void launch(int M, int K, int N, int nslots, const int *vrowptr, const int *vcolind,
             const float *vval, const float *B, long ldb, float *C, long ldc, float beta,
-            unsigned *status, cudaStream_t s) {
+            unsigned *status, const LongList &lr, cudaStream_t s) {
     constexpr int TILE = 32 * Vec<float, VB>::E * CPL;
     dim3 grid(static_cast<unsigned>(ceil_div(M, kThreads / 32)),
               static_cast<unsigned>(ceil_div(N, TILE)));
     spmm_vcsr4<VB, CPL><<<grid, kThreads, 0, s>>>(M, K, N, nslots, vrowptr, vcolind, vval, B, ldb,
-                                                   C, ldc, beta, status);
+                                                   C, ldc, beta, status, lr.thresh, lr.list,
+                                                   lr.counters);
 }
 
 }  // namespace
@@ -97,18 +114,34 @@ as_status spmm_vcsr4_launch(as_ctx *ctx, int M, int K, int N, int nslots, const 
                             const int *vcolind, const float *vval, const float *B, long ldb,
                             float *C, long ldc, float beta, cudaStream_t s) {
     const uintptr_t pb = reinterpret_cast<uintptr_t>(B), pc = reinterpret_cast<uintptr_t>(C);
-    if (N >= 256 && N % 4 == 0 && ldb % 4 == 0 && ldc % 4 == 0 && pb % 16 == 0 && pc % 16 == 0) {
-        if (ceil_div(N, 256) > 65535) return fail(AS_ERR_UNSUPPORTED, "spmm vcsr4: N too large");
-        launch<16, 2>(M, K, N, nslots, vrowptr, vcolind, vval, B, ldb, C, ldc, beta, ctx->d_status, s);
-    } else if (N % 2 == 0 && ldb % 2 == 0 && ldc % 2 == 0 && pb % 8 == 0 && pc % 8 == 0) {
-        if (ceil_div(N, 64) > 65535) return fail(AS_ERR_UNSUPPORTED, "spmm vcsr4: N too large");
-        launch<8, 1>(M, K, N, nslots, vrowptr, vcolind, vval, B, ldb, C, ldc, beta, ctx->d_status, s);
-    } else {
-        if (ceil_div(N, 32) > 65535) return fail(AS_ERR_UNSUPPORTED, "spmm vcsr4: N too large");
-        launch<4, 1>(M, K, N, nslots, vrowptr, vcolind, vval, B, ldb, C, ldc, beta, ctx->d_status, s);
+    const bool wide = N >= 256 && N % 4 == 0 && ldb % 4 == 0 && ldc % 4 == 0 && pb % 16 == 0 && pc % 16 == 0;
+    const bool pairs = N % 2 == 0 && ldb % 2 == 0 && ldc % 2 == 0 && pb % 8 == 0 && pc % 8 == 0;
+    if (ceil_div(N, wide ? 256 : pairs ? 64 : 32) > 65535)
+        return fail(AS_ERR_UNSUPPORTED, "spmm vcsr4: N too large");
+    // rows longer than kLongRow slots go to the long-row kernel when its copies can serve the
+    // layout
+    LongList lr{INT_MAX, nullptr, ctx->d_long};
+    const int granule = nslots > kLongRow && M > 0 ? spmm_long_granule(0, N, ldb, B) : 0;
+    if (granule) {
+        void *p = nullptr;
+        as_status st = scratch(ctx, static_cast<size_t>(M) * sizeof(int), &p);
+        if (st != AS_OK) return st;
+        lr.thresh = kLongRow;
+        lr.list = static_cast<int *>(p);
     }
+    if (wide)
+        launch<16, 2>(M, K, N, nslots, vrowptr, vcolind, vval, B, ldb, C, ldc, beta, ctx->d_status, lr, s);
+    else if (pairs)
+        launch<8, 1>(M, K, N, nslots, vrowptr, vcolind, vval, B, ldb, C, ldc, beta, ctx->d_status, lr, s);
+    else
+        launch<4, 1>(M, K, N, nslots, vrowptr, vcolind, vval, B, ldb, C, ldc, beta, ctx->d_status, lr, s);
     ctx->launches++;
-    return check_cuda(cudaGetLastError(), "spmm vcsr4 launch");
+    as_status st = check_cuda(cudaGetLastError(), "spmm vcsr4 launch");
+    if (st != AS_OK || !granule) return st;
+    SpmmArgs a{M, K, N, nslots, vrowptr, vcolind, vval, B, ldb, C, ldc, beta, ctx->d_status};
+    st = spmm_long_launch(ctx, 0, granule, a, lr.list, s, 4);
+    if (st != AS_OK) cudaMemsetAsync(ctx->d_long, 0, 3 * sizeof(unsigned), s);
+    return st;
 }
 
 }  // namespace as

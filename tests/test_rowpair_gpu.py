@@ -104,3 +104,31 @@ def test_vcsr4_spmm_is_the_csr_chain(oracle, N):
         assert res["pick"] in ("csr", "vcsr4", "rowpair")
         assert all(t["ms"] > 0 for t in res["times"].values())
     A.sync_status()
+
+
+def test_vcsr4_spmm_long_rows(oracle):
+    """Rows past 256 slots (one past 16,384) go to the long-row kernel with its zero-skipping
+    step: still the CSR chain bit for bit, with and without accumulate, for 16-byte (N = 64)
+    and 4-byte (N = 47) copies."""
+    rng = np.random.default_rng(99)
+    n_rows, n_cols = 2000, 40000
+    lens = rng.integers(0, 40, n_rows)
+    lens[[5, 700, 1500]] = [30000, 3000, 300]
+    rp_h = np.zeros(n_rows + 1, np.int32)
+    np.cumsum(lens, out=rp_h[1:])
+    ci_h = np.concatenate([np.sort(rng.choice(n_cols, l, replace=False)) for l in lens]).astype(np.int32)
+    a = S.CSR(rp_h, ci_h, rng.uniform(-1, 1, ci_h.size).astype(np.float32), n_rows, n_cols)
+    rp, ci, v = to_dev(a.rowptr), to_dev(a.colind), to_dev(a.val)
+    vr, vc, vv = A.csr_to_vcsr4(rp, ci, v)
+    assert int(torch.diff(vr).max()) > 16384
+    for N in (47, 64):
+        B = S.dense_uniform((n_cols, N), 100 + N)
+        C = A.spmm_vcsr4(vr, vc, vv, to_dev(B))
+        ref = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, B)
+        assert np.array_equal(bits(C), bits(ref)), N
+        C0 = S.dense_uniform((n_rows, N), 200 + N)
+        C = to_dev(C0)
+        A.spmm_vcsr4(vr, vc, vv, to_dev(B), C=C, beta=1.0)
+        ref = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, B, C=C0)
+        assert np.array_equal(bits(C), bits(ref)), N
+    A.sync_status()
