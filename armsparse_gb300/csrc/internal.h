@@ -87,9 +87,11 @@ as_status spmm_bulk_launch(as_ctx *ctx, int dtype, int lane_bytes, int stages, c
 int spmm_long_granule(int dtype, int N, long ldb, const void *B);
 // `op` is the chain's step: 0 the SpMM's fused multiply-add, 1 the unweighted sum, 2 max from
 // -inf, 3 the DGL max (spmm_reduce.cu's reductions), 4 the fused multiply-add skipping zero
-// values (spmm_vcsr4.cu's empty slots); the steps other than 0 take fp32.
+// values (spmm_vcsr4.cu's empty slots), 5 the row-pair layout's two chains per listed pair
+// (spmm_rowpair.cu; `pair_flag` is its flag array); the steps other than 0 take fp32.
 as_status spmm_long_launch(as_ctx *ctx, int dtype, int granule, const SpmmArgs &a,
-                           const int *list, cudaStream_t s, int op = 0);
+                           const int *list, cudaStream_t s, int op = 0,
+                           const uint8_t *pair_flag = nullptr);
 as_status spgemm_dense_launch(as_ctx *ctx, int M, int K, int N, int nnz_a, const int *rp1,
                               const int *ci1, const float *v1, int nnz_b, const int *rp2,
                               const int *ci2, const float *v2, float *C, long ldc, float beta,

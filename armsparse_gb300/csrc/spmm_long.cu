@@ -58,7 +58,8 @@ struct Layout {
     static constexpr int kSlice = kCols * static_cast<int>(sizeof(T));  // B bytes per entry
     static constexpr int kRing = kStages * kStage * kSlice;
     static constexpr int kVals = kStages * kStage * 4;                  // values as fp32
-    static constexpr int kBytes = kRing + kVals + 2 * kStages * 4 + 16;
+    static constexpr int kMasks = kStages * 8;  // row-pair mode: the stage's include bits
+    static constexpr int kBytes = kRing + kVals + kMasks + 2 * kStages * 4 + 16;
 };
 
 // producer index (0-7) of a warp, or -1 for the consumer and the idle warps
@@ -128,12 +129,15 @@ __device__ __forceinline__ void cp_async_zfill(uint32_t dst, const void *gmem, i
 // The per-entry step of a chain: OP 0 the SpMM's fused multiply-add (acc = fma(b, v, acc)),
 // 1 the unweighted copy-sum (acc + b), 2 max from -inf (fmaxf(acc, v * b)), 3 the DGL max
 // (acc > v * b ? acc : v * b), 4 the fused multiply-add skipping zero values (the 1x4-blocked
-// layout's empty slots); the max forms use b alone when the row has no values.
+// layout's empty slots), 5 the fused multiply-add over the entries a row-pair unit includes
+// (the include mask is applied by the consumer); the max forms use b alone when the row has
+// no values.
 template <int OP>
 __device__ __forceinline__ float step(float acc, float b, float v, bool weighted) {
     if constexpr (OP == 0) return fmaf(b, v, acc);
     if constexpr (OP == 1) return __fadd_rn(acc, b);
     if constexpr (OP == 4) return v != 0.0f ? fmaf(b, v, acc) : acc;
+    if constexpr (OP == 5) return fmaf(b, v, acc);
     const float x = weighted ? __fmul_rn(v, b) : b;
     if constexpr (OP == 2) return fmaxf(acc, x);
     return acc > x ? acc : x;
@@ -147,7 +151,7 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
           const int *__restrict__ colind, const T *__restrict__ val, const T *__restrict__ B,
           long ldb, float *__restrict__ C, long ldc, float beta, unsigned *status,
           const int *__restrict__ list, unsigned *counters, uint16_t *__restrict__ C16,
-          bool relu, unsigned spin_limit) {
+          bool relu, unsigned spin_limit, const uint8_t *__restrict__ pair_flag) {
     using Lay = Layout<T>;
     constexpr int kSlice = Lay::kSlice;
     constexpr int kEsz = static_cast<int>(sizeof(T));
@@ -155,7 +159,8 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *ring = smem;                                  // [kStages][kStage][kSlice]
     float *vals = reinterpret_cast<float *>(smem + Lay::kRing);  // [kStages][kStage]
-    int *full_seq = reinterpret_cast<int *>(smem + Lay::kRing + Lay::kVals);  // stage filled + 1
+    unsigned long long *masks = reinterpret_cast<unsigned long long *>(smem + Lay::kRing + Lay::kVals);
+    int *full_seq = reinterpret_cast<int *>(smem + Lay::kRing + Lay::kVals + Lay::kMasks);  // stage filled + 1
     int *empty_seq = full_seq + kStages;                                       // stage consumed + 1
     volatile int *abort_flag = reinterpret_cast<volatile int *>(empty_seq + kStages);
 
@@ -167,7 +172,9 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
     const int n_long = static_cast<int>(min(*reinterpret_cast<volatile unsigned *>(counters), cap));
     const int n_huge =
         static_cast<int>(min(*reinterpret_cast<volatile unsigned *>(counters + 2), cap));
-    const int n_slices = static_cast<int>(ceil_div(N, kCols));
+    // row-pair mode: a listed item is a pair's even row; each pair gives two rows' units
+    constexpr int kRowsPerItem = OP == 5 ? 2 : 1;
+    const int n_slices = static_cast<int>(ceil_div(N, kCols)) * kRowsPerItem;
     const long units_huge = static_cast<long>(n_huge) * n_slices;
     const long units = units_huge + static_cast<long>(n_long) * n_slices;
     const int pw = producer_of(warp);
@@ -178,14 +185,23 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         const bool huge = u < units_huge;
         const long v = huge ? u : u - units_huge;
         const int item = static_cast<int>(v / n_slices);
-        const int slice0 = static_cast<int>(v - static_cast<long>(item) * n_slices) * kCols;
+        const int sub_unit = static_cast<int>(v - static_cast<long>(item) * n_slices);
+        const int which = sub_unit % kRowsPerItem;   // row-pair mode: 0 the even row, 1 the odd
+        const int slice0 = sub_unit / kRowsPerItem * kCols;
         const int w = min(kCols, N - slice0);        // columns of this slice
         const int pieces = w * kEsz / GB;            // copy pieces per entry
-        const int r = huge ? list[M - 1 - item] : list[item];
-        if (r < 0 || r >= M) continue;
+        const int r0 = huge ? list[M - 1 - item] : list[item];
+        const int r = r0 + which;                    // the output row
+        if (r0 < 0 || r >= M) continue;
         int lo, hi;
-        row_range(rowptr, r, nnz, status, lo, hi);
-        const int L = hi - lo;
+        row_range(rowptr, r0, nnz, status, lo, hi);
+        // Row-pair mode: the even row chains over its segment's unflagged entries (all of them
+        // when it has no partner); the odd row over the even segment's flagged entries, then
+        // over its own segment (entries at positions L1.. map to [lo1, hi1)).
+        int L1 = hi - lo, lo1 = 0, hi1 = 0;
+        const bool partner = OP == 5 && r0 + 1 < M;
+        if (OP == 5 && which == 1) row_range(rowptr, r0 + 1, nnz, status, lo1, hi1);
+        const int L = L1 + (hi1 - lo1);
         const int n_stages = static_cast<int>(ceil_div(L, kStage));
 
         if (tid == 0) {
@@ -201,7 +217,7 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
         const bool weighted = val != nullptr;
         float acc0 = kInit, acc1 = kInit;
         const int c0 = 2 * lane;  // this lane's first column within the slice
-        float *crow = C + static_cast<long>(r) * ldc + slice0;
+        float *crow = C + static_cast<long>(r) * ldc + slice0;  // r: this unit's output row
         if (warp == 0) {
             // ---- consumer: the chains of columns c0 and c0 + 1 ----
             if (beta != 0.0f) {
@@ -222,6 +238,12 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 const int n = min(kStage, L - s * kStage);
                 const uint32_t bs = smem_u32(ring + slot * kStage * kSlice) + c0 * kEsz;
                 const uint32_t vs = smem_u32(vals + slot * kStage);
+                // row-pair mode: entry j of the stage counts when bit j is set
+                const unsigned long long mask = OP == 5 ? masks[slot] : ~0ull;
+                auto st = [&](float acc, float b, float x, int j) {
+                    if constexpr (OP == 5) return ((mask >> j) & 1ull) ? fmaf(b, x, acc) : acc;
+                    return step<OP>(acc, b, x, weighted);
+                };
                 if (n == kStage) {
 #pragma unroll
                     for (int q = 0; q < kStage; q += 16) {
@@ -233,22 +255,23 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                         for (int i = 0; i < 4; ++i) v[i] = lds_vals(vs + (q + 4 * i) * 4);
 #pragma unroll
                         for (int i = 0; i < 4; ++i) {
-                            acc0 = step<OP>(acc0, b[4 * i].x, v[i].x, weighted);
-                            acc1 = step<OP>(acc1, b[4 * i].y, v[i].x, weighted);
-                            acc0 = step<OP>(acc0, b[4 * i + 1].x, v[i].y, weighted);
-                            acc1 = step<OP>(acc1, b[4 * i + 1].y, v[i].y, weighted);
-                            acc0 = step<OP>(acc0, b[4 * i + 2].x, v[i].z, weighted);
-                            acc1 = step<OP>(acc1, b[4 * i + 2].y, v[i].z, weighted);
-                            acc0 = step<OP>(acc0, b[4 * i + 3].x, v[i].w, weighted);
-                            acc1 = step<OP>(acc1, b[4 * i + 3].y, v[i].w, weighted);
+                            const int j = q + 4 * i;
+                            acc0 = st(acc0, b[4 * i].x, v[i].x, j);
+                            acc1 = st(acc1, b[4 * i].y, v[i].x, j);
+                            acc0 = st(acc0, b[4 * i + 1].x, v[i].y, j + 1);
+                            acc1 = st(acc1, b[4 * i + 1].y, v[i].y, j + 1);
+                            acc0 = st(acc0, b[4 * i + 2].x, v[i].z, j + 2);
+                            acc1 = st(acc1, b[4 * i + 2].y, v[i].z, j + 2);
+                            acc0 = st(acc0, b[4 * i + 3].x, v[i].w, j + 3);
+                            acc1 = st(acc1, b[4 * i + 3].y, v[i].w, j + 3);
                         }
                     }
                 } else {
                     for (int j = 0; j < n; ++j) {
                         const float2 b = lds_pair(bs + j * kSlice, T());
                         const float x = vals[slot * kStage + j];
-                        acc0 = step<OP>(acc0, b.x, x, weighted);
-                        acc1 = step<OP>(acc1, b.y, x, weighted);
+                        acc0 = st(acc0, b.x, x, j);
+                        acc1 = st(acc1, b.y, x, j);
                     }
                 }
                 __syncwarp();
@@ -258,22 +281,39 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
             // ---- producer pw: stages pw, pw + kProducers, ... (all in slot pw % kStages) ----
             const int sub = lane >> 3, pl = lane & 7;  // entry of a group of four, lane in it
             // column index and value of this lane's entries (lane, lane + 32) of stage st
-            auto load = [&](int st, int &k0, int &k1, float &x0, float &x1) {
-                k0 = k1 = 0;
-                x0 = x1 = 0.0f;
-                const int e0 = st * kStage + lane, e1 = e0 + 32;
-                if (st < n_stages && e0 < L) {
-                    k0 = ld_stream(colind + lo + e0);
-                    x0 = weighted ? to_f32(ld_stream(val + lo + e0)) : 1.0f;
-                }
-                if (st < n_stages && e1 < L) {
-                    k1 = ld_stream(colind + lo + e1);
-                    x1 = weighted ? to_f32(ld_stream(val + lo + e1)) : 1.0f;
+            // entry position e of the unit -> index in the arrays, and whether it counts
+            // (row-pair mode; every entry counts otherwise)
+            auto entry = [&](int e, int &idx, int &inc) {
+                idx = lo + e;
+                inc = 1;
+                if constexpr (OP == 5) {
+                    if (e >= L1) {
+                        idx = lo1 + (e - L1);
+                    } else if (partner) {
+                        inc = (__ldg(pair_flag + idx) != 0) == (which == 1);
+                    }
                 }
             };
-            int k0, k1;
+            auto load = [&](int st, int &k0, int &k1, float &x0, float &x1, int &f0, int &f1) {
+                k0 = k1 = 0;
+                x0 = x1 = 0.0f;
+                f0 = f1 = 0;
+                const int e0 = st * kStage + lane, e1 = e0 + 32;
+                int i0, i1;
+                if (st < n_stages && e0 < L) {
+                    entry(e0, i0, f0);
+                    k0 = ld_stream(colind + i0);
+                    x0 = weighted ? to_f32(ld_stream(val + i0)) : 1.0f;
+                }
+                if (st < n_stages && e1 < L) {
+                    entry(e1, i1, f1);
+                    k1 = ld_stream(colind + i1);
+                    x1 = weighted ? to_f32(ld_stream(val + i1)) : 1.0f;
+                }
+            };
+            int k0, k1, f0, f1;
             float x0, x1;
-            load(pw, k0, k1, x0, x1);
+            load(pw, k0, k1, x0, x1, f0, f1);
             for (int s = pw; s < n_stages; s += kProducers) {
                 const int slot = s % kStages;
                 if (s >= kStages) {  // the consumer is done with stage s - kStages
@@ -283,20 +323,27 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                                       abort_flag, 64);
                     if (!__shfl_sync(kAll, ok, 0)) break;
                 }
-                int nk0, nk1;
+                int nk0, nk1, nf0, nf1;
                 float nx0, nx1;
-                load(s + kProducers, nk0, nk1, nx0, nx1);  // the next turn's, in flight meanwhile
+                load(s + kProducers, nk0, nk1, nx0, nx1, nf0, nf1);  // the next turn's, in flight meanwhile
                 vals[slot * kStage + lane] = x0;
                 vals[slot * kStage + lane + 32] = x1;
+                if constexpr (OP == 5) {
+                    const unsigned long long m =
+                        __ballot_sync(kAll, f0) | (static_cast<unsigned long long>(__ballot_sync(kAll, f1)) << 32);
+                    if (lane == 0) masks[slot] = m;
+                }
                 const uint32_t dst0 = smem_u32(ring + slot * kStage * kSlice);
 #pragma unroll 4
                 for (int g = 0; g < kStage / 4; ++g) {
                     const int j = 4 * g + sub;
                     int k = __shfl_sync(kAll, g < 8 ? k0 : k1, j & 31);
-                    // OP 4: an empty slot (value 0) may point past K; only a filled one is bad
+                    // OP 4: an empty slot (value 0) may point past K; only a filled one is bad.
+                    // OP 5: an entry the unit leaves out is neither checked nor copied.
                     bool filled = true;
                     if constexpr (OP == 4) filled = __shfl_sync(kAll, g < 8 ? x0 : x1, j & 31) != 0.0f;
-                    if (s * kStage + j < L) {
+                    if constexpr (OP == 5) filled = __shfl_sync(kAll, g < 8 ? f0 : f1, j & 31) != 0;
+                    if (s * kStage + j < L && (OP != 5 || filled)) {
                         const bool bad = static_cast<unsigned>(k) >= static_cast<unsigned>(K);
                         if (bad) {
                             if (filled) flag(status, kFlagBadColind);
@@ -322,6 +369,8 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
                 k1 = nk1;
                 x0 = nx0;
                 x1 = nx1;
+                f0 = nf0;
+                f1 = nf1;
             }
             asm volatile("cp.async.wait_all;\n" ::: "memory");
             __syncwarp();
@@ -355,7 +404,8 @@ spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
 }
 
 template <typename T, int GB, int OP = 0>
-as_status launch(as_ctx *ctx, const SpmmArgs &a, const int *list, cudaStream_t s) {
+as_status launch(as_ctx *ctx, const SpmmArgs &a, const int *list, cudaStream_t s,
+                 const uint8_t *pair_flag = nullptr) {
     auto k = spmm_long<T, GB, OP>;
     constexpr int kBytes = Layout<T>::kBytes;
     static int per_sm[64] = {};  // resident CTAs per multiprocessor, per device
@@ -370,7 +420,7 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, const int *list, cudaStream_t s
         per_sm[dev] = std::max(1, n);
     }
     // one wave of CTAs striding over the (row, slice) units
-    const long max_units = static_cast<long>(a.M) * ceil_div(a.N, kCols);
+    const long max_units = static_cast<long>(a.M) * ceil_div(a.N, kCols) * (OP == 5 ? 2 : 1);
     dim3 grid(static_cast<unsigned>(
         std::max(1L, std::min(max_units, static_cast<long>(per_sm[dev]) * ctx->sms))));
     // programmatic dependent launch (outside stream capture): the CTAs are scheduled while
@@ -390,7 +440,7 @@ as_status launch(as_ctx *ctx, const SpmmArgs &a, const int *list, cudaStream_t s
     cudaError_t e = cudaLaunchKernelEx(&cfg, k, a.M, a.K, a.N, a.nnz, a.rowptr, a.colind,
                                        static_cast<const T *>(a.val), static_cast<const T *>(a.B),
                                        a.ldb, a.C, a.ldc, a.beta, a.status, list, ctx->d_long,
-                                       a.C16, a.relu, ctx->spin_limit);
+                                       a.C16, a.relu, ctx->spin_limit, pair_flag);
     ctx->launches++;
     return check_cuda(e != cudaSuccess ? e : cudaGetLastError(), "spmm long rows launch");
 }
@@ -406,7 +456,7 @@ int spmm_long_granule(int dtype, int N, long ldb, const void *B) {
 }
 
 as_status spmm_long_launch(as_ctx *ctx, int dtype, int granule, const SpmmArgs &a,
-                           const int *list, cudaStream_t s, int op) {
+                           const int *list, cudaStream_t s, int op, const uint8_t *pair_flag) {
     if (op != 0) {  // the reductions and the 1x4-blocked layout: fp32
         if (dtype != 0) return fail(AS_ERR_UNSUPPORTED, "spmm long rows: this step takes fp32");
         switch (op) {
@@ -414,6 +464,10 @@ as_status spmm_long_launch(as_ctx *ctx, int dtype, int granule, const SpmmArgs &
             case 2: return granule == 16 ? launch<float, 16, 2>(ctx, a, list, s) : launch<float, 4, 2>(ctx, a, list, s);
             case 3: return granule == 16 ? launch<float, 16, 3>(ctx, a, list, s) : launch<float, 4, 3>(ctx, a, list, s);
             case 4: return granule == 16 ? launch<float, 16, 4>(ctx, a, list, s) : launch<float, 4, 4>(ctx, a, list, s);
+            case 5:
+                if (!pair_flag) return fail(AS_ERR_INVALID_VALUE, "spmm long rows: row pairs need their flags");
+                return granule == 16 ? launch<float, 16, 5>(ctx, a, list, s, pair_flag)
+                                     : launch<float, 4, 5>(ctx, a, list, s, pair_flag);
         }
         return fail(AS_ERR_INVALID_VALUE, "spmm long rows: unknown reduction");
     }

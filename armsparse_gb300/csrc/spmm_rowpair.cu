@@ -18,6 +18,12 @@
 // A flag is honoured only in the segment of an even row that has a partner; anywhere else it
 // is ignored (the entry counts for its own row), and a flagged first entry of a segment reuses
 // a zero segment. A column index out of range is flagged and its entry skipped.
+//
+// Pairs with more than kLongRow entries are left to the long-row kernel (spmm_long.cu, its
+// row-pair step): a unit per row of the pair runs the same chain over the entries it includes,
+// each with its own column's B segment (identical to the reused one in a well-formed layout).
+#include <limits.h>
+
 #include "common.cuh"
 #include "internal.h"
 #include "spmm_vec.cuh"
@@ -32,7 +38,11 @@ __global__ void __launch_bounds__(kThreads)
 spmm_rowpair(int M, int K, int N, int nnz, const int *__restrict__ rowptr2,
              const int *__restrict__ colind2, const float *__restrict__ val2,
              const uint8_t *__restrict__ flag2, const float *__restrict__ B, long ldb,
-             float *__restrict__ C, long ldc, float beta, unsigned *status) {
+             float *__restrict__ C, long ldc, float beta, unsigned *status, int long_thresh,
+             int *long_list, unsigned *long_count) {
+    // let the long-row kernel (a programmatic dependent) be scheduled early; it waits for this
+    // grid to complete before it reads the list
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
     using V = Vec<float, VB>;
     constexpr int E = V::E;
     constexpr int TILE = 32 * E * CPL;
@@ -41,6 +51,17 @@ spmm_rowpair(int M, int K, int N, int nnz, const int *__restrict__ rowptr2,
     const long ra = 2 * pair;
     if (ra >= M) return;
     const bool paired = ra + 1 < M;
+    {   // a long pair is left to the long-row kernel
+        int plo, phi, qlo, qhi;
+        row_range(rowptr2, static_cast<int>(ra), nnz, status, plo, phi);
+        qlo = qhi = 0;
+        if (paired) row_range(rowptr2, static_cast<int>(ra + 1), nnz, status, qlo, qhi);
+        const int len = (phi - plo) + (qhi - qlo);
+        if (len > long_thresh) {
+            if (blockIdx.y == 0 && lane == 0) list_long_row(ra, len, M, long_list, long_count, status);
+            return;
+        }
+    }
     const int tile0 = blockIdx.y * TILE;
 
     float acc0[CPL][E], acc1[CPL][E], b[CPL][E];
@@ -123,14 +144,16 @@ spmm_rowpair(int M, int K, int N, int nnz, const int *__restrict__ rowptr2,
 }
 
 template <int VB, int CPL>
-void launch(const SpmmArgs &a, const uint8_t *flag2, cudaStream_t s) {
+void launch(const SpmmArgs &a, const uint8_t *flag2, int thresh, int *list, unsigned *counters,
+            cudaStream_t s) {
     constexpr int TILE = 32 * Vec<float, VB>::E * CPL;
     const long pairs = (static_cast<long>(a.M) + 1) / 2;
     dim3 grid(static_cast<unsigned>(ceil_div(pairs, kThreads / 32)),
               static_cast<unsigned>(ceil_div(a.N, TILE)));
     spmm_rowpair<VB, CPL><<<grid, kThreads, 0, s>>>(
         a.M, a.K, a.N, a.nnz, a.rowptr, a.colind, static_cast<const float *>(a.val), flag2,
-        static_cast<const float *>(a.B), a.ldb, a.C, a.ldc, a.beta, a.status);
+        static_cast<const float *>(a.B), a.ldb, a.C, a.ldc, a.beta, a.status, thresh, list,
+        counters);
 }
 
 }  // namespace
@@ -138,20 +161,36 @@ void launch(const SpmmArgs &a, const uint8_t *flag2, cudaStream_t s) {
 as_status spmm_rowpair_launch(as_ctx *ctx, const SpmmArgs &a, const uint8_t *flag2,
                               cudaStream_t s) {
     const uintptr_t pb = reinterpret_cast<uintptr_t>(a.B), pc = reinterpret_cast<uintptr_t>(a.C);
-    // widest vectors the layout allows: float4 x 2 for wide B, float2, then scalars
-    if (a.N >= 256 && a.N % 4 == 0 && a.ldb % 4 == 0 && a.ldc % 4 == 0 && pb % 16 == 0 &&
-        pc % 16 == 0) {
-        if (ceil_div(a.N, 256) > 65535) return fail(AS_ERR_UNSUPPORTED, "spmm rowpair: N too large");
-        launch<16, 2>(a, flag2, s);
-    } else if (a.N % 2 == 0 && a.ldb % 2 == 0 && a.ldc % 2 == 0 && pb % 8 == 0 && pc % 8 == 0) {
-        if (ceil_div(a.N, 64) > 65535) return fail(AS_ERR_UNSUPPORTED, "spmm rowpair: N too large");
-        launch<8, 1>(a, flag2, s);
-    } else {
-        if (ceil_div(a.N, 32) > 65535) return fail(AS_ERR_UNSUPPORTED, "spmm rowpair: N too large");
-        launch<4, 1>(a, flag2, s);
+    const bool wide = a.N >= 256 && a.N % 4 == 0 && a.ldb % 4 == 0 && a.ldc % 4 == 0 &&
+                      pb % 16 == 0 && pc % 16 == 0;
+    const bool pairs = a.N % 2 == 0 && a.ldb % 2 == 0 && a.ldc % 2 == 0 && pb % 8 == 0 && pc % 8 == 0;
+    if (ceil_div(a.N, wide ? 256 : pairs ? 64 : 32) > 65535)
+        return fail(AS_ERR_UNSUPPORTED, "spmm rowpair: N too large");
+    // pairs longer than kLongRow entries go to the long-row kernel when its copies can serve
+    // the layout
+    int thresh = INT_MAX;
+    int *list = nullptr;
+    const int granule = a.nnz > kLongRow && a.M > 0 ? spmm_long_granule(0, a.N, a.ldb, a.B) : 0;
+    if (granule) {
+        void *p = nullptr;
+        as_status st = scratch(ctx, static_cast<size_t>(a.M) * sizeof(int), &p);
+        if (st != AS_OK) return st;
+        thresh = kLongRow;
+        list = static_cast<int *>(p);
     }
+    // widest vectors the layout allows: float4 x 2 for wide B, float2, then scalars
+    if (wide)
+        launch<16, 2>(a, flag2, thresh, list, ctx->d_long, s);
+    else if (pairs)
+        launch<8, 1>(a, flag2, thresh, list, ctx->d_long, s);
+    else
+        launch<4, 1>(a, flag2, thresh, list, ctx->d_long, s);
     ctx->launches++;
-    return check_cuda(cudaGetLastError(), "spmm rowpair launch");
+    as_status st = check_cuda(cudaGetLastError(), "spmm rowpair launch");
+    if (st != AS_OK || !granule) return st;
+    st = spmm_long_launch(ctx, 0, granule, a, list, s, 5, flag2);
+    if (st != AS_OK) cudaMemsetAsync(ctx->d_long, 0, 3 * sizeof(unsigned), s);
+    return st;
 }
 
 }  // namespace as

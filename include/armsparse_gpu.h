@@ -345,7 +345,10 @@ as_status as_csr_to_rowpair_fill(as_ctx *ctx, int M, int nnz, const int *rowptr,
  * (suitesparse_sdmm.cpp:25-44, its saxpy fused per element as OpenBLAS computes it): row 2p is
  * its CSR chain; row 2p+1 chains over the entries it shares with row 2p first (column order),
  * then over its own segment. A flagged entry reuses the B segment of the entry before it (the
- * same column) instead of gathering it again. beta = 1 is the reference's accumulate. */
+ * same column) instead of gathering it again. beta = 1 is the reference's accumulate. Pairs
+ * with more than 256 entries run on the long-row kernel, one unit per row of the pair, which
+ * gathers each entry's own column (the same values in a well-formed layout; a malformed one,
+ * e.g. a flagged first entry, can differ from the short-pair path). */
 as_status as_spmm_rowpair_f32(as_ctx *ctx, int M, int K, int N, int nnz, const int *rowptr2,
                               const int *colind2, const float *val2, const uint8_t *flag2,
                               const float *B, long ldb, float *C, long ldc, float beta,

@@ -132,3 +132,40 @@ def test_vcsr4_spmm_long_rows(oracle):
         ref = oracle.spmm_fma_chain_f32(a.rowptr, a.colind, a.val, B, C=C0)
         assert np.array_equal(bits(C), bits(ref)), N
     A.sync_status()
+
+
+def test_rowpair_long_pairs(oracle):
+    """Pairs past 256 entries (one past 16,384, whose rows share most columns, and one with no
+    partner at the end) go to the long-row kernel's row-pair step: a unit per row of the pair,
+    the odd row chaining over the shared columns first. Bit for bit the oracle's restatement of
+    DataReuseSpmm, with and without accumulate, for 16-byte (N = 64) and 4-byte (N = 47)
+    copies."""
+    rng = np.random.default_rng(101)
+    n_rows, n_cols = 1001, 50000
+    lens = rng.integers(0, 30, n_rows)
+    lens[[10, 11, 400, 1000]] = [20000, 18000, 2000, 700]
+    cols = [np.sort(rng.choice(n_cols, l, replace=False)) for l in lens]
+    # rows 10 and 11 share most of their columns (many flagged entries)
+    shared = np.sort(rng.choice(cols[10], 15000, replace=False))
+    rest = np.setdiff1d(np.arange(n_cols), cols[10])
+    cols[11] = np.sort(np.concatenate([shared, rng.choice(rest, 3000, replace=False)]))
+    lens[11] = cols[11].size
+    rp_h = np.zeros(n_rows + 1, np.int32)
+    np.cumsum(lens, out=rp_h[1:])
+    ci_h = np.concatenate(cols).astype(np.int32)
+    a = S.CSR(rp_h, ci_h, rng.uniform(-1, 1, ci_h.size).astype(np.float32), n_rows, n_cols)
+    rp, ci, v = to_dev(a.rowptr), to_dev(a.colind), to_dev(a.val)
+    rp2, ci2, v2, f2 = A.csr_to_rowpair(rp, ci, v)
+    orp, oci, ov, of = oracle.csr_to_rowpair(a.rowptr, a.colind, a.val)
+    assert of.sum() > 10000
+    for N in (47, 64):
+        B = S.dense_uniform((n_cols, N), 102 + N)
+        C = A.spmm_rowpair(rp2, ci2, v2, f2, to_dev(B))
+        ref = oracle.spmm_rowpair_f32(orp, oci, ov, of, B)
+        assert np.array_equal(bits(C), bits(ref)), N
+        C0 = S.dense_uniform((n_rows, N), 202 + N)
+        C = to_dev(C0)
+        A.spmm_rowpair(rp2, ci2, v2, f2, to_dev(B), C=C, beta=1.0)
+        ref = oracle.spmm_rowpair_f32(orp, oci, ov, of, B, C=C0)
+        assert np.array_equal(bits(C), bits(ref)), N
+    A.sync_status()
