@@ -8,9 +8,14 @@
 // kHugeRow entries are listed from the other end of the list and taken first, so the longest
 // chains start at once instead of behind shorter rows.
 //
-// Each output element is still one fused-FMA chain over the row's entries in CSR order (the
-// order cannot be split without changing the bits), so the speed comes from feeding the
-// chains. A CTA takes one (long row, 64-column slice) at a time; its warps split by role:
+// The same kernel takes the long rows of the other row-oriented SpMMs, with their own chain
+// step (OP below): the reduce aggregations (spmm_reduce.cu), the 1x4-blocked layout
+// (spmm_vcsr4.cu) and the row-pair layout (spmm_rowpair.cu: a listed pair gives a unit per
+// row, whose chain runs over the entries a per-stage include mask keeps).
+//
+// Each output element is still one chain over the row's entries in CSR order (the order
+// cannot be split without changing the bits), so the speed comes from feeding the chains. A
+// CTA takes one (long row, 64-column slice) at a time; its warps split by role:
 //  - warp 0 is the consumer: lane l runs the chains of columns 2l and 2l+1 of the slice out of
 //    shared memory, stage after stage (kStage entries per stage), reading each entry's two B
 //    values with one 64-bit (fp32) or 32-bit (bf16) load and the entry's value from the
@@ -144,7 +149,8 @@ __device__ __forceinline__ float step(float acc, float b, float v, bool weighted
 }
 
 // T: storage type of val and B (float or uint16_t = bf16); GB: cp.async size in bytes; OP: the
-// reduction (step above; the reductions other than 0 take fp32 only).
+// chain step above (the steps other than 0 take fp32 only). pair_flag: the row-pair layout's
+// flags (OP 5 only).
 template <typename T, int GB, int OP>
 __global__ void __launch_bounds__(kThreads, 1)
 spmm_long(int M, int K, int N, int nnz, const int *__restrict__ rowptr,
