@@ -33,14 +33,37 @@ def test_vcsr4_full_size_and_accumulate(oracle):
     A.sync_status()
 
 
+def test_vcsr4_long_rows(oracle):
+    """Rows past 4,096 slots (the longest 93,719 entries) get a CTA each: batches of blocks
+    staged in shared memory, the four chains run in block order by four threads and combined
+    as (s2 + s0) + (s3 + s1): bit for bit the reference's sums, with and without accumulate."""
+    a = S.powerlaw_csr(200_000, 2.2, 10.0, seed=3)
+    vr, vc, vv = oracle.csr_to_vcsr4(a.rowptr, a.colind, a.val)
+    assert np.diff(vr).max() > 4096
+    x = S.dense_uniform(a.n_cols, 7)
+    y0 = S.dense_uniform(a.n_rows, 8)
+    vrd, vcd, vvd, xd = to_dev(vr), to_dev(vc), to_dev(vv), to_dev(x)
+    ref = oracle.spmv_vcsr4_f32(vr, vc, vv, x, fused=True)
+    y = A.spmv_vcsr4(vrd, vcd, vvd, xd)
+    assert np.array_equal(bits(y), bits(ref))
+    ref = oracle.spmv_vcsr4_f32(vr, vc, vv, x, y=y0, fused=True)
+    y = to_dev(y0)
+    A.spmv_vcsr4(vrd, vcd, vvd, xd, y=y, beta=1.0)
+    assert np.array_equal(bits(y), bits(ref))
+    A.sync_status()
+
+
 @pytest.mark.parametrize("M,K,nnz,kind", [(4096, 4096, 167772, "u"), (1, 10, 5, "u"),
-                                           (100000, 100000, 0, "p"), (3000, 3000, 0, "b"),
+                                           (100000, 100000, 0, "p"), (300000, 300000, 0, "h"),
+                                           (3000, 3000, 0, "b"),
                                            (50, 50, 0, "e")])
 def test_csr_against_fp64(oracle, M, K, nnz, kind):
     if kind == "u":
         a = S.uniform_csr(M, K, nnz, seed=1)
     elif kind == "p":
         a = S.powerlaw_csr(M, 2.1, 8.0, seed=2)
+    elif kind == "h":  # a 300,000-entry hub row and many past 4,096 (a CTA each)
+        a = S.powerlaw_csr(M, 2.0, 20.0, seed=0)
     elif kind == "b":
         a = S.banded_csr(M, 9, seed=3)
     else:
