@@ -308,11 +308,15 @@ as_status launch_long(as_ctx *ctx, int M, int K, int nnz, const int *rowptr, con
     return st;
 }
 
-// Scratch for the long-row list when a row can exceed kLongSpmv entries.
-as_status long_list(as_ctx *ctx, int M, int nnz, int *&list, int &thresh) {
+// Scratch for the long-row list when a row can exceed kLongSpmv entries: more than that many
+// entries in all, and more columns (a row of distinct columns holds at most `max_row`, K or K
+// rounded up to whole 1x4 blocks; a malformed row with repeated columns stays on the row
+// kernel, which handles any length). Otherwise no list and no second launch, which matters
+// for a small SpMV.
+as_status long_list(as_ctx *ctx, int M, int nnz, long max_row, int *&list, int &thresh) {
     list = nullptr;
     thresh = INT_MAX;
-    if (nnz <= kLongSpmv || M <= 0) return AS_OK;
+    if (nnz <= kLongSpmv || M <= 0 || max_row <= kLongSpmv) return AS_OK;
     void *p = nullptr;
     as_status st = scratch(ctx, static_cast<size_t>(M) * sizeof(int), &p);
     if (st != AS_OK) return st;
@@ -331,7 +335,7 @@ as_status spmv_csr_launch(as_ctx *ctx, int M, int K, int nnz, const int *rowptr,
     while (group < 32 && group < mean) group <<= 1;
     int *list;
     int thresh;
-    as_status st = long_list(ctx, M, nnz, list, thresh);
+    as_status st = long_list(ctx, M, nnz, K, list, thresh);
     if (st != AS_OK) return st;
     const unsigned grid = static_cast<unsigned>(ceil_div(M, kThreads / group));
 #define AS_SPMV_G(G)                                                                          \
@@ -358,7 +362,7 @@ as_status spmv_vcsr4_launch(as_ctx *ctx, int M, int K, int nslots, const int *ro
         return fail(AS_ERR_INVALID_VALUE, "as_spmv_vcsr4_f32: val must be 16-byte aligned");
     int *list;
     int thresh;
-    as_status st = long_list(ctx, M, nslots, list, thresh);
+    as_status st = long_list(ctx, M, nslots, static_cast<long>(K) + 3, list, thresh);
     if (st != AS_OK) return st;
     const unsigned grid = static_cast<unsigned>(ceil_div(static_cast<long>(M) * 4, kThreads));
     spmv_vcsr4<8><<<grid, kThreads, 0, s>>>(M, K, nslots, rowptr, colind, val, x, y, beta,
